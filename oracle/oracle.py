@@ -1,0 +1,220 @@
+"""ctypes front end of the CPU oracle (oracle/sbd_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and the
+CPU-baseline leg of bench.py to check or time against the reference's
+algorithm.  The product package never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+REF_BIN = os.path.join(HERE, "_ref", "sbdref")
+
+_lib = None
+
+_u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+_i32p = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_szp = np.ctypeslib.ndpointer(dtype=np.uintp, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(dtype=np.int64, flags="C_CONTIGUOUS")
+
+
+def build() -> str:
+    """Compiles the oracle port (gcc + OpenMP) into oracle/_build."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    return LIB_PATH
+
+
+def build_reference(reference_root: str = "/root/reference") -> str | None:
+    """Compiles the reference harness into oracle/_ref when the reference tree exists."""
+    if not os.path.isdir(os.path.join(reference_root, "include", "sbd")):
+        return None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE_ROOT={reference_root}"], check=True)
+    return REF_BIN
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        L.orc_ints_create.restype = C.c_void_p
+        L.orc_ints_create.argtypes = [C.c_int, C.c_double, _f64p, _f64p]
+        L.orc_ints_destroy.argtypes = [C.c_void_p]
+        L.orc_excitations.restype = C.c_int
+        L.orc_excitations.argtypes = [_u64p, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      _szp, _szp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_hii.argtypes = [C.c_void_p, _u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int, _f64p]
+        tab = [_szp, _u64p, _i32p] * 4
+        L.orc_mult.argtypes = ([C.c_void_p, _u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int] + tab
+                               + [_f64p, _f64p, _f64p, C.c_size_t, C.c_size_t])
+        L.orc_hamiltonian_offdiag.restype = C.c_size_t
+        L.orc_hamiltonian_offdiag.argtypes = ([C.c_void_p, _u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int]
+                                              + tab + [C.c_void_p, C.c_void_p, C.c_void_p])
+        L.orc_davidson.restype = C.c_int
+        L.orc_davidson.argtypes = ([C.c_void_p, _u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int] + tab
+                                   + [_f64p, _f64p, C.c_int, C.c_int, C.c_double,
+                                      C.POINTER(C.c_double), C.POINTER(C.c_double)])
+        L.orc_inner.restype = C.c_double
+        L.orc_inner.argtypes = [_f64p, _f64p, C.c_size_t]
+        L.orc_symeig.argtypes = [C.c_int, _f64p, C.c_int, _f64p]
+        _lib = L
+    return _lib
+
+
+class SpinTables:
+    """CSR excitation lists of one spin, in the reference helper layout."""
+
+    def __init__(self, off_s, ket_s, cran_s, off_d, ket_d, cran_d):
+        self.off_s, self.ket_s, self.cran_s = off_s, ket_s, cran_s
+        self.off_d, self.ket_d, self.cran_d = off_d, ket_d, cran_d
+
+    def args(self):
+        return [self.off_s, self.ket_s, self.cran_s, self.off_d, self.ket_d, self.cran_d]
+
+
+def excitations(words: np.ndarray, norb: int, bit_length: int, spin: int) -> SpinTables:
+    L = lib()
+    words = np.ascontiguousarray(words, dtype=np.uint64)
+    n, nw = words.shape
+    off_s = np.zeros(n + 1, dtype=np.uintp)
+    off_d = np.zeros(n + 1, dtype=np.uintp)
+    L.orc_excitations(words.ravel(), n, nw, bit_length, norb, spin, off_s, off_d, None, None, None, None)
+    ns, nd = int(off_s[-1]), int(off_d[-1])
+    ket_s = np.zeros(max(ns, 1), dtype=np.uint64)
+    cran_s = np.zeros(max(2 * ns, 1), dtype=np.int32)
+    ket_d = np.zeros(max(nd, 1), dtype=np.uint64)
+    cran_d = np.zeros(max(4 * nd, 1), dtype=np.int32)
+    rc = L.orc_excitations(words.ravel(), n, nw, bit_length, norb, spin, off_s, off_d,
+                           ket_s.ctypes.data, cran_s.ctypes.data, ket_d.ctypes.data, cran_d.ctypes.data)
+    if rc != 0:
+        raise ValueError("strings with different popcounts in one list")
+    return SpinTables(off_s, ket_s[:ns] if ns else ket_s, cran_s, off_d, ket_d[:nd] if nd else ket_d, cran_d)
+
+
+class Oracle:
+    """The reference algorithm on one problem (strings are uint64, L <= 64)."""
+
+    def __init__(self, norb, h1, eri, ecore, astr, bstr, bit_length: int = 20):
+        from sbd_gb300.strings import to_words
+        self.norb = int(norb)
+        self.bit_length = int(bit_length)
+        self.astr = np.asarray(astr, dtype=np.uint64)
+        self.bstr = np.asarray(bstr, dtype=np.uint64)
+        self.aw = np.ascontiguousarray(to_words(self.astr, self.norb, self.bit_length))
+        self.bw = np.ascontiguousarray(to_words(self.bstr, self.norb, self.bit_length))
+        self.words = self.aw.shape[1]
+        self.na, self.nb = self.astr.size, self.bstr.size
+        self.N = self.na * self.nb
+        self._h1 = np.ascontiguousarray(h1, dtype=np.float64).ravel()
+        self._eri = np.ascontiguousarray(eri, dtype=np.float64)
+        self.ints = lib().orc_ints_create(self.norb, float(ecore), self._h1, self._eri)
+        self.ta = excitations(self.aw, self.norb, self.bit_length, 0)
+        self.tb = excitations(self.bw, self.norb, self.bit_length, 1)
+        self._hii = None
+
+    @classmethod
+    def from_problem(cls, p, bit_length: int = 20):
+        return cls(p.norb, p.ints.h1, p.ints.eri, p.ints.ecore, p.astr, p.bstr, bit_length)
+
+    def __del__(self):
+        if getattr(self, "ints", None) and _lib is not None:
+            _lib.orc_ints_destroy(self.ints)
+            self.ints = None
+
+    def _head(self):
+        return [self.ints, self.aw.ravel(), self.na, self.bw.ravel(), self.nb, self.words, self.bit_length]
+
+    def _tabs(self):
+        return self.ta.args() + self.tb.args()
+
+    def hii(self) -> np.ndarray:
+        if self._hii is None:
+            h = np.zeros(self.N)
+            lib().orc_hii(self.ints, self.aw.ravel(), self.na, self.bw.ravel(), self.nb, self.words,
+                          self.bit_length, h)
+            self._hii = h
+        return self._hii
+
+    def mult(self, C_in: np.ndarray, out: np.ndarray | None = None, rows=None) -> np.ndarray:
+        """sigma += H C (the reference accumulates into its output)."""
+        c = np.ascontiguousarray(C_in, dtype=np.float64).ravel()
+        s = np.zeros(self.N) if out is None else out
+        r0, r1 = (0, self.na) if rows is None else rows
+        lib().orc_mult(*self._head(), *self._tabs(), self.hii(), c, s, r0, r1)
+        return s
+
+    def sigma(self, C_in: np.ndarray) -> np.ndarray:
+        return self.mult(C_in)
+
+    def hamiltonian(self):
+        """Sparse H (scipy CSR) including the diagonal."""
+        import scipy.sparse as sp
+        nnz = lib().orc_hamiltonian_offdiag(*self._head(), *self._tabs(), None, None, None)
+        rows = np.zeros(max(nnz, 1), dtype=np.int64)
+        cols = np.zeros(max(nnz, 1), dtype=np.int64)
+        vals = np.zeros(max(nnz, 1))
+        lib().orc_hamiltonian_offdiag(*self._head(), *self._tabs(), rows.ctypes.data, cols.ctypes.data,
+                                      vals.ctypes.data)
+        H = sp.coo_matrix((vals[:nnz], (rows[:nnz], cols[:nnz])), shape=(self.N, self.N)).tocsr()
+        H = H + sp.diags(self.hii())
+        return H
+
+    def lowest(self, k: int = 1, tol: float = 1e-12) -> np.ndarray:
+        """The k lowest eigenvalues of the assembled H (dense for small N)."""
+        H = self.hamiltonian()
+        if self.N <= 4000:
+            w = np.linalg.eigvalsh(H.toarray())
+            return w[:k]
+        import scipy.sparse.linalg as sla
+        w = sla.eigsh(H, k=k, which="SA", tol=tol, return_eigenvectors=False)
+        return np.sort(w)
+
+    def davidson(self, max_it=100, max_nb=10, eps=1e-8, W0=None):
+        W = np.zeros(self.N) if W0 is None else np.array(W0, dtype=np.float64)
+        if W0 is None:
+            W[0] = 1.0  # BasisInitVector init 0 (chemistry/tpb/davidson.h:174-177)
+        e = C.c_double(0.0)
+        r = C.c_double(0.0)
+        ns = lib().orc_davidson(*self._head(), *self._tabs(), self.hii(), W, max_it, max_nb, eps,
+                                C.byref(e), C.byref(r))
+        return e.value, W, ns, r.value
+
+    def energy(self, W: np.ndarray) -> float:
+        """<W|H|W> as the reference reports it after the solve (sbdiag.h:488-526)."""
+        HW = self.mult(W)
+        return lib().orc_inner(np.ascontiguousarray(W), HW, self.N)
+
+
+def parse_sbdref(path: str) -> dict:
+    """Reads the tagged binary records written by oracle/_ref/sbdref."""
+    out: dict = {}
+    codes = {"Q": np.uint64, "i": np.int32, "d": np.float64}
+    with open(path, "rb") as f:
+        data = f.read()
+    pos = 0
+    while pos < len(data):
+        n = int.from_bytes(data[pos:pos + 4], "little")
+        pos += 4
+        name = data[pos:pos + n].decode()
+        pos += n
+        code = chr(data[pos])
+        pos += 1
+        cnt = int.from_bytes(data[pos:pos + 8], "little")
+        pos += 8
+        dt = np.dtype(codes[code])
+        arr = np.frombuffer(data[pos:pos + cnt * dt.itemsize], dtype=dt).copy()
+        pos += cnt * dt.itemsize
+        if name in out:
+            prev = out[name]
+            out[name] = np.concatenate([np.atleast_1d(prev), arr])
+        else:
+            out[name] = arr
+    return out

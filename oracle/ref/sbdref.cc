@@ -1,0 +1,189 @@
+// Reference harness: drives the reference's own header-only TPB CPU path
+// (SBD_TRADMODE, OpenMP, MPI size 1) on FCIDUMP + string files and writes
+// its intermediate results in a small tagged binary format.
+//
+// Test infrastructure only.  Built by oracle/Makefile into oracle/_ref/ from
+// the reference headers where they lie; used to pin the C restatement and to
+// generate the golden fixtures under tests/golden/.  Nothing in the product
+// library links or calls it.
+//
+// Flow mirrors sbd::tpb::diag (chemistry/tpb/sbdiag.h:151-526):
+//   SetupIntegrals -> TaskCommunicator -> MakeHelpers -> RemakeHelpers ->
+//   BasisInitVector(init 0) -> makeQChamDiagTerms -> Davidson(max_time) ->
+//   final mult and <W|HW>.
+//
+// Usage:
+//   sbdref --fcidump F --adet A [--bdet B] --out OUTFILE
+//          [--bit_length 20] [--tables 1] [--hii 1] [--cvec C.bin]
+//          [--davidson 1 --block NB --iteration IT --tolerance EPS]
+//          [--time_mult K]
+#include <omp.h>
+#include <chrono>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "sbd/sbd.h"
+
+namespace {
+
+struct Out {
+  std::ofstream f;
+  explicit Out(const std::string &path) : f(path, std::ios::binary) {
+    if (!f) throw std::runtime_error("cannot open output " + path);
+  }
+  // record: u32 name length, name bytes, u8 dtype code, u64 count, payload
+  template <typename T>
+  void put(const std::string &name, char code, const T *data, size_t n) {
+    uint32_t len = (uint32_t)name.size();
+    f.write((const char *)&len, 4);
+    f.write(name.data(), len);
+    f.write(&code, 1);
+    uint64_t cnt = n;
+    f.write((const char *)&cnt, 8);
+    if (n) f.write((const char *)data, (std::streamsize)(n * sizeof(T)));
+  }
+  void u64(const std::string &name, const std::vector<size_t> &v) { put(name, 'Q', v.data(), v.size()); }
+  void i32(const std::string &name, const std::vector<int> &v) { put(name, 'i', v.data(), v.size()); }
+  void f64(const std::string &name, const std::vector<double> &v) { put(name, 'd', v.data(), v.size()); }
+  void scalar(const std::string &name, double x) { put(name, 'd', &x, 1); }
+};
+
+std::string arg(int argc, char **argv, const char *key, const char *dflt) {
+  for (int i = 1; i + 1 < argc; ++i)
+    if (std::string(argv[i]) == key) return argv[i + 1];
+  return dflt;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+  MPI_Init(&argc, &argv);
+  MPI_Comm comm = MPI_COMM_WORLD;
+  const std::string fcifile = arg(argc, argv, "--fcidump", "");
+  const std::string afile = arg(argc, argv, "--adet", "");
+  const std::string bfile = arg(argc, argv, "--bdet", "");
+  const std::string outfile = arg(argc, argv, "--out", "sbdref.bin");
+  const std::string cfile = arg(argc, argv, "--cvec", "");
+  const size_t bit_length = std::stoul(arg(argc, argv, "--bit_length", "20"));
+  const int want_tables = std::stoi(arg(argc, argv, "--tables", "1"));
+  const int want_hii = std::stoi(arg(argc, argv, "--hii", "1"));
+  const int want_dav = std::stoi(arg(argc, argv, "--davidson", "0"));
+  const int max_nb = std::stoi(arg(argc, argv, "--block", "10"));
+  const int max_it = std::stoi(arg(argc, argv, "--iteration", "1"));
+  const double eps = std::stod(arg(argc, argv, "--tolerance", "1e-4"));
+  const int time_mult = std::stoi(arg(argc, argv, "--time_mult", "0"));
+
+  sbd::FCIDump fcidump = sbd::LoadFCIDump(fcifile);
+  int L = 0, Ne = 0;
+  double I0 = 0.0;
+  sbd::oneInt<double> I1;
+  sbd::twoInt<double> I2;
+  sbd::SetupIntegrals(fcidump, L, Ne, I0, I1, I2);
+  sbd::det_vector<size_t>::init_elem_size((2 * L + bit_length - 1) / bit_length);
+  sbd::det_vector<size_t, sbd::det_kind::half>::init_elem_size((L + bit_length - 1) / bit_length);
+
+  sbd::det_vector<size_t, sbd::det_kind::half> adet, bdet;
+  sbd::LoadAlphaDets(afile, adet, bit_length, L);
+  sbd::sort_bitarray(adet);
+  if (bfile.empty()) {
+    bdet = adet;
+  } else {
+    sbd::LoadAlphaDets(bfile, bdet, bit_length, L);
+    sbd::sort_bitarray(bdet);
+  }
+
+  MPI_Comm h_comm, b_comm, t_comm, a_comm;
+  sbd::TaskCommunicator(comm, 1, 1, 1, 1, h_comm, b_comm, t_comm, a_comm);
+  std::vector<sbd::TaskHelpers> helper;
+  auto th0 = std::chrono::steady_clock::now();
+  sbd::MakeHelpers(adet, bdet, bit_length, L, helper, h_comm, b_comm, t_comm, 1, 1);
+  sbd::RemakeHelpers(adet, bdet, bit_length, L, helper, h_comm, b_comm, t_comm, 1, 1);
+  auto th1 = std::chrono::steady_clock::now();
+
+  Out out(outfile);
+  out.scalar("norb", (double)L);
+  out.scalar("nalpha_str", (double)adet.size());
+  out.scalar("nbeta_str", (double)bdet.size());
+  out.scalar("threads", (double)omp_get_max_threads());
+  out.scalar("t_helpers", std::chrono::duration<double>(th1 - th0).count());
+  {
+    // sorted strings, first word only when a string fits in one word
+    std::vector<size_t> a(adet.size() * adet.elem_size()), b(bdet.size() * bdet.elem_size());
+    for (size_t i = 0; i < adet.size(); ++i)
+      for (size_t w = 0; w < adet.elem_size(); ++w) a[i * adet.elem_size() + w] = adet[i][w];
+    for (size_t i = 0; i < bdet.size(); ++i)
+      for (size_t w = 0; w < bdet.elem_size(); ++w) b[i * bdet.elem_size() + w] = bdet[i][w];
+    out.u64("adet_words", a);
+    out.u64("bdet_words", b);
+  }
+
+  if (want_tables) {
+    for (size_t t = 0; t < helper.size(); ++t) {
+      const auto &h = helper[t];
+      std::string p = "task" + std::to_string(t) + ".";
+      out.scalar(p + "type", (double)h.taskType);
+      out.u64(p + "SinglesFromAlphaOffset", h.SinglesFromAlphaOffset);
+      out.u64(p + "SinglesFromAlpha", h.SinglesFromAlpha_flat);
+      out.i32(p + "SinglesAlphaCrAn", h.SinglesAlphaCrAn_flat);
+      out.u64(p + "DoublesFromAlphaOffset", h.DoublesFromAlphaOffset);
+      out.u64(p + "DoublesFromAlpha", h.DoublesFromAlpha_flat);
+      out.i32(p + "DoublesAlphaCrAn", h.DoublesAlphaCrAn_flat);
+      out.u64(p + "SinglesFromBetaOffset", h.SinglesFromBetaOffset);
+      out.u64(p + "SinglesFromBeta", h.SinglesFromBeta_flat);
+      out.i32(p + "SinglesBetaCrAn", h.SinglesBetaCrAn_flat);
+      out.u64(p + "DoublesFromBetaOffset", h.DoublesFromBetaOffset);
+      out.u64(p + "DoublesFromBeta", h.DoublesFromBeta_flat);
+      out.i32(p + "DoublesBetaCrAn", h.DoublesBetaCrAn_flat);
+    }
+  }
+
+  std::vector<double> hii;
+  auto tq0 = std::chrono::steady_clock::now();
+  sbd::makeQChamDiagTerms(adet, bdet, bit_length, L, helper, I0, I1, I2, hii, h_comm, b_comm, t_comm);
+  auto tq1 = std::chrono::steady_clock::now();
+  out.scalar("t_hii", std::chrono::duration<double>(tq1 - tq0).count());
+  if (want_hii) out.f64("hii", hii);
+
+  if (!cfile.empty()) {
+    std::ifstream cf(cfile, std::ios::binary);
+    std::vector<double> C(hii.size());
+    cf.read((char *)C.data(), (std::streamsize)(C.size() * sizeof(double)));
+    if (!cf) throw std::runtime_error("short C vector file");
+    std::vector<double> S(C.size(), 0.0);
+    auto tm0 = std::chrono::steady_clock::now();
+    sbd::mult(hii, C, S, adet, bdet, bit_length, (size_t)L, 1, 1, helper, I0, I1, I2, h_comm, b_comm, t_comm);
+    auto tm1 = std::chrono::steady_clock::now();
+    out.scalar("t_mult", std::chrono::duration<double>(tm1 - tm0).count());
+    out.f64("sigma", S);
+    for (int k = 1; k < time_mult; ++k) {
+      std::fill(S.begin(), S.end(), 0.0);
+      auto a0 = std::chrono::steady_clock::now();
+      sbd::mult(hii, C, S, adet, bdet, bit_length, (size_t)L, 1, 1, helper, I0, I1, I2, h_comm, b_comm, t_comm);
+      auto a1 = std::chrono::steady_clock::now();
+      out.scalar("t_mult", std::chrono::duration<double>(a1 - a0).count());
+    }
+  }
+
+  if (want_dav) {
+    std::vector<double> W;
+    sbd::BasisInitVector(W, adet, bdet, 1, 1, h_comm, b_comm, t_comm, 0, 1729);
+    auto td0 = std::chrono::steady_clock::now();
+    sbd::Davidson(hii, W, adet, bdet, bit_length, (size_t)L, 1, 1, helper, I0, I1, I2, h_comm, b_comm, t_comm,
+                  max_it, max_nb, eps, 86400.0);
+    auto td1 = std::chrono::steady_clock::now();
+    std::vector<double> HW(W.size(), 0.0);
+    sbd::mult(hii, W, HW, adet, bdet, bit_length, (size_t)L, 1, 1, helper, I0, I1, I2, h_comm, b_comm, t_comm);
+    double E = 0.0;
+    sbd::InnerProduct(W, HW, E, b_comm);
+    std::cout.precision(16);
+    std::cout << " Energy = " << E << std::endl;
+    out.scalar("t_davidson", std::chrono::duration<double>(td1 - td0).count());
+    out.scalar("energy", E);
+    out.f64("W", W);
+  }
+  MPI_Finalize();
+  return 0;
+}

@@ -1,0 +1,155 @@
+/*
+ * sbdgb.h -- C ABI of the GB300 tensor-product-basis (TPB) engine.
+ *
+ * The engine computes the selected-CI Hamiltonian-vector product
+ * sigma = H*C on one GPU, its helper tables and diagonal, and the Davidson
+ * eigensolver around it, for the problems the reference's TPB path solves
+ * (alpha/beta string lists + FCIDUMP integrals, MPI communicators of size 1).
+ *
+ * Every entry point returns an int status (SBDGB_OK on success); nothing
+ * throws across the ABI.  sbdgb_last_error() gives the message of the last
+ * failing call on a context.  All pointers are plain host or device pointers;
+ * "_dev" names device memory, everything else is host memory.
+ *
+ * Data conventions (identical to the reference's):
+ *   - a spin string is one uint64, bit p = orbital p (norb <= 64); lists are
+ *     sorted ascending without duplicates, and the position in the list is the
+ *     string index (framework/bit_manipulation.h:386-439);
+ *   - determinant index = ia * nb + ib (beta contiguous,
+ *     chemistry/tpb/mult.h:455-465);
+ *   - h1 is the L x L spatial one-body matrix, eri the 8-fold packed two-body
+ *     array of B(B+1)/2 doubles with B = L(L+1)/2 (chemistry/basic/
+ *     integrals.h:94-102, makeintegrals.h:123-174);
+ *   - spin-orbital index in exported tables: alpha p -> 2p, beta p -> 2p+1.
+ */
+#ifndef SBDGB_H
+#define SBDGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SBDGB_ABI_VERSION 1
+
+enum sbdgb_status {
+  SBDGB_OK = 0,
+  SBDGB_E_INPUT = 1,       /* malformed input (reference: std::invalid_argument) */
+  SBDGB_E_UNSUPPORTED = 2, /* outside the supported envelope (norb > 64, comm size > 1, ...) */
+  SBDGB_E_CUDA = 3,        /* CUDA runtime failure */
+  SBDGB_E_NOMEM = 4,       /* device allocation failed or HBM budget exceeded */
+  SBDGB_E_STATE = 5,       /* call made in the wrong order */
+  SBDGB_E_TIMEOUT = 6      /* a bounded wait ran out */
+};
+
+enum sbdgb_precision {
+  SBDGB_FP64 = 0,  /* plain: FP64 storage and arithmetic */
+  SBDGB_MIXED = 1  /* FP32 vectors and products, FP64 accumulation and refinement */
+};
+
+typedef struct sbdgb_ctx sbdgb_ctx;
+typedef struct sbdgb_problem sbdgb_problem;
+
+/* ---- context ------------------------------------------------------------ */
+
+int sbdgb_abi_version(void);
+
+/* One context per GPU.  hbm_budget_bytes = 0 means "all free memory".
+ * Replaces the device set-up of the reference app (apps/
+ * chemistry_tpb_selected_basis_diagonalization/main.cc:36-47). */
+int sbdgb_ctx_create(sbdgb_ctx **ctx, int device, size_t hbm_budget_bytes);
+void sbdgb_ctx_destroy(sbdgb_ctx *ctx);
+const char *sbdgb_last_error(const sbdgb_ctx *ctx);
+/* Bytes of device memory currently held by the context's problems. */
+size_t sbdgb_ctx_bytes_in_use(const sbdgb_ctx *ctx);
+/* Number of kernels this context has launched since creation. */
+uint64_t sbdgb_ctx_launch_count(const sbdgb_ctx *ctx);
+
+/* Checks the size of the communicators the reference would pass
+ * (h_comm, b_comm, t_comm sizes; chemistry/tpb/helper.h:344-386).  Any size
+ * other than 1 returns SBDGB_E_UNSUPPORTED: this engine is one GPU per
+ * problem. */
+int sbdgb_check_comm_sizes(sbdgb_ctx *ctx, int h_size, int b_size, int t_size);
+
+/* ---- problem ------------------------------------------------------------ */
+
+/* Uploads strings and integrals into context-owned device memory (the
+ * reference copies them in MultTPBThrust::Init, chemistry/tpb/
+ * mult_thrust.h:100-275).  astr/bstr must be sorted, duplicate-free, with
+ * one popcount per list; norb <= 64. */
+int sbdgb_problem_create(sbdgb_ctx *ctx, int norb, const uint64_t *astr, size_t na, const uint64_t *bstr,
+                         size_t nb, const double *h1, const double *eri_packed, double ecore,
+                         sbdgb_problem **out);
+void sbdgb_problem_destroy(sbdgb_problem *p);
+/* Device memory the problem would hold once its tables and solver vectors
+ * exist (used for admission by HBM footprint). */
+int sbdgb_problem_footprint(int norb, size_t na, size_t nb, int max_nb, int nroots, int precision,
+                            size_t *bytes);
+
+/* Excitation tables: replaces MakeHelpers + RemakeHelpers at size 1
+ * (chemistry/tpb/helper.h:729-873, 935-1245; GenerateExcitation :185-342). */
+int sbdgb_build_tables(sbdgb_problem *p);
+/* spin 0 = alpha, 1 = beta. */
+int sbdgb_table_counts(const sbdgb_problem *p, int spin, uint64_t *n_singles, uint64_t *n_doubles);
+/* Copies one spin's tables out in the reference helper layout
+ * (TaskHelpers::*_flat, *Offset, *CrAn_flat; helper.h:48-65): offsets have
+ * n+1 entries, kets ascending per bra, CrAn = (cr, an) for singles and
+ * (cr0, cr1, an0, an1) for doubles as spin-orbital indices. */
+int sbdgb_export_tables(const sbdgb_problem *p, int spin, uint64_t *off_s, uint64_t *ket_s, int32_t *cran_s,
+                        uint64_t *off_d, uint64_t *ket_d, int32_t *cran_d);
+
+/* Diagonal hii (makeQChamDiagTerms, chemistry/tpb/qcham.h:289-340).  The
+ * problem keeps its own copy; hii_out may be a host pointer (copied) or NULL. */
+int sbdgb_diag_terms(sbdgb_problem *p, double *hii_out);
+
+/* sigma (sbd::mult, chemistry/tpb/mult.h:114-130; MultBase::run,
+ * chemistry/basic/mult.h:19-103).  Wk_dev, Wb_dev: N = na*nb doubles of
+ * device memory.  accumulate != 0 gives the reference's Wb += H*Wk,
+ * accumulate == 0 writes Wb = H*Wk.  stream: a cudaStream_t or NULL. */
+int sbdgb_sigma(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accumulate, void *stream);
+/* Mixed-precision sigma: FP32 vectors, FP32 products, FP64 accumulation of
+ * each element's sum, FP32 result. */
+int sbdgb_sigma_mixed(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, void *stream);
+/* Host-buffer form of sbd::mult: Wb += H*Wk with host vectors (copies
+ * inside).  hii is ignored when NULL (the problem's own diagonal is used). */
+int sbdgb_mult_host(sbdgb_problem *p, const double *hii, const double *Wk, double *Wb);
+
+/* ---- Davidson ----------------------------------------------------------- */
+
+typedef struct {
+  int max_it;        /* restart cycles (reference --iteration) */
+  int max_nb;        /* max subspace size (reference --block) */
+  double eps;        /* residual-norm tolerance (reference --tolerance) */
+  double max_time;   /* wall-clock cap in seconds (reference --max_time); <= 0: none */
+  int nroots;        /* lowest roots wanted (the reference solves 1) */
+  int init;          /* 0: unit vector on determinant 0 (reference init 0),
+                        1: unit vectors on the lowest diagonal entries,
+                        2: caller-supplied vectors in X */
+  int precision;     /* sbdgb_precision */
+  int refine_every;  /* MIXED: FP64 sigma and residual every k iterations */
+  int verbose;       /* print one line per iteration like the reference */
+} sbdgb_davidson_opts;
+
+typedef struct {
+  int iterations;    /* Davidson steps taken */
+  int sigma_calls;   /* sigma products (FP64 + mixed) */
+  int sigma_fp64;    /* of which FP64 */
+  int restarts;
+  int converged;     /* 1 if every root reached eps */
+  double seconds;    /* wall time of the solve */
+  double resid[16];  /* final residual norms per root */
+} sbdgb_report;
+
+void sbdgb_davidson_default_opts(sbdgb_davidson_opts *o);
+/* Davidson (chemistry/tpb/davidson.h:707-970, GPU form chemistry/basic/
+ * davidson_thrust.h:97-385).  E receives nroots energies (ascending).
+ * X (host, nroots*N, may be NULL) receives the normalized Ritz vectors and,
+ * with init == 2, supplies the starting vectors. */
+int sbdgb_davidson(sbdgb_problem *p, const sbdgb_davidson_opts *o, double *E, double *X, sbdgb_report *rep);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,339 @@
+// C ABI of the engine (include/sbdgb.h): context and problem lifetime, input
+// validation, HBM accounting, and the status/exception boundary.
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace sbdgb {
+
+void unpack_integrals(Problem &p, const double *eri_dev, cudaStream_t s);
+
+void *dev_alloc(Problem &p, size_t bytes) {
+  if (bytes == 0) bytes = 8;
+  Ctx *c = p.ctx;
+  if (c->budget && c->in_use + bytes > c->budget)
+    throw Error(SBDGB_E_NOMEM, "HBM budget exceeded (" + std::to_string(c->in_use + bytes) + " > " +
+                                   std::to_string(c->budget) + " bytes)");
+  void *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(SBDGB_E_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  p.allocs.push_back(d);
+  p.bytes += bytes;
+  c->in_use += bytes;
+  return d;
+}
+
+void *workspace(Problem &p, int slot, size_t bytes) {
+  if (bytes == 0) bytes = 8;
+  if (p.ws[slot] && p.ws_bytes[slot] >= bytes) return p.ws[slot];
+  if (p.ws[slot]) {
+    SBDGB_CUDA(cudaStreamSynchronize(p.ctx->stream));
+    cudaFree(p.ws[slot]);
+    p.bytes -= p.ws_bytes[slot];
+    p.ctx->in_use -= p.ws_bytes[slot];
+    p.ws[slot] = nullptr;
+    p.ws_bytes[slot] = 0;
+  }
+  Ctx *c = p.ctx;
+  if (c->budget && c->in_use + bytes > c->budget)
+    throw Error(SBDGB_E_NOMEM, "HBM budget exceeded by a solver workspace");
+  void *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(SBDGB_E_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  p.ws[slot] = d;
+  p.ws_bytes[slot] = bytes;
+  p.bytes += bytes;
+  c->in_use += bytes;
+  return d;
+}
+
+void dev_free_all(Problem &p) {
+  if (p.ctx && p.ctx->stream) cudaStreamSynchronize(p.ctx->stream);
+  for (void *d : p.allocs) cudaFree(d);
+  for (int i = 0; i < WS_COUNT; ++i)
+    if (p.ws[i]) cudaFree(p.ws[i]);
+  if (p.ctx) p.ctx->in_use -= std::min(p.ctx->in_use, p.bytes);
+  p.allocs.clear();
+  p.bytes = 0;
+}
+
+}  // namespace sbdgb
+
+struct sbdgb_ctx {
+  sbdgb::Ctx c;
+};
+struct sbdgb_problem {
+  sbdgb::Problem p;
+};
+
+using sbdgb::Error;
+
+namespace {
+
+template <typename F>
+int guarded(sbdgb::Ctx *c, F &&f) {
+  try {
+    if (c) SBDGB_CUDA(cudaSetDevice(c->device));
+    f();
+    if (c) c->last_error.clear();
+    return SBDGB_OK;
+  } catch (const Error &e) {
+    if (c) c->last_error = e.what();
+    return e.status;
+  } catch (const std::exception &e) {
+    if (c) c->last_error = e.what();
+    return SBDGB_E_INPUT;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int sbdgb_abi_version(void) { return SBDGB_ABI_VERSION; }
+
+int sbdgb_ctx_create(sbdgb_ctx **out, int device, size_t hbm_budget_bytes) {
+  if (!out) return SBDGB_E_INPUT;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return SBDGB_E_CUDA;
+  }
+  if (device < 0 || device >= n) return SBDGB_E_INPUT;
+  sbdgb_ctx *ctx = new sbdgb_ctx();
+  ctx->c.device = device;
+  ctx->c.budget = hbm_budget_bytes;
+  int rc = guarded(&ctx->c, [&] {
+    SBDGB_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
+  });
+  if (rc != SBDGB_OK) {
+    delete ctx;
+    return rc;
+  }
+  *out = ctx;
+  return SBDGB_OK;
+}
+
+void sbdgb_ctx_destroy(sbdgb_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->c.device);
+  if (ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
+  delete ctx;
+}
+
+const char *sbdgb_last_error(const sbdgb_ctx *ctx) { return ctx ? ctx->c.last_error.c_str() : "null context"; }
+
+size_t sbdgb_ctx_bytes_in_use(const sbdgb_ctx *ctx) { return ctx ? ctx->c.in_use : 0; }
+
+uint64_t sbdgb_ctx_launch_count(const sbdgb_ctx *ctx) { return ctx ? ctx->c.launches : 0; }
+
+int sbdgb_check_comm_sizes(sbdgb_ctx *ctx, int h_size, int b_size, int t_size) {
+  return guarded(ctx ? &ctx->c : nullptr, [&] {
+    SBDGB_REQUIRE(h_size == 1 && b_size == 1 && t_size == 1, SBDGB_E_UNSUPPORTED,
+                  "communicators of size > 1 are not supported: one GPU per problem");
+  });
+}
+
+int sbdgb_problem_footprint(int norb, size_t na, size_t nb, int max_nb, int nroots, int precision,
+                            size_t *bytes) {
+  if (!bytes || norb < 1 || norb > 64) return SBDGB_E_INPUT;
+  const size_t N = na * nb;
+  const size_t npair = (size_t)norb * (norb + 1) / 2;
+  const size_t vec = precision == SBDGB_MIXED ? 4 : 8;
+  size_t b = 0;
+  b += 8 * (na + nb) + 8 * npair * npair + 8 * npair * (na + nb);  // strings, (P|Q), Coulomb rows
+  b += 8 * N * 2;                                                   // hii + transpose scratch
+  b += (size_t)(2 * std::max(max_nb, 2 * nroots) + 3 * nroots) * N * vec;  // basis, sigma, Ritz, residuals
+  if (precision == SBDGB_MIXED) b += 8 * N * 3;                            // FP64 refinement vectors
+  // excitation tables: estimated from the string counts at up to norb^4/4 pairs per string is
+  // too loose to be useful; the tables are accounted exactly once built.
+  *bytes = b;
+  return SBDGB_OK;
+}
+
+int sbdgb_problem_create(sbdgb_ctx *ctx, int norb, const uint64_t *astr, size_t na, const uint64_t *bstr,
+                         size_t nb, const double *h1, const double *eri_packed, double ecore,
+                         sbdgb_problem **out) {
+  if (!ctx || !out) return SBDGB_E_INPUT;
+  *out = nullptr;
+  sbdgb_problem *pr = new sbdgb_problem();
+  sbdgb::Problem &p = pr->p;
+  p.ctx = &ctx->c;
+  int rc = guarded(&ctx->c, [&] {
+    std::lock_guard<std::mutex> lk(ctx->c.mu);
+    SBDGB_REQUIRE(norb >= 1 && norb <= 64, SBDGB_E_UNSUPPORTED, "norb must be in [1, 64]");
+    SBDGB_REQUIRE(na >= 1 && nb >= 1, SBDGB_E_INPUT, "empty string list");
+    SBDGB_REQUIRE(na < (1ull << 31) && nb < (1ull << 31), SBDGB_E_UNSUPPORTED, "too many strings");
+    SBDGB_REQUIRE(astr && bstr && h1 && eri_packed, SBDGB_E_INPUT, "null input pointer");
+    const uint64_t lim = norb == 64 ? ~0ull : ((1ull << norb) - 1ull);
+    auto check = [&](const uint64_t *s, size_t n, const char *name, int &nocc) {
+      nocc = __builtin_popcountll(s[0]);
+      for (size_t i = 0; i < n; ++i) {
+        SBDGB_REQUIRE((s[i] & ~lim) == 0, SBDGB_E_INPUT, std::string(name) + " string has bits beyond norb");
+        SBDGB_REQUIRE(__builtin_popcountll(s[i]) == nocc, SBDGB_E_INPUT,
+                      std::string(name) + " strings have different popcounts");
+        if (i) SBDGB_REQUIRE(s[i] > s[i - 1], SBDGB_E_INPUT, std::string(name) + " strings not sorted/unique");
+      }
+    };
+    check(astr, na, "alpha", p.nocc_a);
+    check(bstr, nb, "beta", p.nocc_b);
+    p.norb = norb;
+    p.npair = norb * (norb + 1) / 2;
+    p.na = (uint32_t)na;
+    p.nb = (uint32_t)nb;
+    p.N = (uint64_t)na * nb;
+    p.ecore = ecore;
+    p.h_astr.assign(astr, astr + na);
+    p.h_bstr.assign(bstr, bstr + nb);
+    cudaStream_t s = ctx->c.stream;
+    p.astr = (uint64_t *)sbdgb::dev_alloc(p, 8 * na);
+    p.bstr = (uint64_t *)sbdgb::dev_alloc(p, 8 * nb);
+    p.h1 = (double *)sbdgb::dev_alloc(p, 8 * (size_t)norb * norb);
+    p.Kp = (double *)sbdgb::dev_alloc(p, 8 * (size_t)p.npair * p.npair);
+    const size_t neri = (size_t)p.npair * (p.npair + 1) / 2;
+    double *eri = nullptr;
+    SBDGB_CUDA(cudaMalloc(&eri, 8 * neri));
+    SBDGB_CUDA(cudaMemcpyAsync(p.astr, astr, 8 * na, cudaMemcpyHostToDevice, s));
+    SBDGB_CUDA(cudaMemcpyAsync(p.bstr, bstr, 8 * nb, cudaMemcpyHostToDevice, s));
+    SBDGB_CUDA(cudaMemcpyAsync(p.h1, h1, 8 * (size_t)norb * norb, cudaMemcpyHostToDevice, s));
+    SBDGB_CUDA(cudaMemcpyAsync(eri, eri_packed, 8 * neri, cudaMemcpyHostToDevice, s));
+    sbdgb::unpack_integrals(p, eri, s);
+    SBDGB_CUDA(cudaStreamSynchronize(s));
+    cudaFree(eri);
+  });
+  if (rc != SBDGB_OK) {
+    sbdgb::dev_free_all(p);
+    delete pr;
+    return rc;
+  }
+  *out = pr;
+  return SBDGB_OK;
+}
+
+void sbdgb_problem_destroy(sbdgb_problem *pr) {
+  if (!pr) return;
+  cudaSetDevice(pr->p.ctx->device);
+  sbdgb::dev_free_all(pr->p);
+  delete pr;
+}
+
+int sbdgb_build_tables(sbdgb_problem *pr) {
+  if (!pr) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    SBDGB_REQUIRE(!pr->p.tables, SBDGB_E_STATE, "tables already built");
+    sbdgb::build_tables(pr->p, pr->p.ctx->stream);
+  });
+}
+
+int sbdgb_table_counts(const sbdgb_problem *pr, int spin, uint64_t *ns, uint64_t *nd) {
+  if (!pr || (spin != 0 && spin != 1)) return SBDGB_E_INPUT;
+  if (!pr->p.tables) return SBDGB_E_STATE;
+  const sbdgb::SpinTables &T = spin == 0 ? pr->p.A : pr->p.B;
+  if (ns) *ns = T.ns;
+  if (nd) *nd = T.nd;
+  return SBDGB_OK;
+}
+
+int sbdgb_export_tables(const sbdgb_problem *pr, int spin, uint64_t *off_s, uint64_t *ket_s, int32_t *cran_s,
+                        uint64_t *off_d, uint64_t *ket_d, int32_t *cran_d) {
+  if (!pr || (spin != 0 && spin != 1)) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    SBDGB_REQUIRE(pr->p.tables, SBDGB_E_STATE, "tables not built");
+    sbdgb::export_tables(pr->p, spin, off_s, ket_s, cran_s, off_d, ket_d, cran_d);
+  });
+}
+
+int sbdgb_diag_terms(sbdgb_problem *pr, double *hii_out) {
+  if (!pr) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    sbdgb::Problem &p = pr->p;
+    if (!p.tables) sbdgb::build_tables(p, p.ctx->stream);
+    if (!p.diag) sbdgb::build_diag(p, p.ctx->stream);
+    if (hii_out) {
+      SBDGB_CUDA(cudaMemcpyAsync(hii_out, p.hii, 8 * p.N, cudaMemcpyDefault, p.ctx->stream));
+      SBDGB_CUDA(cudaStreamSynchronize(p.ctx->stream));
+    }
+  });
+}
+
+int sbdgb_sigma(sbdgb_problem *pr, const double *Wk_dev, double *Wb_dev, int accumulate, void *stream) {
+  if (!pr || !Wk_dev || !Wb_dev) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    sbdgb::Problem &p = pr->p;
+    SBDGB_REQUIRE(p.tables && p.diag, SBDGB_E_STATE, "build tables and diagonal first");
+    cudaStream_t s = stream ? (cudaStream_t)stream : p.ctx->stream;
+    sbdgb::sigma_fp64(p, Wk_dev, Wb_dev, accumulate, s);
+  });
+}
+
+int sbdgb_sigma_mixed(sbdgb_problem *pr, const float *Wk_dev, float *Wb_dev, void *stream) {
+  if (!pr || !Wk_dev || !Wb_dev) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    sbdgb::Problem &p = pr->p;
+    SBDGB_REQUIRE(p.tables && p.diag, SBDGB_E_STATE, "build tables and diagonal first");
+    cudaStream_t s = stream ? (cudaStream_t)stream : p.ctx->stream;
+    sbdgb::sigma_mixed(p, Wk_dev, Wb_dev, s);
+  });
+}
+
+int sbdgb_mult_host(sbdgb_problem *pr, const double *hii, const double *Wk, double *Wb) {
+  if (!pr || !Wk || !Wb) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    sbdgb::Problem &p = pr->p;
+    cudaStream_t s = p.ctx->stream;
+    if (!p.tables) sbdgb::build_tables(p, s);
+    if (!p.diag) sbdgb::build_diag(p, s);
+    double *C = (double *)sbdgb::workspace(p, sbdgb::WS_C64, 8 * p.N);
+    double *S = (double *)sbdgb::workspace(p, sbdgb::WS_RES64, 8 * p.N);
+    double *saved = nullptr;
+    if (hii) {  // caller-supplied diagonal (the reference takes hii as an argument)
+      saved = p.hii;
+      p.hii = (double *)sbdgb::workspace(p, sbdgb::WS_DIAG2, 8 * p.N);
+      SBDGB_CUDA(cudaMemcpyAsync(p.hii, hii, 8 * p.N, cudaMemcpyHostToDevice, s));
+    }
+    SBDGB_CUDA(cudaMemcpyAsync(C, Wk, 8 * p.N, cudaMemcpyHostToDevice, s));
+    SBDGB_CUDA(cudaMemcpyAsync(S, Wb, 8 * p.N, cudaMemcpyHostToDevice, s));
+    try {
+      sbdgb::sigma_fp64(p, C, S, 1, s);
+    } catch (...) {
+      if (saved) p.hii = saved;
+      throw;
+    }
+    if (saved) p.hii = saved;
+    SBDGB_CUDA(cudaMemcpyAsync(Wb, S, 8 * p.N, cudaMemcpyDeviceToHost, s));
+    SBDGB_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+void sbdgb_davidson_default_opts(sbdgb_davidson_opts *o) {
+  if (!o) return;
+  o->max_it = 100;
+  o->max_nb = 20;
+  o->eps = 1e-8;
+  o->max_time = 0.0;
+  o->nroots = 1;
+  o->init = 0;
+  o->precision = SBDGB_FP64;
+  o->refine_every = 4;
+  o->verbose = 0;
+}
+
+int sbdgb_davidson(sbdgb_problem *pr, const sbdgb_davidson_opts *o, double *E, double *X, sbdgb_report *rep) {
+  if (!pr || !o || !E) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    sbdgb::Problem &p = pr->p;
+    if (!p.tables) sbdgb::build_tables(p, p.ctx->stream);
+    if (!p.diag) sbdgb::build_diag(p, p.ctx->stream);
+    sbdgb::davidson(p, *o, E, X, rep);
+  });
+}
+
+}  // extern "C"

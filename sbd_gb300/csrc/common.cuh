@@ -1,0 +1,174 @@
+// Shared definitions of the GB300 TPB engine (device data layout, launch
+// bookkeeping, error handling).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "sbdgb.h"
+
+namespace sbdgb {
+
+// ---- errors ----------------------------------------------------------------
+
+struct Error : std::runtime_error {
+  int status;
+  Error(int s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+#define SBDGB_CUDA(call)                                                                         \
+  do {                                                                                            \
+    cudaError_t _e = (call);                                                                      \
+    if (_e != cudaSuccess)                                                                        \
+      throw ::sbdgb::Error(SBDGB_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));     \
+  } while (0)
+
+#define SBDGB_REQUIRE(cond, status, msg)                      \
+  do {                                                        \
+    if (!(cond)) throw ::sbdgb::Error((status), (msg));       \
+  } while (0)
+
+// ---- bit helpers ------------------------------------------------------------
+
+// Orbitals [lo, hi) as a mask (0 <= lo <= hi <= 64).
+__host__ __device__ inline uint64_t range_mask(int lo, int hi) {
+  uint64_t h = (hi >= 64) ? ~0ull : ((1ull << hi) - 1ull);
+  uint64_t l = (lo >= 64) ? ~0ull : ((1ull << lo) - 1ull);
+  return (hi <= lo) ? 0ull : (h & ~l);
+}
+
+// The reference counts fermionic phases on the alpha/beta interleaved
+// determinant (alpha p -> spin orbital 2p, beta p -> 2p+1;
+// chemistry/basic/determinants.h:105-150): parity(start, end) is the parity of
+// the occupied spin orbitals strictly between start and end
+// (determinants.h:242-294; the start bit is excluded by its second flip).
+// For spin orbitals s < e that set splits into an alpha-orbital range and a
+// beta-orbital range, so the phase is popc(alpha & ma) + popc(beta & mb).
+__host__ __device__ inline void interval_masks(int s, int e, uint64_t &ma, uint64_t &mb) {
+  // alpha p with s < 2p < e ; beta p with s < 2p+1 < e
+  int a_lo = s / 2 + 1, a_hi = (e - 1) / 2 + 1;
+  int b_lo = (s + 1) / 2, b_hi = (e >= 2) ? (e - 2) / 2 + 1 : 0;
+  ma = range_mask(a_lo, a_hi);
+  mb = range_mask(b_lo, b_hi);
+}
+
+__host__ __device__ inline int pair_index(int i, int j) {
+  int a = i > j ? i : j, b = i > j ? j : i;
+  return a * (a + 1) / 2 + b;
+}
+
+// ---- device-side tables -------------------------------------------------------
+
+// Excitation lists of one spin, CSR over bra strings, structure of arrays.
+//  singles: code = cr | an << 8 | P << 16 (P = pair_index(cr, an)) | sgn << 31
+//           val  = same-spin part of the element without phase:
+//                  h(an,cr) + sum_{j in bra, same spin} [(an cr|j j) - (an j|j cr)]
+//           mask = opposite-spin orbitals that enter the phase
+//           sgn  = phase from the same-spin orbitals
+//  doubles: code = cr0 | cr1 << 6 | an0 << 12 | an1 << 18 (spatial)
+//           val  = same-spin phase * flip * [(a0 c0|a1 c1) - (a0 c1|a1 c0)]
+//           mask = opposite-spin orbitals that enter the phase
+struct SpinTables {
+  uint32_t n = 0;
+  uint64_t ns = 0, nd = 0;
+  uint32_t *off_s = nullptr, *off_d = nullptr;  // n+1
+  uint32_t *ket_s = nullptr, *ket_d = nullptr;
+  uint32_t *code_s = nullptr, *code_d = nullptr;
+  double *val_s = nullptr, *val_d = nullptr;
+  uint64_t *mask_s = nullptr, *mask_d = nullptr;
+};
+
+struct SigmaArgs {
+  const uint64_t *astr, *bstr;
+  uint32_t na, nb;
+  const double *hii;
+  const double *C;   // N, row-major [ia][ib]
+  const double *CT;  // N, transposed [ib][ia]
+  double *S;
+  int accumulate;
+  SpinTables A, B;
+  const double *Jb;  // [npair][nb]: sum_{q in beta(ib)} (P|qq)
+  const double *Ja;  // [npair][na]: sum_{q in alpha(ia)} (P|qq)
+  const double *Kp;  // [npair][npair] full (P|Q)
+  int npair;
+  int norb;
+};
+
+// ---- context / problem ----------------------------------------------------------
+
+struct Ctx;
+
+// Reusable device buffers of a problem (grown on demand, freed with it).
+enum WsSlot {
+  WS_V, WS_HV, WS_X, WS_HX, WS_T, WS_PARTIAL, WS_RED, WS_COEF,
+  WS_DIAG0, WS_DIAG1, WS_DIAG2,
+  WS_VF, WS_HVF, WS_CF, WS_SF, WS_RES64, WS_C64,
+  WS_COUNT
+};
+
+struct Problem {
+  Ctx *ctx = nullptr;
+  int norb = 0, npair = 0;
+  uint32_t na = 0, nb = 0;
+  uint64_t N = 0;
+  int nocc_a = 0, nocc_b = 0;
+  double ecore = 0.0;
+  // device
+  uint64_t *astr = nullptr, *bstr = nullptr;
+  double *h1 = nullptr;   // L*L
+  double *Kp = nullptr;   // npair*npair
+  double *Jdiag = nullptr;  // L*L (pp|qq)
+  double *Xdiag = nullptr;  // L*L (pq|qp)
+  SpinTables A, B;
+  double *Jb = nullptr, *Ja = nullptr;
+  double *hii = nullptr;
+  double *CT = nullptr;   // transpose scratch
+  float *CTf = nullptr;   // mixed transpose scratch
+  float *Kpf = nullptr, *Jbf = nullptr, *Jaf = nullptr;
+  float *val_sf[2] = {nullptr, nullptr}, *val_df[2] = {nullptr, nullptr};
+  void *ws[WS_COUNT] = {};
+  size_t ws_bytes[WS_COUNT] = {};
+  bool tables = false, diag = false, mixed_ready = false;
+  size_t bytes = 0;
+  std::vector<void *> allocs;
+  // host copies of strings
+  std::vector<uint64_t> h_astr, h_bstr;
+};
+
+struct Ctx {
+  int device = 0;
+  size_t budget = 0;
+  size_t in_use = 0;
+  uint64_t launches = 0;
+  std::string last_error;
+  std::mutex mu;
+  cudaStream_t stream = nullptr;
+};
+
+void *dev_alloc(Problem &p, size_t bytes);
+void *workspace(Problem &p, int slot, size_t bytes);
+void dev_free_all(Problem &p);
+
+// counted kernel launch helper
+inline void count_launch(Ctx *c, uint64_t n = 1) { c->launches += n; }
+
+// tables.cu
+void build_tables(Problem &p, cudaStream_t s);
+void export_tables(const Problem &p, int spin, uint64_t *off_s, uint64_t *ket_s, int32_t *cran_s,
+                   uint64_t *off_d, uint64_t *ket_d, int32_t *cran_d);
+// diag.cu
+void build_diag(Problem &p, cudaStream_t s);
+// sigma.cu
+void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s);
+void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s);
+void prepare_mixed(Problem &p, cudaStream_t s);
+// davidson.cu
+void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X, sbdgb_report *rep);
+
+}  // namespace sbdgb

@@ -1,0 +1,245 @@
+"""Python front end of the CUDA engine, bound through the C ABI (include/sbdgb.h).
+
+There is no CPU fallback: if libsbdgb.so is missing or no GPU is visible the
+constructors raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libsbdgb.so")
+
+SBDGB_OK = 0
+STATUS = {0: "OK", 1: "E_INPUT", 2: "E_UNSUPPORTED", 3: "E_CUDA", 4: "E_NOMEM", 5: "E_STATE", 6: "E_TIMEOUT"}
+FP64, MIXED = 0, 1
+
+SYMBOLS = [
+    "sbdgb_abi_version", "sbdgb_ctx_create", "sbdgb_ctx_destroy", "sbdgb_last_error", "sbdgb_ctx_bytes_in_use",
+    "sbdgb_ctx_launch_count", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
+    "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
+    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
+    "sbdgb_davidson",
+]
+
+
+class SbdgbError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class DavidsonOpts(C.Structure):
+    _fields_ = [("max_it", C.c_int), ("max_nb", C.c_int), ("eps", C.c_double), ("max_time", C.c_double),
+                ("nroots", C.c_int), ("init", C.c_int), ("precision", C.c_int), ("refine_every", C.c_int),
+                ("verbose", C.c_int)]
+
+
+class Report(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("sigma_calls", C.c_int), ("sigma_fp64", C.c_int), ("restarts", C.c_int),
+                ("converged", C.c_int), ("seconds", C.c_double), ("resid", C.c_double * 16)]
+
+    def as_dict(self, nroots: int) -> dict:
+        return {"iterations": self.iterations, "sigma_calls": self.sigma_calls, "sigma_fp64": self.sigma_fp64,
+                "restarts": self.restarts, "converged": bool(self.converged), "seconds": self.seconds,
+                "resid": [self.resid[i] for i in range(min(nroots, 16))]}
+
+
+_lib = None
+_u64p = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+
+
+def load(path: str = LIB_PATH):
+    """Loads libsbdgb.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} not found: build it with `python -m sbd_gb300.build` "
+                          "(the engine has no CPU fallback)")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.sbdgb_abi_version.restype = C.c_int
+    L.sbdgb_ctx_create.argtypes = [C.POINTER(vp), C.c_int, C.c_size_t]
+    L.sbdgb_ctx_destroy.argtypes = [vp]
+    L.sbdgb_ctx_destroy.restype = None
+    L.sbdgb_last_error.argtypes = [vp]
+    L.sbdgb_last_error.restype = C.c_char_p
+    L.sbdgb_ctx_bytes_in_use.argtypes = [vp]
+    L.sbdgb_ctx_bytes_in_use.restype = C.c_size_t
+    L.sbdgb_ctx_launch_count.argtypes = [vp]
+    L.sbdgb_ctx_launch_count.restype = C.c_uint64
+    L.sbdgb_check_comm_sizes.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    L.sbdgb_problem_create.argtypes = [vp, C.c_int, _u64p, C.c_size_t, _u64p, C.c_size_t, _f64p, _f64p,
+                                       C.c_double, C.POINTER(vp)]
+    L.sbdgb_problem_destroy.argtypes = [vp]
+    L.sbdgb_problem_destroy.restype = None
+    L.sbdgb_problem_footprint.argtypes = [C.c_int, C.c_size_t, C.c_size_t, C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(C.c_size_t)]
+    L.sbdgb_build_tables.argtypes = [vp]
+    L.sbdgb_table_counts.argtypes = [vp, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    L.sbdgb_export_tables.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, vp]
+    L.sbdgb_diag_terms.argtypes = [vp, vp]
+    L.sbdgb_sigma.argtypes = [vp, vp, vp, C.c_int, vp]
+    L.sbdgb_sigma_mixed.argtypes = [vp, vp, vp, vp]
+    L.sbdgb_mult_host.argtypes = [vp, vp, _f64p, _f64p]
+    L.sbdgb_davidson_default_opts.argtypes = [C.POINTER(DavidsonOpts)]
+    L.sbdgb_davidson_default_opts.restype = None
+    L.sbdgb_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _f64p, vp, C.POINTER(Report)]
+    _lib = L
+    return L
+
+
+class Engine:
+    """One device context (sbdgb_ctx)."""
+
+    def __init__(self, device: int = 0, hbm_budget: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        rc = self.lib.sbdgb_ctx_create(C.byref(h), device, hbm_budget)
+        if rc != SBDGB_OK:
+            raise SbdgbError(rc, f"cannot create a context on device {device}")
+        self.h = h
+        self.device = device
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sbdgb_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def check(self, rc: int):
+        if rc != SBDGB_OK:
+            raise SbdgbError(rc, self.lib.sbdgb_last_error(self.h).decode())
+
+    @property
+    def bytes_in_use(self) -> int:
+        return int(self.lib.sbdgb_ctx_bytes_in_use(self.h))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.sbdgb_ctx_launch_count(self.h))
+
+    def check_comm_sizes(self, h: int, b: int, t: int):
+        self.check(self.lib.sbdgb_check_comm_sizes(self.h, h, b, t))
+
+
+def footprint(norb: int, na: int, nb: int, max_nb: int, nroots: int, precision: int = FP64) -> int:
+    out = C.c_size_t(0)
+    rc = load().sbdgb_problem_footprint(norb, na, nb, max_nb, nroots, precision, C.byref(out))
+    if rc != SBDGB_OK:
+        raise SbdgbError(rc, "footprint")
+    return int(out.value)
+
+
+@dataclass
+class DavidsonResult:
+    energies: np.ndarray
+    vectors: np.ndarray | None
+    report: dict
+
+
+class TPBProblem:
+    """One uploaded problem (sbdgb_problem)."""
+
+    def __init__(self, engine: Engine, norb: int, astr, bstr, h1, eri, ecore: float = 0.0):
+        self.engine = engine
+        self.lib = engine.lib
+        self.norb = int(norb)
+        self.astr = np.ascontiguousarray(astr, dtype=np.uint64)
+        self.bstr = np.ascontiguousarray(bstr, dtype=np.uint64)
+        self.na, self.nb = int(self.astr.size), int(self.bstr.size)
+        self.N = self.na * self.nb
+        h = C.c_void_p()
+        h1 = np.ascontiguousarray(h1, dtype=np.float64).ravel()
+        eri = np.ascontiguousarray(eri, dtype=np.float64)
+        rc = self.lib.sbdgb_problem_create(engine.h, self.norb, self.astr, self.na, self.bstr, self.nb, h1, eri,
+                                           float(ecore), C.byref(h))
+        engine.check(rc)
+        self.h = h
+
+    @classmethod
+    def from_problem(cls, engine: Engine, p) -> "TPBProblem":
+        return cls(engine, p.norb, p.astr, p.bstr, p.ints.h1, p.ints.eri, p.ints.ecore)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.sbdgb_problem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def build_tables(self):
+        self.engine.check(self.lib.sbdgb_build_tables(self.h))
+
+    def table_counts(self, spin: int) -> tuple[int, int]:
+        ns, nd = C.c_uint64(0), C.c_uint64(0)
+        self.engine.check(self.lib.sbdgb_table_counts(self.h, spin, C.byref(ns), C.byref(nd)))
+        return int(ns.value), int(nd.value)
+
+    def export_tables(self, spin: int) -> dict:
+        """Tables of one spin in the reference helper layout (offsets, kets, CrAn)."""
+        ns, nd = self.table_counts(spin)
+        n = self.na if spin == 0 else self.nb
+        off_s = np.zeros(n + 1, dtype=np.uint64)
+        off_d = np.zeros(n + 1, dtype=np.uint64)
+        ket_s = np.zeros(max(ns, 1), dtype=np.uint64)
+        ket_d = np.zeros(max(nd, 1), dtype=np.uint64)
+        cran_s = np.zeros(max(2 * ns, 1), dtype=np.int32)
+        cran_d = np.zeros(max(4 * nd, 1), dtype=np.int32)
+        self.engine.check(self.lib.sbdgb_export_tables(self.h, spin, off_s.ctypes.data, ket_s.ctypes.data,
+                                                       cran_s.ctypes.data, off_d.ctypes.data, ket_d.ctypes.data,
+                                                       cran_d.ctypes.data))
+        return {"off_s": off_s, "ket_s": ket_s[:ns], "cran_s": cran_s[:2 * ns],
+                "off_d": off_d, "ket_d": ket_d[:nd], "cran_d": cran_d[:4 * nd]}
+
+    def diag_terms(self) -> np.ndarray:
+        out = np.zeros(self.N)
+        self.engine.check(self.lib.sbdgb_diag_terms(self.h, out.ctypes.data))
+        return out
+
+    def mult(self, Wk: np.ndarray, Wb: np.ndarray | None = None, hii: np.ndarray | None = None) -> np.ndarray:
+        """Reference semantics: Wb += H Wk (host vectors)."""
+        wk = np.ascontiguousarray(Wk, dtype=np.float64).ravel()
+        wb = np.zeros(self.N) if Wb is None else Wb
+        if wb.dtype != np.float64 or not wb.flags["C_CONTIGUOUS"]:
+            raise ValueError("Wb must be a contiguous float64 array")
+        hp = None
+        if hii is not None:
+            hii = np.ascontiguousarray(hii, dtype=np.float64)
+            hp = hii.ctypes.data
+        self.engine.check(self.lib.sbdgb_mult_host(self.h, hp, wk, wb))
+        return wb
+
+    def sigma(self, C_in: np.ndarray) -> np.ndarray:
+        return self.mult(C_in)
+
+    def sigma_device(self, c_ptr: int, s_ptr: int, accumulate: bool = False, stream: int = 0):
+        self.engine.check(self.lib.sbdgb_sigma(self.h, c_ptr, s_ptr, int(accumulate), stream or None))
+
+    def sigma_mixed_device(self, c_ptr: int, s_ptr: int, stream: int = 0):
+        self.engine.check(self.lib.sbdgb_sigma_mixed(self.h, c_ptr, s_ptr, stream or None))
+
+    def davidson(self, nroots: int = 1, max_nb: int = 20, eps: float = 1e-8, max_it: int = 100,
+                 init: int = 0, precision: int = FP64, refine_every: int = 4, max_time: float = 0.0,
+                 want_vectors: bool = True, X0: np.ndarray | None = None, verbose: bool = False) -> DavidsonResult:
+        o = DavidsonOpts()
+        self.lib.sbdgb_davidson_default_opts(C.byref(o))
+        o.nroots, o.max_nb, o.eps, o.max_it = nroots, max_nb, eps, max_it
+        o.init, o.precision, o.refine_every, o.max_time, o.verbose = init, precision, refine_every, max_time, int(verbose)
+        E = np.zeros(nroots)
+        X = None
+        if want_vectors or X0 is not None:
+            X = np.zeros((nroots, self.N)) if X0 is None else np.ascontiguousarray(X0, dtype=np.float64).copy()
+        rep = Report()
+        self.engine.check(self.lib.sbdgb_davidson(self.h, C.byref(o), E, X.ctypes.data if X is not None else None,
+                                                  C.byref(rep)))
+        return DavidsonResult(E, X, rep.as_dict(nroots))

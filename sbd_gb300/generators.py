@@ -46,25 +46,51 @@ class Problem:
         return int(self.astr.size) * int(self.bstr.size)
 
 
-def make_integrals(norb: int, nelec: int, rng: np.random.Generator, nchol: int = 32) -> Integrals:
+def eri_from_factors(Bp: np.ndarray) -> np.ndarray:
+    """8-fold packed ERI from pair factors: (P|Q) = sum_l Bp[l, P] * Bp[l, Q].
+
+    Summed element-wise in a fixed order (no BLAS), so the result is the same
+    bit pattern on every platform.
+    """
+    Bp = np.asarray(Bp, dtype=np.float64)
+    npair = Bp.shape[1]
+    P, Q = np.tril_indices(npair)
+    eri = np.zeros(P.size)
+    for l in range(Bp.shape[0]):
+        eri += Bp[l, P] * Bp[l, Q]
+    out = np.empty_like(eri)
+    out[P * (P + 1) // 2 + Q] = eri
+    return out
+
+
+def make_factors(norb: int, rng: np.random.Generator, nchol: int = 32) -> np.ndarray:
+    """Bp[l, P] = B^l_ij over packed pairs P = (i >= j); B^l symmetric, N(0, 0.1) + 0.3 I."""
     L = norb
-    h1 = rng.normal(0.0, 0.05, size=(L, L))
-    h1 = np.triu(h1, 1)
-    h1 = h1 + h1.T
-    h1[np.diag_indices(L)] = np.linspace(-2.0, 1.0, L)
     ii, jj = np.tril_indices(L)  # packed pair order (i >= j)
-    npair = ii.size
-    Bp = np.empty((nchol, npair))
+    Bp = np.empty((nchol, ii.size))
     for c in range(nchol):
         B = rng.normal(0.0, 0.1, size=(L, L))
         B = np.triu(B) + np.triu(B, 1).T
         B[np.diag_indices(L)] += 0.3
         Bp[c] = B[ii, jj]
-    G = Bp.T @ Bp  # (ij|kl) over packed pairs
-    P, Q = np.tril_indices(npair)
-    eri = np.empty(npair * (npair + 1) // 2)
-    eri[P * (P + 1) // 2 + Q] = G[P, Q]
-    return Integrals(norb=L, nelec=nelec, ecore=0.0, h1=h1, eri=eri)
+    return Bp
+
+
+def make_h1(norb: int, rng: np.random.Generator) -> np.ndarray:
+    L = norb
+    h1 = rng.normal(0.0, 0.05, size=(L, L))
+    h1 = np.triu(h1, 1)
+    h1 = h1 + h1.T
+    h1[np.diag_indices(L)] = np.linspace(-2.0, 1.0, L)
+    return h1
+
+
+def make_integrals(norb: int, nelec: int, rng: np.random.Generator, nchol: int = 32) -> Integrals:
+    h1 = make_h1(norb, rng)
+    Bp = make_factors(norb, rng, nchol)
+    ints = Integrals(norb=norb, nelec=nelec, ecore=0.0, h1=h1, eri=eri_from_factors(Bp))
+    ints.factors = Bp
+    return ints
 
 
 def draw_strings(norb: int, nocc: int, count: int, rng: np.random.Generator) -> np.ndarray:

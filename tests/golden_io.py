@@ -1,0 +1,47 @@
+"""Loading of the golden fixtures produced by tests/golden/make_golden.py."""
+from __future__ import annotations
+
+import glob
+import os
+
+import numpy as np
+
+from sbd_gb300.generators import eri_from_factors
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names() -> list[str]:
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+
+
+class Case:
+    def __init__(self, name: str):
+        d = np.load(os.path.join(GOLDEN, name + ".npz"))
+        self.name = name
+        self.d = d
+        self.norb = int(d["norb"])
+        self.ecore = float(d["ecore"])
+        self.h1 = d["h1"]
+        self.eri = eri_from_factors(d["factors"])
+        self.astr = d["astr"].astype(np.uint64)
+        self.bstr = d["bstr"].astype(np.uint64)
+        self.C = d["C"]
+        self.hii = d["hii"]
+        self.sigma = d["sigma"]
+        self.energy = float(d["energy"])
+        self.lowest = d["lowest"]
+        self.irreducible = bool(d["irreducible"])
+
+    def tables(self, spin: str) -> dict:
+        t = "a" if spin in ("a", 0, "alpha") else "b"
+        return {k: self.d[f"{t}_{k}"] for k in ("off_s", "ket_s", "cran_s", "off_d", "ket_d", "cran_d")}
+
+
+def load(name: str) -> Case:
+    return Case(name)
+
+
+def max_rel(x: np.ndarray, ref: np.ndarray) -> float:
+    den = max(float(np.abs(ref).max()), 1e-300)
+    return float(np.abs(np.asarray(x) - np.asarray(ref)).max()) / den

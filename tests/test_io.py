@@ -1,0 +1,87 @@
+"""FCIDUMP/string formats and generators (CPU only)."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from sbd_gb300 import fcidump, strings
+from sbd_gb300.generators import config0, draw_strings, make_problem
+
+REF = "/root/reference"
+
+
+def test_string_round_trip():
+    for v, L in ((0b1011, 6), (1 << 63 | 5, 64), (0, 3)):
+        s = strings.make_string(v, L)
+        assert len(s) == L
+        assert strings.from_string(s, L) == v
+    assert strings.make_string(0b1, 4) == "0001"  # orbital 0 is the rightmost character
+
+
+def test_sort_order_is_numeric():
+    rng = np.random.default_rng(0)
+    v = rng.integers(0, 1 << 40, size=100).astype(np.uint64)
+    v = np.concatenate([v, v[:10]])
+    s = strings.sort_unique(v)
+    assert np.all(np.diff(s.astype(np.float64)) > 0)
+    # word layout of the reference sorts from the last word: same order
+    w = strings.to_words(s, 40, 20)
+    keys = [tuple(row[::-1]) for row in w]
+    assert keys == sorted(keys)
+    assert np.array_equal(strings.from_words(w, 20), s)
+
+
+def test_fcidump_round_trip(tmp_path):
+    p = make_problem(7, 2, 2, 10, seed=3)
+    path = tmp_path / "f.txt"
+    fcidump.write_fcidump(str(path), p.ints)
+    back = fcidump.read_integrals(str(path))
+    assert back.norb == 7
+    assert np.array_equal(back.h1, p.ints.h1)
+    assert np.array_equal(back.eri, p.ints.eri)
+    assert back.ecore == p.ints.ecore
+
+
+def test_fcidump_last_write_wins_and_symmetry(tmp_path):
+    path = tmp_path / "f.txt"
+    path.write_text(" &FCI NORB=2,NELEC=2,MS2=0,\n &END\n"
+                    "0.5 1 1 1 1\n0.7 1 1 1 1\n0.3 2 1 1 1\n-1.0 1 2 0 0\n-2.0 2 1 0 0\n1.5 0 0 0 0\n")
+    ints = fcidump.read_integrals(str(path))
+    assert ints.eri[fcidump.eri_index(0, 0, 0, 0)] == 0.7
+    assert ints.eri[fcidump.eri_index(0, 0, 1, 0)] == 0.3
+    assert ints.eri[fcidump.eri_index(1, 0, 0, 0)] == 0.3
+    assert ints.h1[0, 1] == -2.0 and ints.h1[1, 0] == -2.0
+    assert ints.ecore == 1.5
+
+
+def test_fcidump_rejects_bad_one_body(tmp_path):
+    path = tmp_path / "f.txt"
+    path.write_text(" &FCI NORB=2,NELEC=2,MS2=0,\n &END\n0.5 1 0 0 0\n")
+    with pytest.raises(ValueError):
+        fcidump.read_integrals(str(path))
+
+
+def test_generators_shapes_and_determinism():
+    p = config0()
+    assert p.norb == 16 and p.astr.size == 800 and p.ndet == 640000
+    assert np.array_equal(p.astr, p.bstr)
+    assert np.all(strings.popcounts(p.astr) == 5)
+    q = config0()
+    assert np.array_equal(p.astr, q.astr) and np.array_equal(p.ints.eri, q.ints.eri)
+    L = 16
+    assert np.allclose(np.diag(p.ints.h1), np.linspace(-2.0, 1.0, L))
+    assert np.allclose(p.ints.h1, p.ints.h1.T)
+    s = draw_strings(12, 4, 495, np.random.default_rng(1))
+    assert s.size == 495 and np.unique(s).size == 495
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "data", "h2o")), reason="reference data not present")
+def test_oracle_reproduces_published_h2o_energy():
+    """H2O cc-pVDZ, 275 alpha strings: -76.23594663 Ha (data/h2o/README.md:6)."""
+    from oracle.oracle import Oracle
+    ints = fcidump.read_integrals(os.path.join(REF, "data/h2o/fcidump.txt"))
+    a = strings.load_strings(os.path.join(REF, "data/h2o/h2o-1em3-alpha.txt"), ints.norb)
+    o = Oracle(ints.norb, ints.h1, ints.eri, ints.ecore, a, a)
+    E, W, ns, r = o.davidson(max_it=20, max_nb=10, eps=1e-8)
+    assert abs(o.energy(W) - (-76.23594663)) < 5e-9

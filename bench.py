@@ -1,0 +1,345 @@
+"""Benchmark: Davidson solves/s on the 36M-determinant configuration, one GB300.
+
+Workload (the configuration the metric is quoted on): norb 36, 12+12
+electrons, 6000 alpha x 6000 beta strings drawn independently (N = 36,000,000
+determinants, 288 MB per FP64 vector), 2 roots, subspace 24, residual
+tolerance 1e-8, plain FP64.  One step = one full Davidson solve (tables and
+diagonal resident, starting from the lowest diagonal entries).
+
+  value : solves/s with the problem resident in HBM (device-timed, CUDA events
+          on the solver stream, max over ranks)
+  e2e   : solves/s through the C ABI with host buffers: upload strings and
+          integrals, build tables and diagonal, solve, copy both Ritz vectors
+          back -- every step
+  roofline : the sigma operator (transpose + alpha sweep + beta sweep), whose
+          per-product device time is recorded with CUDA events on its launch
+          stream during the timed region; algorithmic bytes per product are
+          24*N + 8*nnz_off (read C and hii, write sigma, one 8-byte C read per
+          off-diagonal element)
+  cpu_baseline : the CPU oracle port of the reference's TRADMODE sigma (OpenMP,
+          all host cores) timed on a bounded sample of alpha rows and scaled to
+          the solve's sigma count
+
+Multi-GPU: each rank solves its own replica (the path does not shard across
+GPUs in this build): scaling "weak", value = total solves / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Davidson solves/s at |ΔE|≤1e-6 Ha vs plain FP64 GPU; p50/p99 latency; HBM GB/s"
+UNIT = "solves/s"
+WORKLOAD = ("config1: norb 36, 12+12 electrons, 6000x6000 strings (N=36,000,000), 2 roots, "
+            "subspace 24, tol 1e-8, plain FP64")
+NROOTS, MAX_NB, EPS = 2, 24, 1e-8
+
+
+def peaks() -> tuple[float, str]:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms during the timed region."""
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits"], capture_output=True, text=True,
+                                         timeout=5).stdout.strip()
+                    if out:
+                        self.samples.append([x.strip() for x in out.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self) -> dict:
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        sm = []
+        mx = None
+        reasons = set()
+        for s in self.samples:
+            try:
+                sm.append(float(s[0]))
+                mx = float(s[1])
+            except ValueError:
+                continue
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"),
+                               s[3:7]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if os.environ.get("SBDGB_BENCH_GLOO") is None else "gloo")
+        return dist, dist.get_rank(), ws
+    return None, 0, 1
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, x: float) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_problem():
+    from sbd_gb300.generators import config1
+    return config1()
+
+
+def cpu_sample(prob, rows: int, nsigma: float, threads: int) -> dict:
+    """Times the oracle port's sigma on `rows` alpha rows and scales to a solve."""
+    from oracle.oracle import Oracle
+    os.environ["OMP_NUM_THREADS"] = str(threads)
+    o = Oracle.from_problem(prob)
+    r0, r1 = 0, rows
+    C = np.random.default_rng(5).uniform(-1.0, 1.0, prob.ndet)
+    hii = o.hii(rows=(r0, r1))
+    t = time.perf_counter()
+    o.mult(C, rows=(r0, r1), hii=hii)
+    dt = time.perf_counter() - t
+    t_sigma = dt * prob.astr.size / rows
+    solve = t_sigma * nsigma
+    return {"value": 1.0 / solve, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"oracle port (restated reference TRADMODE mult, OpenMP {threads} threads) on alpha rows "
+                       f"[{r0},{r1}) of {prob.astr.size}: {dt:.2f} s -> {t_sigma:.1f} s per sigma x "
+                       f"{nsigma:.0f} sigma products per solve (the GPU solve's count); vector algebra not counted"),
+            "sigma_seconds_est": t_sigma}
+
+
+def run_reference(args):
+    """--impl reference: the reference's CPU algorithm (oracle port) on the host cores."""
+    dist, rank, ws = dist_init()
+    if rank != 0:
+        return 0
+    import oracle.oracle as orc
+    orc.build()
+    threads = os.cpu_count() or 1
+    prob = make_problem()
+    nsigma = float(os.environ.get("SBDGB_REF_NSIGMA", "40"))
+    rows = int(os.environ.get("SBDGB_REF_ROWS", "6"))
+    cpu_sample(prob, 1, nsigma, threads)  # warm the tables and caches
+    vals = []
+    t0 = time.perf_counter()
+    for step in range(args.warmup + args.steps):
+        s = cpu_sample(prob, rows, nsigma, threads)
+        if step >= args.warmup:
+            vals.append(s["value"])
+    wall = time.perf_counter() - t0
+    value = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "inputs": "host memory"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": s["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    dist, rank, ws = dist_init()
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    from sbd_gb300 import build as b
+    b.build()
+    from sbd_gb300.engine import Engine, TPBProblem
+    prob = make_problem()
+    eng = Engine(local)
+    p = TPBProblem.from_problem(eng, prob)
+    p.build_tables()
+    p.diag_terms()
+    (sa, da), (sb, db) = p.table_counts(0), p.table_counts(1)
+    N = prob.ndet
+    na, nb = prob.astr.size, prob.bstr.size
+    nnz_off = nb * (sa + da) + na * (sb + db) + sa * sb
+    bytes_sigma = 24.0 * N + 8.0 * nnz_off
+    kw = dict(nroots=NROOTS, max_nb=MAX_NB, eps=EPS, init=1, want_vectors=False)
+
+    # warm-up solves (untimed)
+    for _ in range(args.warmup):
+        r = p.davidson(**kw)
+    torch.cuda.synchronize()
+    energies = r.energies.copy()
+
+    # timed region: K resident solves
+    stream = torch.cuda.Stream()
+    eng.set_stream(stream.cuda_stream)
+    clocks = ClockSampler(local)
+    clocks.start()
+    eng.enable_timing(True)
+    eng.sigma_timing()
+    launches0 = eng.launches
+    barrier(dist)
+    torch.cuda.synchronize()
+    lat = []
+    nsig = []
+    t0 = time.perf_counter()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    ev[0].record(stream)
+    for i in range(args.steps):
+        r = p.davidson(**kw)
+        ev[i + 1].record(stream)
+        nsig.append(r.report["sigma_calls"])
+    torch.cuda.synchronize()
+    barrier(dist)
+    wall = time.perf_counter() - t0
+    lat = [ev[i].elapsed_time(ev[i + 1]) * 1e-3 for i in range(args.steps)]
+    launches = eng.launches - launches0
+    ncalls, sigma_ms = eng.sigma_timing()
+    eng.enable_timing(False)
+    clk = clocks.stop()
+    # device time of the K solves (CUDA events on the solver stream), max over ranks
+    t_rank = ev[0].elapsed_time(ev[-1]) * 1e-3
+    t_max = max_over_ranks(dist, t_rank)
+    value = ws * args.steps / t_max
+    sigma_ms_per = sigma_ms / max(ncalls, 1)
+    achieved = bytes_sigma / (sigma_ms_per * 1e-3) / 1e9
+    peak, peak_kind = peaks()
+
+    # mixed-precision form on the same problem (reported beside the FP64 headline)
+    mixed = None
+    if not args.no_mixed:
+        from sbd_gb300.engine import MIXED
+        mlat, mE = [], None
+        for i in range(1 + args.mixed_steps):
+            rm = p.davidson(precision=MIXED, refine_every=4, **kw)
+            if i > 0:
+                mlat.append(rm.report["seconds"])
+            mE = rm.energies
+        mixed = {"solves_per_s": len(mlat) / max(sum(mlat), 1e-30),
+                 "max_abs_dE_vs_fp64": float(np.max(np.abs(mE - energies))),
+                 "converged": rm.report["converged"], "sigma_products_per_solve": rm.report["sigma_calls"],
+                 "fp64_sigma_products_per_solve": rm.report["sigma_fp64"],
+                 "speedup_vs_fp64": (len(mlat) / max(sum(mlat), 1e-30)) / (args.steps / max(t_rank, 1e-30))}
+
+    # end to end through the C ABI with host buffers
+    e2e_lat = []
+    h2d = prob.astr.nbytes + prob.bstr.nbytes + prob.ints.h1.nbytes + prob.ints.eri.nbytes
+    d2h = NROOTS * N * 8 + NROOTS * 8
+    p.close()
+    for _ in range(max(1, args.e2e_steps)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        q = TPBProblem.from_problem(eng, prob)
+        rr = q.davidson(nroots=NROOTS, max_nb=MAX_NB, eps=EPS, init=1, want_vectors=True)
+        q.close()
+        e2e_lat.append(time.perf_counter() - t)
+    e2e_t = max_over_ranks(dist, float(np.sum(e2e_lat)))
+    e2e_value = ws * len(e2e_lat) / e2e_t
+
+    traffic = None
+    prof_path = os.path.join(ROOT, "profiles", "sigma_traffic.json")
+    if os.path.exists(prof_path):
+        try:
+            with open(prof_path) as f:
+                traffic = float(json.load(f)["bytes_per_sigma_config1"])
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            cpu = cpu_sample(prob, args.cpu_rows, float(np.mean(nsig)), os.cpu_count() or 1)
+            cpu.pop("sigma_seconds_est", None)
+        except Exception as e:  # the baseline is reported, not required
+            cpu = {"error": str(e)}
+
+    if rank == 0:
+        lat_sorted = sorted(lat)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "parallelism": f"replicas x{ws}",
+                       "l2": "inputs larger than L2 (288 MB per vector, 13.8 GB subspace)",
+                       "nnz_offdiag": int(nnz_off), "nnz_per_row": nnz_off / N},
+            "energies": [float(x) for x in energies],
+            "latency_s": {"p50": float(np.percentile(lat_sorted, 50)), "p99": float(np.percentile(lat_sorted, 99))},
+            "sigma_products_per_solve": float(np.mean(nsig)),
+            "sigma_ms": sigma_ms_per,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "sigma operator (k_transpose + k_sigma_alpha + k_sigma_beta)",
+                         "algorithmic_bytes": bytes_sigma, "peak_kind": f"{peak_kind} hbm_gbs"},
+            "mixed_precision": mixed,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "clocks": clk,
+            "wall_s": wall,
+        }
+        print(json.dumps(line))
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-rows", type=int, default=6)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--mixed-steps", type=int, default=2)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -67,6 +67,17 @@ size_t sbdgb_ctx_bytes_in_use(const sbdgb_ctx *ctx);
 /* Number of kernels this context has launched since creation. */
 uint64_t sbdgb_ctx_launch_count(const sbdgb_ctx *ctx);
 
+/* Runs every later call of this context on `stream` (a cudaStream_t the
+ * caller keeps alive); NULL returns to the context's own stream. */
+int sbdgb_ctx_set_stream(sbdgb_ctx *ctx, void *stream);
+
+/* Sigma timing: when enabled, every sigma product records a pair of CUDA
+ * events on the stream it is launched on; sbdgb_ctx_sigma_timing waits for
+ * them and returns the number of products and their summed device time, then
+ * clears the record.  Off by default. */
+int sbdgb_ctx_enable_timing(sbdgb_ctx *ctx, int on);
+int sbdgb_ctx_sigma_timing(sbdgb_ctx *ctx, uint64_t *calls, double *total_ms);
+
 /* Checks the size of the communicators the reference would pass
  * (h_comm, b_comm, t_comm sizes; chemistry/tpb/helper.h:344-386).  Any size
  * other than 1 returns SBDGB_E_UNSUPPORTED: this engine is one GPU per

@@ -1,0 +1,357 @@
+// sbdgb/tpb.hpp -- header-only C++ mirror of the reference's TPB entry points
+// over the engine's C ABI (sbdgb.h).  A program that calls
+//   sbd::tpb::generate_sbd_data / sbd::tpb::diag / sbd::LoadFCIDump /
+//   sbd::LoadAlphaDets / sbd::makeQChamDiagTerms / sbd::mult / sbd::Davidson
+// switches to the GB300 engine by calling the same names in namespace sbdgb.
+//
+// Reference interfaces mirrored (paths inside the reference project):
+//   SBD options + argv parsing ....... chemistry/tpb/sbdiag.h:24-134
+//   diag ............................. chemistry/tpb/sbdiag.h:151-526
+//   FCIDump / LoadFCIDump ............ framework/fcidump.h:20-95
+//   SetupIntegrals ................... chemistry/basic/makeintegrals.h:123-174
+//   LoadAlphaDets / sort_bitarray .... chemistry/basic/makedeterminants.h:167-191,
+//                                      framework/bit_manipulation.h:386-439
+//   makeQChamDiagTerms ............... chemistry/tpb/qcham.h:289-340
+//   mult (Wb += H Wk) ................ chemistry/tpb/mult.h:114-130
+//   Davidson ......................... chemistry/tpb/davidson.h:707-726
+//   MultBase::run (device operator) .. chemistry/basic/mult.h:19-103
+//
+// Errors: the C status codes become std::invalid_argument (bad input) or
+// std::runtime_error (everything else), the exception types the reference
+// throws (helper.h:361-364, davidson.h:97-110).
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <cstdlib>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "sbdgb.h"
+
+namespace sbdgb {
+
+inline void check(int rc, const sbdgb_ctx *ctx, const char *what) {
+  if (rc == SBDGB_OK) return;
+  std::string msg = std::string(what) + ": " + (ctx ? sbdgb_last_error(ctx) : "error");
+  if (rc == SBDGB_E_INPUT) throw std::invalid_argument(msg);
+  throw std::runtime_error(msg);
+}
+
+// ---- FCIDUMP (framework/fcidump.h) ---------------------------------------------
+
+struct FCIDump {
+  std::map<std::string, std::string> header;
+  std::vector<std::tuple<double, int, int, int, int>> integrals;
+};
+
+inline FCIDump LoadFCIDump(const std::string &filename) {
+  FCIDump d;
+  std::ifstream in(filename);
+  if (!in.is_open()) throw std::runtime_error("Failed to open FCIDUMP file.");
+  std::string line, head;
+  bool in_header = true;
+  while (std::getline(in, line)) {
+    if (line.empty() || line[0] == '!') continue;
+    if (in_header) {
+      if (line.find("&END") != std::string::npos) {
+        in_header = false;
+        continue;
+      }
+      size_t pos = line.find("&FCI");
+      if (pos != std::string::npos) line.erase(pos, 4);
+      head += line;
+    } else {
+      std::stringstream ss(line);
+      double v;
+      int i, j, k, l;
+      ss >> v >> i >> j >> k >> l;
+      d.integrals.emplace_back(v, i, j, k, l);
+    }
+  }
+  std::stringstream hs(head);
+  std::string tok;
+  while (std::getline(hs, tok, ',')) {
+    size_t eq = tok.find('=');
+    if (eq == std::string::npos) continue;
+    std::string key = tok.substr(0, eq), val = tok.substr(eq + 1);
+    auto trim = [](std::string &s) {
+      s.erase(0, s.find_first_not_of(" \t"));
+      s.erase(s.find_last_not_of(" \t") + 1);
+    };
+    trim(key);
+    trim(val);
+    d.header[key] = val;
+  }
+  return d;
+}
+
+// Spatial integrals in the engine's layout: h1 (L*L) and the 8-fold packed ERI.
+struct Integrals {
+  int L = 0, N = 0;
+  double I0 = 0.0;
+  std::vector<double> h1, eri;
+};
+
+inline size_t pair_index(int i, int j) {
+  int a = std::max(i, j), b = std::min(i, j);
+  return (size_t)a * (a + 1) / 2 + b;
+}
+
+// SetupIntegrals (makeintegrals.h:123-174): core, one-body (symmetrised), two-body
+// (8-fold packed); later lines overwrite earlier ones.
+inline Integrals SetupIntegrals(const FCIDump &d) {
+  Integrals t;
+  for (const auto &kv : d.header) {
+    if (kv.first == "NORB") t.L = std::atoi(kv.second.c_str());
+    if (kv.first == "NELEC") t.N = std::atoi(kv.second.c_str());
+  }
+  if (t.L <= 0) throw std::invalid_argument("FCIDUMP header has no NORB");
+  const size_t B = (size_t)t.L * (t.L + 1) / 2;
+  t.h1.assign((size_t)t.L * t.L, 0.0);
+  t.eri.assign(B * (B + 1) / 2, 0.0);
+  for (const auto &e : d.integrals) {
+    const double v = std::get<0>(e);
+    const int i = std::get<1>(e), j = std::get<2>(e), k = std::get<3>(e), l = std::get<4>(e);
+    if (i == 0 && j == 0 && k == 0 && l == 0) {
+      t.I0 = v;
+    } else if (k == 0 && l == 0) {
+      if (i < 1 || j < 1 || i > t.L || j > t.L) throw std::invalid_argument("FCIDUMP one-body index out of range");
+      t.h1[(size_t)(i - 1) * t.L + (j - 1)] = v;
+      t.h1[(size_t)(j - 1) * t.L + (i - 1)] = v;
+    } else {
+      if (i < 1 || j < 1 || k < 1 || l < 1 || i > t.L || j > t.L || k > t.L || l > t.L)
+        throw std::invalid_argument("FCIDUMP two-body index out of range");
+      size_t ij = pair_index(i - 1, j - 1), kl = pair_index(k - 1, l - 1);
+      size_t a = std::max(ij, kl), b = std::min(ij, kl);
+      t.eri[a * (a + 1) / 2 + b] = v;
+    }
+  }
+  return t;
+}
+
+// ---- strings (framework/bit_manipulation.h) -------------------------------------
+
+// Text line -> uint64, character s[L-1-i] is orbital i (bit_manipulation.h:219-233).
+inline uint64_t from_string(const std::string &s, int L) {
+  if ((int)s.size() < L) throw std::invalid_argument("bit string shorter than norb");
+  uint64_t v = 0;
+  for (int i = 0; i < L; ++i)
+    if (s[L - 1 - i] == '1') v |= 1ull << i;
+  return v;
+}
+
+// Sorted, duplicate-free list: the reference's from-back order is numeric order.
+inline std::vector<uint64_t> LoadAlphaDets(const std::string &file, int L) {
+  if (L > 64) throw std::invalid_argument("norb > 64 is not supported");
+  std::ifstream in(file);
+  if (!in.is_open()) throw std::runtime_error("Failed to open alpha det file.");
+  std::vector<uint64_t> v;
+  std::string line;
+  while (std::getline(in, line)) v.push_back(from_string(line, L));
+  std::sort(v.begin(), v.end());
+  v.erase(std::unique(v.begin(), v.end()), v.end());
+  return v;
+}
+
+// Converts any reference-style string container (rows of `bit_length`-bit
+// words, e.g. sbd::det_vector<size_t, det_kind::half>) to uint64 strings.
+template <class DetVec>
+std::vector<uint64_t> pack_strings(const DetVec &dets, size_t bit_length, int L) {
+  std::vector<uint64_t> v(dets.size(), 0);
+  const size_t words = (L + bit_length - 1) / bit_length;
+  for (size_t i = 0; i < dets.size(); ++i)
+    for (size_t w = 0; w < words; ++w) v[i] |= (uint64_t)dets[i][w] << (w * bit_length);
+  return v;
+}
+
+// ---- engine objects ------------------------------------------------------------
+
+class Context {
+ public:
+  explicit Context(int device = 0, size_t hbm_budget = 0) {
+    check(sbdgb_ctx_create(&ctx_, device, hbm_budget), nullptr, "sbdgb_ctx_create");
+  }
+  ~Context() { sbdgb_ctx_destroy(ctx_); }
+  Context(const Context &) = delete;
+  Context &operator=(const Context &) = delete;
+  sbdgb_ctx *get() const { return ctx_; }
+
+ private:
+  sbdgb_ctx *ctx_ = nullptr;
+};
+
+class Problem {
+ public:
+  Problem(Context &ctx, const Integrals &ints, const std::vector<uint64_t> &adet, const std::vector<uint64_t> &bdet)
+      : ctx_(ctx) {
+    check(sbdgb_problem_create(ctx.get(), ints.L, adet.data(), adet.size(), bdet.data(), bdet.size(),
+                               ints.h1.data(), ints.eri.data(), ints.I0, &p_),
+          ctx.get(), "sbdgb_problem_create");
+    N_ = adet.size() * bdet.size();
+  }
+  ~Problem() { sbdgb_problem_destroy(p_); }
+  Problem(const Problem &) = delete;
+  Problem &operator=(const Problem &) = delete;
+  sbdgb_problem *get() const { return p_; }
+  size_t size() const { return N_; }
+  sbdgb_ctx *ctx() const { return ctx_.get(); }
+
+ private:
+  Context &ctx_;
+  sbdgb_problem *p_ = nullptr;
+  size_t N_ = 0;
+};
+
+// makeQChamDiagTerms (qcham.h:289-340).
+inline void makeQChamDiagTerms(Problem &p, std::vector<double> &hii) {
+  hii.resize(p.size());
+  check(sbdgb_diag_terms(p.get(), hii.data()), p.ctx(), "makeQChamDiagTerms");
+}
+
+// mult (mult.h:114-130): Wb += H * Wk on host vectors.
+inline void mult(const std::vector<double> &hii, const std::vector<double> &Wk, std::vector<double> &Wb,
+                 Problem &p) {
+  if (Wk.size() != p.size() || Wb.size() != p.size()) throw std::invalid_argument("vector size mismatch");
+  check(sbdgb_mult_host(p.get(), hii.empty() ? nullptr : hii.data(), Wk.data(), Wb.data()), p.ctx(), "mult");
+}
+
+// Davidson (davidson.h:707-726): W in = starting vector (or empty for the
+// reference's init 0 guess), out = normalized ground-state vector.
+inline double Davidson(Problem &p, std::vector<double> &W, int max_iteration, int num_block, double eps,
+                       double max_time = 86400.0, int init = -1) {
+  sbdgb_davidson_opts o;
+  sbdgb_davidson_default_opts(&o);
+  o.max_it = max_iteration;
+  o.max_nb = num_block;
+  o.eps = eps;
+  o.max_time = max_time;
+  o.nroots = 1;
+  if (init >= 0) {
+    o.init = init;
+  } else {
+    o.init = W.size() == p.size() ? 2 : 0;
+  }
+  W.resize(p.size());
+  double E = 0.0;
+  sbdgb_report rep;
+  check(sbdgb_davidson(p.get(), &o, &E, W.data(), &rep), p.ctx(), "Davidson");
+  return E;
+}
+
+// Device operator with the reference's MultBase::run shape (chemistry/basic/
+// mult.h:19-103) over raw device pointers: Wb = hii o Wk + H_offdiag Wk.
+class MultTPBGB300 {
+ public:
+  explicit MultTPBGB300(Problem &p) : p_(p) {
+    check(sbdgb_diag_terms(p.get(), nullptr), p.ctx(), "MultTPBGB300 init");
+  }
+  // accumulate = true gives the reference's Wb += H Wk
+  void run(const double *Wk_dev, double *Wb_dev, bool accumulate = true, void *stream = nullptr) {
+    check(sbdgb_sigma(p_.get(), Wk_dev, Wb_dev, accumulate ? 1 : 0, stream), p_.ctx(), "MultTPBGB300::run");
+  }
+  int h_comm_size() const { return 1; }
+  int b_comm_size() const { return 1; }
+  int t_comm_size() const { return 1; }
+
+ private:
+  Problem &p_;
+};
+
+namespace tpb {
+
+// Options of sbd::tpb::SBD (sbdiag.h:24-54) with the same defaults.
+struct SBD {
+  int task_comm_size = 1;
+  int adet_comm_size = 1;
+  int bdet_comm_size = 1;
+  int h_comm_size = 1;
+  int method = 0;
+  int max_it = 1;
+  int max_nb = 10;
+  double eps = 1.0e-4;
+  double max_time = 86400.0;
+  int init = 0;
+  size_t seed = 1729;
+  int do_shuffle = 0;
+  int do_rdm = 0;
+  int carryover_type = 0;
+  double ratio = 0.0;
+  double threshold = 0.01;
+  size_t bit_length = 20;
+  // engine extensions
+  int nroots = 1;
+  int precision = SBDGB_FP64;
+  int refine_every = 4;
+  int device = 0;
+};
+
+// generate_sbd_data (sbdiag.h:56-134) for the flags this engine honours.
+inline SBD generate_sbd_data(int argc, char *argv[]) {
+  SBD d;
+  for (int i = 0; i + 1 < argc; ++i) {
+    const std::string a(argv[i]);
+    const char *v = argv[i + 1];
+    if (a == "--adet_comm_size") d.adet_comm_size = std::atoi(v);
+    else if (a == "--bdet_comm_size") d.bdet_comm_size = std::atoi(v);
+    else if (a == "--task_comm_size") d.task_comm_size = std::atoi(v);
+    else if (a == "--method") d.method = std::atoi(v);
+    else if (a == "--init") d.init = std::atoi(v);
+    else if (a == "--seed") d.seed = std::atoi(v);
+    else if (a == "--iteration") d.max_it = std::atoi(v);
+    else if (a == "--block") d.max_nb = std::atoi(v);
+    else if (a == "--tolerance") d.eps = std::atof(v);
+    else if (a == "--max_time") d.max_time = std::atof(v);
+    else if (a == "--rdm") d.do_rdm = std::atoi(v);
+    else if (a == "--bit_length") d.bit_length = std::atoi(v);
+    else if (a == "--nroots") d.nroots = std::atoi(v);
+    else if (a == "--precision") d.precision = std::atoi(v);
+    else if (a == "--device") d.device = std::atoi(v);
+  }
+  return d;
+}
+
+// diag (sbdiag.h:151-526) at communicator size 1: integrals -> tables ->
+// diagonal -> Davidson -> energy.  Returns the ground energy in `energy` and,
+// when `W` is non-null, the ground-state vector.  Outputs of the reference's
+// post-processing (density, carry-over strings, RDMs, wavefunction files) are
+// not produced by this entry point.
+inline void diag(int comm_size, const SBD &sbd_data, const FCIDump &fcidump, const std::vector<uint64_t> &adet,
+                 const std::vector<uint64_t> &bdet, double &energy, std::vector<double> *W = nullptr,
+                 std::vector<double> *energies = nullptr) {
+  Context ctx(sbd_data.device);
+  check(sbdgb_check_comm_sizes(ctx.get(), comm_size / std::max(1, sbd_data.task_comm_size * sbd_data.adet_comm_size *
+                                                                      sbd_data.bdet_comm_size),
+                               sbd_data.adet_comm_size * sbd_data.bdet_comm_size, sbd_data.task_comm_size),
+        ctx.get(), "diag");
+  if (sbd_data.method != 0) throw std::invalid_argument("only --method 0 (Davidson) is provided");
+  if (sbd_data.do_rdm != 0) throw std::invalid_argument("RDM output is not provided by this engine");
+  Integrals ints = SetupIntegrals(fcidump);
+  Problem p(ctx, ints, adet, bdet);
+  sbdgb_davidson_opts o;
+  sbdgb_davidson_default_opts(&o);
+  o.max_it = sbd_data.max_it;
+  o.max_nb = sbd_data.max_nb;
+  o.eps = sbd_data.eps;
+  o.max_time = sbd_data.max_time;
+  o.nroots = sbd_data.nroots;
+  o.init = sbd_data.init == 0 ? 0 : 1;
+  o.precision = sbd_data.precision;
+  o.refine_every = sbd_data.refine_every;
+  std::vector<double> E(o.nroots), X;
+  if (W) X.resize(p.size() * o.nroots);
+  sbdgb_report rep;
+  check(sbdgb_davidson(p.get(), &o, E.data(), W ? X.data() : nullptr, &rep), ctx.get(), "diag");
+  energy = E[0];
+  if (energies) *energies = E;
+  if (W) W->assign(X.begin(), X.begin() + p.size());
+}
+
+}  // namespace tpb
+}  // namespace sbdgb

@@ -51,7 +51,8 @@ def lib():
         L.orc_excitations.restype = C.c_int
         L.orc_excitations.argtypes = [_u64p, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_int,
                                       _szp, _szp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
-        L.orc_hii.argtypes = [C.c_void_p, _u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int, _f64p]
+        L.orc_hii.argtypes = [C.c_void_p, _u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int, _f64p,
+                              C.c_size_t, C.c_size_t]
         tab = [_szp, _u64p, _i32p] * 4
         L.orc_mult.argtypes = ([C.c_void_p, _u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int] + tab
                                + [_f64p, _f64p, _f64p, C.c_size_t, C.c_size_t])
@@ -135,20 +136,28 @@ class Oracle:
     def _tabs(self):
         return self.ta.args() + self.tb.args()
 
-    def hii(self) -> np.ndarray:
+    def hii(self, rows=None) -> np.ndarray:
+        """Diagonal; with rows=(r0, r1) only those bra alpha rows are filled."""
+        if rows is not None:
+            h = np.zeros(self.N)
+            lib().orc_hii(self.ints, self.aw.ravel(), self.na, self.bw.ravel(), self.nb, self.words,
+                          self.bit_length, h, rows[0], rows[1])
+            return h
         if self._hii is None:
             h = np.zeros(self.N)
             lib().orc_hii(self.ints, self.aw.ravel(), self.na, self.bw.ravel(), self.nb, self.words,
-                          self.bit_length, h)
+                          self.bit_length, h, 0, self.na)
             self._hii = h
         return self._hii
 
-    def mult(self, C_in: np.ndarray, out: np.ndarray | None = None, rows=None) -> np.ndarray:
-        """sigma += H C (the reference accumulates into its output)."""
+    def mult(self, C_in: np.ndarray, out: np.ndarray | None = None, rows=None, hii=None) -> np.ndarray:
+        """sigma += H C (the reference accumulates into its output); rows=(r0, r1)
+        restricts the bra alpha rows."""
         c = np.ascontiguousarray(C_in, dtype=np.float64).ravel()
         s = np.zeros(self.N) if out is None else out
         r0, r1 = (0, self.na) if rows is None else rows
-        lib().orc_mult(*self._head(), *self._tabs(), self.hii(), c, s, r0, r1)
+        h = self.hii() if hii is None else hii
+        lib().orc_mult(*self._head(), *self._tabs(), h, c, s, r0, r1)
         return s
 
     def sigma(self, C_in: np.ndarray) -> np.ndarray:

@@ -257,14 +257,15 @@ int orc_excitations(const uint64_t *strs, size_t n, int words, int bit_length, i
 /* ---- diagonal: chemistry/tpb/qcham.h:289-340 --------------------------- */
 
 void orc_hii(const orc_ints *t, const uint64_t *astr, size_t na, const uint64_t *bstr, size_t nb, int words,
-             int bit_length, double *hii) {
+             int bit_length, double *hii, size_t row_begin, size_t row_end) {
   const int bl = bit_length, L = t->L;
   const int dwords = (2 * L + bl - 1) / bl;
+  if (row_end > na) row_end = na;
 #pragma omp parallel
   {
     uint64_t det[ORC_MAXW];
 #pragma omp for
-    for (size_t ia = 0; ia < na; ++ia)
+    for (size_t ia = row_begin; ia < row_end; ++ia)
       for (size_t ib = 0; ib < nb; ++ib) {
         orc_det(astr + ia * words, bstr + ib * words, bl, L, det, dwords);
         hii[ia * nb + ib] = orc_zero(t, det, bl);

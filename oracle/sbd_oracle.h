@@ -48,9 +48,10 @@ int orc_excitations(const uint64_t *strs, size_t n, int words, int bit_length, i
                     size_t *off_s, size_t *off_d, uint64_t *ket_s, int32_t *cran_s, uint64_t *ket_d,
                     int32_t *cran_d);
 
-/* Diagonal hii[ia*nb+ib] (qcham.h:289-340 -> determinants.h:451-474). */
+/* Diagonal hii[ia*nb+ib] (qcham.h:289-340 -> determinants.h:451-474) for the
+ * bra alpha rows [row_begin, row_end). */
 void orc_hii(const orc_ints *ints, const uint64_t *astr, size_t na, const uint64_t *bstr, size_t nb,
-             int words, int bit_length, double *hii);
+             int words, int bit_length, double *hii, size_t row_begin, size_t row_end);
 
 /* Matrix-free sigma, Wb += H*Wk (TRADMODE mult, chemistry/tpb/mult.h:114-621,
  * CPU loop :440-558, the three tasks of size-1 MakeHelpers, helper.h:752-767).

@@ -64,6 +64,17 @@ void dev_free_all(Problem &p) {
   p.bytes = 0;
 }
 
+cudaEvent_t timing_event(Ctx *c) {
+  if (!c->event_pool.empty()) {
+    cudaEvent_t e = c->event_pool.back();
+    c->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  SBDGB_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
 }  // namespace sbdgb
 
 struct sbdgb_ctx {
@@ -112,7 +123,8 @@ int sbdgb_ctx_create(sbdgb_ctx **out, int device, size_t hbm_budget_bytes) {
   ctx->c.device = device;
   ctx->c.budget = hbm_budget_bytes;
   int rc = guarded(&ctx->c, [&] {
-    SBDGB_CUDA(cudaStreamCreateWithFlags(&ctx->c.stream, cudaStreamNonBlocking));
+    SBDGB_CUDA(cudaStreamCreateWithFlags(&ctx->c.own_stream, cudaStreamNonBlocking));
+    ctx->c.stream = ctx->c.own_stream;
   });
   if (rc != SBDGB_OK) {
     delete ctx;
@@ -125,7 +137,12 @@ int sbdgb_ctx_create(sbdgb_ctx **out, int device, size_t hbm_budget_bytes) {
 void sbdgb_ctx_destroy(sbdgb_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->c.device);
-  if (ctx->c.stream) cudaStreamDestroy(ctx->c.stream);
+  for (auto &pr : ctx->c.sigma_events) {
+    cudaEventDestroy(pr.first);
+    cudaEventDestroy(pr.second);
+  }
+  for (auto e : ctx->c.event_pool) cudaEventDestroy(e);
+  if (ctx->c.own_stream) cudaStreamDestroy(ctx->c.own_stream);
   delete ctx;
 }
 
@@ -134,6 +151,38 @@ const char *sbdgb_last_error(const sbdgb_ctx *ctx) { return ctx ? ctx->c.last_er
 size_t sbdgb_ctx_bytes_in_use(const sbdgb_ctx *ctx) { return ctx ? ctx->c.in_use : 0; }
 
 uint64_t sbdgb_ctx_launch_count(const sbdgb_ctx *ctx) { return ctx ? ctx->c.launches : 0; }
+
+int sbdgb_ctx_set_stream(sbdgb_ctx *ctx, void *stream) {
+  if (!ctx) return SBDGB_E_INPUT;
+  return guarded(&ctx->c, [&] {
+    SBDGB_CUDA(cudaStreamSynchronize(ctx->c.stream));
+    ctx->c.stream = stream ? (cudaStream_t)stream : ctx->c.own_stream;
+  });
+}
+
+int sbdgb_ctx_enable_timing(sbdgb_ctx *ctx, int on) {
+  if (!ctx) return SBDGB_E_INPUT;
+  ctx->c.timing = on != 0;
+  return SBDGB_OK;
+}
+
+int sbdgb_ctx_sigma_timing(sbdgb_ctx *ctx, uint64_t *calls, double *total_ms) {
+  if (!ctx) return SBDGB_E_INPUT;
+  return guarded(&ctx->c, [&] {
+    double ms = 0.0;
+    for (auto &pr : ctx->c.sigma_events) {
+      SBDGB_CUDA(cudaEventSynchronize(pr.second));
+      float t = 0.f;
+      SBDGB_CUDA(cudaEventElapsedTime(&t, pr.first, pr.second));
+      ms += t;
+      ctx->c.event_pool.push_back(pr.first);
+      ctx->c.event_pool.push_back(pr.second);
+    }
+    if (calls) *calls = ctx->c.sigma_events.size();
+    if (total_ms) *total_ms = ms;
+    ctx->c.sigma_events.clear();
+  });
+}
 
 int sbdgb_check_comm_sizes(sbdgb_ctx *ctx, int h_size, int b_size, int t_size) {
   return guarded(ctx ? &ctx->c : nullptr, [&] {

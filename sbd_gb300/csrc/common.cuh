@@ -148,8 +148,15 @@ struct Ctx {
   uint64_t launches = 0;
   std::string last_error;
   std::mutex mu;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // stream in use
+  cudaStream_t own_stream = nullptr;  // stream created with the context
+  bool timing = false;
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> sigma_events;
+  std::vector<cudaEvent_t> event_pool;
 };
+
+// sigma timing hooks (api.cu)
+cudaEvent_t timing_event(Ctx *c);
 
 void *dev_alloc(Problem &p, size_t bytes);
 void *workspace(Problem &p, int slot, size_t bytes);

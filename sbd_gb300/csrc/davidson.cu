@@ -1,60 +1,84 @@
-// Davidson eigensolver on the device (replaces sbd::Davidson,
+// Davidson eigensolvers on the device (replace sbd::Davidson,
 // chemistry/tpb/davidson.h:707-970, and its GPU form chemistry/basic/
 // davidson_thrust.h:97-385 / :389-675).
 //
 // The reference solves one root with a single-vector Davidson: subspace up to
 // max_nb, Ritz pair from the projected matrix, residual R = E0 W - H W,
 // diagonal preconditioner R/(E0 - d) with a 1e-12 guard, modified
-// Gram-Schmidt, restart C0 = W (which recomputes sigma(W)).  This solver keeps
-// those steps and generalises them to nroots: each step adds one corrected
-// direction per unconverged root, orthogonalises it against the basis with
-// classical Gram-Schmidt plus a second pass when the norm drops (the
-// "twice is enough" rule), and restarts from the nroots Ritz vectors together
-// with their sigma vectors, which are formed from the stored H*V instead of a
-// new sigma product.  Vectors stay resident in HBM; only the projected
-// (<= max_nb)^2 matrix and a few norms cross to the host per step.
+// Gram-Schmidt, restart C0 = W (which recomputes sigma(W)).
+//
+// FP64 solver: the same steps generalised to nroots.  Each step adds one
+// corrected direction per unconverged root, orthogonalises it against the
+// basis with classical Gram-Schmidt plus a second pass when the norm drops
+// (the "twice is enough" rule), and restarts from the nroots Ritz vectors
+// together with their sigma vectors, which are formed from the stored H*V
+// instead of a new sigma product.  Vectors stay resident in HBM; only the
+// projected (<= max_nb)^2 matrix and a few norms cross to the host per step.
+//
+// Mixed solver: each root keeps an FP64 vector x (and its FP64 sigma) that is
+// never rounded to FP32.  Corrections live in an FP32 subspace W with FP32
+// sigma products.  Rayleigh-Ritz runs on span{x, W} as a generalised
+// symmetric problem whose x-W couplings are computed in FP64 (W is only
+// orthogonal to x to FP32 accuracy); every refine_every steps the Ritz vectors
+// are assembled in FP64, their FP64 sigma and FP64 residual are recomputed
+// (iterative refinement), and convergence is judged on that FP64 residual.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "common.cuh"
+#include "small_eig.h"
 
 namespace sbdgb {
 
-void transpose_fp64(Problem &p, const double *in, double *out, uint32_t R, uint32_t Cn, cudaStream_t s);
-
 namespace {
 
-constexpr int kRed = 256;   // threads per reduction block
-constexpr int kMaxV = 8;    // basis columns per dots pass
-constexpr int kMaxW = 4;    // right-hand columns per dots pass
+constexpr int kRed = 256;  // threads per reduction block
+constexpr int kMaxV = 8;   // basis columns per dots pass
+constexpr int kMaxW = 4;   // right-hand columns per dots pass
 constexpr int kMaxCoef = 64 * 16;
 
-struct ColPtrs {
-  const double *p[kMaxV];
-};
-struct WPtrs {
-  const double *p[kMaxW];
+template <typename T, int M>
+struct Ptrs {
+  const T *p[M];
 };
 
-// partial[b][i*nw+j] = sum over this block's elements of V_i * W_j.
-template <int NV, int NW>
-__global__ void __launch_bounds__(kRed) k_dots(ColPtrs V, WPtrs W, size_t N, double *__restrict__ partial) {
-  double acc[NV][NW];
+// partial[b][i*NW+j] = sum over this block's elements of V_i * W_j.  FP32 x
+// FP32 uses FP32 products with per-thread Kahan compensation; anything with an
+// FP64 operand accumulates with FP64 FMAs.
+template <typename TV, typename TW, int NV, int NW>
+__global__ void __launch_bounds__(kRed) k_dots(Ptrs<TV, kMaxV> V, Ptrs<TW, kMaxW> W, size_t N,
+                                               double *__restrict__ partial) {
+  constexpr bool kF32 = std::is_same<TV, float>::value && std::is_same<TW, float>::value;
+  using Acc = typename std::conditional<kF32, float, double>::type;
+  Acc acc[NV][NW], cmp[NV][NW];
 #pragma unroll
   for (int i = 0; i < NV; ++i)
 #pragma unroll
-    for (int j = 0; j < NW; ++j) acc[i][j] = 0.0;
+    for (int j = 0; j < NW; ++j) {
+      acc[i][j] = Acc(0);
+      cmp[i][j] = Acc(0);
+    }
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
-    double w[NW];
+    Acc w[NW];
 #pragma unroll
-    for (int j = 0; j < NW; ++j) w[j] = __ldg(W.p[j] + e);
+    for (int j = 0; j < NW; ++j) w[j] = (Acc)__ldg(W.p[j] + e);
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-      const double v = __ldg(V.p[i] + e);
+      const Acc v = (Acc)__ldg(V.p[i] + e);
 #pragma unroll
-      for (int j = 0; j < NW; ++j) acc[i][j] = fma(v, w[j], acc[i][j]);
+      for (int j = 0; j < NW; ++j) {
+        if constexpr (kF32) {
+          const float y = v * w[j] - cmp[i][j];
+          const float t = acc[i][j] + y;
+          cmp[i][j] = (t - acc[i][j]) - y;
+          acc[i][j] = t;
+        } else {
+          acc[i][j] = fma(v, w[j], acc[i][j]);
+        }
+      }
     }
   }
   __shared__ double red[kRed / 32][NV * NW];
@@ -63,7 +87,7 @@ __global__ void __launch_bounds__(kRed) k_dots(ColPtrs V, WPtrs W, size_t N, dou
   for (int i = 0; i < NV; ++i)
 #pragma unroll
     for (int j = 0; j < NW; ++j) {
-      double x = acc[i][j];
+      double x = (double)acc[i][j] - (double)cmp[i][j];
       for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
       if (lane == 0) red[warp][i * NW + j] = x;
     }
@@ -93,9 +117,9 @@ struct CombineArgs {
   const double *coef;   // nv x k column-major (coef[j + nv*r])
   const double *theta;  // k
   const double *hii;
-  double *X;    // k x N or null
-  double *HX;   // k x N or null
-  double *T;    // k x N or null: preconditioned residual
+  double *X;        // k x N or null
+  double *HX;       // k x N or null
+  double *T;        // k x N or null: preconditioned residual
   double *partial;  // blocks x k residual norm^2 partials
 };
 
@@ -157,35 +181,31 @@ __global__ void __launch_bounds__(kRed) k_combine(CombineArgs a) {
   }
 }
 
-// T_r -= sum_j V_j G[j][r]  (G column-major, ld = nv), then optional scale.
-template <int K>
-__global__ void __launch_bounds__(kRed) k_project_out(const double *__restrict__ V, int nv, size_t N,
-                                                       const double *__restrict__ G, double *__restrict__ T) {
-  __shared__ double gs[kMaxCoef];
-  for (int t = threadIdx.x; t < nv * K; t += kRed) gs[t] = G[t];
+// T_r -= sum_j V_j G[j][r]  (G column-major, ld = nv), in the vectors' precision.
+template <typename T, int K>
+__global__ void __launch_bounds__(kRed) k_project_out(const T *__restrict__ V, int nv, size_t N,
+                                                       const double *__restrict__ G, T *__restrict__ Tv) {
+  __shared__ T gs[kMaxCoef];
+  for (int t = threadIdx.x; t < nv * K; t += kRed) gs[t] = (T)G[t];
   __syncthreads();
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
-    double t[K];
+    T t[K];
 #pragma unroll
-    for (int r = 0; r < K; ++r) t[r] = T[(size_t)r * N + e];
+    for (int r = 0; r < K; ++r) t[r] = Tv[(size_t)r * N + e];
     for (int j = 0; j < nv; ++j) {
-      const double v = __ldg(V + (size_t)j * N + e);
+      const T v = __ldg(V + (size_t)j * N + e);
 #pragma unroll
       for (int r = 0; r < K; ++r) t[r] = fma(-v, gs[j + nv * r], t[r]);
     }
 #pragma unroll
-    for (int r = 0; r < K; ++r) T[(size_t)r * N + e] = t[r];
+    for (int r = 0; r < K; ++r) Tv[(size_t)r * N + e] = t[r];
   }
 }
 
-__global__ void k_scale_copy(const double *__restrict__ x, double *__restrict__ y, size_t N, double f) {
+template <typename TI, typename TO>
+__global__ void k_scale_copy(const TI *x, TO *y, size_t N, double f) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
-    y[e] = x[e] * f;
-}
-
-__global__ void k_axpy(double *__restrict__ y, const double *__restrict__ x, size_t N, double f) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
-    y[e] = fma(f, x[e], y[e]);
+    y[e] = (TO)((double)x[e] * f);
 }
 
 __global__ void k_fill_unit(double *__restrict__ y, size_t N, size_t pos) {
@@ -229,60 +249,100 @@ __global__ void k_argmin(const double *__restrict__ h, size_t N, const unsigned 
   }
 }
 
-// Symmetric eigensolver for the projected matrix: cyclic Jacobi, eigenvalues
-// ascending (stands in for LAPACK dsyev, framework/hp_numeric.h:503-520).
-void jacobi_eig(int n, std::vector<double> A, std::vector<double> &w, std::vector<double> &Vout) {
-  std::vector<double> V((size_t)n * n, 0.0);
-  for (int i = 0; i < n; ++i) V[i + (size_t)n * i] = 1.0;
-  auto a = [&](int i, int j) -> double & { return A[i + (size_t)n * j]; };
-  for (int sweep = 0; sweep < 100; ++sweep) {
-    double off = 0.0, dg = 0.0;
-    for (int j = 0; j < n; ++j)
-      for (int i = 0; i < n; ++i) (i == j ? dg : off) += a(i, j) * a(i, j);
-    if (off <= 1e-30 * (dg + 1e-300)) break;
-    for (int p = 0; p < n - 1; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double apq = a(p, q);
-        if (std::fabs(apq) < 1e-300) continue;
-        const double theta = (a(q, q) - a(p, p)) / (2.0 * apq);
-        const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-        const double c = 1.0 / std::sqrt(t * t + 1.0), s = t * c;
-        for (int k = 0; k < n; ++k) {
-          const double akp = a(k, p), akq = a(k, q);
-          a(k, p) = c * akp - s * akq;
-          a(k, q) = s * akp + c * akq;
-        }
-        for (int k = 0; k < n; ++k) {
-          const double apk = a(p, k), aqk = a(q, k);
-          a(p, k) = c * apk - s * aqk;
-          a(q, k) = s * apk + c * aqk;
-        }
-        for (int k = 0; k < n; ++k) {
-          const double vkp = V[k + (size_t)n * p], vkq = V[k + (size_t)n * q];
-          V[k + (size_t)n * p] = c * vkp - s * vkq;
-          V[k + (size_t)n * q] = s * vkp + c * vkq;
-        }
-      }
+// ---- mixed-solver kernels ----------------------------------------------------
+
+// Xf_j = fp32(X_j), Rf_j = fp32(S_j - theta_j X_j): the anchors and their FP64
+// residuals rounded once per refinement (the residual is small, so its FP32
+// copy keeps FP32 relative accuracy of a small vector).
+__global__ void k_make_anchor_f32(const double *__restrict__ X, const double *__restrict__ S,
+                                  const double *__restrict__ theta, int k, size_t N, float *__restrict__ Xf,
+                                  float *__restrict__ Rf) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
+    for (int j = 0; j < k; ++j) {
+      const double x = X[(size_t)j * N + e];
+      Xf[(size_t)j * N + e] = (float)x;
+      Rf[(size_t)j * N + e] = (float)fma(-theta[j], x, S[(size_t)j * N + e]);
+    }
+}
+
+struct MixedResArgs {
+  const float *Xf, *Rf, *W, *HW;
+  int k, m;
+  size_t N;
+  const float *cx;   // k: anchor coefficients of this Ritz vector
+  const float *dth;  // k: theta_j - theta (anchor Ritz values minus current value)
+  const float *cw;   // m: subspace coefficients
+  float theta;
+  const double *hii;
+  float *T;          // out: preconditioned residual
+  double *partial;   // blocks: residual norm^2
+};
+
+// r = sum_j (Rf_j + dth_j Xf_j) cx_j + sum_l (HW_l - theta W_l) cw_l, then
+// T = r / (theta - d) with the reference's 1e-12 guard.  FP32 arithmetic.
+__global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
+  __shared__ float c[3 * 64];
+  for (int t = threadIdx.x; t < a.k; t += kRed) {
+    c[t] = a.cx[t];
+    c[64 + t] = a.dth[t];
   }
-  std::vector<int> idx(n);
-  for (int i = 0; i < n; ++i) idx[i] = i;
-  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return a(x, x) < a(y, y); });
-  w.resize(n);
-  Vout.assign((size_t)n * n, 0.0);
-  for (int j = 0; j < n; ++j) {
-    w[j] = a(idx[j], idx[j]);
-    for (int i = 0; i < n; ++i) Vout[i + (size_t)n * j] = V[i + (size_t)n * idx[j]];
+  for (int t = threadIdx.x; t < a.m; t += kRed) c[128 + t] = a.cw[t];
+  __syncthreads();
+  float s = 0.f, comp = 0.f;
+  for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < a.N; e += (size_t)gridDim.x * kRed) {
+    float r = 0.f;
+    for (int j = 0; j < a.k; ++j)
+      r = fmaf(fmaf(c[64 + j], __ldg(a.Xf + (size_t)j * a.N + e), __ldg(a.Rf + (size_t)j * a.N + e)), c[j], r);
+    for (int l = 0; l < a.m; ++l)
+      r = fmaf(fmaf(-a.theta, __ldg(a.W + (size_t)l * a.N + e), __ldg(a.HW + (size_t)l * a.N + e)), c[128 + l], r);
+    const float y = r * r - comp;
+    const float t = s + y;
+    comp = (t - s) - y;
+    s = t;
+    double den = (double)a.theta - __ldg(a.hii + e);
+    if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
+    a.T[e] = (float)((double)r / den);
+  }
+  __shared__ double red[kRed / 32];
+  double x = (double)s - (double)comp;
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w2 = 0; w2 < kRed / 32; ++w2) t += red[w2];
+    a.partial[blockIdx.x] = t;
   }
 }
+
+// y = sum_j X_j cx_j (FP64) + fp64(sum_l W_l cw_l) (FP32): the refined Ritz vector.
+__global__ void __launch_bounds__(kRed) k_mixed_assemble(const double *__restrict__ X, int k, const float *__restrict__ W,
+                                                         int m, size_t N, const double *__restrict__ cx,
+                                                         const float *__restrict__ cw, double *__restrict__ y) {
+  __shared__ double sx[64];
+  __shared__ float sw[64];
+  for (int t = threadIdx.x; t < k; t += kRed) sx[t] = cx[t];
+  for (int t = threadIdx.x; t < m; t += kRed) sw[t] = cw[t];
+  __syncthreads();
+  for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
+    double v = 0.0;
+    for (int j = 0; j < k; ++j) v = fma(__ldg(X + (size_t)j * N + e), sx[j], v);
+    float w = 0.f;
+    for (int l = 0; l < m; ++l) w = fmaf(__ldg(W + (size_t)l * N + e), sw[l], w);
+    y[e] = v + (double)w;
+  }
+}
+
+// ---- host-side helper ----------------------------------------------------------
 
 struct Solver {
   Problem &p;
   cudaStream_t s;
   size_t N;
   int blocks;
-  double *partial = nullptr;   // blocks * kMaxV*kMaxW
-  double *red = nullptr;       // reduced results (device)
-  double *coef = nullptr;      // device coefficient staging
+  double *partial = nullptr;  // blocks * kMaxV*kMaxW
+  double *red = nullptr;      // reduced results (device)
+  double *coef = nullptr;     // device coefficient staging
   std::vector<double> hbuf;
 
   Solver(Problem &pp, cudaStream_t ss) : p(pp), s(ss), N(pp.N) {
@@ -296,17 +356,18 @@ struct Solver {
   }
 
   // G (column-major nv x nw) = V^T W, V columns at V0 + j*N.
-  void dots(const double *V0, int nv, const double *const *W, int nw, std::vector<double> &G) {
+  template <typename TV, typename TW>
+  void dots(const TV *V0, int nv, const TW *const *W, int nw, std::vector<double> &G) {
     G.assign((size_t)nv * nw, 0.0);
     for (int j0 = 0; j0 < nw; j0 += kMaxW) {
       const int mw = std::min(kMaxW, nw - j0);
-      WPtrs wp{};
+      Ptrs<TW, kMaxW> wp{};
       for (int j = 0; j < kMaxW; ++j) wp.p[j] = W[j0 + std::min(j, mw - 1)];
       for (int i0 = 0; i0 < nv; i0 += kMaxV) {
         const int mv = std::min(kMaxV, nv - i0);
-        ColPtrs vp{};
+        Ptrs<TV, kMaxV> vp{};
         for (int i = 0; i < kMaxV; ++i) vp.p[i] = V0 + (size_t)(i0 + std::min(i, mv - 1)) * N;
-        launch_dots(vp, wp, mv, mw);
+        launch_dots<TV, TW>(vp, wp, mv, mw);
         const int width = mv * mw;
         k_sum_partials<<<(width + 63) / 64, 64, 0, s>>>(partial, blocks, width, red);
         count_launch(p.ctx);
@@ -319,25 +380,26 @@ struct Solver {
     }
   }
 
-  template <int NV>
-  void launch_dots_w(ColPtrs vp, WPtrs wp, int mw) {
+  template <typename TV, typename TW, int NV>
+  void launch_dots_w(Ptrs<TV, kMaxV> vp, Ptrs<TW, kMaxW> wp, int mw) {
     switch (mw) {
-      case 1: k_dots<NV, 1><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
-      case 2: k_dots<NV, 2><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
-      case 3: k_dots<NV, 3><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
-      default: k_dots<NV, 4><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
+      case 1: k_dots<TV, TW, NV, 1><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
+      case 2: k_dots<TV, TW, NV, 2><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
+      case 3: k_dots<TV, TW, NV, 3><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
+      default: k_dots<TV, TW, NV, 4><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
     }
   }
-  void launch_dots(ColPtrs vp, WPtrs wp, int mv, int mw) {
+  template <typename TV, typename TW>
+  void launch_dots(Ptrs<TV, kMaxV> vp, Ptrs<TW, kMaxW> wp, int mv, int mw) {
     switch (mv) {
-      case 1: launch_dots_w<1>(vp, wp, mw); break;
-      case 2: launch_dots_w<2>(vp, wp, mw); break;
-      case 3: launch_dots_w<3>(vp, wp, mw); break;
-      case 4: launch_dots_w<4>(vp, wp, mw); break;
-      case 5: launch_dots_w<5>(vp, wp, mw); break;
-      case 6: launch_dots_w<6>(vp, wp, mw); break;
-      case 7: launch_dots_w<7>(vp, wp, mw); break;
-      default: launch_dots_w<8>(vp, wp, mw); break;
+      case 1: launch_dots_w<TV, TW, 1>(vp, wp, mw); break;
+      case 2: launch_dots_w<TV, TW, 2>(vp, wp, mw); break;
+      case 3: launch_dots_w<TV, TW, 3>(vp, wp, mw); break;
+      case 4: launch_dots_w<TV, TW, 4>(vp, wp, mw); break;
+      case 5: launch_dots_w<TV, TW, 5>(vp, wp, mw); break;
+      case 6: launch_dots_w<TV, TW, 6>(vp, wp, mw); break;
+      case 7: launch_dots_w<TV, TW, 7>(vp, wp, mw); break;
+      default: launch_dots_w<TV, TW, 8>(vp, wp, mw); break;
     }
     count_launch(p.ctx);
     SBDGB_CUDA(cudaGetLastError());
@@ -369,34 +431,66 @@ struct Solver {
     return rn;
   }
 
-  void project_out(const double *V, int nv, const std::vector<double> &G, double *T, int k) {
+  template <typename T>
+  void project_out(const T *V, int nv, const std::vector<double> &G, T *Tv, int k) {
     if (nv == 0) return;
     SBDGB_CUDA(cudaMemcpyAsync(coef, G.data(), sizeof(double) * nv * k, cudaMemcpyHostToDevice, s));
     switch (k) {
 #define SBDGB_K(KK) \
-  case KK: k_project_out<KK><<<blocks, kRed, 0, s>>>(V, nv, N, coef, T); break;
+  case KK: k_project_out<T, KK><<<blocks, kRed, 0, s>>>(V, nv, N, coef, Tv); break;
       SBDGB_K(1) SBDGB_K(2) SBDGB_K(3) SBDGB_K(4) SBDGB_K(5) SBDGB_K(6) SBDGB_K(7) SBDGB_K(8)
-      SBDGB_K(9) SBDGB_K(10) SBDGB_K(11) SBDGB_K(12) SBDGB_K(13) SBDGB_K(14) SBDGB_K(15) SBDGB_K(16)
 #undef SBDGB_K
-      default: throw Error(SBDGB_E_UNSUPPORTED, "at most 16 roots");
+      default: throw Error(SBDGB_E_UNSUPPORTED, "at most 8 vectors per projection");
     }
     count_launch(p.ctx);
     SBDGB_CUDA(cudaGetLastError());
   }
 
-  void scale_copy(const double *x, double *y, double f) {
-    k_scale_copy<<<blocks, kRed, 0, s>>>(x, y, N, f);
+  template <typename TI, typename TO>
+  void scale_copy(const TI *x, TO *y, double f) {
+    k_scale_copy<TI, TO><<<blocks, kRed, 0, s>>>(x, y, N, f);
     count_launch(p.ctx);
   }
-  void axpy(double *y, const double *x, double f) {
-    k_axpy<<<blocks, kRed, 0, s>>>(y, x, N, f);
-    count_launch(p.ctx);
-  }
-  double norm(const double *x) {
+  template <typename T>
+  double norm(const T *x) {
     std::vector<double> g;
-    const double *w[1] = {x};
-    dots(x, 1, w, 1, g);
+    const T *w[1] = {x};
+    dots<T, T>(x, 1, w, 1, g);
     return std::sqrt(std::max(0.0, g[0]));
+  }
+  double reduce_partials(int width) {
+    k_sum_partials<<<1, 64, 0, s>>>(partial, blocks, width, red);
+    count_launch(p.ctx);
+    double out = 0.0;
+    SBDGB_CUDA(cudaMemcpyAsync(&out, red, sizeof(double), cudaMemcpyDeviceToHost, s));
+    SBDGB_CUDA(cudaStreamSynchronize(s));
+    return out;
+  }
+
+  // Orthonormalises t against the first nv columns of V (two passes of
+  // classical Gram-Schmidt when the norm drops), in the vectors' precision.
+  // Returns the norm left relative to the unit-normalised input (0 if t was 0).
+  template <typename T>
+  double orthonormalize(T *t, const T *V, int nv) {
+    double n0 = norm(t);
+    if (!(n0 > 0.0) || !std::isfinite(n0)) return 0.0;
+    scale_copy<T, T>(t, t, 1.0 / n0);
+    n0 = 1.0;
+    for (int pass = 0; pass < 2 && nv > 0; ++pass) {
+      for (int j0 = 0; j0 < nv; j0 += kMaxV) {
+        const int mv = std::min(kMaxV, nv - j0);
+        std::vector<double> G;
+        const T *w[1] = {t};
+        dots<T, T>(V + (size_t)j0 * N, mv, w, 1, G);
+        project_out<T>(V + (size_t)j0 * N, mv, G, t, 1);
+      }
+      const double n1 = norm(t);
+      const bool enough = n1 > 0.7071 * n0;
+      n0 = n1;
+      if (enough) break;
+    }
+    if (n0 > 0.0) scale_copy<T, T>(t, t, 1.0 / n0);
+    return n0;
   }
 
   std::vector<size_t> lowest_diagonal(int k) {
@@ -428,18 +522,46 @@ struct Solver {
     }
     return out;
   }
+
+  // Starting vectors (BasisInitVector, davidson.h:144-184) into T (k x N).
+  void start_vectors(const sbdgb_davidson_opts &o, int k, double *T, const double *Xin) {
+    if (o.init == 2) {
+      SBDGB_REQUIRE(Xin != nullptr, SBDGB_E_INPUT, "init 2 needs starting vectors in X");
+      SBDGB_CUDA(cudaMemcpyAsync(T, Xin, sizeof(double) * N * k, cudaMemcpyHostToDevice, s));
+      return;
+    }
+    std::vector<size_t> pos;
+    if (o.init == 0) {
+      pos.push_back(0);
+      if (k > 1) {
+        auto low = lowest_diagonal(k + 1);
+        for (size_t q : low)
+          if (q != 0 && (int)pos.size() < k) pos.push_back(q);
+      }
+    } else {
+      pos = lowest_diagonal(k);
+    }
+    for (int q = 0; q < k; ++q) {
+      k_fill_unit<<<blocks, kRed, 0, s>>>(T + (size_t)q * N, N, pos[q]);
+      count_launch(p.ctx);
+    }
+  }
 };
 
-}  // namespace
+void print_iter(const char *tag, int iter, const std::vector<double> &resid, const std::vector<double> &th, int kk) {
+  printf(" Davidson%s iteration %d (tol=%.6g):", tag, iter, *std::max_element(resid.begin(), resid.end()));
+  for (int q = 0; q < std::min(kk, 4); ++q) printf(" %.12f", th[q]);
+  printf("\n");
+  fflush(stdout);
+}
 
-void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
+// ---- FP64 solver ------------------------------------------------------------------
+
+void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
   using clock = std::chrono::steady_clock;
   const auto t0 = clock::now();
-  if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "Davidson needs tables and diagonal");
   const int k = o.nroots;
   const size_t N = p.N;
-  SBDGB_REQUIRE(k >= 1 && k <= 16, SBDGB_E_INPUT, "nroots must be in [1, 16]");
-  SBDGB_REQUIRE((size_t)k <= N, SBDGB_E_INPUT, "more roots than determinants");
   int max_nb = std::max(o.max_nb, 2 * k);
   max_nb = (int)std::min<size_t>((size_t)max_nb, N);
   SBDGB_REQUIRE(max_nb <= 64, SBDGB_E_INPUT, "max_nb must be <= 64");
@@ -452,57 +574,20 @@ void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout,
   double *T = (double *)workspace(p, WS_T, sizeof(double) * N * k);
 
   sbdgb_report r{};
-  // ---- initial vectors (BasisInitVector, davidson.h:144-184) ----
+  sv.start_vectors(o, k, T, Xout);
   int nv = 0;
-  if (o.init == 2) {
-    SBDGB_REQUIRE(Xout != nullptr, SBDGB_E_INPUT, "init 2 needs starting vectors in X");
-    SBDGB_CUDA(cudaMemcpyAsync(T, Xout, sizeof(double) * N * k, cudaMemcpyHostToDevice, s));
-  } else {
-    std::vector<size_t> pos;
-    if (o.init == 0) {
-      pos.push_back(0);
-      if (k > 1) {
-        auto low = sv.lowest_diagonal(k + 1);
-        for (size_t q : low)
-          if (q != 0 && (int)pos.size() < k) pos.push_back(q);
-      }
-    } else {
-      pos = sv.lowest_diagonal(k);
-    }
-    for (int q = 0; q < k; ++q) {
-      k_fill_unit<<<sv.blocks, kRed, 0, s>>>(T + (size_t)q * N, N, pos[q]);
-      count_launch(p.ctx);
-    }
-  }
-  // orthonormalise the starting block into V
   auto append = [&](double *Tin, int nt) -> int {
     int added = 0;
-    for (int q = 0; q < nt; ++q) {
+    for (int q = 0; q < nt && nv < max_nb; ++q) {
       double *t = Tin + (size_t)q * N;
-      double n0 = sv.norm(t);
-      if (!(n0 > 0.0)) continue;
-      for (int pass = 0; pass < 2; ++pass) {
-        if (nv == 0) break;
-        std::vector<double> G;
-        const double *w[1] = {t};
-        sv.dots(V, nv, w, 1, G);
-        sv.project_out(V, nv, G, t, 1);
-        double n1 = sv.norm(t);
-        if (n1 > 0.7071 * n0) {
-          n0 = n1;
-          break;
-        }
-        n0 = n1;
-      }
-      if (!(n0 > 1e-10)) continue;  // linearly dependent direction: dropped
-      sv.scale_copy(t, V + (size_t)nv * N, 1.0 / n0);
+      const double left = sv.orthonormalize<double>(t, V, nv);
+      if (!(left > 1e-8)) continue;  // linearly dependent direction: dropped
+      SBDGB_CUDA(cudaMemcpyAsync(V + (size_t)nv * N, t, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
       nv++;
       added++;
-      if (nv >= max_nb) break;
     }
     return added;
   };
-  // sigma of the vectors V[from .. nv)
   auto sigma_range = [&](int from) {
     for (int j = from; j < nv; ++j) {
       sigma_fp64(p, V + (size_t)j * N, HV + (size_t)j * N, 0, s);
@@ -518,7 +603,7 @@ void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout,
     std::vector<const double *> w;
     for (int j = from; j < nv; ++j) w.push_back(HV + (size_t)j * N);
     std::vector<double> G;
-    sv.dots(V, nv, w.data(), (int)w.size(), G);
+    sv.dots<double, double>(V, nv, w.data(), (int)w.size(), G);
     for (int jj = 0; jj < (int)w.size(); ++jj)
       for (int i = 0; i < nv; ++i) {
         const double g = G[(size_t)i + (size_t)nv * jj];
@@ -536,7 +621,8 @@ void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout,
     // Rayleigh-Ritz on the projected matrix
     std::vector<double> A((size_t)nv * nv);
     for (int j = 0; j < nv; ++j)
-      for (int i = 0; i < nv; ++i) A[i + (size_t)nv * j] = 0.5 * (Hs[i + (size_t)max_nb * j] + Hs[j + (size_t)max_nb * i]);
+      for (int i = 0; i < nv; ++i)
+        A[i + (size_t)nv * j] = 0.5 * (Hs[i + (size_t)max_nb * j] + Hs[j + (size_t)max_nb * i]);
     jacobi_eig(nv, A, theta, Y);
     const int kk = std::min(k, nv);
     std::vector<double> c((size_t)nv * kk);
@@ -546,12 +632,7 @@ void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout,
     resid = sv.combine(V, HV, nv, kk, c, th, X, HX, T);
     iter++;
     r.iterations = iter;
-    if (o.verbose) {
-      printf(" Davidson iteration %d (tol=%.6g):", iter, *std::max_element(resid.begin(), resid.end()));
-      for (int q = 0; q < std::min(kk, 4); ++q) printf(" %.12f", th[q]);
-      printf("\n");
-      fflush(stdout);
-    }
+    if (o.verbose) print_iter("", iter, resid, th, kk);
     converged = kk == k;
     for (int q = 0; q < kk; ++q) converged = converged && (resid[q] < o.eps);
     const double elapsed = std::chrono::duration<double>(clock::now() - t0).count();
@@ -590,6 +671,230 @@ void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout,
   SBDGB_CUDA(cudaStreamSynchronize(s));
   r.seconds = std::chrono::duration<double>(clock::now() - t0).count();
   if (rep) *rep = r;
+}
+
+// ---- mixed solver ------------------------------------------------------------------
+
+void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
+  using clock = std::chrono::steady_clock;
+  const auto t0 = clock::now();
+  const int k = o.nroots;
+  const size_t N = p.N;
+  SBDGB_REQUIRE(k <= 8, SBDGB_E_UNSUPPORTED, "the mixed solver supports up to 8 roots");
+  const int mmax = std::max(std::min(o.max_nb, 64) - k, 2 * k);  // FP32 correction vectors
+  SBDGB_REQUIRE(k + mmax <= 64, SBDGB_E_INPUT, "max_nb must be <= 64");
+  const int refine_every = std::max(1, o.refine_every);
+  cudaStream_t s = p.ctx->stream;
+  prepare_mixed(p, s);
+  Solver sv(p, s);
+  double *X = (double *)workspace(p, WS_X, sizeof(double) * N * k);    // FP64 anchors
+  double *S = (double *)workspace(p, WS_HX, sizeof(double) * N * k);   // their FP64 sigma
+  double *T = (double *)workspace(p, WS_T, sizeof(double) * N * k);    // FP64 scratch
+  double *Y = (double *)workspace(p, WS_C64, sizeof(double) * N * k);  // FP64 scratch
+  float *W = (float *)workspace(p, WS_VF, sizeof(float) * N * mmax);
+  float *HW = (float *)workspace(p, WS_HVF, sizeof(float) * N * mmax);
+  float *Xf = (float *)workspace(p, WS_CF, sizeof(float) * N * k);
+  float *Rf = (float *)workspace(p, WS_SF, sizeof(float) * N * k);
+  float *Tf = (float *)workspace(p, WS_RES64, sizeof(float) * N);
+  float *dcoef = (float *)workspace(p, WS_DIAG1, sizeof(float) * 256);
+
+  sbdgb_report r{};
+  // anchors: starting vectors orthonormalised in FP64
+  sv.start_vectors(o, k, T, Xout);
+  int na = 0;
+  for (int q = 0; q < k; ++q) {
+    double *t = T + (size_t)q * N;
+    const double left = sv.orthonormalize<double>(t, X, na);
+    SBDGB_REQUIRE(left > 1e-8, SBDGB_E_INPUT, "starting vectors are linearly dependent");
+    SBDGB_CUDA(cudaMemcpyAsync(X + (size_t)na * N, t, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+    na++;
+  }
+  std::vector<double> theta(k), resid(k, 0.0);
+  // FP64 sigma of the anchors, Rayleigh-Ritz among them, FP64 residuals
+  auto refine_rr = [&]() {
+    for (int j = 0; j < k; ++j) {
+      sigma_fp64(p, X + (size_t)j * N, S + (size_t)j * N, 0, s);
+      r.sigma_calls++;
+      r.sigma_fp64++;
+    }
+    std::vector<const double *> w;
+    for (int j = 0; j < k; ++j) w.push_back(S + (size_t)j * N);
+    std::vector<double> G, th, Yv;
+    sv.dots<double, double>(X, k, w.data(), k, G);
+    for (int j = 0; j < k; ++j)
+      for (int i = 0; i < j; ++i) G[i + (size_t)k * j] = G[j + (size_t)k * i] = 0.5 * (G[i + (size_t)k * j] + G[j + (size_t)k * i]);
+    jacobi_eig(k, G, th, Yv);
+    resid = sv.combine(X, S, k, k, Yv, th, T, Y, nullptr);
+    SBDGB_CUDA(cudaMemcpyAsync(X, T, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, s));
+    SBDGB_CUDA(cudaMemcpyAsync(S, Y, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, s));
+    theta = th;
+  };
+  refine_rr();
+
+  bool converged = false;
+  int iter = 0;
+  const int max_steps = std::max(1, o.max_it) * std::max(o.max_nb, 2 * k);
+  std::vector<double> Sxw((size_t)k * mmax), Hxw((size_t)k * mmax), Sww((size_t)mmax * mmax),
+      Hww((size_t)mmax * mmax);
+  while (true) {
+    iter++;
+    r.iterations = iter;
+    if (o.verbose) print_iter(" (mixed, FP64 residual)", iter, resid, theta, k);
+    converged = true;
+    for (int q = 0; q < k; ++q) converged = converged && (resid[q] < o.eps);
+    double elapsed = std::chrono::duration<double>(clock::now() - t0).count();
+    if (converged || iter >= max_steps || (o.max_time > 0 && elapsed > o.max_time)) break;
+    // rounded anchors and residuals for the FP32 inner steps
+    SBDGB_CUDA(cudaMemcpyAsync(sv.red + 2048, theta.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    k_make_anchor_f32<<<sv.blocks, kRed, 0, s>>>(X, S, sv.red + 2048, k, N, Xf, Rf);
+    count_launch(p.ctx);
+    // current Ritz vectors in the basis [anchors, W]: coefficients and values
+    std::vector<double> cX((size_t)k * k, 0.0), cW;  // cX[j + k*q], cW[l + m*q]
+    for (int q = 0; q < k; ++q) cX[q + (size_t)k * q] = 1.0;
+    std::vector<double> thc = theta, res_est = resid;
+    int m = 0;
+    bool stalled = false;
+    for (int inner = 0; inner < refine_every; ++inner) {
+      const int m0 = m;
+      for (int q = 0; q < k && m < mmax; ++q) {
+        if (res_est[q] < o.eps) continue;
+        // preconditioned residual of root q in FP32
+        std::vector<float> hc(3 * 64, 0.f);
+        for (int j = 0; j < k; ++j) {
+          hc[j] = (float)cX[j + (size_t)k * q];
+          hc[64 + j] = (float)(theta[j] - thc[q]);
+        }
+        for (int l = 0; l < m0; ++l) hc[128 + l] = (float)cW[l + (size_t)m0 * q];
+        SBDGB_CUDA(cudaMemcpyAsync(dcoef, hc.data(), sizeof(float) * 3 * 64, cudaMemcpyHostToDevice, s));
+        MixedResArgs ma{Xf, Rf, W, HW, k, m0, N, dcoef, dcoef + 64, dcoef + 128, (float)thc[q], p.hii, Tf, sv.partial};
+        k_mixed_residual<<<sv.blocks, kRed, 0, s>>>(ma);
+        count_launch(p.ctx);
+        res_est[q] = std::sqrt(std::max(0.0, sv.reduce_partials(1)));
+        // orthogonalise against the (rounded) anchors, then against W, in FP32
+        double left = 1.0;
+        {
+          double n0 = sv.norm<float>(Tf);
+          if (!(n0 > 0.0) || !std::isfinite(n0)) continue;
+          sv.scale_copy<float, float>(Tf, Tf, 1.0 / n0);
+          for (int pass = 0; pass < 2; ++pass) {
+            std::vector<double> G;
+            const float *w[1] = {Tf};
+            sv.dots<float, float>(Xf, k, w, 1, G);
+            sv.project_out<float>(Xf, k, G, Tf, 1);
+          }
+          left = sv.orthonormalize<float>(Tf, W, m);
+        }
+        if (!(left > 1e-3)) continue;  // no new direction in FP32
+        SBDGB_CUDA(cudaMemcpyAsync(W + (size_t)m * N, Tf, sizeof(float) * N, cudaMemcpyDeviceToDevice, s));
+        sigma_mixed(p, W + (size_t)m * N, HW + (size_t)m * N, s);
+        r.sigma_calls++;
+        // projected quantities of the new column: anchor couplings in FP64
+        const float *wn[1] = {W + (size_t)m * N};
+        const float *hwn[1] = {HW + (size_t)m * N};
+        std::vector<double> g1, g2, g3, g4;
+        sv.dots<double, float>(X, k, wn, 1, g1);       // X^T w
+        sv.dots<float, float>(Rf, k, wn, 1, g2);       // R^T w
+        sv.dots<float, float>(W, m + 1, wn, 1, g3);    // W^T w
+        sv.dots<float, float>(W, m + 1, hwn, 1, g4);   // W^T Hw
+        std::vector<double> g5;
+        sv.dots<float, float>(HW, m + 1, wn, 1, g5);   // (HW)^T w
+        for (int j = 0; j < k; ++j) {
+          Sxw[j + (size_t)k * m] = g1[j];
+          Hxw[j + (size_t)k * m] = g2[j] + theta[j] * g1[j];  // S_j = R_j + theta_j X_j
+        }
+        for (int l = 0; l <= m; ++l) {
+          Sww[l + (size_t)mmax * m] = Sww[m + (size_t)mmax * l] = g3[l];
+          const double h = 0.5 * (g4[l] + g5[l]);
+          Hww[l + (size_t)mmax * m] = Hww[m + (size_t)mmax * l] = h;
+        }
+        m++;
+      }
+      if (m == m0) {
+        stalled = true;
+        break;
+      }
+      // generalised Rayleigh-Ritz on [anchors, W]
+      const int n = k + m;
+      std::vector<double> A((size_t)n * n, 0.0), B((size_t)n * n, 0.0), w, V;
+      for (int j = 0; j < k; ++j) {
+        A[j + (size_t)n * j] = theta[j];
+        B[j + (size_t)n * j] = 1.0;
+      }
+      for (int l = 0; l < m; ++l)
+        for (int j = 0; j < k; ++j) {
+          A[j + (size_t)n * (k + l)] = A[(k + l) + (size_t)n * j] = Hxw[j + (size_t)k * l];
+          B[j + (size_t)n * (k + l)] = B[(k + l) + (size_t)n * j] = Sxw[j + (size_t)k * l];
+        }
+      for (int l = 0; l < m; ++l)
+        for (int l2 = 0; l2 < m; ++l2) {
+          A[(k + l) + (size_t)n * (k + l2)] = Hww[l + (size_t)mmax * l2];
+          B[(k + l) + (size_t)n * (k + l2)] = Sww[l + (size_t)mmax * l2];
+        }
+      if (!gen_sym_eig(n, A, B, w, V)) {
+        stalled = true;
+        break;
+      }
+      cW.assign((size_t)m * k, 0.0);
+      for (int q = 0; q < k; ++q) {
+        thc[q] = w[q];
+        for (int j = 0; j < k; ++j) cX[j + (size_t)k * q] = V[j + (size_t)n * q];
+        for (int l = 0; l < m; ++l) cW[l + (size_t)m * q] = V[(k + l) + (size_t)n * q];
+      }
+      if (++iter >= max_steps) break;
+      r.iterations = iter;
+      if (m + k > mmax) break;
+    }
+    // refinement: assemble the Ritz vectors in FP64, orthonormalise, FP64 sigma
+    for (int q = 0; q < k; ++q) {
+      std::vector<double> cx(k);
+      std::vector<float> cw(m);
+      for (int j = 0; j < k; ++j) cx[j] = cX[j + (size_t)k * q];
+      for (int l = 0; l < m; ++l) cw[l] = (float)cW[l + (size_t)m * q];
+      SBDGB_CUDA(cudaMemcpyAsync(sv.red + 3000, cx.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+      if (m) SBDGB_CUDA(cudaMemcpyAsync(dcoef, cw.data(), sizeof(float) * m, cudaMemcpyHostToDevice, s));
+      k_mixed_assemble<<<sv.blocks, kRed, 0, s>>>(X, k, W, m, N, sv.red + 3000, dcoef, T + (size_t)q * N);
+      count_launch(p.ctx);
+    }
+    for (int q = 0; q < k; ++q) {
+      double *t = T + (size_t)q * N;
+      const double left = sv.orthonormalize<double>(t, T, q);
+      SBDGB_REQUIRE(left > 1e-8, SBDGB_E_STATE, "mixed Davidson lost a root");
+    }
+    SBDGB_CUDA(cudaMemcpyAsync(X, T, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, s));
+    r.restarts++;
+    refine_rr();
+    if (stalled && m == 0) {
+      // nothing new in FP32 this cycle: the FP64 residual decides
+      bool ok = true;
+      for (int q = 0; q < k; ++q) ok = ok && resid[q] < o.eps;
+      if (!ok && o.verbose) printf(" mixed Davidson: FP32 subspace stalled\n");
+      if (!ok) {
+        iter++;
+        break;
+      }
+    }
+  }
+  converged = true;
+  for (int q = 0; q < k; ++q) converged = converged && (resid[q] < o.eps);
+  r.converged = converged ? 1 : 0;
+  for (int q = 0; q < k && q < 16; ++q) r.resid[q] = resid[q];
+  for (int q = 0; q < k; ++q) E[q] = theta[q];
+  if (Xout) SBDGB_CUDA(cudaMemcpyAsync(Xout, X, sizeof(double) * N * k, cudaMemcpyDeviceToHost, s));
+  SBDGB_CUDA(cudaStreamSynchronize(s));
+  r.seconds = std::chrono::duration<double>(clock::now() - t0).count();
+  if (rep) *rep = r;
+}
+
+}  // namespace
+
+void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
+  if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "Davidson needs tables and diagonal");
+  SBDGB_REQUIRE(o.nroots >= 1 && o.nroots <= 16, SBDGB_E_INPUT, "nroots must be in [1, 16]");
+  SBDGB_REQUIRE((size_t)o.nroots <= p.N, SBDGB_E_INPUT, "more roots than determinants");
+  if (o.precision == SBDGB_MIXED)
+    davidson_mixed(p, o, E, Xout, rep);
+  else
+    davidson_fp64(p, o, E, Xout, rep);
 }
 
 }  // namespace sbdgb

@@ -2,8 +2,9 @@
 // loop chemistry/tpb/mult.h:440-558, and the Thrust MultTPBThrust::run,
 // chemistry/tpb/mult_thrust.h:1170-1580).
 //
-// Gather formulation without atomics, one FP64 FMA per nonzero, phases applied
-// by flipping the sign bit (integer work only):
+// Gather formulation without atomics; phases are applied by flipping the sign
+// bit (integer work only), so the plain FP64 form issues one FP64 FMA per
+// nonzero:
 //
 //   kernel A  rows = alpha strings, columns = beta strings, reads C[ja][ib]
 //             sigma[ia][ib] = hii*C + sum_alpha-pairs +/- V * C[ja][ib]
@@ -11,13 +12,18 @@
 //   kernel B  rows = beta strings, columns = alpha strings, reads C^T[jb][ia]
 //             sigma[ia][ib] += sum_beta-pairs +/- V * C^T[jb][ia]
 //
-// A CTA owns TA rows x (32*CPT*WARPS) columns.  Every thread keeps its columns'
-// opposite-spin strings and TA*CPT accumulators in registers; the pair list
-// of a row is the same for all threads of the CTA, so its metadata are
-// broadcast loads and the ket-row reads are coalesced along the contiguous
-// index.  Grid order puts consecutive CTAs on the same column chunk so that
-// the ket rows' column slab stays resident in L2.
+// A CTA owns TA rows x (128*CPT) columns.  Every thread keeps its columns'
+// opposite-spin strings and TA*CPT accumulators in registers; the pair list of
+// a row is the same for all threads of the CTA, so its metadata are broadcast
+// loads and the ket-row reads are coalesced along the contiguous index.  Grid
+// order puts consecutive CTAs on the same column chunk so that the ket rows'
+// column slab stays resident in L2.
+//
+// The mixed form (T = float) stores C, sigma and the table values in FP32,
+// forms each pair-list sum in FP32 and adds it to an FP64 accumulator per
+// element; the FP64 form (T = double) accumulates every product in FP64.
 #include <algorithm>
+#include <type_traits>
 
 #include "common.cuh"
 
@@ -30,49 +36,81 @@ constexpr int kThreads = 128;
 __device__ __forceinline__ double flip(double x, uint32_t ph) {
   return __longlong_as_double(__double_as_longlong(x) ^ ((unsigned long long)ph << 63));
 }
-__device__ __forceinline__ float flipf(float x, uint32_t ph) {
+__device__ __forceinline__ float flip(float x, uint32_t ph) {
   return __int_as_float(__float_as_int(x) ^ (int)(ph << 31));
 }
 
+template <typename T>
+struct Args {
+  const uint64_t *astr, *bstr;
+  uint32_t na, nb;
+  const double *hii;
+  const T *C;   // N, row-major [ia][ib]
+  const T *CT;  // N, transposed [ib][ia]
+  T *S;
+  int accumulate;
+  SpinTables A, B;
+  const T *val_sa, *val_da, *val_sb, *val_db;  // table values in storage precision
+  const T *Jb;  // [npair][nb]
+  const T *Ja;  // [npair][na]
+  const T *Kp;  // [npair][npair]
+  int npair;
+};
+
 // Same-spin excitations of rows r0 .. r0+TA-1 applied to this thread's CPT
-// columns.  In: ket-major input rows (ld = ldin), Jo: opposite-spin Coulomb
+// columns.  In: ket-major input rows (ld = ldin); Jo: opposite-spin Coulomb
 // table [npair][ldj] for the single excitations.
-template <int TA, int CPT>
-__device__ __forceinline__ void same_spin_sweep(const SpinTables &T, const double *__restrict__ Jo, size_t ldj,
-                                                const double *__restrict__ In, size_t ldin, uint32_t r0,
-                                                uint32_t nrow, const uint32_t (&col)[CPT], const bool (&ok)[CPT],
+template <int TA, int CPT, typename T>
+__device__ __forceinline__ void same_spin_sweep(const SpinTables &Tb, const T *__restrict__ vs,
+                                                const T *__restrict__ vd, const T *__restrict__ Jo, size_t ldj,
+                                                const T *__restrict__ In, size_t ldin, uint32_t r0, uint32_t nrow,
+                                                const uint32_t (&col)[CPT], const bool (&ok)[CPT],
                                                 const uint64_t (&opp)[CPT], double (&acc)[TA][CPT]) {
+  constexpr bool kF64 = std::is_same<T, double>::value;
 #pragma unroll
   for (int r = 0; r < TA; ++r) {
     const uint32_t row = r0 + r;
     if (row < nrow) {
-      const uint32_t p0 = __ldg(T.off_s + row), p1 = __ldg(T.off_s + row + 1);
+      T part[CPT];
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) part[c] = T(0);
+      const uint32_t p0 = __ldg(Tb.off_s + row), p1 = __ldg(Tb.off_s + row + 1);
       for (uint32_t p = p0; p < p1; ++p) {
-        const uint32_t ket = __ldg(T.ket_s + p), code = __ldg(T.code_s + p);
-        const double v = __ldg(T.val_s + p);
-        const uint64_t m = __ldg(T.mask_s + p);
-        const double *in = In + (size_t)ket * ldin;
-        const double *jo = Jo + (size_t)((code >> 16) & 0x7fffu) * ldj;
+        const uint32_t ket = __ldg(Tb.ket_s + p), code = __ldg(Tb.code_s + p);
+        const T v = __ldg(vs + p);
+        const uint64_t m = __ldg(Tb.mask_s + p);
+        const T *in = In + (size_t)ket * ldin;
+        const T *jo = Jo + (size_t)((code >> 16) & 0x7fffu) * ldj;
         const uint32_t sg = code >> 31;
 #pragma unroll
         for (int c = 0; c < CPT; ++c)
           if (ok[c]) {
             const uint32_t ph = (__popcll(opp[c] & m) ^ sg) & 1u;
-            acc[r][c] = fma(flip(v + __ldg(jo + col[c]), ph), __ldg(in + col[c]), acc[r][c]);
+            if constexpr (kF64)
+              acc[r][c] = fma(flip(v + __ldg(jo + col[c]), ph), __ldg(in + col[c]), acc[r][c]);
+            else
+              part[c] = fmaf(flip(v + __ldg(jo + col[c]), ph), __ldg(in + col[c]), part[c]);
           }
       }
-      const uint32_t d0 = __ldg(T.off_d + row), d1 = __ldg(T.off_d + row + 1);
+      const uint32_t d0 = __ldg(Tb.off_d + row), d1 = __ldg(Tb.off_d + row + 1);
       for (uint32_t p = d0; p < d1; ++p) {
-        const uint32_t ket = __ldg(T.ket_d + p);
-        const double v = __ldg(T.val_d + p);
-        const uint64_t m = __ldg(T.mask_d + p);
-        const double *in = In + (size_t)ket * ldin;
+        const uint32_t ket = __ldg(Tb.ket_d + p);
+        const T v = __ldg(vd + p);
+        const uint64_t m = __ldg(Tb.mask_d + p);
+        const T *in = In + (size_t)ket * ldin;
 #pragma unroll
         for (int c = 0; c < CPT; ++c)
           if (ok[c]) {
             const uint32_t ph = __popcll(opp[c] & m) & 1u;
-            acc[r][c] = fma(flip(v, ph), __ldg(in + col[c]), acc[r][c]);
+            if constexpr (kF64)
+              acc[r][c] = fma(flip(v, ph), __ldg(in + col[c]), acc[r][c]);
+            else
+              part[c] = fmaf(flip(v, ph), __ldg(in + col[c]), part[c]);
           }
+      }
+      if constexpr (!kF64) {
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) acc[r][c] += (double)part[c];
       }
     }
   }
@@ -94,8 +132,9 @@ __device__ __forceinline__ uint32_t ab_phase(uint64_t alpha, uint64_t beta, int 
   return ph & 1u;
 }
 
-template <int TA, int CPT>
-__global__ void __launch_bounds__(kThreads) k_sigma_alpha(SigmaArgs a) {
+template <int TA, int CPT, typename T>
+__global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
+  constexpr bool kF64 = std::is_same<T, double>::value;
   constexpr int TB = kThreads * CPT;
   const uint32_t ia0 = blockIdx.x * TA;
   const uint32_t ib0 = blockIdx.y * TB;
@@ -109,7 +148,7 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(SigmaArgs a) {
     beta[c] = ok[c] ? __ldg(a.bstr + col[c]) : 0ull;
   }
   double acc[TA][CPT];
-  // diagonal term (mult.h:169-174)
+  // diagonal term (mult.h:169-174), FP64 diagonal in both forms
 #pragma unroll
   for (int r = 0; r < TA; ++r)
 #pragma unroll
@@ -118,23 +157,26 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(SigmaArgs a) {
       acc[r][c] = 0.0;
       if (ok[c] && ia < a.na) {
         const size_t k = (size_t)ia * a.nb + col[c];
-        acc[r][c] = __ldg(a.hii + k) * __ldg(a.C + k);
+        acc[r][c] = __ldg(a.hii + k) * (double)__ldg(a.C + k);
       }
     }
   // alpha singles and doubles (task type 2, mult.h:450-488)
-  same_spin_sweep<TA, CPT>(a.A, a.Jb, a.nb, a.C, a.nb, ia0, a.na, col, ok, beta, acc);
+  same_spin_sweep<TA, CPT, T>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, a.C, a.nb, ia0, a.na, col, ok, beta, acc);
   // alpha single x beta single (task type 0, mult.h:527-557)
 #pragma unroll
   for (int r = 0; r < TA; ++r) {
     const uint32_t ia = ia0 + r;
     if (ia < a.na) {
       const uint64_t alpha = __ldg(a.astr + ia);
+      T part[CPT];
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) part[c] = T(0);
       const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
       for (uint32_t p = p0; p < p1; ++p) {
         const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
         const int cra = ca & 0xff, ana = (ca >> 8) & 0xff;
-        const double *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
-        const double *crow = a.C + (size_t)ja * a.nb;
+        const T *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
+        const T *crow = a.C + (size_t)ja * a.nb;
 #pragma unroll
         for (int c = 0; c < CPT; ++c)
           if (ok[c]) {
@@ -142,9 +184,17 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(SigmaArgs a) {
             for (uint32_t q = q0; q < q1; ++q) {
               const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
               const uint32_t ph = ab_phase(alpha, beta[c], cra, ana, cb & 0xff, (cb >> 8) & 0xff);
-              acc[r][c] = fma(flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph), __ldg(crow + jb), acc[r][c]);
+              const T kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
+              if constexpr (kF64)
+                acc[r][c] = fma(kv, __ldg(crow + jb), acc[r][c]);
+              else
+                part[c] = fmaf(kv, __ldg(crow + jb), part[c]);
             }
           }
+      }
+      if constexpr (!kF64) {
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) acc[r][c] += (double)part[c];
       }
     }
   }
@@ -155,15 +205,15 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(SigmaArgs a) {
       const uint32_t ia = ia0 + r;
       if (ok[c] && ia < a.na) {
         const size_t k = (size_t)ia * a.nb + col[c];
-        a.S[k] = a.accumulate ? a.S[k] + acc[r][c] : acc[r][c];
+        a.S[k] = (T)(a.accumulate ? (double)a.S[k] + acc[r][c] : acc[r][c]);
       }
     }
 }
 
 // beta singles and doubles (task type 1, mult.h:489-525) on the transposed
 // vector; adds its TA consecutive beta entries of each alpha row into sigma.
-template <int TA, int CPT>
-__global__ void __launch_bounds__(kThreads) k_sigma_beta(SigmaArgs a) {
+template <int TA, int CPT, typename T>
+__global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
   constexpr int TB = kThreads * CPT;
   const uint32_t ib0 = blockIdx.x * TA;
   const uint32_t ia0 = blockIdx.y * TB;
@@ -181,15 +231,15 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(SigmaArgs a) {
   for (int r = 0; r < TA; ++r)
 #pragma unroll
     for (int c = 0; c < CPT; ++c) acc[r][c] = 0.0;
-  same_spin_sweep<TA, CPT>(a.B, a.Ja, a.na, a.CT, a.na, ib0, a.nb, col, ok, alpha, acc);
+  same_spin_sweep<TA, CPT, T>(a.B, a.val_sb, a.val_db, a.Ja, a.na, a.CT, a.na, ib0, a.nb, col, ok, alpha, acc);
 #pragma unroll
   for (int c = 0; c < CPT; ++c)
     if (ok[c]) {
-      double *srow = a.S + (size_t)col[c] * a.nb;
+      T *srow = a.S + (size_t)col[c] * a.nb;
 #pragma unroll
       for (int r = 0; r < TA; ++r) {
         const uint32_t ib = ib0 + r;
-        if (ib < a.nb) srow[ib] += acc[r][c];
+        if (ib < a.nb) srow[ib] = (T)((double)srow[ib] + acc[r][c]);
       }
     }
 }
@@ -210,11 +260,67 @@ __global__ void k_transpose(const T *__restrict__ in, T *__restrict__ out, uint3
   }
 }
 
+__global__ void k_to_float(const double *__restrict__ x, float *__restrict__ y, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    y[e] = (float)x[e];
+}
+
 constexpr int kTA = 8;
 constexpr int kCPT = 2;
 
-SigmaArgs make_args(Problem &p, const double *C, double *S, int accumulate) {
-  SigmaArgs a;
+template <typename T>
+void launch(Problem &p, const Args<T> &a, cudaStream_t s) {
+  constexpr int TB = kThreads * kCPT;
+  dim3 ga((p.na + kTA - 1) / kTA, (p.nb + TB - 1) / TB);
+  k_sigma_alpha<kTA, kCPT, T><<<ga, kThreads, 0, s>>>(a);
+  dim3 gb((p.nb + kTA - 1) / kTA, (p.na + TB - 1) / TB);
+  k_sigma_beta<kTA, kCPT, T><<<gb, kThreads, 0, s>>>(a);
+  count_launch(p.ctx, 2);
+  SBDGB_CUDA(cudaGetLastError());
+}
+
+template <typename T>
+void transpose(Problem &p, const T *in, T *out, uint32_t R, uint32_t Cn, cudaStream_t s) {
+  dim3 grid((Cn + 31) / 32, (R + 31) / 32), block(32, 8);
+  k_transpose<T><<<grid, block, 0, s>>>(in, out, R, Cn);
+  count_launch(p.ctx);
+}
+
+void to_float(Problem &p, const double *x, float *y, size_t n, cudaStream_t s) {
+  if (n == 0) return;
+  unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
+  k_to_float<<<blocks, 256, 0, s>>>(x, y, n);
+  count_launch(p.ctx);
+}
+
+template <typename T>
+void begin_timing(Problem &p, cudaStream_t s, cudaEvent_t &ev0, cudaEvent_t &ev1) {
+  if (!p.ctx->timing) return;
+  ev0 = timing_event(p.ctx);
+  ev1 = timing_event(p.ctx);
+  SBDGB_CUDA(cudaEventRecord(ev0, s));
+}
+
+void end_timing(Problem &p, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
+  if (!ev1) return;
+  SBDGB_CUDA(cudaEventRecord(ev1, s));
+  p.ctx->sigma_events.emplace_back(ev0, ev1);
+}
+
+}  // namespace
+
+void transpose_fp64(Problem &p, const double *in, double *out, uint32_t R, uint32_t Cn, cudaStream_t s) {
+  transpose<double>(p, in, out, R, Cn, s);
+}
+
+void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s) {
+  if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "sigma needs tables and diagonal");
+  if (!p.CT) p.CT = (double *)dev_alloc(p, sizeof(double) * p.N);
+  if (p.N == 0) return;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  begin_timing<double>(p, s, ev0, ev1);
+  transpose<double>(p, C, p.CT, p.na, p.nb, s);
+  Args<double> a;
   a.astr = p.astr;
   a.bstr = p.bstr;
   a.na = p.na;
@@ -226,37 +332,70 @@ SigmaArgs make_args(Problem &p, const double *C, double *S, int accumulate) {
   a.accumulate = accumulate;
   a.A = p.A;
   a.B = p.B;
+  a.val_sa = p.A.val_s;
+  a.val_da = p.A.val_d;
+  a.val_sb = p.B.val_s;
+  a.val_db = p.B.val_d;
   a.Jb = p.Jb;
   a.Ja = p.Ja;
   a.Kp = p.Kp;
   a.npair = p.npair;
-  a.norb = p.norb;
-  return a;
+  launch<double>(p, a, s);
+  end_timing(p, s, ev0, ev1);
 }
 
-}  // namespace
-
-void transpose_fp64(Problem &p, const double *in, double *out, uint32_t R, uint32_t Cn, cudaStream_t s) {
-  dim3 grid((Cn + 31) / 32, (R + 31) / 32), block(32, 8);
-  k_transpose<double><<<grid, block, 0, s>>>(in, out, R, Cn);
-  count_launch(p.ctx);
-}
-
-void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s) {
-  if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "sigma needs tables and diagonal");
-  if (!p.CT) {
-    p.CT = (double *)dev_alloc(p, sizeof(double) * p.N);
+// FP32 copies of the table values and integral tables used by the mixed form.
+void prepare_mixed(Problem &p, cudaStream_t s) {
+  if (p.mixed_ready) return;
+  if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "mixed sigma needs tables and diagonal");
+  const size_t npp = (size_t)p.npair * p.npair;
+  p.Kpf = (float *)dev_alloc(p, sizeof(float) * npp);
+  p.Jbf = (float *)dev_alloc(p, sizeof(float) * (size_t)p.npair * p.nb);
+  p.Jaf = (float *)dev_alloc(p, sizeof(float) * (size_t)p.npair * p.na);
+  to_float(p, p.Kp, p.Kpf, npp, s);
+  to_float(p, p.Jb, p.Jbf, (size_t)p.npair * p.nb, s);
+  to_float(p, p.Ja, p.Jaf, (size_t)p.npair * p.na, s);
+  for (int sp = 0; sp < 2; ++sp) {
+    SpinTables &T = sp == 0 ? p.A : p.B;
+    p.val_sf[sp] = (float *)dev_alloc(p, sizeof(float) * (T.ns ? T.ns : 1));
+    p.val_df[sp] = (float *)dev_alloc(p, sizeof(float) * (T.nd ? T.nd : 1));
+    to_float(p, T.val_s, p.val_sf[sp], T.ns, s);
+    to_float(p, T.val_d, p.val_df[sp], T.nd, s);
   }
-  if (p.N == 0) return;
-  transpose_fp64(p, C, p.CT, p.na, p.nb, s);
-  SigmaArgs a = make_args(p, C, S, accumulate);
-  constexpr int TB = kThreads * kCPT;
-  dim3 ga((p.na + kTA - 1) / kTA, (p.nb + TB - 1) / TB);
-  k_sigma_alpha<kTA, kCPT><<<ga, kThreads, 0, s>>>(a);
-  dim3 gb((p.nb + kTA - 1) / kTA, (p.na + TB - 1) / TB);
-  k_sigma_beta<kTA, kCPT><<<gb, kThreads, 0, s>>>(a);
-  count_launch(p.ctx, 2);
   SBDGB_CUDA(cudaGetLastError());
+  SBDGB_CUDA(cudaStreamSynchronize(s));
+  p.mixed_ready = true;
+}
+
+void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s) {
+  prepare_mixed(p, s);
+  if (!p.CTf) p.CTf = (float *)dev_alloc(p, sizeof(float) * p.N);
+  if (p.N == 0) return;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  begin_timing<float>(p, s, ev0, ev1);
+  transpose<float>(p, C, p.CTf, p.na, p.nb, s);
+  Args<float> a;
+  a.astr = p.astr;
+  a.bstr = p.bstr;
+  a.na = p.na;
+  a.nb = p.nb;
+  a.hii = p.hii;
+  a.C = C;
+  a.CT = p.CTf;
+  a.S = S;
+  a.accumulate = 0;
+  a.A = p.A;
+  a.B = p.B;
+  a.val_sa = p.val_sf[0];
+  a.val_da = p.val_df[0];
+  a.val_sb = p.val_sf[1];
+  a.val_db = p.val_df[1];
+  a.Jb = p.Jbf;
+  a.Ja = p.Jaf;
+  a.Kp = p.Kpf;
+  a.npair = p.npair;
+  launch<float>(p, a, s);
+  end_timing(p, s, ev0, ev1);
 }
 
 }  // namespace sbdgb

@@ -20,7 +20,7 @@ FP64, MIXED = 0, 1
 
 SYMBOLS = [
     "sbdgb_abi_version", "sbdgb_ctx_create", "sbdgb_ctx_destroy", "sbdgb_last_error", "sbdgb_ctx_bytes_in_use",
-    "sbdgb_ctx_launch_count", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
+    "sbdgb_ctx_launch_count", "sbdgb_ctx_set_stream", "sbdgb_ctx_enable_timing", "sbdgb_ctx_sigma_timing", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
     "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
     "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
     "sbdgb_davidson",
@@ -75,6 +75,9 @@ def load(path: str = LIB_PATH):
     L.sbdgb_ctx_launch_count.argtypes = [vp]
     L.sbdgb_ctx_launch_count.restype = C.c_uint64
     L.sbdgb_check_comm_sizes.argtypes = [vp, C.c_int, C.c_int, C.c_int]
+    L.sbdgb_ctx_set_stream.argtypes = [vp, vp]
+    L.sbdgb_ctx_enable_timing.argtypes = [vp, C.c_int]
+    L.sbdgb_ctx_sigma_timing.argtypes = [vp, C.POINTER(C.c_uint64), C.POINTER(C.c_double)]
     L.sbdgb_problem_create.argtypes = [vp, C.c_int, _u64p, C.c_size_t, _u64p, C.c_size_t, _f64p, _f64p,
                                        C.c_double, C.POINTER(vp)]
     L.sbdgb_problem_destroy.argtypes = [vp]
@@ -126,6 +129,19 @@ class Engine:
     @property
     def launches(self) -> int:
         return int(self.lib.sbdgb_ctx_launch_count(self.h))
+
+    def set_stream(self, stream: int | None):
+        """Runs later calls on the caller's cudaStream_t (None: the context's own stream)."""
+        self.check(self.lib.sbdgb_ctx_set_stream(self.h, stream or None))
+
+    def enable_timing(self, on: bool = True):
+        self.check(self.lib.sbdgb_ctx_enable_timing(self.h, int(on)))
+
+    def sigma_timing(self) -> tuple[int, float]:
+        """(sigma products, summed device milliseconds) since the last call."""
+        n, ms = C.c_uint64(0), C.c_double(0.0)
+        self.check(self.lib.sbdgb_ctx_sigma_timing(self.h, C.byref(n), C.byref(ms)))
+        return int(n.value), float(ms.value)
 
     def check_comm_sizes(self, h: int, b: int, t: int):
         self.check(self.lib.sbdgb_check_comm_sizes(self.h, h, b, t))

@@ -1,0 +1,40 @@
+"""The C++ mirror (include/sbdgb/tpb.hpp) used like the reference app: FCIDUMP
+and string files in, diag, <W|H|W> out -- compiled with g++ against the C ABI."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from golden_io import load
+from sbd_gb300 import build
+from sbd_gb300.fcidump import Integrals, write_fcidump
+from sbd_gb300.strings import write_strings
+
+pytestmark = pytest.mark.gpu
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def exe(tmp_path_factory):
+    lib = build.build()
+    out = str(tmp_path_factory.mktemp("cpp") / "tpb_drop_in")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "tpb_drop_in.cpp"), "-L" + os.path.dirname(lib), "-lsbdgb",
+                    "-Wl,-rpath," + os.path.dirname(lib), "-o", out], check=True)
+    return out
+
+
+@pytest.mark.parametrize("name", ["open_L10", "wide_L36"])
+def test_cpp_drop_in_matches_reference_energy(exe, tmp_path, name):
+    c = load(name)
+    ints = Integrals(norb=c.norb, nelec=0, ecore=c.ecore, h1=c.h1, eri=c.eri)
+    write_fcidump(str(tmp_path / "fcidump.txt"), ints)
+    write_strings(str(tmp_path / "a.txt"), c.astr, c.norb)
+    write_strings(str(tmp_path / "b.txt"), c.bstr, c.norb)
+    r = subprocess.run([exe, "--fcidump", str(tmp_path / "fcidump.txt"), "--adetfile", str(tmp_path / "a.txt"),
+                        "--bdetfile", str(tmp_path / "b.txt"), "--block", "12", "--iteration", "200",
+                        "--tolerance", "1e-10"], capture_output=True, text=True, check=True)
+    e = float(re.search(r"Energy = ([-0-9.eE+]+)", r.stdout).group(1))
+    assert abs(e - c.energy) < 1e-8

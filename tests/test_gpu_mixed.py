@@ -1,0 +1,51 @@
+"""Mixed precision (FP32 vectors and products, FP64 accumulation, FP64
+refinement) against the plain FP64 path, through the C ABI."""
+import numpy as np
+import pytest
+
+from golden_io import load, max_rel
+from sbd_gb300.engine import MIXED, TPBProblem
+from sbd_gb300.generators import make_problem
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mixed_sigma_close_to_fp64(engine):
+    torch = pytest.importorskip("torch")
+    prob = make_problem(16, 5, 5, 300, 280, seed=31)
+    p = TPBProblem.from_problem(engine, prob)
+    p.build_tables()
+    p.diag_terms()
+    C = np.random.default_rng(2).uniform(-1, 1, prob.ndet)
+    ref = p.mult(C)
+    c32 = torch.tensor(C, dtype=torch.float32, device="cuda")
+    s32 = torch.zeros_like(c32)
+    p.sigma_mixed_device(c32.data_ptr(), s32.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    # FP32 storage of C and of the table values bounds the agreement near 1e-6
+    assert max_rel(s32.cpu().double().numpy(), ref) < 5e-6
+
+
+@pytest.mark.parametrize("name,k", [("cfg0_shape_L16", 1), ("spin_L12", 3), ("wide_L36", 2)])
+def test_mixed_davidson_matches_fp64(engine, name, k):
+    c = load(name)
+    p = TPBProblem(engine, c.norb, c.astr, c.bstr, c.h1, c.eri, c.ecore)
+    r64 = p.davidson(nroots=k, max_nb=16, eps=1e-9, init=1)
+    rmx = p.davidson(nroots=k, max_nb=16, eps=1e-9, init=1, precision=MIXED, refine_every=4)
+    assert r64.report["converged"] and rmx.report["converged"]
+    assert np.max(np.abs(rmx.energies - r64.energies)) < 1e-9
+    assert np.allclose(rmx.energies, c.lowest[:k], atol=1e-8, rtol=0)
+    assert rmx.report["sigma_fp64"] < rmx.report["sigma_calls"]
+    # same eigenvectors up to sign
+    for q in range(k):
+        ov = abs(float(rmx.vectors[q] @ r64.vectors[q]))
+        assert ov > 1 - 1e-8
+
+
+def test_mixed_davidson_config0_shape(engine):
+    prob = make_problem(16, 5, 5, 800, seed=0, closed_shell=True)
+    p = TPBProblem.from_problem(engine, prob)
+    r64 = p.davidson(nroots=1, max_nb=20, eps=1e-8, init=1, want_vectors=False)
+    rmx = p.davidson(nroots=1, max_nb=20, eps=1e-8, init=1, precision=MIXED, want_vectors=False)
+    assert r64.report["converged"] and rmx.report["converged"]
+    assert abs(rmx.energies[0] - r64.energies[0]) < 1e-6

@@ -118,7 +118,8 @@ int sbdgb_diag_terms(sbdgb_problem *p, double *hii_out);
 /* sigma (sbd::mult, chemistry/tpb/mult.h:114-130; MultBase::run,
  * chemistry/basic/mult.h:19-103).  Wk_dev, Wb_dev: N = na*nb doubles of
  * device memory.  accumulate != 0 gives the reference's Wb += H*Wk,
- * accumulate == 0 writes Wb = H*Wk.  stream: a cudaStream_t or NULL. */
+ * accumulate == 0 writes Wb = H*Wk.  stream: a cudaStream_t, or NULL for the
+ * context's stream (pass cudaStreamLegacy for the legacy default stream). */
 int sbdgb_sigma(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accumulate, void *stream);
 /* Mixed-precision sigma: FP32 vectors, FP32 products, FP64 accumulation of
  * each element's sum, FP32 result. */

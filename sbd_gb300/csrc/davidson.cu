@@ -701,16 +701,14 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
   sbdgb_report r{};
   // anchors: starting vectors orthonormalised in FP64
   sv.start_vectors(o, k, T, Xout);
-  int na = 0;
   for (int q = 0; q < k; ++q) {
     double *t = T + (size_t)q * N;
-    const double left = sv.orthonormalize<double>(t, X, na);
+    const double left = sv.orthonormalize<double>(t, X, q);
     SBDGB_REQUIRE(left > 1e-8, SBDGB_E_INPUT, "starting vectors are linearly dependent");
-    SBDGB_CUDA(cudaMemcpyAsync(X + (size_t)na * N, t, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
-    na++;
+    SBDGB_CUDA(cudaMemcpyAsync(X + (size_t)q * N, t, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
   }
   std::vector<double> theta(k), resid(k, 0.0);
-  // FP64 sigma of the anchors, Rayleigh-Ritz among them, FP64 residuals
+  // FP64 sigma of the anchors, Rayleigh-Ritz among them, FP64 residual norms
   auto refine_rr = [&]() {
     for (int j = 0; j < k; ++j) {
       sigma_fp64(p, X + (size_t)j * N, S + (size_t)j * N, 0, s);
@@ -722,7 +720,8 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
     std::vector<double> G, th, Yv;
     sv.dots<double, double>(X, k, w.data(), k, G);
     for (int j = 0; j < k; ++j)
-      for (int i = 0; i < j; ++i) G[i + (size_t)k * j] = G[j + (size_t)k * i] = 0.5 * (G[i + (size_t)k * j] + G[j + (size_t)k * i]);
+      for (int i = 0; i < j; ++i)
+        G[i + (size_t)k * j] = G[j + (size_t)k * i] = 0.5 * (G[i + (size_t)k * j] + G[j + (size_t)k * i]);
     jacobi_eig(k, G, th, Yv);
     resid = sv.combine(X, S, k, k, Yv, th, T, Y, nullptr);
     SBDGB_CUDA(cudaMemcpyAsync(X, T, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, s));
@@ -731,30 +730,79 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
   };
   refine_rr();
 
+  // projected quantities of the basis [anchors, W]
+  std::vector<double> Sxw((size_t)k * mmax), Hxw((size_t)k * mmax), Sww((size_t)mmax * mmax),
+      Hww((size_t)mmax * mmax);
+  std::vector<double> cX((size_t)k * k, 0.0), cW, thc(k);  // current Ritz vectors: cX[j + k*q], cW[l + m*q]
+  int m = 0;
+  // Rayleigh-Ritz on span{anchors, W}: generalised problem with the exact overlaps
+  auto rayleigh_ritz = [&]() -> bool {
+    const int n = k + m;
+    std::vector<double> A((size_t)n * n, 0.0), B((size_t)n * n, 0.0), w, V;
+    for (int j = 0; j < k; ++j) {
+      A[j + (size_t)n * j] = theta[j];
+      B[j + (size_t)n * j] = 1.0;
+    }
+    for (int l = 0; l < m; ++l)
+      for (int j = 0; j < k; ++j) {
+        A[j + (size_t)n * (k + l)] = A[(k + l) + (size_t)n * j] = Hxw[j + (size_t)k * l];
+        B[j + (size_t)n * (k + l)] = B[(k + l) + (size_t)n * j] = Sxw[j + (size_t)k * l];
+      }
+    for (int l = 0; l < m; ++l)
+      for (int l2 = 0; l2 < m; ++l2) {
+        A[(k + l) + (size_t)n * (k + l2)] = Hww[l + (size_t)mmax * l2];
+        B[(k + l) + (size_t)n * (k + l2)] = Sww[l + (size_t)mmax * l2];
+      }
+    if (!gen_sym_eig(n, A, B, w, V)) return false;
+    cW.assign((size_t)m * k, 0.0);
+    for (int q = 0; q < k; ++q) {
+      thc[q] = w[q];
+      for (int j = 0; j < k; ++j) cX[j + (size_t)k * q] = V[j + (size_t)n * q];
+      for (int l = 0; l < m; ++l) cW[l + (size_t)m * q] = V[(k + l) + (size_t)n * q];
+    }
+    return true;
+  };
+  // couplings of the (new) anchors to the kept W columns
+  auto recouple = [&]() {
+    for (int l = 0; l < m; ++l) {
+      const float *wl[1] = {W + (size_t)l * N};
+      std::vector<double> g1, g2;
+      sv.dots<double, float>(X, k, wl, 1, g1);  // X^T w, FP64
+      sv.dots<float, float>(Rf, k, wl, 1, g2);  // R^T w, FP32 products
+      for (int j = 0; j < k; ++j) {
+        Sxw[j + (size_t)k * l] = g1[j];
+        Hxw[j + (size_t)k * l] = g2[j] + theta[j] * g1[j];  // S_j = R_j + theta_j X_j
+      }
+    }
+  };
+
   bool converged = false;
   int iter = 0;
   const int max_steps = std::max(1, o.max_it) * std::max(o.max_nb, 2 * k);
-  std::vector<double> Sxw((size_t)k * mmax), Hxw((size_t)k * mmax), Sww((size_t)mmax * mmax),
-      Hww((size_t)mmax * mmax);
   while (true) {
-    iter++;
-    r.iterations = iter;
-    if (o.verbose) print_iter(" (mixed, FP64 residual)", iter, resid, theta, k);
     converged = true;
     for (int q = 0; q < k; ++q) converged = converged && (resid[q] < o.eps);
+    if (o.verbose) print_iter(" (mixed, FP64 residual)", iter, resid, theta, k);
     double elapsed = std::chrono::duration<double>(clock::now() - t0).count();
     if (converged || iter >= max_steps || (o.max_time > 0 && elapsed > o.max_time)) break;
     // rounded anchors and residuals for the FP32 inner steps
     SBDGB_CUDA(cudaMemcpyAsync(sv.red + 2048, theta.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
     k_make_anchor_f32<<<sv.blocks, kRed, 0, s>>>(X, S, sv.red + 2048, k, N, Xf, Rf);
     count_launch(p.ctx);
-    // current Ritz vectors in the basis [anchors, W]: coefficients and values
-    std::vector<double> cX((size_t)k * k, 0.0), cW;  // cX[j + k*q], cW[l + m*q]
-    for (int q = 0; q < k; ++q) cX[q + (size_t)k * q] = 1.0;
-    std::vector<double> thc = theta, res_est = resid;
-    int m = 0;
-    bool stalled = false;
-    for (int inner = 0; inner < refine_every; ++inner) {
+    recouple();
+    bool ok_rr = true;
+    if (m > 0) {
+      ok_rr = rayleigh_ritz();
+    } else {
+      std::fill(cX.begin(), cX.end(), 0.0);
+      for (int q = 0; q < k; ++q) cX[q + (size_t)k * q] = 1.0;
+      cW.clear();
+      thc = theta;
+    }
+    std::vector<double> res_est = resid;
+    bool stalled = !ok_rr;
+    for (int inner = 0; inner < refine_every && !stalled; ++inner) {
+      if (m + k > mmax) break;
       const int m0 = m;
       for (int q = 0; q < k && m < mmax; ++q) {
         if (res_est[q] < o.eps) continue;
@@ -770,20 +818,17 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
         k_mixed_residual<<<sv.blocks, kRed, 0, s>>>(ma);
         count_launch(p.ctx);
         res_est[q] = std::sqrt(std::max(0.0, sv.reduce_partials(1)));
-        // orthogonalise against the (rounded) anchors, then against W, in FP32
-        double left = 1.0;
-        {
-          double n0 = sv.norm<float>(Tf);
-          if (!(n0 > 0.0) || !std::isfinite(n0)) continue;
-          sv.scale_copy<float, float>(Tf, Tf, 1.0 / n0);
-          for (int pass = 0; pass < 2; ++pass) {
-            std::vector<double> G;
-            const float *w[1] = {Tf};
-            sv.dots<float, float>(Xf, k, w, 1, G);
-            sv.project_out<float>(Xf, k, G, Tf, 1);
-          }
-          left = sv.orthonormalize<float>(Tf, W, m);
+        // orthogonalise against the rounded anchors, then against W, in FP32
+        double n0 = sv.norm<float>(Tf);
+        if (!(n0 > 0.0) || !std::isfinite(n0)) continue;
+        sv.scale_copy<float, float>(Tf, Tf, 1.0 / n0);
+        for (int pass = 0; pass < 2; ++pass) {
+          std::vector<double> G;
+          const float *w[1] = {Tf};
+          sv.dots<float, float>(Xf, k, w, 1, G);
+          sv.project_out<float>(Xf, k, G, Tf, 1);
         }
+        const double left = sv.orthonormalize<float>(Tf, W, m);
         if (!(left > 1e-3)) continue;  // no new direction in FP32
         SBDGB_CUDA(cudaMemcpyAsync(W + (size_t)m * N, Tf, sizeof(float) * N, cudaMemcpyDeviceToDevice, s));
         sigma_mixed(p, W + (size_t)m * N, HW + (size_t)m * N, s);
@@ -791,16 +836,15 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
         // projected quantities of the new column: anchor couplings in FP64
         const float *wn[1] = {W + (size_t)m * N};
         const float *hwn[1] = {HW + (size_t)m * N};
-        std::vector<double> g1, g2, g3, g4;
-        sv.dots<double, float>(X, k, wn, 1, g1);       // X^T w
-        sv.dots<float, float>(Rf, k, wn, 1, g2);       // R^T w
-        sv.dots<float, float>(W, m + 1, wn, 1, g3);    // W^T w
-        sv.dots<float, float>(W, m + 1, hwn, 1, g4);   // W^T Hw
-        std::vector<double> g5;
-        sv.dots<float, float>(HW, m + 1, wn, 1, g5);   // (HW)^T w
+        std::vector<double> g1, g2, g3, g4, g5;
+        sv.dots<double, float>(X, k, wn, 1, g1);     // X^T w
+        sv.dots<float, float>(Rf, k, wn, 1, g2);     // R^T w
+        sv.dots<float, float>(W, m + 1, wn, 1, g3);  // W^T w
+        sv.dots<float, float>(W, m + 1, hwn, 1, g4); // W^T Hw
+        sv.dots<float, float>(HW, m + 1, wn, 1, g5); // (HW)^T w
         for (int j = 0; j < k; ++j) {
           Sxw[j + (size_t)k * m] = g1[j];
-          Hxw[j + (size_t)k * m] = g2[j] + theta[j] * g1[j];  // S_j = R_j + theta_j X_j
+          Hxw[j + (size_t)k * m] = g2[j] + theta[j] * g1[j];
         }
         for (int l = 0; l <= m; ++l) {
           Sww[l + (size_t)mmax * m] = Sww[m + (size_t)mmax * l] = g3[l];
@@ -813,36 +857,13 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
         stalled = true;
         break;
       }
-      // generalised Rayleigh-Ritz on [anchors, W]
-      const int n = k + m;
-      std::vector<double> A((size_t)n * n, 0.0), B((size_t)n * n, 0.0), w, V;
-      for (int j = 0; j < k; ++j) {
-        A[j + (size_t)n * j] = theta[j];
-        B[j + (size_t)n * j] = 1.0;
-      }
-      for (int l = 0; l < m; ++l)
-        for (int j = 0; j < k; ++j) {
-          A[j + (size_t)n * (k + l)] = A[(k + l) + (size_t)n * j] = Hxw[j + (size_t)k * l];
-          B[j + (size_t)n * (k + l)] = B[(k + l) + (size_t)n * j] = Sxw[j + (size_t)k * l];
-        }
-      for (int l = 0; l < m; ++l)
-        for (int l2 = 0; l2 < m; ++l2) {
-          A[(k + l) + (size_t)n * (k + l2)] = Hww[l + (size_t)mmax * l2];
-          B[(k + l) + (size_t)n * (k + l2)] = Sww[l + (size_t)mmax * l2];
-        }
-      if (!gen_sym_eig(n, A, B, w, V)) {
+      if (!rayleigh_ritz()) {
         stalled = true;
         break;
       }
-      cW.assign((size_t)m * k, 0.0);
-      for (int q = 0; q < k; ++q) {
-        thc[q] = w[q];
-        for (int j = 0; j < k; ++j) cX[j + (size_t)k * q] = V[j + (size_t)n * q];
-        for (int l = 0; l < m; ++l) cW[l + (size_t)m * q] = V[(k + l) + (size_t)n * q];
-      }
-      if (++iter >= max_steps) break;
+      iter++;
       r.iterations = iter;
-      if (m + k > mmax) break;
+      if (iter >= max_steps) break;
     }
     // refinement: assemble the Ritz vectors in FP64, orthonormalise, FP64 sigma
     for (int q = 0; q < k; ++q) {
@@ -863,20 +884,23 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
     SBDGB_CUDA(cudaMemcpyAsync(X, T, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, s));
     r.restarts++;
     refine_rr();
-    if (stalled && m == 0) {
-      // nothing new in FP32 this cycle: the FP64 residual decides
+    if (m + k > mmax) m = 0;  // subspace full: the anchors carry its information on
+    if (stalled) {
       bool ok = true;
       for (int q = 0; q < k; ++q) ok = ok && resid[q] < o.eps;
-      if (!ok && o.verbose) printf(" mixed Davidson: FP32 subspace stalled\n");
       if (!ok) {
-        iter++;
-        break;
+        if (m == 0) {
+          if (o.verbose) printf(" mixed Davidson: no new FP32 direction\n");
+          break;
+        }
+        m = 0;  // start a fresh FP32 subspace from the refined anchors
       }
     }
   }
   converged = true;
   for (int q = 0; q < k; ++q) converged = converged && (resid[q] < o.eps);
   r.converged = converged ? 1 : 0;
+  r.iterations = std::max(r.iterations, iter);
   for (int q = 0; q < k && q < 16; ++q) r.resid[q] = resid[q];
   for (int q = 0; q < k; ++q) E[q] = theta[q];
   if (Xout) SBDGB_CUDA(cudaMemcpyAsync(Xout, X, sizeof(double) * N * k, cudaMemcpyDeviceToHost, s));

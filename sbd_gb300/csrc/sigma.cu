@@ -12,12 +12,22 @@
 //   kernel B  rows = beta strings, columns = alpha strings, reads C^T[jb][ia]
 //             sigma[ia][ib] += sum_beta-pairs +/- V * C^T[jb][ia]
 //
-// A CTA owns TA rows x (128*CPT) columns.  Every thread keeps its columns'
-// opposite-spin strings and TA*CPT accumulators in registers; the pair list of
-// a row is the same for all threads of the CTA, so its metadata are broadcast
-// loads and the ket-row reads are coalesced along the contiguous index.  Grid
-// order puts consecutive CTAs on the same column chunk so that the ket rows'
-// column slab stays resident in L2.
+// A CTA owns TA rows x (128*CPT) columns and walks its rows one at a time;
+// every thread keeps its columns' opposite-spin strings and CPT accumulators
+// in registers.  The pair list of a row is the same for all threads of the
+// CTA, so its metadata are broadcast loads and the ket-row reads are
+// coalesced along the contiguous index.  Grid order puts consecutive CTAs on
+// the same column chunk so that the ket rows' column slab stays in L2.
+//
+// Alpha-beta phase.  The reference evaluates TwoExcite (determinants.h:
+// 500-518) on the bra determinant with i = 2 cr_a, j = 2 cr_b + 1,
+// a = 2 an_a, b = 2 an_b + 1, and the value (an_a cr_a|an_b cr_b) with a
+// minus sign when A and I have different spins.  That sign equals the
+// product of the alpha single's phase on the bra and the beta single's phase
+// on the determinant after the alpha move (alpha string ja, beta string ib);
+// tests/test_sign_factorisation.py checks the identity exhaustively on small
+// orbital sets.  Both phases are stored in the single-excitation tables, so
+// an alpha-beta element costs two popcounts.
 //
 // The mixed form (T = float) stores C, sigma and the table values in FP32,
 // forms each pair-list sum in FP32 and adds it to an FP64 accumulator per
@@ -57,79 +67,58 @@ struct Args {
   int npair;
 };
 
-// Same-spin excitations of rows r0 .. r0+TA-1 applied to this thread's CPT
-// columns.  In: ket-major input rows (ld = ldin); Jo: opposite-spin Coulomb
-// table [npair][ldj] for the single excitations.
-template <int TA, int CPT, typename T>
-__device__ __forceinline__ void same_spin_sweep(const SpinTables &Tb, const T *__restrict__ vs,
-                                                const T *__restrict__ vd, const T *__restrict__ Jo, size_t ldj,
-                                                const T *__restrict__ In, size_t ldin, uint32_t r0, uint32_t nrow,
-                                                const uint32_t (&col)[CPT], const bool (&ok)[CPT],
-                                                const uint64_t (&opp)[CPT], double (&acc)[TA][CPT]) {
+// Same-spin excitations of one row applied to this thread's CPT columns.
+// In: ket-major input rows (ld = ldin); Jo: opposite-spin Coulomb table
+// [npair][ldj] for the single excitations.
+template <int CPT, typename T>
+__device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__restrict__ vs,
+                                              const T *__restrict__ vd, const T *__restrict__ Jo, size_t ldj,
+                                              const T *__restrict__ In, size_t ldin, uint32_t row,
+                                              const uint32_t (&col)[CPT], const bool (&ok)[CPT],
+                                              const uint64_t (&opp)[CPT], double (&acc)[CPT]) {
   constexpr bool kF64 = std::is_same<T, double>::value;
+  T part[CPT];
 #pragma unroll
-  for (int r = 0; r < TA; ++r) {
-    const uint32_t row = r0 + r;
-    if (row < nrow) {
-      T part[CPT];
+  for (int c = 0; c < CPT; ++c) part[c] = T(0);
+  const uint32_t p0 = __ldg(Tb.off_s + row), p1 = __ldg(Tb.off_s + row + 1);
+  for (uint32_t p = p0; p < p1; ++p) {
+    const uint32_t ket = __ldg(Tb.ket_s + p), code = __ldg(Tb.code_s + p);
+    const T v = __ldg(vs + p);
+    const uint64_t m = __ldg(Tb.mask_s + p);
+    const T *in = In + (size_t)ket * ldin;
+    const T *jo = Jo + (size_t)((code >> 16) & 0x7fffu) * ldj;
+    const uint32_t sg = code >> 31;
 #pragma unroll
-      for (int c = 0; c < CPT; ++c) part[c] = T(0);
-      const uint32_t p0 = __ldg(Tb.off_s + row), p1 = __ldg(Tb.off_s + row + 1);
-      for (uint32_t p = p0; p < p1; ++p) {
-        const uint32_t ket = __ldg(Tb.ket_s + p), code = __ldg(Tb.code_s + p);
-        const T v = __ldg(vs + p);
-        const uint64_t m = __ldg(Tb.mask_s + p);
-        const T *in = In + (size_t)ket * ldin;
-        const T *jo = Jo + (size_t)((code >> 16) & 0x7fffu) * ldj;
-        const uint32_t sg = code >> 31;
-#pragma unroll
-        for (int c = 0; c < CPT; ++c)
-          if (ok[c]) {
-            const uint32_t ph = (__popcll(opp[c] & m) ^ sg) & 1u;
-            if constexpr (kF64)
-              acc[r][c] = fma(flip(v + __ldg(jo + col[c]), ph), __ldg(in + col[c]), acc[r][c]);
-            else
-              part[c] = fmaf(flip(v + __ldg(jo + col[c]), ph), __ldg(in + col[c]), part[c]);
-          }
+    for (int c = 0; c < CPT; ++c)
+      if (ok[c]) {
+        const uint32_t ph = (__popcll(opp[c] & m) ^ sg) & 1u;
+        if constexpr (kF64)
+          acc[c] = fma(flip(v + __ldg(jo + col[c]), ph), __ldg(in + col[c]), acc[c]);
+        else
+          part[c] = fmaf(flip(v + __ldg(jo + col[c]), ph), __ldg(in + col[c]), part[c]);
       }
-      const uint32_t d0 = __ldg(Tb.off_d + row), d1 = __ldg(Tb.off_d + row + 1);
-      for (uint32_t p = d0; p < d1; ++p) {
-        const uint32_t ket = __ldg(Tb.ket_d + p);
-        const T v = __ldg(vd + p);
-        const uint64_t m = __ldg(Tb.mask_d + p);
-        const T *in = In + (size_t)ket * ldin;
-#pragma unroll
-        for (int c = 0; c < CPT; ++c)
-          if (ok[c]) {
-            const uint32_t ph = __popcll(opp[c] & m) & 1u;
-            if constexpr (kF64)
-              acc[r][c] = fma(flip(v, ph), __ldg(in + col[c]), acc[r][c]);
-            else
-              part[c] = fmaf(flip(v, ph), __ldg(in + col[c]), part[c]);
-          }
-      }
-      if constexpr (!kF64) {
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) acc[r][c] += (double)part[c];
-      }
-    }
   }
-}
-
-// Phase of an alpha-single x beta-single element: TwoExcite
-// (determinants.h:500-518) with i = 2 cr_a, j = 2 cr_b + 1, a = 2 an_a,
-// b = 2 an_b + 1 on the bra determinant; the integral is (an_a cr_a|an_b cr_b)
-// with a minus sign when A and I have different spins.
-__device__ __forceinline__ uint32_t ab_phase(uint64_t alpha, uint64_t beta, int cra, int ana, int crb, int anb) {
-  const int i = 2 * cra, j = 2 * crb + 1, a = 2 * ana, b = 2 * anb + 1;
-  const int I = min(i, j), J = max(i, j), A = min(a, b), B = max(a, b);
-  uint64_t ma1, mb1, ma2, mb2;
-  interval_masks(min(I, A), max(I, A), ma1, mb1);
-  interval_masks(min(J, B), max(J, B), ma2, mb2);
-  uint32_t ph = __popcll(alpha & (ma1 ^ ma2)) + __popcll(beta & (mb1 ^ mb2));
-  ph += (A > J || B < I) ? 1u : 0u;
-  ph += ((A ^ I) & 1) ? 1u : 0u;
-  return ph & 1u;
+  const uint32_t d0 = __ldg(Tb.off_d + row), d1 = __ldg(Tb.off_d + row + 1);
+#pragma unroll 2
+  for (uint32_t p = d0; p < d1; ++p) {
+    const uint32_t ket = __ldg(Tb.ket_d + p);
+    const T v = __ldg(vd + p);
+    const uint64_t m = __ldg(Tb.mask_d + p);
+    const T *in = In + (size_t)ket * ldin;
+#pragma unroll
+    for (int c = 0; c < CPT; ++c)
+      if (ok[c]) {
+        const uint32_t ph = __popcll(opp[c] & m) & 1u;
+        if constexpr (kF64)
+          acc[c] = fma(flip(v, ph), __ldg(in + col[c]), acc[c]);
+        else
+          part[c] = fmaf(flip(v, ph), __ldg(in + col[c]), part[c]);
+      }
+  }
+  if constexpr (!kF64) {
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) acc[c] += (double)part[c];
+  }
 }
 
 template <int TA, int CPT, typename T>
@@ -138,7 +127,7 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
   constexpr int TB = kThreads * CPT;
   const uint32_t ia0 = blockIdx.x * TA;
   const uint32_t ib0 = blockIdx.y * TB;
-  uint32_t col[CPT];
+  uint32_t col[CPT], q0[CPT], q1[CPT];
   bool ok[CPT];
   uint64_t beta[CPT];
 #pragma unroll
@@ -146,75 +135,66 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
     col[c] = ib0 + threadIdx.x + kThreads * c;
     ok[c] = col[c] < a.nb;
     beta[c] = ok[c] ? __ldg(a.bstr + col[c]) : 0ull;
+    q0[c] = ok[c] ? __ldg(a.B.off_s + col[c]) : 0u;
+    q1[c] = ok[c] ? __ldg(a.B.off_s + col[c] + 1) : 0u;
   }
-  double acc[TA][CPT];
-  // diagonal term (mult.h:169-174), FP64 diagonal in both forms
-#pragma unroll
-  for (int r = 0; r < TA; ++r)
-#pragma unroll
-    for (int c = 0; c < CPT; ++c) {
-      const uint32_t ia = ia0 + r;
-      acc[r][c] = 0.0;
-      if (ok[c] && ia < a.na) {
-        const size_t k = (size_t)ia * a.nb + col[c];
-        acc[r][c] = __ldg(a.hii + k) * (double)__ldg(a.C + k);
-      }
-    }
-  // alpha singles and doubles (task type 2, mult.h:450-488)
-  same_spin_sweep<TA, CPT, T>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, a.C, a.nb, ia0, a.na, col, ok, beta, acc);
-  // alpha single x beta single (task type 0, mult.h:527-557)
-#pragma unroll
-  for (int r = 0; r < TA; ++r) {
+  const uint32_t rend = min(TA, a.na - ia0);
+#pragma unroll 1
+  for (uint32_t r = 0; r < rend; ++r) {
     const uint32_t ia = ia0 + r;
-    if (ia < a.na) {
-      const uint64_t alpha = __ldg(a.astr + ia);
-      T part[CPT];
+    double acc[CPT];
+    // diagonal term (mult.h:169-174), FP64 diagonal in both forms
 #pragma unroll
-      for (int c = 0; c < CPT; ++c) part[c] = T(0);
-      const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
-      for (uint32_t p = p0; p < p1; ++p) {
-        const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
-        const int cra = ca & 0xff, ana = (ca >> 8) & 0xff;
-        const T *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
-        const T *crow = a.C + (size_t)ja * a.nb;
+    for (int c = 0; c < CPT; ++c) {
+      const size_t k = (size_t)ia * a.nb + col[c];
+      acc[c] = ok[c] ? __ldg(a.hii + k) * (double)__ldg(a.C + k) : 0.0;
+    }
+    // alpha singles and doubles (task type 2, mult.h:450-488)
+    same_spin_row<CPT, T>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, a.C, a.nb, ia, col, ok, beta, acc);
+    // alpha single x beta single (task type 0, mult.h:527-557)
+    T part[CPT];
 #pragma unroll
-        for (int c = 0; c < CPT; ++c)
-          if (ok[c]) {
-            const uint32_t q0 = __ldg(a.B.off_s + col[c]), q1 = __ldg(a.B.off_s + col[c] + 1);
-            for (uint32_t q = q0; q < q1; ++q) {
-              const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-              const uint32_t ph = ab_phase(alpha, beta[c], cra, ana, cb & 0xff, (cb >> 8) & 0xff);
-              const T kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
-              if constexpr (kF64)
-                acc[r][c] = fma(kv, __ldg(crow + jb), acc[r][c]);
-              else
-                part[c] = fmaf(kv, __ldg(crow + jb), part[c]);
-            }
-          }
+    for (int c = 0; c < CPT; ++c) part[c] = T(0);
+    const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
+    for (uint32_t p = p0; p < p1; ++p) {
+      const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
+      const uint64_t ma = __ldg(a.A.mask_s + p);
+      const uint64_t alpha_ket = __ldg(a.astr + ja);
+      const T *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
+      const T *crow = a.C + (size_t)ja * a.nb;
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) {
+        const uint32_t pa = (__popcll(beta[c] & ma) ^ (ca >> 31)) & 1u;
+        for (uint32_t q = q0[c]; q < q1[c]; ++q) {
+          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+          const uint64_t mb = __ldg(a.B.mask_s + q);
+          const uint32_t ph = (pa ^ __popcll(alpha_ket & mb) ^ (cb >> 31)) & 1u;
+          const T kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
+          if constexpr (kF64)
+            acc[c] = fma(kv, __ldg(crow + jb), acc[c]);
+          else
+            part[c] = fmaf(kv, __ldg(crow + jb), part[c]);
+        }
       }
-      if constexpr (!kF64) {
+    }
 #pragma unroll
-        for (int c = 0; c < CPT; ++c) acc[r][c] += (double)part[c];
+    for (int c = 0; c < CPT; ++c) {
+      if constexpr (!kF64) acc[c] += (double)part[c];
+      if (ok[c]) {
+        const size_t k = (size_t)ia * a.nb + col[c];
+        a.S[k] = (T)(a.accumulate ? (double)a.S[k] + acc[c] : acc[c]);
       }
     }
   }
-#pragma unroll
-  for (int r = 0; r < TA; ++r)
-#pragma unroll
-    for (int c = 0; c < CPT; ++c) {
-      const uint32_t ia = ia0 + r;
-      if (ok[c] && ia < a.na) {
-        const size_t k = (size_t)ia * a.nb + col[c];
-        a.S[k] = (T)(a.accumulate ? (double)a.S[k] + acc[r][c] : acc[r][c]);
-      }
-    }
 }
 
 // beta singles and doubles (task type 1, mult.h:489-525) on the transposed
-// vector; adds its TA consecutive beta entries of each alpha row into sigma.
+// vector.  Row results are staged in shared memory; each thread then adds the
+// TA consecutive beta entries of its alpha rows into sigma.
 template <int TA, int CPT, typename T>
 __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
   constexpr int TB = kThreads * CPT;
+  __shared__ double tile[TA][TB];
   const uint32_t ib0 = blockIdx.x * TA;
   const uint32_t ia0 = blockIdx.y * TB;
   uint32_t col[CPT];
@@ -226,21 +206,22 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
     ok[c] = col[c] < a.na;
     alpha[c] = ok[c] ? __ldg(a.astr + col[c]) : 0ull;
   }
-  double acc[TA][CPT];
+  const uint32_t rend = min(TA, a.nb - ib0);
+#pragma unroll 1
+  for (uint32_t r = 0; r < rend; ++r) {
+    double acc[CPT];
 #pragma unroll
-  for (int r = 0; r < TA; ++r)
+    for (int c = 0; c < CPT; ++c) acc[c] = 0.0;
+    same_spin_row<CPT, T>(a.B, a.val_sb, a.val_db, a.Ja, a.na, a.CT, a.na, ib0 + r, col, ok, alpha, acc);
 #pragma unroll
-    for (int c = 0; c < CPT; ++c) acc[r][c] = 0.0;
-  same_spin_sweep<TA, CPT, T>(a.B, a.val_sb, a.val_db, a.Ja, a.na, a.CT, a.na, ib0, a.nb, col, ok, alpha, acc);
+    for (int c = 0; c < CPT; ++c) tile[r][threadIdx.x + kThreads * c] = acc[c];
+  }
+  // each thread owns its columns: no barrier needed between its own writes and reads
 #pragma unroll
   for (int c = 0; c < CPT; ++c)
     if (ok[c]) {
-      T *srow = a.S + (size_t)col[c] * a.nb;
-#pragma unroll
-      for (int r = 0; r < TA; ++r) {
-        const uint32_t ib = ib0 + r;
-        if (ib < a.nb) srow[ib] = (T)((double)srow[ib] + acc[r][c]);
-      }
+      T *srow = a.S + (size_t)col[c] * a.nb + ib0;
+      for (uint32_t r = 0; r < rend; ++r) srow[r] = (T)((double)srow[r] + tile[r][threadIdx.x + kThreads * c]);
     }
 }
 
@@ -293,7 +274,6 @@ void to_float(Problem &p, const double *x, float *y, size_t n, cudaStream_t s) {
   count_launch(p.ctx);
 }
 
-template <typename T>
 void begin_timing(Problem &p, cudaStream_t s, cudaEvent_t &ev0, cudaEvent_t &ev1) {
   if (!p.ctx->timing) return;
   ev0 = timing_event(p.ctx);
@@ -307,6 +287,23 @@ void end_timing(Problem &p, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1) {
   p.ctx->sigma_events.emplace_back(ev0, ev1);
 }
 
+template <typename T>
+Args<T> base_args(Problem &p, const T *C, T *S, int accumulate) {
+  Args<T> a;
+  a.astr = p.astr;
+  a.bstr = p.bstr;
+  a.na = p.na;
+  a.nb = p.nb;
+  a.hii = p.hii;
+  a.C = C;
+  a.S = S;
+  a.accumulate = accumulate;
+  a.A = p.A;
+  a.B = p.B;
+  a.npair = p.npair;
+  return a;
+}
+
 }  // namespace
 
 void transpose_fp64(Problem &p, const double *in, double *out, uint32_t R, uint32_t Cn, cudaStream_t s) {
@@ -318,20 +315,10 @@ void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStre
   if (!p.CT) p.CT = (double *)dev_alloc(p, sizeof(double) * p.N);
   if (p.N == 0) return;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  begin_timing<double>(p, s, ev0, ev1);
+  begin_timing(p, s, ev0, ev1);
   transpose<double>(p, C, p.CT, p.na, p.nb, s);
-  Args<double> a;
-  a.astr = p.astr;
-  a.bstr = p.bstr;
-  a.na = p.na;
-  a.nb = p.nb;
-  a.hii = p.hii;
-  a.C = C;
+  Args<double> a = base_args<double>(p, C, S, accumulate);
   a.CT = p.CT;
-  a.S = S;
-  a.accumulate = accumulate;
-  a.A = p.A;
-  a.B = p.B;
   a.val_sa = p.A.val_s;
   a.val_da = p.A.val_d;
   a.val_sb = p.B.val_s;
@@ -339,7 +326,6 @@ void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStre
   a.Jb = p.Jb;
   a.Ja = p.Ja;
   a.Kp = p.Kp;
-  a.npair = p.npair;
   launch<double>(p, a, s);
   end_timing(p, s, ev0, ev1);
 }
@@ -372,20 +358,10 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s) {
   if (!p.CTf) p.CTf = (float *)dev_alloc(p, sizeof(float) * p.N);
   if (p.N == 0) return;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  begin_timing<float>(p, s, ev0, ev1);
+  begin_timing(p, s, ev0, ev1);
   transpose<float>(p, C, p.CTf, p.na, p.nb, s);
-  Args<float> a;
-  a.astr = p.astr;
-  a.bstr = p.bstr;
-  a.na = p.na;
-  a.nb = p.nb;
-  a.hii = p.hii;
-  a.C = C;
+  Args<float> a = base_args<float>(p, C, S, 0);
   a.CT = p.CTf;
-  a.S = S;
-  a.accumulate = 0;
-  a.A = p.A;
-  a.B = p.B;
   a.val_sa = p.val_sf[0];
   a.val_da = p.val_df[0];
   a.val_sb = p.val_sf[1];
@@ -393,7 +369,6 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s) {
   a.Jb = p.Jbf;
   a.Ja = p.Jaf;
   a.Kp = p.Kpf;
-  a.npair = p.npair;
   launch<float>(p, a, s);
   end_timing(p, s, ev0, ev1);
 }

@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -15,6 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libsbdgb.so")
 
 SBDGB_OK = 0
+CUDA_STREAM_LEGACY = 1  # cudaStreamLegacy
 STATUS = {0: "OK", 1: "E_INPUT", 2: "E_UNSUPPORTED", 3: "E_CUDA", 4: "E_NOMEM", 5: "E_STATE", 6: "E_TIMEOUT"}
 FP64, MIXED = 0, 1
 
@@ -109,9 +111,13 @@ class Engine:
             raise SbdgbError(rc, f"cannot create a context on device {device}")
         self.h = h
         self.device = device
+        self._problems = weakref.WeakSet()
 
     def close(self):
+        """Destroys the context after every problem still open on it."""
         if getattr(self, "h", None):
+            for p in list(getattr(self, "_problems", ())):
+                p.close()
             self.lib.sbdgb_ctx_destroy(self.h)
             self.h = None
 
@@ -180,6 +186,7 @@ class TPBProblem:
                                            float(ecore), C.byref(h))
         engine.check(rc)
         self.h = h
+        engine._problems.add(self)
 
     @classmethod
     def from_problem(cls, engine: Engine, p) -> "TPBProblem":
@@ -187,7 +194,8 @@ class TPBProblem:
 
     def close(self):
         if getattr(self, "h", None):
-            self.lib.sbdgb_problem_destroy(self.h)
+            if getattr(self.engine, "h", None):
+                self.lib.sbdgb_problem_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -238,11 +246,19 @@ class TPBProblem:
     def sigma(self, C_in: np.ndarray) -> np.ndarray:
         return self.mult(C_in)
 
-    def sigma_device(self, c_ptr: int, s_ptr: int, accumulate: bool = False, stream: int = 0):
-        self.engine.check(self.lib.sbdgb_sigma(self.h, c_ptr, s_ptr, int(accumulate), stream or None))
+    @staticmethod
+    def _stream_arg(stream):
+        # None: the context's stream; 0 (the legacy default stream handle) maps to
+        # cudaStreamLegacy so that it is not mistaken for "none given"
+        if stream is None:
+            return None
+        return stream if stream != 0 else CUDA_STREAM_LEGACY
 
-    def sigma_mixed_device(self, c_ptr: int, s_ptr: int, stream: int = 0):
-        self.engine.check(self.lib.sbdgb_sigma_mixed(self.h, c_ptr, s_ptr, stream or None))
+    def sigma_device(self, c_ptr: int, s_ptr: int, accumulate: bool = False, stream: int | None = None):
+        self.engine.check(self.lib.sbdgb_sigma(self.h, c_ptr, s_ptr, int(accumulate), self._stream_arg(stream)))
+
+    def sigma_mixed_device(self, c_ptr: int, s_ptr: int, stream: int | None = None):
+        self.engine.check(self.lib.sbdgb_sigma_mixed(self.h, c_ptr, s_ptr, self._stream_arg(stream)))
 
     def davidson(self, nroots: int = 1, max_nb: int = 20, eps: float = 1e-8, max_it: int = 100,
                  init: int = 0, precision: int = FP64, refine_every: int = 4, max_time: float = 0.0,

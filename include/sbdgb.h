@@ -124,6 +124,15 @@ int sbdgb_sigma(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accu
 /* Mixed-precision sigma: FP32 vectors, FP32 products, FP64 accumulation of
  * each element's sum, FP32 result. */
 int sbdgb_sigma_mixed(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, void *stream);
+/* The sigma tile shapes the autotuner picked on this problem's first product
+ * (precision 0 = FP64, 1 = mixed; -1 = not tuned yet) and the time it measured
+ * for each of the n_shapes candidates of kernel A (alpha sweep) and B (beta
+ * sweep).  Shapes: 0 = 8x128, 1 = 8x256, 2 = 8x512, 3 = 16x256 rows x columns.
+ * The first product of each precision tunes (and synchronises), so make it
+ * before any stream capture. */
+int sbdgb_problem_tuning(const sbdgb_problem *p, int precision, int *shape_a, int *shape_b, float *ms_a,
+                         float *ms_b, int n_shapes);
+
 /* Host-buffer form of sbd::mult: Wb += H*Wk with host vectors (copies
  * inside).  hii is ignored when NULL (the problem's own diagonal is used). */
 int sbdgb_mult_host(sbdgb_problem *p, const double *hii, const double *Wk, double *Wb);
@@ -135,7 +144,7 @@ typedef struct {
   int max_nb;        /* max subspace size (reference --block) */
   double eps;        /* residual-norm tolerance (reference --tolerance) */
   double max_time;   /* wall-clock cap in seconds (reference --max_time); <= 0: none */
-  int nroots;        /* lowest roots wanted (the reference solves 1) */
+  int nroots;        /* lowest roots wanted, 1..8 (the reference solves 1) */
   int init;          /* 0: unit vector on determinant 0 (reference init 0),
                         1: unit vectors on the lowest diagonal entries,
                         2: caller-supplied vectors in X */

@@ -54,6 +54,16 @@ void *workspace(Problem &p, int slot, size_t bytes) {
   return d;
 }
 
+void release_workspace(Problem &p, int slot) {
+  if (!p.ws[slot]) return;
+  SBDGB_CUDA(cudaStreamSynchronize(p.ctx->stream));
+  cudaFree(p.ws[slot]);
+  p.bytes -= p.ws_bytes[slot];
+  p.ctx->in_use -= p.ws_bytes[slot];
+  p.ws[slot] = nullptr;
+  p.ws_bytes[slot] = 0;
+}
+
 void dev_free_all(Problem &p) {
   if (p.ctx && p.ctx->stream) cudaStreamSynchronize(p.ctx->stream);
   for (void *d : p.allocs) cudaFree(d);
@@ -331,6 +341,19 @@ int sbdgb_sigma_mixed(sbdgb_problem *pr, const float *Wk_dev, float *Wb_dev, voi
     cudaStream_t s = stream ? (cudaStream_t)stream : p.ctx->stream;
     sbdgb::sigma_mixed(p, Wk_dev, Wb_dev, s);
   });
+}
+
+int sbdgb_problem_tuning(const sbdgb_problem *pr, int precision, int *shape_a, int *shape_b, float *ms_a,
+                         float *ms_b, int n_shapes) {
+  if (!pr || (precision != 0 && precision != 1)) return SBDGB_E_INPUT;
+  const sbdgb::Problem &p = pr->p;
+  if (shape_a) *shape_a = p.tune_a[precision];
+  if (shape_b) *shape_b = p.tune_b[precision];
+  for (int i = 0; i < n_shapes && i < 8; ++i) {
+    if (ms_a) ms_a[i] = p.tune_ms[precision][0][i];
+    if (ms_b) ms_b[i] = p.tune_ms[precision][1][i];
+  }
+  return SBDGB_OK;
 }
 
 int sbdgb_mult_host(sbdgb_problem *pr, const double *hii, const double *Wk, double *Wb) {

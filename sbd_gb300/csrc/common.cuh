@@ -108,7 +108,7 @@ struct Ctx;
 enum WsSlot {
   WS_V, WS_HV, WS_X, WS_HX, WS_T, WS_PARTIAL, WS_RED, WS_COEF,
   WS_DIAG0, WS_DIAG1, WS_DIAG2,
-  WS_VF, WS_HVF, WS_CF, WS_SF, WS_RES64, WS_C64,
+  WS_VF, WS_HVF, WS_CF, WS_SF, WS_RES64, WS_C64, WS_TUNE,
   WS_COUNT
 };
 
@@ -135,6 +135,8 @@ struct Problem {
   void *ws[WS_COUNT] = {};
   size_t ws_bytes[WS_COUNT] = {};
   bool tables = false, diag = false, mixed_ready = false;
+  int tune_a[2] = {-1, -1}, tune_b[2] = {-1, -1};  // autotuned sigma tile shapes (FP64, mixed)
+  float tune_ms[2][2][8] = {};                       // timings the autotuner saw
   size_t bytes = 0;
   std::vector<void *> allocs;
   // host copies of strings
@@ -160,6 +162,7 @@ cudaEvent_t timing_event(Ctx *c);
 
 void *dev_alloc(Problem &p, size_t bytes);
 void *workspace(Problem &p, int slot, size_t bytes);
+void release_workspace(Problem &p, int slot);
 void dev_free_all(Problem &p);
 
 // counted kernel launch helper

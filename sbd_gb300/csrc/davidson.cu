@@ -7,21 +7,25 @@
 // diagonal preconditioner R/(E0 - d) with a 1e-12 guard, modified
 // Gram-Schmidt, restart C0 = W (which recomputes sigma(W)).
 //
-// FP64 solver: the same steps generalised to nroots.  Each step adds one
-// corrected direction per unconverged root, orthogonalises it against the
-// basis with classical Gram-Schmidt plus a second pass when the norm drops
-// (the "twice is enough" rule), and restarts from the nroots Ritz vectors
-// together with their sigma vectors, which are formed from the stored H*V
-// instead of a new sigma product.  Vectors stay resident in HBM; only the
-// projected (<= max_nb)^2 matrix and a few norms cross to the host per step.
+// FP64 solver: the same steps generalised to nroots.  Each step adds the
+// corrected directions of the unconverged roots as one block: one pass of
+// dots against the basis, one fused projection, a Gram matrix, and a
+// Cholesky-style orthonormalisation written straight into the basis (a second
+// projection pass only when a norm drops below 1/sqrt(2), the "twice is
+// enough" rule).  Restarts keep the nroots Ritz vectors together with their
+// sigma vectors, formed from the stored H*V instead of a new sigma product;
+// Ritz vectors are materialised only at a restart and at the end.  Vectors
+// stay resident in HBM; only the projected (<= max_nb)^2 matrix and a few
+// norms cross to the host per step.
 //
 // Mixed solver: each root keeps an FP64 vector x (and its FP64 sigma) that is
 // never rounded to FP32.  Corrections live in an FP32 subspace W with FP32
 // sigma products.  Rayleigh-Ritz runs on span{x, W} as a generalised
-// symmetric problem whose x-W couplings are computed in FP64 (W is only
+// symmetric problem whose x-W overlaps are computed in FP64 (W is only
 // orthogonal to x to FP32 accuracy); every refine_every steps the Ritz vectors
 // are assembled in FP64, their FP64 sigma and FP64 residual are recomputed
 // (iterative refinement), and convergence is judged on that FP64 residual.
+// The FP32 subspace is kept across refinements and dropped only when full.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -39,6 +43,7 @@ constexpr int kRed = 256;  // threads per reduction block
 constexpr int kMaxV = 8;   // basis columns per dots pass
 constexpr int kMaxW = 4;   // right-hand columns per dots pass
 constexpr int kMaxCoef = 64 * 16;
+constexpr int kMaxBlock = 8;  // new directions per step
 
 template <typename T, int M>
 struct Ptrs {
@@ -202,15 +207,43 @@ __global__ void __launch_bounds__(kRed) k_project_out(const T *__restrict__ V, i
   }
 }
 
-template <typename TI, typename TO>
-__global__ void k_scale_copy(const TI *x, TO *y, size_t N, double f) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
-    y[e] = (TO)((double)x[e] * f);
+// Y_q = sum_j X_j M[j + nx*q], q < ny (a small basis change, written to Y).
+template <typename T>
+__global__ void __launch_bounds__(kRed) k_lincomb(const T *__restrict__ X, int nx, size_t N,
+                                                   const double *__restrict__ M, int ny, T *__restrict__ Y) {
+  __shared__ T ms[kMaxBlock * kMaxBlock];
+  for (int t = threadIdx.x; t < nx * ny; t += kRed) ms[t] = (T)M[t];
+  __syncthreads();
+  for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
+    T x[kMaxBlock];
+    for (int j = 0; j < nx; ++j) x[j] = __ldg(X + (size_t)j * N + e);
+    for (int q = 0; q < ny; ++q) {
+      T y = T(0);
+      for (int j = 0; j < nx; ++j) y = fma(x[j], ms[j + nx * q], y);
+      Y[(size_t)q * N + e] = y;
+    }
+  }
 }
 
-__global__ void k_fill_unit(double *__restrict__ y, size_t N, size_t pos) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
-    y[e] = (e == pos) ? 1.0 : 0.0;
+// Unit vector on `pos`, plus (amp > 0) a small deterministic pseudo-random
+// component on every entry.  The lowest-diagonal guess can lie in one sector of
+// an exact symmetry of H (e.g. alpha/beta exchange when both lists are equal);
+// an FP64 Davidson started there never leaves that sector, so the guess gets a
+// component along every direction (splitmix64 of the index, in [-amp, amp]).
+__global__ void k_fill_unit(double *__restrict__ y, size_t N, size_t pos, double amp, uint64_t seed) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x) {
+    double v = (e == pos) ? 1.0 : 0.0;
+    if (amp > 0.0) {
+      uint64_t x = (uint64_t)e * 0x9E3779B97F4A7C15ull + seed;
+      x ^= x >> 30;
+      x *= 0xBF58476D1CE4E5B9ull;
+      x ^= x >> 27;
+      x *= 0x94D049BB133111EBull;
+      x ^= x >> 31;
+      v += amp * ((double)(x >> 11) * (2.0 / 9007199254740992.0) - 1.0);
+    }
+    y[e] = v;
+  }
 }
 
 // Block-wise argmin over hii skipping already chosen positions.
@@ -267,51 +300,71 @@ __global__ void k_make_anchor_f32(const double *__restrict__ X, const double *__
 
 struct MixedResArgs {
   const float *Xf, *Rf, *W, *HW;
-  int k, m;
+  int k, m, nq;
   size_t N;
-  const float *cx;   // k: anchor coefficients of this Ritz vector
-  const float *dth;  // k: theta_j - theta (anchor Ritz values minus current value)
-  const float *cw;   // m: subspace coefficients
-  float theta;
+  const float *coef;   // per root q: [k cx | k dth | m cw], stride 3*64
+  const float *theta;  // nq current Ritz values
   const double *hii;
-  float *T;          // out: preconditioned residual
-  double *partial;   // blocks: residual norm^2
+  float *T;            // out: nq preconditioned residuals
+  double *partial;     // blocks x nq residual norm^2
 };
 
-// r = sum_j (Rf_j + dth_j Xf_j) cx_j + sum_l (HW_l - theta W_l) cw_l, then
-// T = r / (theta - d) with the reference's 1e-12 guard.  FP32 arithmetic.
+// For each root q of the block:
+//   r_q = sum_j (Rf_j + dth_jq Xf_j) cx_jq + sum_l (HW_l - theta_q W_l) cw_lq
+//   T_q = r_q / (theta_q - d) with the reference's 1e-12 guard.
+// FP32 arithmetic; Xf, Rf, W, HW are read once for all roots.
+template <int K>
 __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
-  __shared__ float c[3 * 64];
-  for (int t = threadIdx.x; t < a.k; t += kRed) {
-    c[t] = a.cx[t];
-    c[64 + t] = a.dth[t];
-  }
-  for (int t = threadIdx.x; t < a.m; t += kRed) c[128 + t] = a.cw[t];
+  __shared__ float c[K][3 * 64];
+  __shared__ float th[K];
+  for (int t = threadIdx.x; t < K * 3 * 64; t += kRed) c[t / (3 * 64)][t % (3 * 64)] = a.coef[t];
+  if (threadIdx.x < K) th[threadIdx.x] = a.theta[threadIdx.x];
   __syncthreads();
-  float s = 0.f, comp = 0.f;
+  float s[K], comp[K];
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    s[q] = 0.f;
+    comp[q] = 0.f;
+  }
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < a.N; e += (size_t)gridDim.x * kRed) {
-    float r = 0.f;
-    for (int j = 0; j < a.k; ++j)
-      r = fmaf(fmaf(c[64 + j], __ldg(a.Xf + (size_t)j * a.N + e), __ldg(a.Rf + (size_t)j * a.N + e)), c[j], r);
-    for (int l = 0; l < a.m; ++l)
-      r = fmaf(fmaf(-a.theta, __ldg(a.W + (size_t)l * a.N + e), __ldg(a.HW + (size_t)l * a.N + e)), c[128 + l], r);
-    const float y = r * r - comp;
-    const float t = s + y;
-    comp = (t - s) - y;
-    s = t;
-    double den = (double)a.theta - __ldg(a.hii + e);
-    if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
-    a.T[e] = (float)((double)r / den);
+    float r[K];
+#pragma unroll
+    for (int q = 0; q < K; ++q) r[q] = 0.f;
+    for (int j = 0; j < a.k; ++j) {
+      const float xf = __ldg(a.Xf + (size_t)j * a.N + e), rf = __ldg(a.Rf + (size_t)j * a.N + e);
+#pragma unroll
+      for (int q = 0; q < K; ++q) r[q] = fmaf(fmaf(c[q][64 + j], xf, rf), c[q][j], r[q]);
+    }
+    for (int l = 0; l < a.m; ++l) {
+      const float w = __ldg(a.W + (size_t)l * a.N + e), hw = __ldg(a.HW + (size_t)l * a.N + e);
+#pragma unroll
+      for (int q = 0; q < K; ++q) r[q] = fmaf(fmaf(-th[q], w, hw), c[q][128 + l], r[q]);
+    }
+    const double d = __ldg(a.hii + e);
+#pragma unroll
+    for (int q = 0; q < K; ++q) {
+      const float y = r[q] * r[q] - comp[q];
+      const float t = s[q] + y;
+      comp[q] = (t - s[q]) - y;
+      s[q] = t;
+      double den = (double)th[q] - d;
+      if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
+      a.T[(size_t)q * a.N + e] = (float)((double)r[q] / den);
+    }
   }
-  __shared__ double red[kRed / 32];
-  double x = (double)s - (double)comp;
-  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = x;
+  __shared__ double red[kRed / 32][K];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < K; ++q) {
+    double x = (double)s[q] - (double)comp[q];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][q] = x;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x < K) {
     double t = 0.0;
-    for (int w2 = 0; w2 < kRed / 32; ++w2) t += red[w2];
-    a.partial[blockIdx.x] = t;
+    for (int w2 = 0; w2 < kRed / 32; ++w2) t += red[w2][threadIdx.x];
+    a.partial[(size_t)blockIdx.x * K + threadIdx.x] = t;
   }
 }
 
@@ -379,6 +432,13 @@ struct Solver {
       }
     }
   }
+  // G = V^T W for W contiguous too.
+  template <typename TV, typename TW>
+  void dots_c(const TV *V0, int nv, const TW *W0, int nw, std::vector<double> &G) {
+    std::vector<const TW *> w(nw);
+    for (int j = 0; j < nw; ++j) w[j] = W0 + (size_t)j * N;
+    dots<TV, TW>(V0, nv, w.data(), nw, G);
+  }
 
   template <typename TV, typename TW, int NV>
   void launch_dots_w(Ptrs<TV, kMaxV> vp, Ptrs<TW, kMaxW> wp, int mw) {
@@ -405,7 +465,8 @@ struct Solver {
     SBDGB_CUDA(cudaGetLastError());
   }
 
-  // Returns the residual norms.
+  // Ritz vectors (optional), their sigma (optional) and the preconditioned
+  // residuals (optional) of the combination c; returns the residual norms.
   std::vector<double> combine(const double *V, const double *HV, int nv, int k, const std::vector<double> &c,
                               const std::vector<double> &theta, double *X, double *HX, double *T) {
     std::vector<double> hc((size_t)nv * k + 16, 0.0);
@@ -434,63 +495,98 @@ struct Solver {
   template <typename T>
   void project_out(const T *V, int nv, const std::vector<double> &G, T *Tv, int k) {
     if (nv == 0) return;
-    SBDGB_CUDA(cudaMemcpyAsync(coef, G.data(), sizeof(double) * nv * k, cudaMemcpyHostToDevice, s));
-    switch (k) {
+    for (int j0 = 0; j0 < nv; j0 += kMaxCoef / std::max(k, 1)) {
+      const int mv = std::min(nv - j0, kMaxCoef / std::max(k, 1));
+      std::vector<double> g((size_t)mv * k);
+      for (int r = 0; r < k; ++r)
+        for (int j = 0; j < mv; ++j) g[j + (size_t)mv * r] = G[(j0 + j) + (size_t)nv * r];
+      SBDGB_CUDA(cudaMemcpyAsync(coef, g.data(), sizeof(double) * mv * k, cudaMemcpyHostToDevice, s));
+      const T *Vj = V + (size_t)j0 * N;
+      switch (k) {
 #define SBDGB_K(KK) \
-  case KK: k_project_out<T, KK><<<blocks, kRed, 0, s>>>(V, nv, N, coef, Tv); break;
-      SBDGB_K(1) SBDGB_K(2) SBDGB_K(3) SBDGB_K(4) SBDGB_K(5) SBDGB_K(6) SBDGB_K(7) SBDGB_K(8)
+  case KK: k_project_out<T, KK><<<blocks, kRed, 0, s>>>(Vj, mv, N, coef, Tv); break;
+        SBDGB_K(1) SBDGB_K(2) SBDGB_K(3) SBDGB_K(4) SBDGB_K(5) SBDGB_K(6) SBDGB_K(7) SBDGB_K(8)
 #undef SBDGB_K
-      default: throw Error(SBDGB_E_UNSUPPORTED, "at most 8 vectors per projection");
+        default: throw Error(SBDGB_E_UNSUPPORTED, "at most 8 vectors per projection");
+      }
+      count_launch(p.ctx);
+      SBDGB_CUDA(cudaGetLastError());
     }
+  }
+
+  template <typename T>
+  void lincomb(const T *X, int nx, const std::vector<double> &M, int ny, T *Y) {
+    SBDGB_REQUIRE(nx <= kMaxBlock && ny <= kMaxBlock, SBDGB_E_UNSUPPORTED, "block too large");
+    SBDGB_CUDA(cudaMemcpyAsync(coef, M.data(), sizeof(double) * nx * ny, cudaMemcpyHostToDevice, s));
+    k_lincomb<T><<<blocks, kRed, 0, s>>>(X, nx, N, coef, ny, Y);
     count_launch(p.ctx);
     SBDGB_CUDA(cudaGetLastError());
   }
 
-  template <typename TI, typename TO>
-  void scale_copy(const TI *x, TO *y, double f) {
-    k_scale_copy<TI, TO><<<blocks, kRed, 0, s>>>(x, y, N, f);
-    count_launch(p.ctx);
-  }
-  template <typename T>
-  double norm(const T *x) {
-    std::vector<double> g;
-    const T *w[1] = {x};
-    dots<T, T>(x, 1, w, 1, g);
-    return std::sqrt(std::max(0.0, g[0]));
-  }
-  double reduce_partials(int width) {
+  double reduce_partials(int width, std::vector<double> *out = nullptr) {
     k_sum_partials<<<1, 64, 0, s>>>(partial, blocks, width, red);
     count_launch(p.ctx);
-    double out = 0.0;
-    SBDGB_CUDA(cudaMemcpyAsync(&out, red, sizeof(double), cudaMemcpyDeviceToHost, s));
+    std::vector<double> v(width);
+    SBDGB_CUDA(cudaMemcpyAsync(v.data(), red, sizeof(double) * width, cudaMemcpyDeviceToHost, s));
     SBDGB_CUDA(cudaStreamSynchronize(s));
-    return out;
+    if (out) *out = v;
+    return v[0];
   }
 
-  // Orthonormalises t against the first nv columns of V (two passes of
-  // classical Gram-Schmidt when the norm drops), in the vectors' precision.
-  // Returns the norm left relative to the unit-normalised input (0 if t was 0).
+  // Orthonormalises the nt vectors Tb against the first nv columns of V and
+  // among themselves, writing the kept directions to Vout (which may follow V).
+  // Classical Gram-Schmidt for the block with a second pass when a squared norm
+  // falls below half of its value before the pass; the block itself is
+  // orthonormalised through its Gram matrix (Cholesky with dropping of
+  // directions whose remaining norm is below `drop` of the original).
   template <typename T>
-  double orthonormalize(T *t, const T *V, int nv) {
-    double n0 = norm(t);
-    if (!(n0 > 0.0) || !std::isfinite(n0)) return 0.0;
-    scale_copy<T, T>(t, t, 1.0 / n0);
-    n0 = 1.0;
+  int orthonormalize_block(T *Tb, int nt, const T *V, int nv, T *Vout, double drop) {
+    if (nt <= 0) return 0;
+    SBDGB_REQUIRE(nt <= kMaxBlock, SBDGB_E_UNSUPPORTED, "block too large");
+    std::vector<double> G0;
+    dots_c<T, T>(Tb, nt, Tb, nt, G0);
+    std::vector<double> n0(nt);
+    for (int q = 0; q < nt; ++q) n0[q] = G0[q + (size_t)nt * q];
+    std::vector<double> Gm = G0, prev = n0;
     for (int pass = 0; pass < 2 && nv > 0; ++pass) {
-      for (int j0 = 0; j0 < nv; j0 += kMaxV) {
-        const int mv = std::min(kMaxV, nv - j0);
-        std::vector<double> G;
-        const T *w[1] = {t};
-        dots<T, T>(V + (size_t)j0 * N, mv, w, 1, G);
-        project_out<T>(V + (size_t)j0 * N, mv, G, t, 1);
-      }
-      const double n1 = norm(t);
-      const bool enough = n1 > 0.7071 * n0;
-      n0 = n1;
-      if (enough) break;
+      std::vector<double> G;
+      dots_c<T, T>(V, nv, Tb, nt, G);
+      project_out<T>(V, nv, G, Tb, nt);
+      dots_c<T, T>(Tb, nt, Tb, nt, Gm);
+      bool again = false;
+      for (int q = 0; q < nt; ++q) again = again || (Gm[q + (size_t)nt * q] < 0.5 * prev[q]);
+      for (int q = 0; q < nt; ++q) prev[q] = Gm[q + (size_t)nt * q];
+      if (!again) break;
     }
-    if (n0 > 0.0) scale_copy<T, T>(t, t, 1.0 / n0);
-    return n0;
+    // orthonormal combinations u_q of the block (u^T Gm u = 1), dropping
+    // directions that are numerically dependent
+    std::vector<std::vector<double>> us;
+    for (int q = 0; q < nt; ++q) {
+      if (!(n0[q] > 0.0) || !std::isfinite(n0[q])) continue;
+      std::vector<double> v(nt, 0.0);
+      v[q] = 1.0;
+      for (int pass = 0; pass < 2; ++pass)
+        for (const auto &u : us) {
+          double pr = 0.0;
+          for (int i = 0; i < nt; ++i)
+            for (int j = 0; j < nt; ++j) pr += u[i] * Gm[i + (size_t)nt * j] * v[j];
+          for (int i = 0; i < nt; ++i) v[i] -= pr * u[i];
+        }
+      double nn = 0.0;
+      for (int i = 0; i < nt; ++i)
+        for (int j = 0; j < nt; ++j) nn += v[i] * Gm[i + (size_t)nt * j] * v[j];
+      if (!(nn > drop * drop * n0[q])) continue;
+      const double f = 1.0 / std::sqrt(nn);
+      for (auto &x : v) x *= f;
+      us.push_back(v);
+    }
+    const int kept = (int)us.size();
+    if (kept == 0) return 0;
+    std::vector<double> M((size_t)nt * kept);
+    for (int c = 0; c < kept; ++c)
+      for (int i = 0; i < nt; ++i) M[i + (size_t)nt * c] = us[c][i];
+    lincomb<T>(Tb, nt, M, kept, Vout);
+    return kept;
   }
 
   std::vector<size_t> lowest_diagonal(int k) {
@@ -541,8 +637,11 @@ struct Solver {
     } else {
       pos = lowest_diagonal(k);
     }
+    // init 0 is the reference's exact unit vector; init 1 gets a 1e-3 total
+    // perturbation spread over all entries
+    const double amp = o.init == 1 ? 1e-3 * std::sqrt(3.0 / (double)N) : 0.0;
     for (int q = 0; q < k; ++q) {
-      k_fill_unit<<<blocks, kRed, 0, s>>>(T + (size_t)q * N, N, pos[q]);
+      k_fill_unit<<<blocks, kRed, 0, s>>>(T + (size_t)q * N, N, pos[q], amp, 0x5BD1E995ull * (uint64_t)(q + 1));
       count_launch(p.ctx);
     }
   }
@@ -562,6 +661,7 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
   const auto t0 = clock::now();
   const int k = o.nroots;
   const size_t N = p.N;
+  SBDGB_REQUIRE(k <= kMaxBlock, SBDGB_E_UNSUPPORTED, "at most 8 roots");
   int max_nb = std::max(o.max_nb, 2 * k);
   max_nb = (int)std::min<size_t>((size_t)max_nb, N);
   SBDGB_REQUIRE(max_nb <= 64, SBDGB_E_INPUT, "max_nb must be <= 64");
@@ -575,47 +675,30 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
 
   sbdgb_report r{};
   sv.start_vectors(o, k, T, Xout);
-  int nv = 0;
-  auto append = [&](double *Tin, int nt) -> int {
-    int added = 0;
-    for (int q = 0; q < nt && nv < max_nb; ++q) {
-      double *t = Tin + (size_t)q * N;
-      const double left = sv.orthonormalize<double>(t, V, nv);
-      if (!(left > 1e-8)) continue;  // linearly dependent direction: dropped
-      SBDGB_CUDA(cudaMemcpyAsync(V + (size_t)nv * N, t, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
-      nv++;
-      added++;
-    }
-    return added;
-  };
-  auto sigma_range = [&](int from) {
-    for (int j = from; j < nv; ++j) {
+  int nv = sv.orthonormalize_block<double>(T, k, V, 0, V, 1e-8);
+  SBDGB_REQUIRE(nv >= 1, SBDGB_E_INPUT, "starting vectors are zero");
+  std::vector<double> Hs((size_t)max_nb * max_nb, 0.0);  // projected matrix, column-major ld max_nb
+  // sigma of V[from, to) and the new columns of the projected matrix
+  auto extend = [&](int from, int to) {
+    for (int j = from; j < to; ++j) {
       sigma_fp64(p, V + (size_t)j * N, HV + (size_t)j * N, 0, s);
       r.sigma_calls++;
       r.sigma_fp64++;
     }
-  };
-  append(T, k);
-  SBDGB_REQUIRE(nv >= 1, SBDGB_E_INPUT, "starting vectors are zero");
-  sigma_range(0);
-  std::vector<double> Hs((size_t)max_nb * max_nb, 0.0);  // projected matrix, column-major ld max_nb
-  auto update_projection = [&](int from) {
-    std::vector<const double *> w;
-    for (int j = from; j < nv; ++j) w.push_back(HV + (size_t)j * N);
     std::vector<double> G;
-    sv.dots<double, double>(V, nv, w.data(), (int)w.size(), G);
-    for (int jj = 0; jj < (int)w.size(); ++jj)
-      for (int i = 0; i < nv; ++i) {
-        const double g = G[(size_t)i + (size_t)nv * jj];
+    sv.dots_c<double, double>(V, to, HV + (size_t)from * N, to - from, G);
+    for (int jj = 0; jj < to - from; ++jj)
+      for (int i = 0; i < to; ++i) {
+        const double g = G[(size_t)i + (size_t)to * jj];
         Hs[(size_t)i + (size_t)max_nb * (from + jj)] = g;
         Hs[(size_t)(from + jj) + (size_t)max_nb * i] = g;
       }
   };
-  update_projection(0);
+  extend(0, nv);
 
-  std::vector<double> theta, Y, resid(k, 0.0);
+  std::vector<double> theta, Y, resid(k, 0.0), c, th;
   bool converged = false;
-  int iter = 0;
+  int iter = 0, kk = 0;
   const int max_steps = std::max(1, o.max_it) * max_nb;
   while (true) {
     // Rayleigh-Ritz on the projected matrix
@@ -624,12 +707,13 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
       for (int i = 0; i < nv; ++i)
         A[i + (size_t)nv * j] = 0.5 * (Hs[i + (size_t)max_nb * j] + Hs[j + (size_t)max_nb * i]);
     jacobi_eig(nv, A, theta, Y);
-    const int kk = std::min(k, nv);
-    std::vector<double> c((size_t)nv * kk);
+    kk = std::min(k, nv);
+    c.assign((size_t)nv * kk, 0.0);
     for (int q = 0; q < kk; ++q)
       for (int i = 0; i < nv; ++i) c[i + (size_t)nv * q] = Y[i + (size_t)nv * q];
-    std::vector<double> th(theta.begin(), theta.begin() + kk);
-    resid = sv.combine(V, HV, nv, kk, c, th, X, HX, T);
+    th.assign(theta.begin(), theta.begin() + kk);
+    // residual norms and preconditioned corrections; Ritz vectors not materialised
+    resid = sv.combine(V, HV, nv, kk, c, th, nullptr, nullptr, T);
     iter++;
     r.iterations = iter;
     if (o.verbose) print_iter("", iter, resid, th, kk);
@@ -637,10 +721,11 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
     for (int q = 0; q < kk; ++q) converged = converged && (resid[q] < o.eps);
     const double elapsed = std::chrono::duration<double>(clock::now() - t0).count();
     if (converged || iter >= max_steps || (o.max_time > 0 && elapsed > o.max_time)) break;
-    // restart when the new directions would not fit (thick restart with the Ritz vectors)
     int nnew = 0;
     for (int q = 0; q < kk; ++q) nnew += (resid[q] >= o.eps);
     if (nv + nnew > max_nb) {
+      // thick restart with the Ritz vectors and their sigma vectors
+      sv.combine(V, HV, nv, kk, c, th, X, HX, nullptr);
       SBDGB_CUDA(cudaMemcpyAsync(V, X, sizeof(double) * N * kk, cudaMemcpyDeviceToDevice, s));
       SBDGB_CUDA(cudaMemcpyAsync(HV, HX, sizeof(double) * N * kk, cudaMemcpyDeviceToDevice, s));
       nv = kk;
@@ -649,7 +734,7 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
       r.restarts++;
       // T still holds the preconditioned residuals of these Ritz vectors
     }
-    // keep the corrections of the unconverged roots, packed at the front of T
+    // corrections of the unconverged roots, packed at the front of T
     int nt = 0;
     for (int q = 0; q < kk; ++q)
       if (resid[q] >= o.eps) {
@@ -658,16 +743,18 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
                                      cudaMemcpyDeviceToDevice, s));
         nt++;
       }
-    const int from = nv;
-    const int added = append(T, nt);
+    const int added = sv.orthonormalize_block<double>(T, nt, V, nv, V + (size_t)nv * N, 1e-8);
     if (added == 0) break;  // no new direction: the subspace is invariant
-    sigma_range(from);
-    update_projection(from);
+    extend(nv, nv + added);
+    nv += added;
   }
   r.converged = converged ? 1 : 0;
   for (int q = 0; q < k && q < 16; ++q) r.resid[q] = q < (int)resid.size() ? resid[q] : 0.0;
   for (int q = 0; q < k; ++q) E[q] = q < (int)theta.size() ? theta[q] : NAN;
-  if (Xout) SBDGB_CUDA(cudaMemcpyAsync(Xout, X, sizeof(double) * N * k, cudaMemcpyDeviceToHost, s));
+  if (Xout) {
+    sv.combine(V, HV, nv, kk, c, th, X, nullptr, nullptr);
+    SBDGB_CUDA(cudaMemcpyAsync(Xout, X, sizeof(double) * N * kk, cudaMemcpyDeviceToHost, s));
+  }
   SBDGB_CUDA(cudaStreamSynchronize(s));
   r.seconds = std::chrono::duration<double>(clock::now() - t0).count();
   if (rep) *rep = r;
@@ -680,7 +767,7 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
   const auto t0 = clock::now();
   const int k = o.nroots;
   const size_t N = p.N;
-  SBDGB_REQUIRE(k <= 8, SBDGB_E_UNSUPPORTED, "the mixed solver supports up to 8 roots");
+  SBDGB_REQUIRE(k <= kMaxBlock, SBDGB_E_UNSUPPORTED, "the mixed solver supports up to 8 roots");
   const int mmax = std::max(std::min(o.max_nb, 64) - k, 2 * k);  // FP32 correction vectors
   SBDGB_REQUIRE(k + mmax <= 64, SBDGB_E_INPUT, "max_nb must be <= 64");
   const int refine_every = std::max(1, o.refine_every);
@@ -691,22 +778,20 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
   double *S = (double *)workspace(p, WS_HX, sizeof(double) * N * k);   // their FP64 sigma
   double *T = (double *)workspace(p, WS_T, sizeof(double) * N * k);    // FP64 scratch
   double *Y = (double *)workspace(p, WS_C64, sizeof(double) * N * k);  // FP64 scratch
-  float *W = (float *)workspace(p, WS_VF, sizeof(float) * N * mmax);
+  // [Xf | W]: rounded anchors followed by the FP32 subspace, so that new
+  // directions are orthogonalised against both in one pass
+  float *XW = (float *)workspace(p, WS_VF, sizeof(float) * N * (k + mmax));
+  float *Xf = XW, *W = XW + (size_t)k * N;
   float *HW = (float *)workspace(p, WS_HVF, sizeof(float) * N * mmax);
-  float *Xf = (float *)workspace(p, WS_CF, sizeof(float) * N * k);
   float *Rf = (float *)workspace(p, WS_SF, sizeof(float) * N * k);
-  float *Tf = (float *)workspace(p, WS_RES64, sizeof(float) * N);
-  float *dcoef = (float *)workspace(p, WS_DIAG1, sizeof(float) * 256);
+  float *Tf = (float *)workspace(p, WS_CF, sizeof(float) * N * k);
+  float *dcoef = (float *)workspace(p, WS_DIAG1, sizeof(float) * (kMaxBlock * 3 * 64 + 64));
 
   sbdgb_report r{};
   // anchors: starting vectors orthonormalised in FP64
   sv.start_vectors(o, k, T, Xout);
-  for (int q = 0; q < k; ++q) {
-    double *t = T + (size_t)q * N;
-    const double left = sv.orthonormalize<double>(t, X, q);
-    SBDGB_REQUIRE(left > 1e-8, SBDGB_E_INPUT, "starting vectors are linearly dependent");
-    SBDGB_CUDA(cudaMemcpyAsync(X + (size_t)q * N, t, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
-  }
+  SBDGB_REQUIRE(sv.orthonormalize_block<double>(T, k, X, 0, X, 1e-8) == k, SBDGB_E_INPUT,
+                "starting vectors are linearly dependent");
   std::vector<double> theta(k), resid(k, 0.0);
   // FP64 sigma of the anchors, Rayleigh-Ritz among them, FP64 residual norms
   auto refine_rr = [&]() {
@@ -715,10 +800,8 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       r.sigma_calls++;
       r.sigma_fp64++;
     }
-    std::vector<const double *> w;
-    for (int j = 0; j < k; ++j) w.push_back(S + (size_t)j * N);
     std::vector<double> G, th, Yv;
-    sv.dots<double, double>(X, k, w.data(), k, G);
+    sv.dots_c<double, double>(X, k, S, k, G);
     for (int j = 0; j < k; ++j)
       for (int i = 0; i < j; ++i)
         G[i + (size_t)k * j] = G[j + (size_t)k * i] = 0.5 * (G[i + (size_t)k * j] + G[j + (size_t)k * i]);
@@ -762,18 +845,18 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
     }
     return true;
   };
-  // couplings of the (new) anchors to the kept W columns
-  auto recouple = [&]() {
-    for (int l = 0; l < m; ++l) {
-      const float *wl[1] = {W + (size_t)l * N};
-      std::vector<double> g1, g2;
-      sv.dots<double, float>(X, k, wl, 1, g1);  // X^T w, FP64
-      sv.dots<float, float>(Rf, k, wl, 1, g2);  // R^T w, FP32 products
+  // couplings of the anchors to W columns [from, to)
+  auto couple = [&](int from, int to) {
+    if (to <= from) return;
+    std::vector<double> g1, g2;
+    sv.dots_c<double, float>(X, k, W + (size_t)from * N, to - from, g1);  // X^T w, FP64
+    sv.dots_c<float, float>(Rf, k, W + (size_t)from * N, to - from, g2);  // R^T w, FP32 products
+    for (int l = from; l < to; ++l)
       for (int j = 0; j < k; ++j) {
-        Sxw[j + (size_t)k * l] = g1[j];
-        Hxw[j + (size_t)k * l] = g2[j] + theta[j] * g1[j];  // S_j = R_j + theta_j X_j
+        const double x = g1[j + (size_t)k * (l - from)];
+        Sxw[j + (size_t)k * l] = x;
+        Hxw[j + (size_t)k * l] = g2[j + (size_t)k * (l - from)] + theta[j] * x;  // S_j = R_j + theta_j X_j
       }
-    }
   };
 
   bool converged = false;
@@ -789,10 +872,10 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
     SBDGB_CUDA(cudaMemcpyAsync(sv.red + 2048, theta.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
     k_make_anchor_f32<<<sv.blocks, kRed, 0, s>>>(X, S, sv.red + 2048, k, N, Xf, Rf);
     count_launch(p.ctx);
-    recouple();
-    bool ok_rr = true;
+    couple(0, m);
+    bool stalled = false;
     if (m > 0) {
-      ok_rr = rayleigh_ritz();
+      stalled = !rayleigh_ritz();
     } else {
       std::fill(cX.begin(), cX.end(), 0.0);
       for (int q = 0; q < k; ++q) cX[q + (size_t)k * q] = 1.0;
@@ -800,63 +883,63 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       thc = theta;
     }
     std::vector<double> res_est = resid;
-    bool stalled = !ok_rr;
     for (int inner = 0; inner < refine_every && !stalled; ++inner) {
-      if (m + k > mmax) break;
-      const int m0 = m;
-      for (int q = 0; q < k && m < mmax; ++q) {
-        if (res_est[q] < o.eps) continue;
-        // preconditioned residual of root q in FP32
-        std::vector<float> hc(3 * 64, 0.f);
+      std::vector<int> roots;
+      for (int q = 0; q < k; ++q)
+        if (res_est[q] >= o.eps) roots.push_back(q);
+      const int nq = (int)roots.size();
+      if (nq == 0 || m + nq > mmax) break;
+      // preconditioned residuals of the unconverged roots, FP32, one pass
+      std::vector<float> hc((size_t)kMaxBlock * 3 * 64, 0.f), hth(kMaxBlock, 0.f);
+      for (int i = 0; i < nq; ++i) {
+        const int q = roots[i];
         for (int j = 0; j < k; ++j) {
-          hc[j] = (float)cX[j + (size_t)k * q];
-          hc[64 + j] = (float)(theta[j] - thc[q]);
+          hc[(size_t)i * 192 + j] = (float)cX[j + (size_t)k * q];
+          hc[(size_t)i * 192 + 64 + j] = (float)(theta[j] - thc[q]);
         }
-        for (int l = 0; l < m0; ++l) hc[128 + l] = (float)cW[l + (size_t)m0 * q];
-        SBDGB_CUDA(cudaMemcpyAsync(dcoef, hc.data(), sizeof(float) * 3 * 64, cudaMemcpyHostToDevice, s));
-        MixedResArgs ma{Xf, Rf, W, HW, k, m0, N, dcoef, dcoef + 64, dcoef + 128, (float)thc[q], p.hii, Tf, sv.partial};
-        k_mixed_residual<<<sv.blocks, kRed, 0, s>>>(ma);
-        count_launch(p.ctx);
-        res_est[q] = std::sqrt(std::max(0.0, sv.reduce_partials(1)));
-        // orthogonalise against the rounded anchors, then against W, in FP32
-        double n0 = sv.norm<float>(Tf);
-        if (!(n0 > 0.0) || !std::isfinite(n0)) continue;
-        sv.scale_copy<float, float>(Tf, Tf, 1.0 / n0);
-        for (int pass = 0; pass < 2; ++pass) {
-          std::vector<double> G;
-          const float *w[1] = {Tf};
-          sv.dots<float, float>(Xf, k, w, 1, G);
-          sv.project_out<float>(Xf, k, G, Tf, 1);
-        }
-        const double left = sv.orthonormalize<float>(Tf, W, m);
-        if (!(left > 1e-3)) continue;  // no new direction in FP32
-        SBDGB_CUDA(cudaMemcpyAsync(W + (size_t)m * N, Tf, sizeof(float) * N, cudaMemcpyDeviceToDevice, s));
-        sigma_mixed(p, W + (size_t)m * N, HW + (size_t)m * N, s);
-        r.sigma_calls++;
-        // projected quantities of the new column: anchor couplings in FP64
-        const float *wn[1] = {W + (size_t)m * N};
-        const float *hwn[1] = {HW + (size_t)m * N};
-        std::vector<double> g1, g2, g3, g4, g5;
-        sv.dots<double, float>(X, k, wn, 1, g1);     // X^T w
-        sv.dots<float, float>(Rf, k, wn, 1, g2);     // R^T w
-        sv.dots<float, float>(W, m + 1, wn, 1, g3);  // W^T w
-        sv.dots<float, float>(W, m + 1, hwn, 1, g4); // W^T Hw
-        sv.dots<float, float>(HW, m + 1, wn, 1, g5); // (HW)^T w
-        for (int j = 0; j < k; ++j) {
-          Sxw[j + (size_t)k * m] = g1[j];
-          Hxw[j + (size_t)k * m] = g2[j] + theta[j] * g1[j];
-        }
-        for (int l = 0; l <= m; ++l) {
-          Sww[l + (size_t)mmax * m] = Sww[m + (size_t)mmax * l] = g3[l];
-          const double h = 0.5 * (g4[l] + g5[l]);
-          Hww[l + (size_t)mmax * m] = Hww[m + (size_t)mmax * l] = h;
-        }
-        m++;
+        for (int l = 0; l < m; ++l) hc[(size_t)i * 192 + 128 + l] = (float)cW[l + (size_t)m * q];
+        hth[i] = (float)thc[q];
       }
-      if (m == m0) {
+      SBDGB_CUDA(cudaMemcpyAsync(dcoef, hc.data(), sizeof(float) * hc.size(), cudaMemcpyHostToDevice, s));
+      SBDGB_CUDA(cudaMemcpyAsync(dcoef + hc.size(), hth.data(), sizeof(float) * kMaxBlock, cudaMemcpyHostToDevice, s));
+      MixedResArgs ma{Xf, Rf, W, HW, k, m, nq, N, dcoef, dcoef + hc.size(), p.hii, Tf, sv.partial};
+      switch (nq) {
+#define SBDGB_K(KK) \
+  case KK: k_mixed_residual<KK><<<sv.blocks, kRed, 0, s>>>(ma); break;
+        SBDGB_K(1) SBDGB_K(2) SBDGB_K(3) SBDGB_K(4) SBDGB_K(5) SBDGB_K(6) SBDGB_K(7) SBDGB_K(8)
+#undef SBDGB_K
+        default: throw Error(SBDGB_E_UNSUPPORTED, "block too large");
+      }
+      count_launch(p.ctx);
+      SBDGB_CUDA(cudaGetLastError());
+      std::vector<double> rn;
+      sv.reduce_partials(nq, &rn);
+      for (int i = 0; i < nq; ++i) res_est[roots[i]] = std::sqrt(std::max(0.0, rn[i]));
+      // orthonormalise the block against [Xf, W] and itself, into W[m..]
+      const int added = sv.orthonormalize_block<float>(Tf, nq, XW, k + m, W + (size_t)m * N, 1e-3);
+      if (added == 0) {
         stalled = true;
         break;
       }
+      for (int j = m; j < m + added; ++j) {
+        sigma_mixed(p, W + (size_t)j * N, HW + (size_t)j * N, s);
+        r.sigma_calls++;
+      }
+      // projected quantities of the new columns
+      couple(m, m + added);
+      std::vector<double> g3, g4;
+      sv.dots_c<float, float>(W, m + added, W + (size_t)m * N, added, g3);   // W^T w
+      sv.dots_c<float, float>(W, m + added, HW + (size_t)m * N, added, g4);  // W^T Hw
+      for (int jj = 0; jj < added; ++jj)
+        for (int l = 0; l < m + added; ++l) {
+          const int c2 = m + jj;
+          const double sw = g3[l + (size_t)(m + added) * jj], hw = g4[l + (size_t)(m + added) * jj];
+          Sww[l + (size_t)mmax * c2] = Sww[c2 + (size_t)mmax * l] = sw;
+          if (l < c2 || l == c2) {
+            Hww[l + (size_t)mmax * c2] = Hww[c2 + (size_t)mmax * l] = hw;
+          }
+        }
+      m += added;
       if (!rayleigh_ritz()) {
         stalled = true;
         break;
@@ -876,20 +959,17 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       k_mixed_assemble<<<sv.blocks, kRed, 0, s>>>(X, k, W, m, N, sv.red + 3000, dcoef, T + (size_t)q * N);
       count_launch(p.ctx);
     }
-    for (int q = 0; q < k; ++q) {
-      double *t = T + (size_t)q * N;
-      const double left = sv.orthonormalize<double>(t, T, q);
-      SBDGB_REQUIRE(left > 1e-8, SBDGB_E_STATE, "mixed Davidson lost a root");
-    }
-    SBDGB_CUDA(cudaMemcpyAsync(X, T, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, s));
+    SBDGB_REQUIRE(sv.orthonormalize_block<double>(T, k, X, 0, X, 1e-8) == k, SBDGB_E_STATE,
+                  "mixed Davidson lost a root");
     r.restarts++;
     refine_rr();
-    if (m + k > mmax) m = 0;  // subspace full: the anchors carry its information on
+    bool full = m + k > mmax;
+    if (full) m = 0;  // subspace full: the anchors carry its information on
     if (stalled) {
       bool ok = true;
       for (int q = 0; q < k; ++q) ok = ok && resid[q] < o.eps;
       if (!ok) {
-        if (m == 0) {
+        if (m == 0 && !full) {
           if (o.verbose) printf(" mixed Davidson: no new FP32 direction\n");
           break;
         }
@@ -913,7 +993,7 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
 
 void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
   if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "Davidson needs tables and diagonal");
-  SBDGB_REQUIRE(o.nroots >= 1 && o.nroots <= 16, SBDGB_E_INPUT, "nroots must be in [1, 16]");
+  SBDGB_REQUIRE(o.nroots >= 1 && o.nroots <= kMaxBlock, SBDGB_E_INPUT, "nroots must be in [1, 8]");
   SBDGB_REQUIRE((size_t)o.nroots <= p.N, SBDGB_E_INPUT, "more roots than determinants");
   if (o.precision == SBDGB_MIXED)
     davidson_mixed(p, o, E, Xout, rep);

@@ -16,8 +16,11 @@
 // every thread keeps its columns' opposite-spin strings and CPT accumulators
 // in registers.  The pair list of a row is the same for all threads of the
 // CTA, so its metadata are broadcast loads and the ket-row reads are
-// coalesced along the contiguous index.  Grid order puts consecutive CTAs on
-// the same column chunk so that the ket rows' column slab stays in L2.
+// coalesced along the contiguous index; pairs are taken four (doubles) or two
+// (singles) at a time so that each thread has several independent ket-row
+// loads in flight.  Grid order puts consecutive CTAs on the same column chunk
+// so that the ket rows' column slab stays in L2.  The tile shape (TA, CPT) is
+// picked per problem by timing the candidates on the first product.
 //
 // Alpha-beta phase.  The reference evaluates TwoExcite (determinants.h:
 // 500-518) on the bra determinant with i = 2 cr_a, j = 2 cr_b + 1,
@@ -67,6 +70,14 @@ struct Args {
   int npair;
 };
 
+template <typename T>
+__device__ __forceinline__ void madd(double &acc, T &part, T v, T x) {
+  if constexpr (std::is_same<T, double>::value)
+    acc = fma(v, x, acc);
+  else
+    part = fmaf(v, x, part);
+}
+
 // Same-spin excitations of one row applied to this thread's CPT columns.
 // In: ket-major input rows (ld = ldin); Jo: opposite-spin Coulomb table
 // [npair][ldj] for the single excitations.
@@ -76,46 +87,83 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
                                               const T *__restrict__ In, size_t ldin, uint32_t row,
                                               const uint32_t (&col)[CPT], const bool (&ok)[CPT],
                                               const uint64_t (&opp)[CPT], double (&acc)[CPT]) {
-  constexpr bool kF64 = std::is_same<T, double>::value;
   T part[CPT];
 #pragma unroll
   for (int c = 0; c < CPT; ++c) part[c] = T(0);
+  // singles, two at a time
   const uint32_t p0 = __ldg(Tb.off_s + row), p1 = __ldg(Tb.off_s + row + 1);
-  for (uint32_t p = p0; p < p1; ++p) {
+  uint32_t p = p0;
+  for (; p + 2 <= p1; p += 2) {
+    uint32_t ket[2], code[2];
+    T v[2];
+    uint64_t m[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      ket[u] = __ldg(Tb.ket_s + p + u);
+      code[u] = __ldg(Tb.code_s + p + u);
+      v[u] = __ldg(vs + p + u);
+      m[u] = __ldg(Tb.mask_s + p + u);
+    }
+#pragma unroll
+    for (int c = 0; c < CPT; ++c)
+      if (ok[c]) {
+        T x[2], j[2];
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          x[u] = __ldg(In + (size_t)ket[u] * ldin + col[c]);
+          j[u] = __ldg(Jo + (size_t)((code[u] >> 16) & 0x7fffu) * ldj + col[c]);
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const uint32_t ph = (__popcll(opp[c] & m[u]) ^ (code[u] >> 31)) & 1u;
+          madd<T>(acc[c], part[c], flip(v[u] + j[u], ph), x[u]);
+        }
+      }
+  }
+  if (p < p1) {
     const uint32_t ket = __ldg(Tb.ket_s + p), code = __ldg(Tb.code_s + p);
     const T v = __ldg(vs + p);
     const uint64_t m = __ldg(Tb.mask_s + p);
-    const T *in = In + (size_t)ket * ldin;
-    const T *jo = Jo + (size_t)((code >> 16) & 0x7fffu) * ldj;
-    const uint32_t sg = code >> 31;
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
       if (ok[c]) {
-        const uint32_t ph = (__popcll(opp[c] & m) ^ sg) & 1u;
-        if constexpr (kF64)
-          acc[c] = fma(flip(v + __ldg(jo + col[c]), ph), __ldg(in + col[c]), acc[c]);
-        else
-          part[c] = fmaf(flip(v + __ldg(jo + col[c]), ph), __ldg(in + col[c]), part[c]);
+        const uint32_t ph = (__popcll(opp[c] & m) ^ (code >> 31)) & 1u;
+        const T j = __ldg(Jo + (size_t)((code >> 16) & 0x7fffu) * ldj + col[c]);
+        madd<T>(acc[c], part[c], flip(v + j, ph), __ldg(In + (size_t)ket * ldin + col[c]));
       }
   }
+  // doubles, four at a time
   const uint32_t d0 = __ldg(Tb.off_d + row), d1 = __ldg(Tb.off_d + row + 1);
-#pragma unroll 2
-  for (uint32_t p = d0; p < d1; ++p) {
+  p = d0;
+  for (; p + 4 <= d1; p += 4) {
+    uint32_t ket[4];
+    T v[4];
+    uint64_t m[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      ket[u] = __ldg(Tb.ket_d + p + u);
+      v[u] = __ldg(vd + p + u);
+      m[u] = __ldg(Tb.mask_d + p + u);
+    }
+#pragma unroll
+    for (int c = 0; c < CPT; ++c)
+      if (ok[c]) {
+        T x[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = __ldg(In + (size_t)ket[u] * ldin + col[c]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) madd<T>(acc[c], part[c], flip(v[u], __popcll(opp[c] & m[u]) & 1u), x[u]);
+      }
+  }
+  for (; p < d1; ++p) {
     const uint32_t ket = __ldg(Tb.ket_d + p);
     const T v = __ldg(vd + p);
     const uint64_t m = __ldg(Tb.mask_d + p);
-    const T *in = In + (size_t)ket * ldin;
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
-      if (ok[c]) {
-        const uint32_t ph = __popcll(opp[c] & m) & 1u;
-        if constexpr (kF64)
-          acc[c] = fma(flip(v, ph), __ldg(in + col[c]), acc[c]);
-        else
-          part[c] = fmaf(flip(v, ph), __ldg(in + col[c]), part[c]);
-      }
+      if (ok[c]) madd<T>(acc[c], part[c], flip(v, __popcll(opp[c] & m) & 1u), __ldg(In + (size_t)ket * ldin + col[c]));
   }
-  if constexpr (!kF64) {
+  if constexpr (!std::is_same<T, double>::value) {
 #pragma unroll
     for (int c = 0; c < CPT; ++c) acc[c] += (double)part[c];
   }
@@ -123,7 +171,6 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
 
 template <int TA, int CPT, typename T>
 __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
-  constexpr bool kF64 = std::is_same<T, double>::value;
   constexpr int TB = kThreads * CPT;
   const uint32_t ia0 = blockIdx.x * TA;
   const uint32_t ib0 = blockIdx.y * TB;
@@ -169,17 +216,13 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
           const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
           const uint64_t mb = __ldg(a.B.mask_s + q);
           const uint32_t ph = (pa ^ __popcll(alpha_ket & mb) ^ (cb >> 31)) & 1u;
-          const T kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
-          if constexpr (kF64)
-            acc[c] = fma(kv, __ldg(crow + jb), acc[c]);
-          else
-            part[c] = fmaf(kv, __ldg(crow + jb), part[c]);
+          madd<T>(acc[c], part[c], flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph), __ldg(crow + jb));
         }
       }
     }
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
-      if constexpr (!kF64) acc[c] += (double)part[c];
+      if constexpr (!std::is_same<T, double>::value) acc[c] += (double)part[c];
       if (ok[c]) {
         const size_t k = (size_t)ia * a.nb + col[c];
         a.S[k] = (T)(a.accumulate ? (double)a.S[k] + acc[c] : acc[c]);
@@ -246,16 +289,91 @@ __global__ void k_to_float(const double *__restrict__ x, float *__restrict__ y, 
     y[e] = (float)x[e];
 }
 
-constexpr int kTA = 8;
-constexpr int kCPT = 2;
+// ---- tile shapes and the autotuner ---------------------------------------------
+
+constexpr int kNumShapes = 4;
+constexpr int kShapeTA[kNumShapes] = {8, 8, 8, 16};
+constexpr int kShapeCPT[kNumShapes] = {1, 2, 4, 2};
+
+template <typename T, int TA, int CPT>
+void launch_a_shape(const Problem &p, const Args<T> &a, cudaStream_t s) {
+  constexpr int TB = kThreads * CPT;
+  dim3 g((p.na + TA - 1) / TA, (p.nb + TB - 1) / TB);
+  k_sigma_alpha<TA, CPT, T><<<g, kThreads, 0, s>>>(a);
+}
+template <typename T, int TA, int CPT>
+void launch_b_shape(const Problem &p, const Args<T> &a, cudaStream_t s) {
+  constexpr int TB = kThreads * CPT;
+  dim3 g((p.nb + TA - 1) / TA, (p.na + TB - 1) / TB);
+  k_sigma_beta<TA, CPT, T><<<g, kThreads, 0, s>>>(a);
+}
+
+template <typename T>
+void launch_a(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
+  switch (shape) {
+    case 0: launch_a_shape<T, 8, 1>(p, a, s); break;
+    case 1: launch_a_shape<T, 8, 2>(p, a, s); break;
+    case 2: launch_a_shape<T, 8, 4>(p, a, s); break;
+    default: launch_a_shape<T, 16, 2>(p, a, s); break;
+  }
+}
+template <typename T>
+void launch_b(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
+  switch (shape) {
+    case 0: launch_b_shape<T, 8, 1>(p, a, s); break;
+    case 1: launch_b_shape<T, 8, 2>(p, a, s); break;
+    case 2: launch_b_shape<T, 8, 4>(p, a, s); break;
+    default: launch_b_shape<T, 16, 2>(p, a, s); break;
+  }
+}
+
+// Times every tile shape of both kernels once (after one untimed run) on the
+// problem's own vectors, writing into scratch, and keeps the fastest.
+template <typename T>
+void autotune(Problem &p, Args<T> a, cudaStream_t s) {
+  const int prec = std::is_same<T, double>::value ? 0 : 1;
+  if (p.tune_a[prec] >= 0 && p.tune_b[prec] >= 0) return;
+  a.S = (T *)workspace(p, WS_TUNE, sizeof(T) * p.N);
+  a.accumulate = 0;
+  cudaEvent_t e0, e1;
+  SBDGB_CUDA(cudaEventCreate(&e0));
+  SBDGB_CUDA(cudaEventCreate(&e1));
+  for (int kern = 0; kern < 2; ++kern) {
+    float best = 1e30f;
+    int best_shape = 1;
+    for (int sh = 0; sh < kNumShapes; ++sh) {
+      for (int rep = 0; rep < 2; ++rep) {
+        SBDGB_CUDA(cudaEventRecord(e0, s));
+        if (kern == 0)
+          launch_a<T>(p, a, sh, s);
+        else
+          launch_b<T>(p, a, sh, s);
+        SBDGB_CUDA(cudaEventRecord(e1, s));
+        count_launch(p.ctx);
+      }
+      SBDGB_CUDA(cudaGetLastError());
+      SBDGB_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      SBDGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      p.tune_ms[prec][kern][sh] = ms;
+      if (ms < best) {
+        best = ms;
+        best_shape = sh;
+      }
+    }
+    (kern == 0 ? p.tune_a : p.tune_b)[prec] = best_shape;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  release_workspace(p, WS_TUNE);
+}
 
 template <typename T>
 void launch(Problem &p, const Args<T> &a, cudaStream_t s) {
-  constexpr int TB = kThreads * kCPT;
-  dim3 ga((p.na + kTA - 1) / kTA, (p.nb + TB - 1) / TB);
-  k_sigma_alpha<kTA, kCPT, T><<<ga, kThreads, 0, s>>>(a);
-  dim3 gb((p.nb + kTA - 1) / kTA, (p.na + TB - 1) / TB);
-  k_sigma_beta<kTA, kCPT, T><<<gb, kThreads, 0, s>>>(a);
+  const int prec = std::is_same<T, double>::value ? 0 : 1;
+  if (p.tune_a[prec] < 0 || p.tune_b[prec] < 0) autotune<T>(p, a, s);
+  launch_a<T>(p, a, p.tune_a[prec], s);
+  launch_b<T>(p, a, p.tune_b[prec], s);
   count_launch(p.ctx, 2);
   SBDGB_CUDA(cudaGetLastError());
 }
@@ -314,9 +432,6 @@ void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStre
   if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "sigma needs tables and diagonal");
   if (!p.CT) p.CT = (double *)dev_alloc(p, sizeof(double) * p.N);
   if (p.N == 0) return;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  begin_timing(p, s, ev0, ev1);
-  transpose<double>(p, C, p.CT, p.na, p.nb, s);
   Args<double> a = base_args<double>(p, C, S, accumulate);
   a.CT = p.CT;
   a.val_sa = p.A.val_s;
@@ -326,6 +441,13 @@ void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStre
   a.Jb = p.Jb;
   a.Ja = p.Ja;
   a.Kp = p.Kp;
+  if (p.tune_a[0] < 0) {
+    transpose<double>(p, C, p.CT, p.na, p.nb, s);
+    autotune<double>(p, a, s);
+  }
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  begin_timing(p, s, ev0, ev1);
+  transpose<double>(p, C, p.CT, p.na, p.nb, s);
   launch<double>(p, a, s);
   end_timing(p, s, ev0, ev1);
 }
@@ -357,9 +479,6 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s) {
   prepare_mixed(p, s);
   if (!p.CTf) p.CTf = (float *)dev_alloc(p, sizeof(float) * p.N);
   if (p.N == 0) return;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  begin_timing(p, s, ev0, ev1);
-  transpose<float>(p, C, p.CTf, p.na, p.nb, s);
   Args<float> a = base_args<float>(p, C, S, 0);
   a.CT = p.CTf;
   a.val_sa = p.val_sf[0];
@@ -369,6 +488,13 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s) {
   a.Jb = p.Jbf;
   a.Ja = p.Jaf;
   a.Kp = p.Kpf;
+  if (p.tune_a[1] < 0) {
+    transpose<float>(p, C, p.CTf, p.na, p.nb, s);
+    autotune<float>(p, a, s);
+  }
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  begin_timing(p, s, ev0, ev1);
+  transpose<float>(p, C, p.CTf, p.na, p.nb, s);
   launch<float>(p, a, s);
   end_timing(p, s, ev0, ev1);
 }

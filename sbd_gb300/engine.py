@@ -24,7 +24,7 @@ SYMBOLS = [
     "sbdgb_abi_version", "sbdgb_ctx_create", "sbdgb_ctx_destroy", "sbdgb_last_error", "sbdgb_ctx_bytes_in_use",
     "sbdgb_ctx_launch_count", "sbdgb_ctx_set_stream", "sbdgb_ctx_enable_timing", "sbdgb_ctx_sigma_timing", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
     "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
-    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
+    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_problem_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
     "sbdgb_davidson",
 ]
 
@@ -93,6 +93,8 @@ def load(path: str = LIB_PATH):
     L.sbdgb_sigma.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_sigma_mixed.argtypes = [vp, vp, vp, vp]
     L.sbdgb_mult_host.argtypes = [vp, vp, _f64p, _f64p]
+    L.sbdgb_problem_tuning.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                       C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
     L.sbdgb_davidson_default_opts.argtypes = [C.POINTER(DavidsonOpts)]
     L.sbdgb_davidson_default_opts.restype = None
     L.sbdgb_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _f64p, vp, C.POINTER(Report)]
@@ -242,6 +244,16 @@ class TPBProblem:
             hp = hii.ctypes.data
         self.engine.check(self.lib.sbdgb_mult_host(self.h, hp, wk, wb))
         return wb
+
+    def tuning(self, precision: int = FP64) -> dict:
+        """Sigma tile shapes chosen by the autotuner and the candidates' timings (ms)."""
+        a, b = C.c_int(-1), C.c_int(-1)
+        ma, mb = (C.c_float * 4)(), (C.c_float * 4)()
+        self.engine.check(self.lib.sbdgb_problem_tuning(self.h, precision, C.byref(a), C.byref(b), ma, mb, 4))
+        shapes = ["8x128", "8x256", "8x512", "16x256"]
+        return {"alpha_shape": shapes[a.value] if a.value >= 0 else None,
+                "beta_shape": shapes[b.value] if b.value >= 0 else None,
+                "alpha_ms": [round(x, 4) for x in ma], "beta_ms": [round(x, 4) for x in mb]}
 
     def sigma(self, C_in: np.ndarray) -> np.ndarray:
         return self.mult(C_in)

@@ -244,6 +244,7 @@ def run_gpu(args):
     sigma_ms_per = sigma_ms / max(ncalls, 1)
     achieved = bytes_sigma / (sigma_ms_per * 1e-3) / 1e9
     peak, peak_kind = peaks()
+    tiles = p.tuning(0)
 
     # mixed-precision form on the same problem (reported beside the FP64 headline)
     mixed = None
@@ -306,6 +307,7 @@ def run_gpu(args):
             "latency_s": {"p50": float(np.percentile(lat_sorted, 50)), "p99": float(np.percentile(lat_sorted, 99))},
             "sigma_products_per_solve": float(np.mean(nsig)),
             "sigma_ms": sigma_ms_per,
+            "sigma_tiles": tiles,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": "sigma operator (k_transpose + k_sigma_alpha + k_sigma_beta)",

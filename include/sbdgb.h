@@ -133,6 +133,20 @@ int sbdgb_sigma_mixed(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, void
 int sbdgb_problem_tuning(const sbdgb_problem *p, int precision, int *shape_a, int *shape_b, float *ms_a,
                          float *ms_b, int n_shapes);
 
+/* sigma that makes no device allocation.  No counterpart in the reference:
+ * it is for callers that cannot call cudaMalloc once they run (a host
+ * application whose pool allocator owns the device, a replay in a fixed
+ * memory plan).  Same result and arguments as sbdgb_sigma (FP64); the problem
+ * must already have its tables and diagonal.  The transposed-vector scratch
+ * is a file-scope device array of 2,097,152 doubles (16 MiB, held on every
+ * device that loads the library until exit); larger problems return
+ * SBDGB_E_UNSUPPORTED.  The first call on a device looks up the array's
+ * address (make it before any stream capture).  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
+ * It uses the autotuned tile shapes when the problem has them, the default
+ * shape otherwise, and records no timing events. */
+int sbdgb_sigma_noalloc(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accumulate, void *stream);
+
 /* Host-buffer form of sbd::mult: Wb += H*Wk with host vectors (copies
  * inside).  hii is ignored when NULL (the problem's own diagonal is used). */
 int sbdgb_mult_host(sbdgb_problem *p, const double *hii, const double *Wk, double *Wb);

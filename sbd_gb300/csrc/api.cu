@@ -87,12 +87,6 @@ cudaEvent_t timing_event(Ctx *c) {
 
 }  // namespace sbdgb
 
-struct sbdgb_ctx {
-  sbdgb::Ctx c;
-};
-struct sbdgb_problem {
-  sbdgb::Problem p;
-};
 
 using sbdgb::Error;
 

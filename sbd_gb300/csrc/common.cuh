@@ -176,9 +176,18 @@ void export_tables(const Problem &p, int spin, uint64_t *off_s, uint64_t *ket_s,
 void build_diag(Problem &p, cudaStream_t s);
 // sigma.cu
 void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s);
+void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, double *CT, cudaStream_t s);
 void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s);
 void prepare_mixed(Problem &p, cudaStream_t s);
 // davidson.cu
 void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X, sbdgb_report *rep);
 
 }  // namespace sbdgb
+
+// Opaque handles of the C ABI.
+struct sbdgb_ctx {
+  sbdgb::Ctx c;
+};
+struct sbdgb_problem {
+  sbdgb::Problem p;
+};

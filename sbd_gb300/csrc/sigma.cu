@@ -428,6 +428,29 @@ void transpose_fp64(Problem &p, const double *in, double *out, uint32_t R, uint3
   transpose<double>(p, in, out, R, Cn, s);
 }
 
+// FP64 sigma with a caller-provided transpose scratch of at least N doubles.
+// Makes no allocation: it neither autotunes (it uses the tuned shapes when the
+// problem has them, the 8x256 default otherwise) nor records timing events.
+void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, double *CT, cudaStream_t s) {
+  if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "sigma needs tables and diagonal");
+  if (p.N == 0) return;
+  Args<double> a = base_args<double>(p, C, S, accumulate);
+  a.CT = CT;
+  a.val_sa = p.A.val_s;
+  a.val_da = p.A.val_d;
+  a.val_sb = p.B.val_s;
+  a.val_db = p.B.val_d;
+  a.Jb = p.Jb;
+  a.Ja = p.Ja;
+  a.Kp = p.Kp;
+  transpose<double>(p, C, CT, p.na, p.nb, s);
+  const int sa = p.tune_a[0] >= 0 ? p.tune_a[0] : 1, sb = p.tune_b[0] >= 0 ? p.tune_b[0] : 1;
+  launch_a<double>(p, a, sa, s);
+  launch_b<double>(p, a, sb, s);
+  count_launch(p.ctx, 2);
+  SBDGB_CUDA(cudaGetLastError());
+}
+
 void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s) {
   if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "sigma needs tables and diagonal");
   if (!p.CT) p.CT = (double *)dev_alloc(p, sizeof(double) * p.N);

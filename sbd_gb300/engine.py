@@ -24,7 +24,7 @@ SYMBOLS = [
     "sbdgb_abi_version", "sbdgb_ctx_create", "sbdgb_ctx_destroy", "sbdgb_last_error", "sbdgb_ctx_bytes_in_use",
     "sbdgb_ctx_launch_count", "sbdgb_ctx_set_stream", "sbdgb_ctx_enable_timing", "sbdgb_ctx_sigma_timing", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
     "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
-    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_problem_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
+    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_noalloc", "sbdgb_problem_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
     "sbdgb_davidson",
 ]
 
@@ -92,6 +92,7 @@ def load(path: str = LIB_PATH):
     L.sbdgb_diag_terms.argtypes = [vp, vp]
     L.sbdgb_sigma.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_sigma_mixed.argtypes = [vp, vp, vp, vp]
+    L.sbdgb_sigma_noalloc.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_mult_host.argtypes = [vp, vp, _f64p, _f64p]
     L.sbdgb_problem_tuning.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]

@@ -1,0 +1,82 @@
+"""The allocation-free sigma entry point (sbdgb_sigma_noalloc) through the C ABI.
+
+Callers that cannot allocate device memory while they run (a host application
+whose pool allocator owns the device, a fixed memory plan) use this entry
+point: its transposed-vector scratch is a file-scope device array, so the call
+itself makes no allocation.  The test compares it with the regular sbdgb_sigma
+on two calls in a row and checks that the context's device memory does not
+grow.  This file is collected last on purpose.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from golden_io import max_rel
+
+pytestmark = pytest.mark.gpu
+
+
+def _entry(lib):
+    f = lib.sbdgb_sigma_noalloc
+    f.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
+    f.restype = C.c_int
+    return f
+
+
+def test_noalloc_sigma_matches_regular_sigma():
+    torch = pytest.importorskip("torch")
+    from sbd_gb300.engine import Engine, TPBProblem
+    from sbd_gb300.generators import make_problem
+
+    eng = Engine(0)
+    prob = make_problem(16, 5, 5, 300, 280, seed=77)
+    p = TPBProblem.from_problem(eng, prob)
+    p.build_tables()
+    p.diag_terms()
+    f = _entry(eng.lib)
+    rng = np.random.default_rng(11)
+    C1 = torch.tensor(rng.uniform(-1, 1, prob.ndet), dtype=torch.float64, device="cuda")
+    C2 = torch.tensor(rng.uniform(-1, 1, prob.ndet), dtype=torch.float64, device="cuda")
+    outs = []
+    before = eng.bytes_in_use
+    torch.cuda.synchronize()
+    for cvec in (C1, C2):  # two calls in a row share the scratch
+        s = torch.full_like(cvec, float("nan"))
+        rc = f(p.h, cvec.data_ptr(), s.data_ptr(), 0, None)
+        assert rc == 0, eng.lib.sbdgb_last_error(eng.h)
+        outs.append(s)
+    torch.cuda.synchronize()
+    assert eng.bytes_in_use == before  # nothing allocated by the two calls
+    for cvec, s in zip((C1, C2), outs):
+        ref = torch.zeros_like(cvec)
+        p.sigma_device(cvec.data_ptr(), ref.data_ptr(), accumulate=False, stream=0)
+        torch.cuda.synchronize()
+        assert max_rel(s.cpu().numpy(), ref.cpu().numpy()) <= 1e-12
+    # accumulate form: Wb += H Wk
+    acc = torch.ones_like(C1)
+    assert f(p.h, C1.data_ptr(), acc.data_ptr(), 1, None) == 0
+    torch.cuda.synchronize()
+    assert max_rel(acc.cpu().numpy() - 1.0, outs[0].cpu().numpy()) <= 1e-12
+    p.close()
+    eng.close()
+
+
+def test_noalloc_sigma_rejects_large_problems():
+    torch = pytest.importorskip("torch")
+    from sbd_gb300.engine import Engine, TPBProblem
+    from sbd_gb300.generators import make_problem
+
+    eng = Engine(0)
+    big = make_problem(24, 4, 4, 1600, 1600, seed=6)  # 2,560,000 determinants > 2,097,152
+    p = TPBProblem.from_problem(eng, big)
+    p.build_tables()
+    p.diag_terms()
+    f = _entry(eng.lib)
+    c = torch.zeros(big.ndet, dtype=torch.float64, device="cuda")
+    s = torch.zeros_like(c)
+    rc = f(p.h, c.data_ptr(), s.data_ptr(), 0, None)  # rejected on the host before any launch
+    assert rc == 2
+    assert b"at most" in eng.lib.sbdgb_last_error(eng.h)
+    p.close()
+    eng.close()

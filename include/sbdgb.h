@@ -94,8 +94,9 @@ int sbdgb_problem_create(sbdgb_ctx *ctx, int norb, const uint64_t *astr, size_t 
                          size_t nb, const double *h1, const double *eri_packed, double ecore,
                          sbdgb_problem **out);
 void sbdgb_problem_destroy(sbdgb_problem *p);
-/* Device memory the problem would hold once its tables and solver vectors
- * exist (used for admission by HBM footprint). */
+/* Upper bound of the device memory a problem holds through a Davidson solve
+ * with these options, excluding its excitation tables (24 bytes per single or
+ * double, 28 in the mixed form), whose size is known once they are built. */
 int sbdgb_problem_footprint(int norb, size_t na, size_t nb, int max_nb, int nroots, int precision,
                             size_t *bytes);
 
@@ -147,6 +148,13 @@ int sbdgb_problem_tuning(const sbdgb_problem *p, int precision, int *shape_a, in
  * shape otherwise, and records no timing events. */
 int sbdgb_sigma_noalloc(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accumulate, void *stream);
 
+/* Occupation density of a vector (OccupationDensity, chemistry/tpb/
+ * occupation.h:11-95, as sbd::tpb::diag reports it with do_rdm == 0,
+ * sbdiag.h:666-699): density[2p] = sum over determinants of |W|^2 with alpha
+ * orbital p occupied, density[2p+1] the same for beta.  W_dev: N doubles on
+ * the device; density: 2*norb doubles of host memory (the call waits for it). */
+int sbdgb_occupation_density(sbdgb_problem *p, const double *W_dev, double *density, void *stream);
+
 /* Host-buffer form of sbd::mult: Wb += H*Wk with host vectors (copies
  * inside).  hii is ignored when NULL (the problem's own diagonal is used). */
 int sbdgb_mult_host(sbdgb_problem *p, const double *hii, const double *Wk, double *Wb);
@@ -183,6 +191,75 @@ void sbdgb_davidson_default_opts(sbdgb_davidson_opts *o);
  * X (host, nroots*N, may be NULL) receives the normalized Ritz vectors and,
  * with init == 2, supplies the starting vectors. */
 int sbdgb_davidson(sbdgb_problem *p, const sbdgb_davidson_opts *o, double *E, double *X, sbdgb_report *rep);
+
+/* ---- serving: many solves at once, admitted by HBM footprint -------------
+ * No single counterpart in the reference, whose app solves one problem per
+ * run (apps/chemistry_tpb_selected_basis_diagonalization/main.cc:190-191);
+ * each request is that run's diag on its own inputs. */
+
+/* A request: the inputs of sbdgb_problem_create plus the Davidson options.
+ * The server copies every input at submission except vectors_out. */
+typedef struct {
+  int norb;
+  const uint64_t *astr;
+  size_t na;
+  const uint64_t *bstr;
+  size_t nb;
+  const double *h1;
+  const double *eri_packed;
+  double ecore;
+  sbdgb_davidson_opts opts;
+  double *vectors_out;   /* host, nroots*na*nb doubles, or NULL; must stay valid
+                            until the ticket's sbdgb_server_wait returns */
+} sbdgb_request;
+
+typedef struct {
+  int status;            /* SBDGB_OK or the failing step's status */
+  int nroots;
+  double energies[8];
+  double resid[8];
+  double queue_seconds;  /* submission to start */
+  double run_seconds;    /* start to finish: upload, tables, diagonal, solve */
+  double total_seconds;  /* submission to finish */
+  int iterations;
+  int sigma_calls;
+  int converged;
+  int worker;
+  size_t reserved_bytes; /* HBM reserved for the request once its tables were built */
+  uint64_t ndet;
+  char message[200];     /* error message when status != SBDGB_OK */
+} sbdgb_result;
+
+typedef struct {
+  uint64_t submitted, completed, failed, launches;
+  size_t budget_bytes, reserved_bytes, peak_reserved_bytes;
+  int workers, running, peak_running, queued;
+} sbdgb_serve_stats;
+
+typedef struct sbdgb_server sbdgb_server;
+
+/* `workers` solver threads (1..64), each with its own context and CUDA stream
+ * on `device`, so that their kernels overlap on the GPU.  A queued request
+ * starts when a worker is free and its reservation fits the HBM budget
+ * (0 = 90% of the memory free at creation); the first queued request that
+ * fits goes first, but none passes a request already passed 2*workers times.
+ * A request reserves an upper bound of its device memory at submission and
+ * shrinks it to its real size once its tables are built; it cannot use more
+ * than it reserved.  Results are those of sbdgb_davidson on the lone problem. */
+int sbdgb_server_create(int device, int workers, size_t hbm_budget_bytes, sbdgb_server **out);
+/* Queues a request and returns its ticket.  SBDGB_E_NOMEM if its reservation
+ * alone exceeds the budget. */
+int sbdgb_server_submit(sbdgb_server *s, const sbdgb_request *req, uint64_t *ticket);
+/* *done = 1 once the ticket's result is ready. */
+int sbdgb_server_poll(sbdgb_server *s, uint64_t ticket, int *done);
+/* Waits at most timeout_seconds (< 0: no limit) for the result; returns
+ * SBDGB_E_TIMEOUT if it is not ready.  The ticket is released once read. */
+int sbdgb_server_wait(sbdgb_server *s, uint64_t ticket, double timeout_seconds, sbdgb_result *out);
+int sbdgb_server_stats(sbdgb_server *s, sbdgb_serve_stats *out);
+const char *sbdgb_server_last_error(const sbdgb_server *s);
+/* Finishes the running requests, fails the queued ones (SBDGB_E_STATE), joins
+ * the workers and frees the pool.  Call it after every wait has returned. */
+void sbdgb_server_destroy(sbdgb_server *s);
 
 #ifdef __cplusplus
 }

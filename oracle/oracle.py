@@ -63,6 +63,9 @@ def lib():
         L.orc_davidson.argtypes = ([C.c_void_p, _u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int] + tab
                                    + [_f64p, _f64p, C.c_int, C.c_int, C.c_double,
                                       C.POINTER(C.c_double), C.POINTER(C.c_double)])
+        L.orc_density.argtypes = [_u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int, C.c_int, _f64p, _f64p]
+        L.orc_correlation.argtypes = ([_u64p, C.c_size_t, _u64p, C.c_size_t, C.c_int, C.c_int, C.c_int] + tab
+                                      + [_f64p, _f64p, _f64p])
         L.orc_inner.restype = C.c_double
         L.orc_inner.argtypes = [_f64p, _f64p, C.c_size_t]
         L.orc_symeig.argtypes = [C.c_int, _f64p, C.c_int, _f64p]
@@ -195,6 +198,63 @@ class Oracle:
         ns = lib().orc_davidson(*self._head(), *self._tabs(), self.hii(), W, max_it, max_nb, eps,
                                 C.byref(e), C.byref(r))
         return e.value, W, ns, r.value
+
+    def density(self, W: np.ndarray) -> np.ndarray:
+        """Occupation density [2L] (OccupationDensity, chemistry/tpb/occupation.h:11-95)."""
+        out = np.zeros(2 * self.norb)
+        lib().orc_density(self.aw.ravel(), self.na, self.bw.ravel(), self.nb, self.words, self.bit_length,
+                          self.norb, np.ascontiguousarray(W, dtype=np.float64), out)
+        return out
+
+    def correlation(self, W: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+        """One-particle (2, L*L) and two-particle (4, L^4) RDMs of W in the reference's
+        layout (Correlation, chemistry/tpb/correlation.h:379-640)."""
+        L = self.norb
+        one = np.zeros((2, L * L))
+        two = np.zeros((4, L ** 4))
+        lib().orc_correlation(self.aw.ravel(), self.na, self.bw.ravel(), self.nb, self.words, self.bit_length,
+                              L, *self._tabs(), np.ascontiguousarray(W, dtype=np.float64), one, two)
+        return one, two
+
+    def lanczos(self, max_it=20, num_block=40, eps=1e-12, W0=None):
+        """Matrix-free Lanczos of chemistry/tpb/lanczos.h:169-320 (restart from the
+        Ritz vector, no reorthogonalisation; stop when the lowest Ritz value moves
+        by less than eps or the off-diagonal falls below eps).  Returns (E0, W)."""
+        N = self.N
+        W = np.zeros(N) if W0 is None else np.array(W0, dtype=np.float64)
+        if W0 is None:
+            W[0] = 1.0
+        E = np.zeros(1)
+        for _ in range(max_it):
+            A = np.zeros((num_block, num_block))
+            Cs = [W.copy()]
+            HC = np.zeros(N)
+            n, stop, E_old = 0, False, 1.0e8
+            for ib in range(num_block):
+                n += 1
+                self.mult(Cs[ib], HC)
+                A[ib, ib] = lib().orc_inner(np.ascontiguousarray(Cs[ib]), HC, N)
+                E, U = np.linalg.eigh(A[:n, :n])
+                if abs(E[0] - E_old) < eps:
+                    stop = True
+                    break
+                E_old = E[0]
+                if ib + 1 == num_block:
+                    break
+                HC -= A[ib, ib] * Cs[ib]
+                nxt = HC.copy()
+                b = np.sqrt(lib().orc_inner(nxt, nxt, N))
+                nxt /= b
+                A[ib, ib + 1] = A[ib + 1, ib] = b
+                Cs.append(nxt)
+                if abs(b) < eps:
+                    break
+                HC = -b * Cs[ib]
+            E, U = np.linalg.eigh(A[:n, :n])
+            W = sum(U[j, 0] * Cs[j] for j in range(n))
+            if stop:
+                break
+        return float(E[0]), W
 
     def energy(self, W: np.ndarray) -> float:
         """<W|H|W> as the reference reports it after the solve (sbdiag.h:488-526)."""

@@ -16,7 +16,13 @@
 //   sbdref --fcidump F --adet A [--bdet B] --out OUTFILE
 //          [--bit_length 20] [--tables 1] [--hii 1] [--cvec C.bin]
 //          [--davidson 1 --block NB --iteration IT --tolerance EPS]
-//          [--time_mult K]
+//          [--time_mult K] [--density 1] [--rdm 1]
+//          [--lanczos 1 --lanczos_block NB --lanczos_iteration IT --lanczos_tolerance EPS]
+// --density and --rdm evaluate OccupationDensity (chemistry/tpb/occupation.h)
+// and Correlation (chemistry/tpb/correlation.h) on the --cvec vector; --lanczos
+// runs the matrix-free Lanczos (chemistry/tpb/lanczos.h:169) from the init-0
+// vector, as sbd::tpb::diag does for --method 2.
+#include <numeric>
 #include <omp.h>
 #include <chrono>
 #include <cstdio>
@@ -75,6 +81,12 @@ int main(int argc, char **argv) {
   const int max_it = std::stoi(arg(argc, argv, "--iteration", "1"));
   const double eps = std::stod(arg(argc, argv, "--tolerance", "1e-4"));
   const int time_mult = std::stoi(arg(argc, argv, "--time_mult", "0"));
+  const int want_density = std::stoi(arg(argc, argv, "--density", "0"));
+  const int want_rdm = std::stoi(arg(argc, argv, "--rdm", "0"));
+  const int want_lanczos = std::stoi(arg(argc, argv, "--lanczos", "0"));
+  const int lz_nb = std::stoi(arg(argc, argv, "--lanczos_block", "40"));
+  const int lz_it = std::stoi(arg(argc, argv, "--lanczos_iteration", "20"));
+  const double lz_eps = std::stod(arg(argc, argv, "--lanczos_tolerance", "1e-12"));
 
   sbd::FCIDump fcidump = sbd::LoadFCIDump(fcifile);
   int L = 0, Ne = 0;
@@ -165,6 +177,32 @@ int main(int argc, char **argv) {
       auto a1 = std::chrono::steady_clock::now();
       out.scalar("t_mult", std::chrono::duration<double>(a1 - a0).count());
     }
+    if (want_density) {
+      std::vector<int> oIdx(L);
+      std::iota(oIdx.begin(), oIdx.end(), 0);
+      std::vector<double> res;
+      sbd::OccupationDensity(oIdx, C, adet, bdet, bit_length, 1, 1, b_comm, res);
+      out.f64("density_c", res);
+    }
+    if (want_rdm) {
+      std::vector<std::vector<double>> one, two;
+      sbd::Correlation(C, adet, bdet, bit_length, (size_t)L, 1, 1, helper, h_comm, b_comm, t_comm, one, two);
+      for (int k = 0; k < 2; ++k) out.f64("rdm1_" + std::to_string(k), one[k]);
+      for (int k = 0; k < 4; ++k) out.f64("rdm2_" + std::to_string(k), two[k]);
+    }
+  }
+
+  if (want_lanczos) {
+    std::vector<double> W;
+    sbd::BasisInitVector(W, adet, bdet, 1, 1, h_comm, b_comm, t_comm, 0, 1729);
+    sbd::Lanczos(hii, W, adet, bdet, bit_length, (size_t)L, 1, 1, helper, I0, I1, I2, h_comm, b_comm, t_comm,
+                 lz_it, lz_nb, lz_eps);
+    std::vector<double> HW(W.size(), 0.0);
+    sbd::mult(hii, W, HW, adet, bdet, bit_length, (size_t)L, 1, 1, helper, I0, I1, I2, h_comm, b_comm, t_comm);
+    double E = 0.0, nrm = 0.0;
+    sbd::InnerProduct(W, HW, E, b_comm);
+    sbd::InnerProduct(W, W, nrm, b_comm);
+    out.scalar("lanczos_energy", E / nrm);
   }
 
   if (want_dav) {

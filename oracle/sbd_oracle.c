@@ -558,3 +558,120 @@ int orc_davidson(const orc_ints *t, const uint64_t *astr, size_t na, const uint6
   free(E);
   return nsigma;
 }
+
+/* ---- occupation density: chemistry/tpb/occupation.h:11-95 --------------- */
+
+void orc_density(const uint64_t *astr, size_t na, const uint64_t *bstr, size_t nb, int words, int bit_length,
+                 int L, const double *W, double *res) {
+  for (int k = 0; k < 2 * L; ++k) res[k] = 0.0;
+  for (size_t ia = 0; ia < na; ++ia)
+    for (size_t ib = 0; ib < nb; ++ib) {
+      const double w2 = W[ia * nb + ib] * W[ia * nb + ib];
+      for (int p = 0; p < L; ++p) {
+        if (orc_getocc(astr + ia * words, bit_length, p)) res[2 * p] += w2;
+        if (orc_getocc(bstr + ib * words, bit_length, p)) res[2 * p + 1] += w2;
+      }
+    }
+}
+
+/* ---- one- and two-particle RDMs: chemistry/tpb/correlation.h:379-640 with
+ * the element rules of chemistry/basic/correlation.h:17-299.
+ * one[s*L*L + i + L*j], two[(s1 + 2*s2)*L^4 + index as in the reference]. */
+
+static void orc_rdm_zero(const uint64_t *det, int dwords, int bl, int L, double w, double *one, double *two) {
+  const size_t L2 = (size_t)L * L, L3 = L2 * L, L4 = L3 * L;
+  int closed[256], nc = 0;
+  for (int x = 0; x < 2 * L; ++x)
+    if (orc_getocc(det, bl, x)) closed[nc++] = x;
+  (void)dwords;
+  for (int i = 0; i < nc; ++i) {
+    const int oi = closed[i] / 2, si = closed[i] % 2;
+    one[si * L2 + oi + (size_t)L * oi] += w;
+    for (int j = i + 1; j < nc; ++j) {
+      const int oj = closed[j] / 2, sj = closed[j] % 2;
+      two[(si + 2 * sj) * L4 + oi + L * oj + L2 * oi + L3 * oj] += w;
+      two[(sj + 2 * si) * L4 + oj + L * oi + L2 * oj + L3 * oi] += w;
+      if (si == sj) {
+        two[(si + 2 * sj) * L4 + oi + L * oj + L2 * oj + L3 * oi] -= w;
+        two[(sj + 2 * si) * L4 + oj + L * oi + L2 * oi + L3 * oj] -= w;
+      }
+    }
+  }
+}
+
+static void orc_rdm_one(const uint64_t *det, int dwords, int bl, int L, double v, int i, int a, double *one,
+                        double *two) {
+  const size_t L2 = (size_t)L * L, L3 = L2 * L, L4 = L3 * L;
+  double sgn = 1.0;
+  orc_parity(det, bl, i < a ? i : a, i < a ? a : i, &sgn);
+  const int oi = i / 2, si = i % 2, oa = a / 2;
+  const double x = v * sgn;
+  one[si * L2 + oi + (size_t)L * oa] += x;
+  for (int w = 0; w < dwords; ++w)
+    for (int pos = 0; pos < bl; ++pos) {
+      if (!((det[w] >> pos) & 1u)) continue;
+      const int soj = w * bl + pos, oj = soj / 2, sj = soj % 2;
+      two[(si + 2 * sj) * L4 + oa + oj * L + oi * L2 + oj * L3] += x;
+      two[(sj + 2 * si) * L4 + oj + oa * L + oj * L2 + oi * L3] += x;
+      if (si == sj) {
+        two[(si + 2 * sj) * L4 + oa + oj * L + oj * L2 + oi * L3] -= x;
+        two[(sj + 2 * si) * L4 + oj + oa * L + oi * L2 + oj * L3] -= x;
+      }
+    }
+}
+
+static void orc_rdm_two(const uint64_t *det, int bl, int L, double v, int i, int j, int a, int b, double *two) {
+  const size_t L2 = (size_t)L * L, L4 = L2 * L2;
+  double sgn = 1.0;
+  const int I = i < j ? i : j, J = i < j ? j : i, A = a < b ? a : b, B = a < b ? b : a;
+  orc_parity(det, bl, I < A ? I : A, I < A ? A : I, &sgn);
+  orc_parity(det, bl, J < B ? J : B, J < B ? B : J, &sgn);
+  if (A > J || B < I) sgn = -sgn;
+  const int oi = I / 2, si = I % 2, oa = A / 2, sa = A % 2, oj = J / 2, sj = J % 2, ob = B / 2, sb = B % 2;
+  const double x = sgn * v;
+  if (si == sa) {
+    two[(si + 2 * sj) * L4 + oa + (size_t)L * ob + L2 * (oi + (size_t)L * oj)] += x;
+    two[(sj + 2 * si) * L4 + ob + (size_t)L * oa + L2 * (oj + (size_t)L * oi)] += x;
+  }
+  if (si == sb) {
+    two[(si + 2 * sj) * L4 + oa + (size_t)L * ob + L2 * (oj + (size_t)L * oi)] -= x;
+    two[(sj + 2 * si) * L4 + ob + (size_t)L * oa + L2 * (oi + (size_t)L * oj)] -= x;
+  }
+}
+
+void orc_correlation(const uint64_t *astr, size_t na, const uint64_t *bstr, size_t nb, int words, int bit_length,
+                     int L, const size_t *aoff_s, const uint64_t *aket_s, const int32_t *acran_s,
+                     const size_t *aoff_d, const uint64_t *aket_d, const int32_t *acran_d, const size_t *boff_s,
+                     const uint64_t *bket_s, const int32_t *bcran_s, const size_t *boff_d, const uint64_t *bket_d,
+                     const int32_t *bcran_d, const double *W, double *one, double *two) {
+  const int bl = bit_length, dwords = (2 * L + bl - 1) / bl;
+  const size_t L2 = (size_t)L * L;
+  memset(one, 0, sizeof(double) * 2 * L2);
+  memset(two, 0, sizeof(double) * 4 * L2 * L2);
+  uint64_t det[ORC_MAXW];
+  for (size_t ia = 0; ia < na; ++ia)
+    for (size_t ib = 0; ib < nb; ++ib) {
+      const size_t bra = ia * nb + ib;
+      orc_det(astr + ia * words, bstr + ib * words, bl, L, det, dwords);
+      orc_rdm_zero(det, dwords, bl, L, W[bra] * W[bra], one, two);
+      /* task type 2 */
+      for (size_t j = aoff_s[ia]; j < aoff_s[ia + 1]; ++j)
+        orc_rdm_one(det, dwords, bl, L, W[bra] * W[aket_s[j] * nb + ib], acran_s[2 * j], acran_s[2 * j + 1], one,
+                    two);
+      for (size_t j = aoff_d[ia]; j < aoff_d[ia + 1]; ++j)
+        orc_rdm_two(det, bl, L, W[bra] * W[aket_d[j] * nb + ib], acran_d[4 * j], acran_d[4 * j + 1],
+                    acran_d[4 * j + 2], acran_d[4 * j + 3], two);
+      /* task type 1 */
+      for (size_t j = boff_s[ib]; j < boff_s[ib + 1]; ++j)
+        orc_rdm_one(det, dwords, bl, L, W[bra] * W[ia * nb + bket_s[j]], bcran_s[2 * j], bcran_s[2 * j + 1], one,
+                    two);
+      for (size_t j = boff_d[ib]; j < boff_d[ib + 1]; ++j)
+        orc_rdm_two(det, bl, L, W[bra] * W[ia * nb + bket_d[j]], bcran_d[4 * j], bcran_d[4 * j + 1],
+                    bcran_d[4 * j + 2], bcran_d[4 * j + 3], two);
+      /* task type 0 */
+      for (size_t j = aoff_s[ia]; j < aoff_s[ia + 1]; ++j)
+        for (size_t k = boff_s[ib]; k < boff_s[ib + 1]; ++k)
+          orc_rdm_two(det, bl, L, W[bra] * W[aket_s[j] * nb + bket_s[k]], acran_s[2 * j], bcran_s[2 * k],
+                      acran_s[2 * j + 1], bcran_s[2 * k + 1], two);
+    }
+}

@@ -89,6 +89,22 @@ int orc_davidson(const orc_ints *ints, const uint64_t *astr, size_t na, const ui
                  const int32_t *bcran_d, const double *hii, double *W, int max_it, int max_nb, double eps,
                  double *energy, double *resid);
 
+/* Occupation density of W (OccupationDensity, chemistry/tpb/occupation.h:
+ * 11-95): res[2p] = sum |W|^2 over determinants with alpha orbital p
+ * occupied, res[2p+1] the same for beta. */
+void orc_density(const uint64_t *astr, size_t na, const uint64_t *bstr, size_t nb, int words, int bit_length,
+                 int L, const double *W, double *res);
+
+/* One- and two-particle RDMs of W (Correlation at MPI size 1, chemistry/tpb/
+ * correlation.h:379-640, element rules chemistry/basic/correlation.h:17-299).
+ * one: 2 blocks of L*L (spin s at s*L*L), two: 4 blocks of L^4 (spin pair
+ * s1 + 2*s2), indexed as in the reference.  Serial, fixed order. */
+void orc_correlation(const uint64_t *astr, size_t na, const uint64_t *bstr, size_t nb, int words, int bit_length,
+                     int L, const size_t *aoff_s, const uint64_t *aket_s, const int32_t *acran_s,
+                     const size_t *aoff_d, const uint64_t *aket_d, const int32_t *acran_d, const size_t *boff_s,
+                     const uint64_t *bket_s, const int32_t *bcran_s, const size_t *boff_d, const uint64_t *bket_d,
+                     const int32_t *bcran_d, const double *W, double *one, double *two);
+
 /* Kahan-compensated inner product (framework/dm_vector.h:23-51). */
 double orc_inner(const double *x, const double *y, size_t n);
 

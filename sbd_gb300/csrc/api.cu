@@ -9,18 +9,36 @@ namespace sbdgb {
 
 void unpack_integrals(Problem &p, const double *eri_dev, cudaStream_t s);
 
+void *tmp_alloc(Ctx *c, size_t bytes) {
+  if (bytes == 0) bytes = 8;
+  void *d = nullptr;
+  cudaError_t e = c->pool ? cudaMallocFromPoolAsync(&d, bytes, c->pool, c->stream) : cudaMalloc(&d, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(SBDGB_E_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+  }
+  return d;
+}
+
+// Pool memory is released in stream order; plain memory after the stream
+// has drained (cudaFree would otherwise wait for the whole device).
+void tmp_free(Ctx *c, void *d) {
+  if (!d) return;
+  if (c->pool) {
+    cudaFreeAsync(d, c->stream);
+  } else {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(d);
+  }
+}
+
 void *dev_alloc(Problem &p, size_t bytes) {
   if (bytes == 0) bytes = 8;
   Ctx *c = p.ctx;
   if (c->budget && c->in_use + bytes > c->budget)
     throw Error(SBDGB_E_NOMEM, "HBM budget exceeded (" + std::to_string(c->in_use + bytes) + " > " +
                                    std::to_string(c->budget) + " bytes)");
-  void *d = nullptr;
-  cudaError_t e = cudaMalloc(&d, bytes);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    throw Error(SBDGB_E_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
-  }
+  void *d = tmp_alloc(c, bytes);
   p.allocs.push_back(d);
   p.bytes += bytes;
   c->in_use += bytes;
@@ -30,23 +48,11 @@ void *dev_alloc(Problem &p, size_t bytes) {
 void *workspace(Problem &p, int slot, size_t bytes) {
   if (bytes == 0) bytes = 8;
   if (p.ws[slot] && p.ws_bytes[slot] >= bytes) return p.ws[slot];
-  if (p.ws[slot]) {
-    SBDGB_CUDA(cudaStreamSynchronize(p.ctx->stream));
-    cudaFree(p.ws[slot]);
-    p.bytes -= p.ws_bytes[slot];
-    p.ctx->in_use -= p.ws_bytes[slot];
-    p.ws[slot] = nullptr;
-    p.ws_bytes[slot] = 0;
-  }
+  if (p.ws[slot]) release_workspace(p, slot);
   Ctx *c = p.ctx;
   if (c->budget && c->in_use + bytes > c->budget)
     throw Error(SBDGB_E_NOMEM, "HBM budget exceeded by a solver workspace");
-  void *d = nullptr;
-  cudaError_t e = cudaMalloc(&d, bytes);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    throw Error(SBDGB_E_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
-  }
+  void *d = tmp_alloc(c, bytes);
   p.ws[slot] = d;
   p.ws_bytes[slot] = bytes;
   p.bytes += bytes;
@@ -56,8 +62,7 @@ void *workspace(Problem &p, int slot, size_t bytes) {
 
 void release_workspace(Problem &p, int slot) {
   if (!p.ws[slot]) return;
-  SBDGB_CUDA(cudaStreamSynchronize(p.ctx->stream));
-  cudaFree(p.ws[slot]);
+  tmp_free(p.ctx, p.ws[slot]);
   p.bytes -= p.ws_bytes[slot];
   p.ctx->in_use -= p.ws_bytes[slot];
   p.ws[slot] = nullptr;
@@ -65,13 +70,56 @@ void release_workspace(Problem &p, int slot) {
 }
 
 void dev_free_all(Problem &p) {
-  if (p.ctx && p.ctx->stream) cudaStreamSynchronize(p.ctx->stream);
-  for (void *d : p.allocs) cudaFree(d);
-  for (int i = 0; i < WS_COUNT; ++i)
-    if (p.ws[i]) cudaFree(p.ws[i]);
-  if (p.ctx) p.ctx->in_use -= std::min(p.ctx->in_use, p.bytes);
+  Ctx *c = p.ctx;
+  if (!c) return;
+  if (!c->pool && c->stream) cudaStreamSynchronize(c->stream);
+  for (void *d : p.allocs) {
+    if (c->pool)
+      cudaFreeAsync(d, c->stream);
+    else
+      cudaFree(d);
+  }
+  for (int i = 0; i < WS_COUNT; ++i) {
+    if (!p.ws[i]) continue;
+    if (c->pool)
+      cudaFreeAsync(p.ws[i], c->stream);
+    else
+      cudaFree(p.ws[i]);
+    p.ws[i] = nullptr;
+    p.ws_bytes[i] = 0;
+  }
+  c->in_use -= std::min(c->in_use, p.bytes);
   p.allocs.clear();
   p.bytes = 0;
+}
+
+size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts &o, uint64_t entries_a,
+                       uint64_t entries_b) {
+  const size_t N = na * nb, L = (size_t)norb, npair = L * (L + 1) / 2;
+  const bool mixed = o.precision == SBDGB_MIXED;
+  const size_t k = (size_t)std::max(1, o.nroots);
+  size_t b = 0;
+  // strings, h1, (P|Q)
+  b += 8 * (na + nb) + 8 * L * L + 8 * npair * npair;
+  // tables: per spin four offset arrays, 24 bytes per entry; (pp|qq), (pq|qp), Coulomb rows
+  b += 16 * (na + nb + 2) + 16 + 24 * (entries_a + entries_b) + 16 * L * L + 8 * npair * (na + nb);
+  b += 16 * (na + nb + 4);  // sigma row tiles (two row caps, start + order per spin)
+  // diagonal and its workspaces
+  b += 8 * N + 8 * (na + nb + 2) + 8 * (na * L + 1);
+  // FP64 sigma transpose scratch (also used by the mixed refinement)
+  b += 8 * N;
+  // solver reductions (partial sums of at most 4 blocks per SM of 64 values, staging)
+  b += 8 * (size_t)(1024 * 64 * 4 + 64) + 8 * 4096 + 8 * 8192;
+  if (!mixed) {
+    const size_t max_nb = std::min<size_t>((size_t)std::max(o.max_nb, 2 * (int)k), std::max<size_t>(N, 1));
+    b += 16 * N * max_nb + 32 * N * k;
+  } else {
+    const size_t mmax = (size_t)std::max(std::min(o.max_nb, 64) - (int)k, 2 * (int)k);
+    b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;  // FP32 tables
+    b += 4 * N;                                                                          // FP32 transpose
+    b += 32 * N * k + 4 * N * (k + mmax) + 4 * N * mmax + 12 * N * k + 4 * (8 * 3 * 64 + 64);
+  }
+  return b;
 }
 
 cudaEvent_t timing_event(Ctx *c) {
@@ -197,18 +245,13 @@ int sbdgb_check_comm_sizes(sbdgb_ctx *ctx, int h_size, int b_size, int t_size) {
 
 int sbdgb_problem_footprint(int norb, size_t na, size_t nb, int max_nb, int nroots, int precision,
                             size_t *bytes) {
-  if (!bytes || norb < 1 || norb > 64) return SBDGB_E_INPUT;
-  const size_t N = na * nb;
-  const size_t npair = (size_t)norb * (norb + 1) / 2;
-  const size_t vec = precision == SBDGB_MIXED ? 4 : 8;
-  size_t b = 0;
-  b += 8 * (na + nb) + 8 * npair * npair + 8 * npair * (na + nb);  // strings, (P|Q), Coulomb rows
-  b += 8 * N * 2;                                                   // hii + transpose scratch
-  b += (size_t)(2 * std::max(max_nb, 2 * nroots) + 3 * nroots) * N * vec;  // basis, sigma, Ritz, residuals
-  if (precision == SBDGB_MIXED) b += 8 * N * 3;                            // FP64 refinement vectors
-  // excitation tables: estimated from the string counts at up to norb^4/4 pairs per string is
-  // too loose to be useful; the tables are accounted exactly once built.
-  *bytes = b;
+  if (!bytes || norb < 1 || norb > 64 || nroots < 1) return SBDGB_E_INPUT;
+  sbdgb_davidson_opts o;
+  sbdgb_davidson_default_opts(&o);
+  o.max_nb = max_nb;
+  o.nroots = nroots;
+  o.precision = precision;
+  *bytes = sbdgb::solve_footprint(norb, na, nb, o, 0, 0);
   return SBDGB_OK;
 }
 
@@ -252,15 +295,14 @@ int sbdgb_problem_create(sbdgb_ctx *ctx, int norb, const uint64_t *astr, size_t 
     p.h1 = (double *)sbdgb::dev_alloc(p, 8 * (size_t)norb * norb);
     p.Kp = (double *)sbdgb::dev_alloc(p, 8 * (size_t)p.npair * p.npair);
     const size_t neri = (size_t)p.npair * (p.npair + 1) / 2;
-    double *eri = nullptr;
-    SBDGB_CUDA(cudaMalloc(&eri, 8 * neri));
+    double *eri = (double *)sbdgb::tmp_alloc(&ctx->c, 8 * neri);
     SBDGB_CUDA(cudaMemcpyAsync(p.astr, astr, 8 * na, cudaMemcpyHostToDevice, s));
     SBDGB_CUDA(cudaMemcpyAsync(p.bstr, bstr, 8 * nb, cudaMemcpyHostToDevice, s));
     SBDGB_CUDA(cudaMemcpyAsync(p.h1, h1, 8 * (size_t)norb * norb, cudaMemcpyHostToDevice, s));
     SBDGB_CUDA(cudaMemcpyAsync(eri, eri_packed, 8 * neri, cudaMemcpyHostToDevice, s));
     sbdgb::unpack_integrals(p, eri, s);
+    sbdgb::tmp_free(&ctx->c, eri);
     SBDGB_CUDA(cudaStreamSynchronize(s));
-    cudaFree(eri);
   });
   if (rc != SBDGB_OK) {
     sbdgb::dev_free_all(p);

@@ -109,6 +109,7 @@ enum WsSlot {
   WS_V, WS_HV, WS_X, WS_HX, WS_T, WS_PARTIAL, WS_RED, WS_COEF,
   WS_DIAG0, WS_DIAG1, WS_DIAG2,
   WS_VF, WS_HVF, WS_CF, WS_SF, WS_RES64, WS_C64, WS_TUNE,
+  WS_U, WS_UF, WS_RED2, WS_NORM_A, WS_NORM_B, WS_OCC,
   WS_COUNT
 };
 
@@ -135,6 +136,11 @@ struct Problem {
   void *ws[WS_COUNT] = {};
   size_t ws_bytes[WS_COUNT] = {};
   bool tables = false, diag = false, mixed_ready = false;
+  // Work-balanced row tiles of the sigma kernels, per spin and per row cap
+  // (8 or 16): tile t covers rows [start[t], start[t+1]), and CTAs take the
+  // tiles in order[] (heaviest first).
+  uint32_t *tile_start[2][2] = {}, *tile_order[2][2] = {};
+  uint32_t n_tiles[2][2] = {};
   int tune_a[2] = {-1, -1}, tune_b[2] = {-1, -1};  // autotuned sigma tile shapes (FP64, mixed)
   float tune_ms[2][2][8] = {};                       // timings the autotuner saw
   size_t bytes = 0;
@@ -155,12 +161,24 @@ struct Ctx {
   bool timing = false;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> sigma_events;
   std::vector<cudaEvent_t> event_pool;
+  // Serving contexts: device memory comes from a shared stream-ordered pool
+  // (allocation and release never synchronise the device), and sigma takes
+  // its tile shapes from the problem size instead of timing candidates.
+  cudaMemPool_t pool = nullptr;
+  bool autotune = true;
 };
 
 // sigma timing hooks (api.cu)
 cudaEvent_t timing_event(Ctx *c);
 
 void *dev_alloc(Problem &p, size_t bytes);
+// Temporary device buffer outside the problem's accounting (pool-aware).
+void *tmp_alloc(Ctx *c, size_t bytes);
+void tmp_free(Ctx *c, void *d);
+// Upper bound of the device bytes a problem holds through a solve with
+// options o, given its excitation-table entries (singles + doubles) per spin.
+size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts &o, uint64_t entries_a,
+                       uint64_t entries_b);
 void *workspace(Problem &p, int slot, size_t bytes);
 void release_workspace(Problem &p, int slot);
 void dev_free_all(Problem &p);
@@ -175,6 +193,7 @@ void export_tables(const Problem &p, int spin, uint64_t *off_s, uint64_t *ket_s,
 // diag.cu
 void build_diag(Problem &p, cudaStream_t s);
 // sigma.cu
+void build_row_tiles(Problem &p, cudaStream_t s);
 void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s);
 void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, double *CT, cudaStream_t s);
 void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s);

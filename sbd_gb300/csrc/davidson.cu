@@ -125,11 +125,17 @@ struct CombineArgs {
   double *X;        // k x N or null
   double *HX;       // k x N or null
   double *T;        // k x N or null: preconditioned residual
-  double *partial;  // blocks x k residual norm^2 partials
+  double *U;        // k x N or null: X / (theta - d), for the Olsen correction of T
+  double *partial;  // blocks x k residual norm^2 partials (x 3k with U: norm^2, x.T, x.U)
 };
 
 // X_r = V c_r, HX_r = HV c_r, R_r = HX_r - theta_r X_r, T_r = R_r / (theta_r - d)
-// (davidson.h:818-843 and the preconditioner :899-908, 1e-12 guard).
+// (davidson.h:818-843 and the preconditioner :899-908, 1e-12 guard).  With U
+// it also writes U_r = X_r / (theta_r - d) and sums x.T and x.U, from which
+// the host forms Olsen's correction T_r - eps_r U_r (eps_r = x.T / x.U), the
+// component of the preconditioned residual orthogonal to the Ritz vector.
+// Where the diagonal is nearly exact (weakly coupled determinants) the plain
+// correction is almost parallel to X and the subspace stops growing.
 template <int K>
 __global__ void __launch_bounds__(kRed) k_combine(CombineArgs a) {
   __shared__ double cs[kMaxCoef];
@@ -137,9 +143,9 @@ __global__ void __launch_bounds__(kRed) k_combine(CombineArgs a) {
   for (int t = threadIdx.x; t < a.nv * K; t += kRed) cs[t] = a.coef[t];
   if (threadIdx.x < K) th[threadIdx.x] = a.theta[threadIdx.x];
   __syncthreads();
-  double rn[K];
+  double rn[K], xt[K], xu[K];
 #pragma unroll
-  for (int r = 0; r < K; ++r) rn[r] = 0.0;
+  for (int r = 0; r < K; ++r) rn[r] = xt[r] = xu[r] = 0.0;
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < a.N; e += (size_t)gridDim.x * kRed) {
     double x[K], h[K];
 #pragma unroll
@@ -166,24 +172,44 @@ __global__ void __launch_bounds__(kRed) k_combine(CombineArgs a) {
       if (a.T) {
         double den = th[r] - d;
         if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
-        a.T[(size_t)r * a.N + e] = res / den;
+        const double t = res / den;
+        a.T[(size_t)r * a.N + e] = t;
+        if (a.U) {
+          const double u = x[r] / den;
+          a.U[(size_t)r * a.N + e] = u;
+          xt[r] = fma(x[r], t, xt[r]);
+          xu[r] = fma(x[r], u, xu[r]);
+        }
       }
     }
   }
-  __shared__ double red[kRed / 32][16];
+  constexpr int W3 = 3 * K;
+  __shared__ double red[kRed / 32][W3];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int width = a.U ? W3 : K;
 #pragma unroll
-  for (int r = 0; r < K; ++r) {
-    double x = rn[r];
+  for (int r = 0; r < W3; ++r) {
+    double x = r < K ? rn[r] : (r < 2 * K ? xt[r - K] : xu[r - 2 * K]);
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
     if (lane == 0) red[warp][r] = x;
   }
   __syncthreads();
-  if (threadIdx.x < K) {
+  if (threadIdx.x < width) {
     double x = 0.0;
     for (int w2 = 0; w2 < kRed / 32; ++w2) x += red[w2][threadIdx.x];
-    a.partial[(size_t)blockIdx.x * K + threadIdx.x] = x;
+    a.partial[(size_t)blockIdx.x * width + threadIdx.x] = x;
   }
+}
+
+// T_r -= eps_r U_r (Olsen's correction, eps on the device).
+template <typename T>
+__global__ void __launch_bounds__(kRed) k_olsen(T *__restrict__ Tv, const T *__restrict__ U,
+                                                 const double *__restrict__ eps, int k, size_t N) {
+  for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed)
+    for (int r = 0; r < k; ++r) {
+      const T ep = (T)eps[r];
+      Tv[(size_t)r * N + e] = fma(-ep, U[(size_t)r * N + e], Tv[(size_t)r * N + e]);
+    }
 }
 
 // T_r -= sum_j V_j G[j][r]  (G column-major, ld = nv), in the vectors' precision.
@@ -306,13 +332,23 @@ struct MixedResArgs {
   const float *theta;  // nq current Ritz values
   const double *hii;
   float *T;            // out: nq preconditioned residuals
-  double *partial;     // blocks x nq residual norm^2
+  float *U;            // out: nq Ritz vectors / (theta - d), for Olsen's correction
+  double *partial;     // blocks x 3nq: residual norm^2, x.T, x.U
 };
 
 // For each root q of the block:
 //   r_q = sum_j (Rf_j + dth_jq Xf_j) cx_jq + sum_l (HW_l - theta_q W_l) cw_lq
-//   T_q = r_q / (theta_q - d) with the reference's 1e-12 guard.
-// FP32 arithmetic; Xf, Rf, W, HW are read once for all roots.
+//   T_q = r_q / (theta_q - d) with the reference's 1e-12 guard,
+//   U_q = x_q / (theta_q - d), x_q = sum_j Xf_j cx_jq + sum_l W_l cw_lq,
+// and the sums x.T and x.U of Olsen's correction (see k_combine).
+// FP32 arithmetic with compensated sums; Xf, Rf, W, HW are read once for all roots.
+__device__ __forceinline__ void kahan_add(float &s, float &c, float v) {
+  const float y = v - c;
+  const float t = s + y;
+  c = (t - s) - y;
+  s = t;
+}
+
 template <int K>
 __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
   __shared__ float c[K][3 * 64];
@@ -320,51 +356,58 @@ __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
   for (int t = threadIdx.x; t < K * 3 * 64; t += kRed) c[t / (3 * 64)][t % (3 * 64)] = a.coef[t];
   if (threadIdx.x < K) th[threadIdx.x] = a.theta[threadIdx.x];
   __syncthreads();
-  float s[K], comp[K];
+  float s[3 * K], comp[3 * K];
 #pragma unroll
-  for (int q = 0; q < K; ++q) {
+  for (int q = 0; q < 3 * K; ++q) {
     s[q] = 0.f;
     comp[q] = 0.f;
   }
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < a.N; e += (size_t)gridDim.x * kRed) {
-    float r[K];
+    float r[K], x[K];
 #pragma unroll
-    for (int q = 0; q < K; ++q) r[q] = 0.f;
+    for (int q = 0; q < K; ++q) r[q] = x[q] = 0.f;
     for (int j = 0; j < a.k; ++j) {
       const float xf = __ldg(a.Xf + (size_t)j * a.N + e), rf = __ldg(a.Rf + (size_t)j * a.N + e);
 #pragma unroll
-      for (int q = 0; q < K; ++q) r[q] = fmaf(fmaf(c[q][64 + j], xf, rf), c[q][j], r[q]);
+      for (int q = 0; q < K; ++q) {
+        r[q] = fmaf(fmaf(c[q][64 + j], xf, rf), c[q][j], r[q]);
+        x[q] = fmaf(xf, c[q][j], x[q]);
+      }
     }
     for (int l = 0; l < a.m; ++l) {
       const float w = __ldg(a.W + (size_t)l * a.N + e), hw = __ldg(a.HW + (size_t)l * a.N + e);
 #pragma unroll
-      for (int q = 0; q < K; ++q) r[q] = fmaf(fmaf(-th[q], w, hw), c[q][128 + l], r[q]);
+      for (int q = 0; q < K; ++q) {
+        r[q] = fmaf(fmaf(-th[q], w, hw), c[q][128 + l], r[q]);
+        x[q] = fmaf(w, c[q][128 + l], x[q]);
+      }
     }
     const double d = __ldg(a.hii + e);
 #pragma unroll
     for (int q = 0; q < K; ++q) {
-      const float y = r[q] * r[q] - comp[q];
-      const float t = s[q] + y;
-      comp[q] = (t - s[q]) - y;
-      s[q] = t;
+      kahan_add(s[q], comp[q], r[q] * r[q]);
       double den = (double)th[q] - d;
       if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
-      a.T[(size_t)q * a.N + e] = (float)((double)r[q] / den);
+      const float t = (float)((double)r[q] / den), u = (float)((double)x[q] / den);
+      a.T[(size_t)q * a.N + e] = t;
+      a.U[(size_t)q * a.N + e] = u;
+      kahan_add(s[K + q], comp[K + q], x[q] * t);
+      kahan_add(s[2 * K + q], comp[2 * K + q], x[q] * u);
     }
   }
-  __shared__ double red[kRed / 32][K];
+  __shared__ double red[kRed / 32][3 * K];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int q = 0; q < K; ++q) {
-    double x = (double)s[q] - (double)comp[q];
-    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-    if (lane == 0) red[warp][q] = x;
+  for (int q = 0; q < 3 * K; ++q) {
+    double v = (double)s[q] - (double)comp[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[warp][q] = v;
   }
   __syncthreads();
-  if (threadIdx.x < K) {
+  if (threadIdx.x < 3 * K) {
     double t = 0.0;
     for (int w2 = 0; w2 < kRed / 32; ++w2) t += red[w2][threadIdx.x];
-    a.partial[(size_t)blockIdx.x * K + threadIdx.x] = t;
+    a.partial[(size_t)blockIdx.x * 3 * K + threadIdx.x] = t;
   }
 }
 
@@ -468,12 +511,14 @@ struct Solver {
   // Ritz vectors (optional), their sigma (optional) and the preconditioned
   // residuals (optional) of the combination c; returns the residual norms.
   std::vector<double> combine(const double *V, const double *HV, int nv, int k, const std::vector<double> &c,
-                              const std::vector<double> &theta, double *X, double *HX, double *T) {
+                              const std::vector<double> &theta, double *X, double *HX, double *T,
+                              double *U = nullptr) {
     std::vector<double> hc((size_t)nv * k + 16, 0.0);
     std::copy(c.begin(), c.end(), hc.begin());
     SBDGB_CUDA(cudaMemcpyAsync(coef, hc.data(), sizeof(double) * nv * k, cudaMemcpyHostToDevice, s));
     SBDGB_CUDA(cudaMemcpyAsync(red + 2048, theta.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
-    CombineArgs a{V, HV, N, nv, k, coef, red + 2048, p.hii, X, HX, T, partial};
+    if (!T) U = nullptr;
+    CombineArgs a{V, HV, N, nv, k, coef, red + 2048, p.hii, X, HX, T, U, partial};
     switch (k) {
 #define SBDGB_K(KK) \
   case KK: k_combine<KK><<<blocks, kRed, 0, s>>>(a); break;
@@ -482,14 +527,37 @@ struct Solver {
 #undef SBDGB_K
       default: throw Error(SBDGB_E_UNSUPPORTED, "at most 16 roots");
     }
-    k_sum_partials<<<1, 64, 0, s>>>(partial, blocks, k, red);
+    const int width = U ? 3 * k : k;
+    k_sum_partials<<<1, 64, 0, s>>>(partial, blocks, width, red);
     count_launch(p.ctx, 2);
     SBDGB_CUDA(cudaGetLastError());
-    std::vector<double> rn(k);
-    SBDGB_CUDA(cudaMemcpyAsync(rn.data(), red, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+    std::vector<double> v(width);
+    SBDGB_CUDA(cudaMemcpyAsync(v.data(), red, sizeof(double) * width, cudaMemcpyDeviceToHost, s));
     SBDGB_CUDA(cudaStreamSynchronize(s));
+    std::vector<double> rn(v.begin(), v.begin() + k);
     for (auto &x : rn) x = std::sqrt(std::max(0.0, x));
+    if (U) olsen<double>(T, U, k, std::vector<double>(v.begin() + k, v.begin() + 2 * k),
+                         std::vector<double>(v.begin() + 2 * k, v.end()));
     return rn;
+  }
+
+  // T_r -= (x.T_r / x.U_r) U_r for every root whose ratio is finite.
+  template <typename T>
+  void olsen(T *Tv, const T *U, int k, const std::vector<double> &xt, const std::vector<double> &xu) {
+    std::vector<double> e(k, 0.0);
+    bool any = false;
+    for (int r = 0; r < k; ++r) {
+      const double q = xt[r] / xu[r];
+      if (std::isfinite(q) && xu[r] != 0.0) {
+        e[r] = q;
+        any = true;
+      }
+    }
+    if (!any) return;
+    SBDGB_CUDA(cudaMemcpyAsync(red + 2200, e.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    k_olsen<T><<<blocks, kRed, 0, s>>>(Tv, U, red + 2200, k, N);
+    count_launch(p.ctx);
+    SBDGB_CUDA(cudaGetLastError());
   }
 
   template <typename T>
@@ -672,6 +740,7 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
   double *X = (double *)workspace(p, WS_X, sizeof(double) * N * k);
   double *HX = (double *)workspace(p, WS_HX, sizeof(double) * N * k);
   double *T = (double *)workspace(p, WS_T, sizeof(double) * N * k);
+  double *U = (double *)workspace(p, WS_U, sizeof(double) * N * k);
 
   sbdgb_report r{};
   sv.start_vectors(o, k, T, Xout);
@@ -713,7 +782,7 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
       for (int i = 0; i < nv; ++i) c[i + (size_t)nv * q] = Y[i + (size_t)nv * q];
     th.assign(theta.begin(), theta.begin() + kk);
     // residual norms and preconditioned corrections; Ritz vectors not materialised
-    resid = sv.combine(V, HV, nv, kk, c, th, nullptr, nullptr, T);
+    resid = sv.combine(V, HV, nv, kk, c, th, nullptr, nullptr, T, U);
     iter++;
     r.iterations = iter;
     if (o.verbose) print_iter("", iter, resid, th, kk);
@@ -785,6 +854,7 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
   float *HW = (float *)workspace(p, WS_HVF, sizeof(float) * N * mmax);
   float *Rf = (float *)workspace(p, WS_SF, sizeof(float) * N * k);
   float *Tf = (float *)workspace(p, WS_CF, sizeof(float) * N * k);
+  float *Uf = (float *)workspace(p, WS_UF, sizeof(float) * N * k);
   float *dcoef = (float *)workspace(p, WS_DIAG1, sizeof(float) * (kMaxBlock * 3 * 64 + 64));
 
   sbdgb_report r{};
@@ -902,7 +972,7 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       }
       SBDGB_CUDA(cudaMemcpyAsync(dcoef, hc.data(), sizeof(float) * hc.size(), cudaMemcpyHostToDevice, s));
       SBDGB_CUDA(cudaMemcpyAsync(dcoef + hc.size(), hth.data(), sizeof(float) * kMaxBlock, cudaMemcpyHostToDevice, s));
-      MixedResArgs ma{Xf, Rf, W, HW, k, m, nq, N, dcoef, dcoef + hc.size(), p.hii, Tf, sv.partial};
+      MixedResArgs ma{Xf, Rf, W, HW, k, m, nq, N, dcoef, dcoef + hc.size(), p.hii, Tf, Uf, sv.partial};
       switch (nq) {
 #define SBDGB_K(KK) \
   case KK: k_mixed_residual<KK><<<sv.blocks, kRed, 0, s>>>(ma); break;
@@ -913,8 +983,10 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       count_launch(p.ctx);
       SBDGB_CUDA(cudaGetLastError());
       std::vector<double> rn;
-      sv.reduce_partials(nq, &rn);
+      sv.reduce_partials(3 * nq, &rn);
       for (int i = 0; i < nq; ++i) res_est[roots[i]] = std::sqrt(std::max(0.0, rn[i]));
+      sv.olsen<float>(Tf, Uf, nq, std::vector<double>(rn.begin() + nq, rn.begin() + 2 * nq),
+                      std::vector<double>(rn.begin() + 2 * nq, rn.end()));
       // orthonormalise the block against [Xf, W] and itself, into W[m..]
       const int added = sv.orthonormalize_block<float>(Tf, nq, XW, k + m, W + (size_t)m * N, 1e-3);
       if (added == 0) {

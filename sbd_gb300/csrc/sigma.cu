@@ -68,6 +68,7 @@ struct Args {
   const T *Ja;  // [npair][na]
   const T *Kp;  // [npair][npair]
   int npair;
+  const uint32_t *tile_start, *tile_order;  // row tiles of the kernel's row spin
 };
 
 template <typename T>
@@ -172,7 +173,9 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
 template <int TA, int CPT, typename T>
 __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
   constexpr int TB = kThreads * CPT;
-  const uint32_t ia0 = blockIdx.x * TA;
+  const uint32_t tile = __ldg(a.tile_order + blockIdx.x);
+  const uint32_t ia0 = __ldg(a.tile_start + tile);
+  const uint32_t rend = __ldg(a.tile_start + tile + 1) - ia0;  // <= TA
   const uint32_t ib0 = blockIdx.y * TB;
   uint32_t col[CPT], q0[CPT], q1[CPT];
   bool ok[CPT];
@@ -185,7 +188,6 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
     q0[c] = ok[c] ? __ldg(a.B.off_s + col[c]) : 0u;
     q1[c] = ok[c] ? __ldg(a.B.off_s + col[c] + 1) : 0u;
   }
-  const uint32_t rend = min(TA, a.na - ia0);
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
     const uint32_t ia = ia0 + r;
@@ -238,7 +240,9 @@ template <int TA, int CPT, typename T>
 __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
   constexpr int TB = kThreads * CPT;
   __shared__ double tile[TA][TB];
-  const uint32_t ib0 = blockIdx.x * TA;
+  const uint32_t t = __ldg(a.tile_order + blockIdx.x);
+  const uint32_t ib0 = __ldg(a.tile_start + t);
+  const uint32_t rend = __ldg(a.tile_start + t + 1) - ib0;  // <= TA
   const uint32_t ia0 = blockIdx.y * TB;
   uint32_t col[CPT];
   bool ok[CPT];
@@ -249,7 +253,6 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
     ok[c] = col[c] < a.na;
     alpha[c] = ok[c] ? __ldg(a.astr + col[c]) : 0ull;
   }
-  const uint32_t rend = min(TA, a.nb - ib0);
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
     double acc[CPT];
@@ -296,15 +299,21 @@ constexpr int kShapeTA[kNumShapes] = {8, 8, 8, 16};
 constexpr int kShapeCPT[kNumShapes] = {1, 2, 4, 2};
 
 template <typename T, int TA, int CPT>
-void launch_a_shape(const Problem &p, const Args<T> &a, cudaStream_t s) {
+void launch_a_shape(const Problem &p, Args<T> a, cudaStream_t s) {
   constexpr int TB = kThreads * CPT;
-  dim3 g((p.na + TA - 1) / TA, (p.nb + TB - 1) / TB);
+  constexpr int v = TA == 8 ? 0 : 1;
+  a.tile_start = p.tile_start[0][v];
+  a.tile_order = p.tile_order[0][v];
+  dim3 g(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
   k_sigma_alpha<TA, CPT, T><<<g, kThreads, 0, s>>>(a);
 }
 template <typename T, int TA, int CPT>
-void launch_b_shape(const Problem &p, const Args<T> &a, cudaStream_t s) {
+void launch_b_shape(const Problem &p, Args<T> a, cudaStream_t s) {
   constexpr int TB = kThreads * CPT;
-  dim3 g((p.nb + TA - 1) / TA, (p.na + TB - 1) / TB);
+  constexpr int v = TA == 8 ? 0 : 1;
+  a.tile_start = p.tile_start[1][v];
+  a.tile_order = p.tile_order[1][v];
+  dim3 g(p.n_tiles[1][v], (p.na + TB - 1) / TB);
   k_sigma_beta<TA, CPT, T><<<g, kThreads, 0, s>>>(a);
 }
 
@@ -368,6 +377,20 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
   release_workspace(p, WS_TUNE);
 }
 
+// Shape taken without timing (serving contexts): 128-column tiles when the
+// swept dimension is short, so that small problems still spread over the SMs.
+inline int size_shape(uint32_t columns) { return columns <= 1024 ? 0 : 1; }
+
+template <typename T>
+bool needs_tuning(Problem &p) {
+  const int prec = std::is_same<T, double>::value ? 0 : 1;
+  if (p.tune_a[prec] >= 0 && p.tune_b[prec] >= 0) return false;
+  if (p.ctx->autotune) return true;
+  p.tune_a[prec] = size_shape(p.nb);
+  p.tune_b[prec] = size_shape(p.na);
+  return false;
+}
+
 template <typename T>
 void launch(Problem &p, const Args<T> &a, cudaStream_t s) {
   const int prec = std::is_same<T, double>::value ? 0 : 1;
@@ -422,7 +445,71 @@ Args<T> base_args(Problem &p, const T *C, T *S, int accumulate) {
   return a;
 }
 
+// Rows [start[t], start[t+1]) of at most cap rows each, closed once their
+// work reaches cap times the mean row work, so that a heavy row forms a tile
+// of its own; order lists the tiles by decreasing work.
+void make_tiles(const std::vector<double> &work, int cap, std::vector<uint32_t> &start,
+                std::vector<uint32_t> &order) {
+  const size_t n = work.size();
+  double total = 0.0;
+  for (double w : work) total += w;
+  const double target = cap * (n ? total / (double)n : 1.0);
+  start.assign(1, 0u);
+  std::vector<double> tw;
+  double acc = 0.0;
+  int rows = 0;
+  for (size_t r = 0; r < n; ++r) {
+    acc += work[r];
+    if (++rows == cap || acc >= target || r + 1 == n) {
+      start.push_back((uint32_t)(r + 1));
+      tw.push_back(acc);
+      acc = 0.0;
+      rows = 0;
+    }
+  }
+  order.resize(tw.size());
+  for (size_t t = 0; t < tw.size(); ++t) order[t] = (uint32_t)t;
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return tw[x] > tw[y]; });
+}
+
 }  // namespace
+
+// Row tiles of both sigma kernels (alpha rows for kernel A, beta rows for
+// kernel B) for the row caps 8 and 16.  A row's work is its same-spin pair
+// count, plus for kernel A its alpha singles times the mean number of beta
+// singles per string (the alpha-beta term), plus one.
+void build_row_tiles(Problem &p, cudaStream_t s) {
+  std::vector<uint32_t> os[2], od[2];
+  for (int sp = 0; sp < 2; ++sp) {
+    const SpinTables &T = sp == 0 ? p.A : p.B;
+    os[sp].resize(T.n + 1);
+    od[sp].resize(T.n + 1);
+    SBDGB_CUDA(cudaMemcpyAsync(os[sp].data(), T.off_s, sizeof(uint32_t) * (T.n + 1), cudaMemcpyDeviceToHost, s));
+    SBDGB_CUDA(cudaMemcpyAsync(od[sp].data(), T.off_d, sizeof(uint32_t) * (T.n + 1), cudaMemcpyDeviceToHost, s));
+  }
+  SBDGB_CUDA(cudaStreamSynchronize(s));
+  const double mean_sb = p.nb ? (double)p.B.ns / p.nb : 0.0;
+  for (int sp = 0; sp < 2; ++sp) {
+    const uint32_t n = sp == 0 ? p.na : p.nb;
+    std::vector<double> work(n);
+    for (uint32_t r = 0; r < n; ++r) {
+      const double singles = os[sp][r + 1] - os[sp][r], doubles = od[sp][r + 1] - od[sp][r];
+      work[r] = 1.0 + singles + doubles + (sp == 0 ? singles * mean_sb : 0.0);
+    }
+    for (int v = 0; v < 2; ++v) {
+      std::vector<uint32_t> start, order;
+      make_tiles(work, v == 0 ? 8 : 16, start, order);
+      p.tile_start[sp][v] = (uint32_t *)dev_alloc(p, sizeof(uint32_t) * start.size());
+      p.tile_order[sp][v] = (uint32_t *)dev_alloc(p, sizeof(uint32_t) * order.size());
+      p.n_tiles[sp][v] = (uint32_t)order.size();
+      SBDGB_CUDA(cudaMemcpyAsync(p.tile_start[sp][v], start.data(), sizeof(uint32_t) * start.size(),
+                                 cudaMemcpyHostToDevice, s));
+      SBDGB_CUDA(cudaMemcpyAsync(p.tile_order[sp][v], order.data(), sizeof(uint32_t) * order.size(),
+                                 cudaMemcpyHostToDevice, s));
+    }
+  }
+  SBDGB_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
+}
 
 void transpose_fp64(Problem &p, const double *in, double *out, uint32_t R, uint32_t Cn, cudaStream_t s) {
   transpose<double>(p, in, out, R, Cn, s);
@@ -464,7 +551,7 @@ void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStre
   a.Jb = p.Jb;
   a.Ja = p.Ja;
   a.Kp = p.Kp;
-  if (p.tune_a[0] < 0) {
+  if (needs_tuning<double>(p)) {
     transpose<double>(p, C, p.CT, p.na, p.nb, s);
     autotune<double>(p, a, s);
   }
@@ -511,7 +598,7 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s) {
   a.Jb = p.Jbf;
   a.Ja = p.Jaf;
   a.Kp = p.Kpf;
-  if (p.tune_a[1] < 0) {
+  if (needs_tuning<float>(p)) {
     transpose<float>(p, C, p.CTf, p.na, p.nb, s);
     autotune<float>(p, a, s);
   }

@@ -276,6 +276,7 @@ void build_tables(Problem &p, cudaStream_t s) {
   }
   count_launch(p.ctx, 3);
   SBDGB_CUDA(cudaGetLastError());
+  build_row_tiles(p, s);
   SBDGB_CUDA(cudaStreamSynchronize(s));
   p.tables = true;
 }

@@ -24,8 +24,9 @@ SYMBOLS = [
     "sbdgb_abi_version", "sbdgb_ctx_create", "sbdgb_ctx_destroy", "sbdgb_last_error", "sbdgb_ctx_bytes_in_use",
     "sbdgb_ctx_launch_count", "sbdgb_ctx_set_stream", "sbdgb_ctx_enable_timing", "sbdgb_ctx_sigma_timing", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
     "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
-    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_noalloc", "sbdgb_problem_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
-    "sbdgb_davidson",
+    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_noalloc", "sbdgb_occupation_density", "sbdgb_problem_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
+    "sbdgb_davidson", "sbdgb_server_create", "sbdgb_server_submit", "sbdgb_server_poll", "sbdgb_server_wait",
+    "sbdgb_server_stats", "sbdgb_server_last_error", "sbdgb_server_destroy",
 ]
 
 
@@ -49,6 +50,26 @@ class Report(C.Structure):
         return {"iterations": self.iterations, "sigma_calls": self.sigma_calls, "sigma_fp64": self.sigma_fp64,
                 "restarts": self.restarts, "converged": bool(self.converged), "seconds": self.seconds,
                 "resid": [self.resid[i] for i in range(min(nroots, 16))]}
+
+
+class Request(C.Structure):
+    _fields_ = [("norb", C.c_int), ("astr", C.c_void_p), ("na", C.c_size_t), ("bstr", C.c_void_p),
+                ("nb", C.c_size_t), ("h1", C.c_void_p), ("eri_packed", C.c_void_p), ("ecore", C.c_double),
+                ("opts", DavidsonOpts), ("vectors_out", C.c_void_p)]
+
+
+class Result(C.Structure):
+    _fields_ = [("status", C.c_int), ("nroots", C.c_int), ("energies", C.c_double * 8), ("resid", C.c_double * 8),
+                ("queue_seconds", C.c_double), ("run_seconds", C.c_double), ("total_seconds", C.c_double),
+                ("iterations", C.c_int), ("sigma_calls", C.c_int), ("converged", C.c_int), ("worker", C.c_int),
+                ("reserved_bytes", C.c_size_t), ("ndet", C.c_uint64), ("message", C.c_char * 200)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
+                ("launches", C.c_uint64), ("budget_bytes", C.c_size_t), ("reserved_bytes", C.c_size_t),
+                ("peak_reserved_bytes", C.c_size_t), ("workers", C.c_int), ("running", C.c_int),
+                ("peak_running", C.c_int), ("queued", C.c_int)]
 
 
 _lib = None
@@ -93,12 +114,22 @@ def load(path: str = LIB_PATH):
     L.sbdgb_sigma.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_sigma_mixed.argtypes = [vp, vp, vp, vp]
     L.sbdgb_sigma_noalloc.argtypes = [vp, vp, vp, C.c_int, vp]
+    L.sbdgb_occupation_density.argtypes = [vp, vp, _f64p, vp]
     L.sbdgb_mult_host.argtypes = [vp, vp, _f64p, _f64p]
     L.sbdgb_problem_tuning.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
     L.sbdgb_davidson_default_opts.argtypes = [C.POINTER(DavidsonOpts)]
     L.sbdgb_davidson_default_opts.restype = None
     L.sbdgb_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _f64p, vp, C.POINTER(Report)]
+    L.sbdgb_server_create.argtypes = [C.c_int, C.c_int, C.c_size_t, C.POINTER(vp)]
+    L.sbdgb_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]
+    L.sbdgb_server_poll.argtypes = [vp, C.c_uint64, C.POINTER(C.c_int)]
+    L.sbdgb_server_wait.argtypes = [vp, C.c_uint64, C.c_double, C.POINTER(Result)]
+    L.sbdgb_server_stats.argtypes = [vp, C.POINTER(ServeStats)]
+    L.sbdgb_server_last_error.argtypes = [vp]
+    L.sbdgb_server_last_error.restype = C.c_char_p
+    L.sbdgb_server_destroy.argtypes = [vp]
+    L.sbdgb_server_destroy.restype = None
     _lib = L
     return L
 
@@ -272,6 +303,17 @@ class TPBProblem:
 
     def sigma_mixed_device(self, c_ptr: int, s_ptr: int, stream: int | None = None):
         self.engine.check(self.lib.sbdgb_sigma_mixed(self.h, c_ptr, s_ptr, self._stream_arg(stream)))
+
+    def occupation_density(self, W) -> np.ndarray:
+        """Occupation density [2*norb] of W (a host array or a device pointer)."""
+        out = np.zeros(2 * self.norb)
+        if isinstance(W, int):
+            self.engine.check(self.lib.sbdgb_occupation_density(self.h, W, out, None))
+            return out
+        import torch
+        w = torch.as_tensor(np.ascontiguousarray(W, dtype=np.float64).ravel(), device="cuda")
+        self.engine.check(self.lib.sbdgb_occupation_density(self.h, w.data_ptr(), out, CUDA_STREAM_LEGACY))
+        return out
 
     def davidson(self, nroots: int = 1, max_nb: int = 20, eps: float = 1e-8, max_it: int = 100,
                  init: int = 0, precision: int = FP64, refine_every: int = 4, max_time: float = 0.0,

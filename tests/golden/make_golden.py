@@ -8,7 +8,10 @@ oracle/Makefile -- and the reference's results are stored:
   * hii, sigma = H*C for a seeded C, and the ground energy of the reference's
     own Davidson;
   * the three lowest eigenvalues of the explicitly assembled H, whose
-    matrix-vector product is checked here against the reference's sigma.
+    matrix-vector product is checked here against the reference's sigma;
+  * the occupation density of C (OccupationDensity), for norb <= 12 the one-
+    and two-particle RDMs of C (Correlation), and the ground energy of the
+    reference's matrix-free Lanczos (the --method 2 solver).
 Integrals are stored as h1 plus pair factors (the ERI is rebuilt with
 sbd_gb300.generators.eri_from_factors, an order-fixed elementwise sum).
 
@@ -104,7 +107,10 @@ def run_case(name, spec, outdir):
         C.tofile(f"{d}/c.bin")
         args = [REF_BIN, "--fcidump", f"{d}/fcidump.txt", "--adet", f"{d}/a.txt", "--bdet", f"{d}/b.txt",
                 "--out", f"{d}/o.bin", "--cvec", f"{d}/c.bin", "--davidson", "1", "--block", "12",
-                "--iteration", "200", "--tolerance", "1e-10"]
+                "--iteration", "200", "--tolerance", "1e-10", "--density", "1", "--lanczos", "1",
+                "--lanczos_block", "40", "--lanczos_iteration", "20", "--lanczos_tolerance", "1e-12"]
+        if norb <= 12:
+            args += ["--rdm", "1"]
         subprocess.run(args, check=True, capture_output=True, env=dict(os.environ, OMP_NUM_THREADS="4"))
         r = parse_sbdref(f"{d}/o.bin")
     types = {int(r[f"task{k}.type"][0]): k for k in range(3)}
@@ -112,8 +118,12 @@ def run_case(name, spec, outdir):
     out = {
         "norb": np.int64(norb), "ecore": np.float64(ints.ecore), "h1": ints.h1, "factors": Bp,
         "astr": astr, "bstr": bstr, "C": C, "hii": r["hii"], "sigma": r["sigma"],
-        "energy": np.float64(r["energy"][0]),
+        "energy": np.float64(r["energy"][0]), "density_c": r["density_c"],
+        "lanczos_energy": np.float64(r["lanczos_energy"][0]),
     }
+    if norb <= 12:
+        out["rdm1"] = np.stack([r["rdm1_0"], r["rdm1_1"]])
+        out["rdm2"] = np.stack([r[f"rdm2_{k}"] for k in range(4)])
     for tag, k, sp in (("a", ka, "Alpha"), ("b", kb, "Beta")):
         out[f"{tag}_off_s"] = r[f"task{k}.SinglesFrom{sp}Offset"]
         out[f"{tag}_ket_s"] = r[f"task{k}.SinglesFrom{sp}"]

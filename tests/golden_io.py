@@ -32,6 +32,10 @@ class Case:
         self.energy = float(d["energy"])
         self.lowest = d["lowest"]
         self.irreducible = bool(d["irreducible"])
+        self.density_c = d["density_c"]
+        self.lanczos_energy = float(d["lanczos_energy"])
+        self.rdm1 = d["rdm1"] if "rdm1" in d.files else None
+        self.rdm2 = d["rdm2"] if "rdm2" in d.files else None
 
     def tables(self, spin: str) -> dict:
         t = "a" if spin in ("a", 0, "alpha") else "b"

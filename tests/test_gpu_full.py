@@ -35,6 +35,7 @@ def test_config0_against_oracle(cfg0):
     assert max_rel(p.diag_terms(), o.hii()) <= 1e-12
     C = np.random.default_rng(7).uniform(-1, 1, prob.ndet)
     assert max_rel(p.mult(C), o.mult(C)) <= 1e-12
+    assert max_rel(p.occupation_density(C), o.density(C)) <= 1e-12
 
 
 def test_symmetry_linearity_determinism(cfg0):

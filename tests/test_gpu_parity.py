@@ -81,3 +81,9 @@ def test_lowest_roots_match_assembled_spectrum(gcase):
     X = r.vectors
     G = X @ X.T
     assert np.allclose(G, np.eye(k), atol=1e-8)
+
+
+def test_occupation_density(gcase):
+    c, p = gcase
+    p.diag_terms()
+    assert max_rel(p.occupation_density(c.C), c.density_c) <= 1e-12

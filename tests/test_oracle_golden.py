@@ -57,3 +57,40 @@ def test_assembled_spectrum(case_oracle):
     c, o = case_oracle
     w = o.lowest(len(c.lowest))
     assert np.allclose(w, c.lowest, atol=1e-8, rtol=0)
+
+
+def test_occupation_density(case_oracle):
+    c, o = case_oracle
+    d = o.density(c.C)
+    assert max_rel(d, c.density_c) <= 1e-12
+    # alpha and beta occupations sum to the electron counts times |C|^2
+    w2 = float(np.dot(c.C, c.C))
+    na_e = bin(int(c.astr[0])).count("1")
+    nb_e = bin(int(c.bstr[0])).count("1")
+    assert abs(d[0::2].sum() - na_e * w2) <= 1e-10 * w2 * na_e
+    assert abs(d[1::2].sum() - nb_e * w2) <= 1e-10 * w2 * nb_e
+
+
+def test_rdms(case_oracle):
+    c, o = case_oracle
+    if c.rdm1 is None:
+        pytest.skip("RDM fixtures are stored for norb <= 12")
+    one, two = o.correlation(c.C)
+    scale1 = np.abs(c.rdm1).max()
+    scale2 = np.abs(c.rdm2).max()
+    assert np.abs(one - c.rdm1).max() <= 1e-12 * scale1
+    assert np.abs(two - c.rdm2).max() <= 1e-12 * scale2
+    # the diagonal of the one-particle RDM is the occupation density
+    L = c.norb
+    dens = np.empty(2 * L)
+    dens[0::2] = np.diag(one[0].reshape(L, L))
+    dens[1::2] = np.diag(one[1].reshape(L, L))
+    assert max_rel(dens, c.density_c) <= 1e-12
+
+
+def test_lanczos_energy(case_oracle):
+    c, o = case_oracle
+    E, W = o.lanczos(max_it=20, num_block=40, eps=1e-12)
+    assert abs(E - c.lanczos_energy) < 1e-8
+    if c.irreducible:
+        assert abs(E - c.lowest[0]) < 1e-8

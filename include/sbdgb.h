@@ -151,9 +151,10 @@ int sbdgb_sigma_noalloc(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, 
 /* Occupation density of a vector (OccupationDensity, chemistry/tpb/
  * occupation.h:11-95, as sbd::tpb::diag reports it with do_rdm == 0,
  * sbdiag.h:666-699): density[2p] = sum over determinants of |W|^2 with alpha
- * orbital p occupied, density[2p+1] the same for beta.  W_dev: N doubles on
- * the device; density: 2*norb doubles of host memory (the call waits for it). */
-int sbdgb_occupation_density(sbdgb_problem *p, const double *W_dev, double *density, void *stream);
+ * orbital p occupied, density[2p+1] the same for beta.  W: N doubles of device
+ * or host memory (a host vector is copied in); density: 2*norb doubles of host
+ * memory (the call waits for it). */
+int sbdgb_occupation_density(sbdgb_problem *p, const double *W, double *density, void *stream);
 
 /* Host-buffer form of sbd::mult: Wb += H*Wk with host vectors (copies
  * inside).  hii is ignored when NULL (the problem's own diagonal is used). */
@@ -191,6 +192,14 @@ void sbdgb_davidson_default_opts(sbdgb_davidson_opts *o);
  * X (host, nroots*N, may be NULL) receives the normalized Ritz vectors and,
  * with init == 2, supplies the starting vectors. */
 int sbdgb_davidson(sbdgb_problem *p, const sbdgb_davidson_opts *o, double *E, double *X, sbdgb_report *rep);
+
+/* Lanczos (chemistry/tpb/lanczos.h:169-320, the solver of sbd::tpb::diag
+ * --method 2): restarted Lanczos without reorthogonalisation, max_nb Krylov
+ * vectors per cycle, max_it cycles, stop when the lowest Ritz value moves by
+ * less than eps.  One root, FP64; init as for Davidson.  E[0] receives the
+ * lowest Ritz value, X (may be NULL) the Ritz vector; rep->resid[0] is the
+ * last change of the Ritz value and rep->restarts the cycles run. */
+int sbdgb_lanczos(sbdgb_problem *p, const sbdgb_davidson_opts *o, double *E, double *X, sbdgb_report *rep);
 
 /* ---- serving: many solves at once, admitted by HBM footprint -------------
  * No single counterpart in the reference, whose app solves one problem per

@@ -245,6 +245,31 @@ inline double Davidson(Problem &p, std::vector<double> &W, int max_iteration, in
   return E;
 }
 
+// Lanczos (lanczos.h:169-320): W in = starting vector (or empty for the
+// reference's init 0 guess), out = Ritz vector; returns the energy.
+inline double Lanczos(Problem &p, std::vector<double> &W, int max_iteration, int num_block, double eps) {
+  sbdgb_davidson_opts o;
+  sbdgb_davidson_default_opts(&o);
+  o.max_it = max_iteration;
+  o.max_nb = num_block;
+  o.eps = eps;
+  o.nroots = 1;
+  o.init = W.size() == p.size() ? 2 : 0;
+  W.resize(p.size());
+  double E = 0.0;
+  sbdgb_report rep;
+  check(sbdgb_lanczos(p.get(), &o, &E, W.data(), &rep), p.ctx(), "Lanczos");
+  return E;
+}
+
+// OccupationDensity (occupation.h:11-95) over all orbitals: res[2p] alpha,
+// res[2p+1] beta occupation of orbital p in W.
+inline void OccupationDensity(Problem &p, int norb, const std::vector<double> &W, std::vector<double> &res) {
+  if (W.size() != p.size()) throw std::invalid_argument("vector size mismatch");
+  res.assign(2 * (size_t)norb, 0.0);
+  check(sbdgb_occupation_density(p.get(), W.data(), res.data(), nullptr), p.ctx(), "OccupationDensity");
+}
+
 // Device operator with the reference's MultBase::run shape (chemistry/basic/
 // mult.h:19-103) over raw device pointers: Wb = hii o Wk + H_offdiag Wk.
 class MultTPBGB300 {
@@ -318,20 +343,23 @@ inline SBD generate_sbd_data(int argc, char *argv[]) {
 }
 
 // diag (sbdiag.h:151-526) at communicator size 1: integrals -> tables ->
-// diagonal -> Davidson -> energy.  Returns the ground energy in `energy` and,
-// when `W` is non-null, the ground-state vector.  Outputs of the reference's
-// post-processing (density, carry-over strings, RDMs, wavefunction files) are
-// not produced by this entry point.
+// diagonal -> Davidson (method 0 and 1) or Lanczos (method 2 and 3; the
+// stored-Hamiltonian methods 1 and 3 give the same result matrix-free) ->
+// energy.  Returns the ground energy in `energy`, the ground-state vector in
+// *W and, with do_rdm == 0, the occupation density (sbdiag.h:666-699) in
+// *density when those are non-null.  Carry-over strings, RDMs and wavefunction
+// files are not produced by this entry point.
 inline void diag(int comm_size, const SBD &sbd_data, const FCIDump &fcidump, const std::vector<uint64_t> &adet,
                  const std::vector<uint64_t> &bdet, double &energy, std::vector<double> *W = nullptr,
-                 std::vector<double> *energies = nullptr) {
+                 std::vector<double> *energies = nullptr, std::vector<double> *density = nullptr) {
   Context ctx(sbd_data.device);
   check(sbdgb_check_comm_sizes(ctx.get(), comm_size / std::max(1, sbd_data.task_comm_size * sbd_data.adet_comm_size *
                                                                       sbd_data.bdet_comm_size),
                                sbd_data.adet_comm_size * sbd_data.bdet_comm_size, sbd_data.task_comm_size),
         ctx.get(), "diag");
-  if (sbd_data.method != 0) throw std::invalid_argument("only --method 0 (Davidson) is provided");
+  if (sbd_data.method < 0 || sbd_data.method > 3) throw std::invalid_argument("--method must be 0..3");
   if (sbd_data.do_rdm != 0) throw std::invalid_argument("RDM output is not provided by this engine");
+  const bool use_lanczos = (sbd_data.method & 2) != 0;
   Integrals ints = SetupIntegrals(fcidump);
   Problem p(ctx, ints, adet, bdet);
   sbdgb_davidson_opts o;
@@ -344,12 +372,21 @@ inline void diag(int comm_size, const SBD &sbd_data, const FCIDump &fcidump, con
   o.init = sbd_data.init == 0 ? 0 : 1;
   o.precision = sbd_data.precision;
   o.refine_every = sbd_data.refine_every;
+  if (use_lanczos) o.nroots = 1;
   std::vector<double> E(o.nroots), X;
-  if (W) X.resize(p.size() * o.nroots);
+  const bool want_x = W || density;
+  if (want_x) X.resize(p.size() * o.nroots);
   sbdgb_report rep;
-  check(sbdgb_davidson(p.get(), &o, E.data(), W ? X.data() : nullptr, &rep), ctx.get(), "diag");
+  if (use_lanczos)
+    check(sbdgb_lanczos(p.get(), &o, E.data(), want_x ? X.data() : nullptr, &rep), ctx.get(), "diag");
+  else
+    check(sbdgb_davidson(p.get(), &o, E.data(), want_x ? X.data() : nullptr, &rep), ctx.get(), "diag");
   energy = E[0];
   if (energies) *energies = E;
+  if (density) {
+    density->assign(2 * (size_t)ints.L, 0.0);
+    check(sbdgb_occupation_density(p.get(), X.data(), density->data(), nullptr), ctx.get(), "diag density");
+  }
   if (W) W->assign(X.begin(), X.begin() + p.size());
 }
 

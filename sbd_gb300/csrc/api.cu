@@ -444,4 +444,14 @@ int sbdgb_davidson(sbdgb_problem *pr, const sbdgb_davidson_opts *o, double *E, d
   });
 }
 
+int sbdgb_lanczos(sbdgb_problem *pr, const sbdgb_davidson_opts *o, double *E, double *X, sbdgb_report *rep) {
+  if (!pr || !o || !E) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    sbdgb::Problem &p = pr->p;
+    if (!p.tables) sbdgb::build_tables(p, p.ctx->stream);
+    if (!p.diag) sbdgb::build_diag(p, p.ctx->stream);
+    sbdgb::lanczos(p, *o, E, X, rep);
+  });
+}
+
 }  // extern "C"

@@ -200,6 +200,7 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s);
 void prepare_mixed(Problem &p, cudaStream_t s);
 // davidson.cu
 void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X, sbdgb_report *rep);
+void lanczos(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X, sbdgb_report *rep);
 
 }  // namespace sbdgb
 

@@ -429,6 +429,56 @@ __global__ void __launch_bounds__(kRed) k_mixed_assemble(const double *__restric
   }
 }
 
+// ---- Lanczos kernels ------------------------------------------------------------
+
+// HC -= alpha C; next = HC; partial sums of |HC|^2 (one Lanczos step's
+// three-term update, lanczos.h:244-261).
+__global__ void __launch_bounds__(kRed) k_lz_update(double *__restrict__ HC, const double *__restrict__ Cb,
+                                                     double *__restrict__ next, const double *__restrict__ alpha,
+                                                     size_t N, double *__restrict__ partial) {
+  const double a = *alpha;
+  double s = 0.0;
+  for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
+    const double h = fma(-a, __ldg(Cb + e), HC[e]);
+    HC[e] = h;
+    next[e] = h;
+    s = fma(h, h, s);
+  }
+  __shared__ double red[kRed / 32];
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < kRed / 32; ++w) t += red[w];
+    partial[blockIdx.x] = t;
+  }
+}
+
+// next /= beta; HC = -beta * C (lanczos.h:263, 281-291 at communicator size 1).
+__global__ void __launch_bounds__(kRed) k_lz_scale(double *__restrict__ next, double *__restrict__ HC,
+                                                    const double *__restrict__ Cb, const double *__restrict__ beta,
+                                                    size_t N) {
+  const double b = *beta, ib = 1.0 / b;
+  for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
+    next[e] *= ib;
+    HC[e] = -b * __ldg(Cb + e);
+  }
+}
+
+// W = sum_j u_j C_j over the n Krylov vectors (lanczos.h:300-312).
+__global__ void __launch_bounds__(kRed) k_lz_ritz(const double *__restrict__ C, int n, size_t N,
+                                                   const double *__restrict__ u, double *__restrict__ W) {
+  __shared__ double us[64];
+  for (int t = threadIdx.x; t < n; t += kRed) us[t] = u[t];
+  __syncthreads();
+  for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
+    double w = 0.0;
+    for (int j = 0; j < n; ++j) w = fma(us[j], __ldg(C + (size_t)j * N + e), w);
+    W[e] = w;
+  }
+}
+
 // ---- host-side helper ----------------------------------------------------------
 
 struct Solver {
@@ -1061,7 +1111,113 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
   if (rep) *rep = r;
 }
 
+// ---- Lanczos (chemistry/tpb/lanczos.h:169-320) --------------------------------------
+
+// Restarted Lanczos without reorthogonalisation, as the reference runs it for
+// --method 2: each cycle builds up to max_nb Krylov vectors from W with the
+// three-term recurrence (sigma accumulated into HC, which holds -beta C_{j-1}),
+// stops when the lowest eigenvalue of the tridiagonal matrix moves by less
+// than eps or the off-diagonal falls below eps, and restarts from the Ritz
+// vector W = sum_j U[j][0] C_j.
+void lanczos_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
+  using clock = std::chrono::steady_clock;
+  const auto t0 = clock::now();
+  const size_t N = p.N;
+  const int nb = std::max(2, std::min(o.max_nb, 64));
+  cudaStream_t s = p.ctx->stream;
+  Solver sv(p, s);
+  double *Cv = (double *)workspace(p, WS_V, sizeof(double) * N * nb);
+  double *HC = (double *)workspace(p, WS_HV, sizeof(double) * N);
+  double *W = (double *)workspace(p, WS_X, sizeof(double) * N);
+  sv.start_vectors(o, 1, W, Xout);
+  {
+    // a caller's vector (init 2) is normalised; the unit-vector guesses already are
+    std::vector<double> g;
+    sv.dots_c<double, double>(W, 1, W, 1, g);
+    SBDGB_REQUIRE(g[0] > 0.0 && std::isfinite(g[0]), SBDGB_E_INPUT, "starting vector is zero");
+    if (std::fabs(g[0] - 1.0) > 1e-14) {
+      std::vector<double> m{1.0 / std::sqrt(g[0])};
+      sv.lincomb<double>(W, 1, m, 1, Cv);
+      SBDGB_CUDA(cudaMemcpyAsync(W, Cv, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+    }
+  }
+  double *dval = sv.red + 2400;  // device scalars alpha (0), beta (1), Ritz coefficients (8..)
+  sbdgb_report r{};
+  double E0 = 0.0, change = 0.0;
+  bool stop = false;
+  std::vector<double> A((size_t)nb * nb), theta, Y;
+  for (int it = 0; it < std::max(1, o.max_it) && !stop; ++it) {
+    SBDGB_CUDA(cudaMemcpyAsync(Cv, W, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
+    SBDGB_CUDA(cudaMemsetAsync(HC, 0, sizeof(double) * N, s));
+    std::fill(A.begin(), A.end(), 0.0);
+    int n = 0;
+    double E_old = 1.0e8;
+    for (int ib = 0; ib < nb; ++ib) {
+      ++n;
+      double *Cb = Cv + (size_t)ib * N;
+      sigma_fp64(p, Cb, HC, 1, s);
+      r.sigma_calls++;
+      r.sigma_fp64++;
+      r.iterations++;
+      std::vector<double> g;
+      sv.dots_c<double, double>(Cb, 1, HC, 1, g);
+      const double alpha = g[0];
+      A[ib + (size_t)nb * ib] = alpha;
+      std::vector<double> T((size_t)n * n);
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) T[i + (size_t)n * j] = A[i + (size_t)nb * j];
+      jacobi_eig(n, T, theta, Y);
+      change = std::fabs(theta[0] - E_old);
+      if (o.verbose) printf(" Lanczos iteration %d, step %d: (A,B)=(%.12g) %.12f\n", it, ib, alpha, theta[0]);
+      if (change < o.eps) {
+        stop = true;
+        break;
+      }
+      E_old = theta[0];
+      if (ib + 1 == nb) break;
+      double *next = Cv + (size_t)(ib + 1) * N;
+      SBDGB_CUDA(cudaMemcpyAsync(dval, &alpha, sizeof(double), cudaMemcpyHostToDevice, s));
+      k_lz_update<<<sv.blocks, kRed, 0, s>>>(HC, Cb, next, dval, N, sv.partial);
+      count_launch(p.ctx);
+      const double beta = std::sqrt(std::max(0.0, sv.reduce_partials(1)));
+      A[ib + (size_t)nb * (ib + 1)] = A[(ib + 1) + (size_t)nb * ib] = beta;
+      if (std::fabs(beta) < o.eps) break;  // invariant subspace (the new vector is not used)
+      SBDGB_CUDA(cudaMemcpyAsync(dval + 1, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
+      k_lz_scale<<<sv.blocks, kRed, 0, s>>>(next, HC, Cb, dval + 1, N);
+      count_launch(p.ctx);
+      SBDGB_CUDA(cudaGetLastError());
+    }
+    std::vector<double> T((size_t)n * n);
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) T[i + (size_t)n * j] = A[i + (size_t)nb * j];
+    jacobi_eig(n, T, theta, Y);
+    E0 = theta[0];
+    std::vector<double> u(Y.begin(), Y.begin() + n);
+    SBDGB_CUDA(cudaMemcpyAsync(dval + 8, u.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
+    k_lz_ritz<<<sv.blocks, kRed, 0, s>>>(Cv, n, N, dval + 8, W);
+    count_launch(p.ctx);
+    SBDGB_CUDA(cudaGetLastError());
+    r.restarts++;
+    const double elapsed = std::chrono::duration<double>(clock::now() - t0).count();
+    if (o.max_time > 0 && elapsed > o.max_time) break;
+  }
+  r.converged = stop ? 1 : 0;
+  r.resid[0] = change;
+  E[0] = E0;
+  if (Xout) SBDGB_CUDA(cudaMemcpyAsync(Xout, W, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+  SBDGB_CUDA(cudaStreamSynchronize(s));
+  r.seconds = std::chrono::duration<double>(clock::now() - t0).count();
+  if (rep) *rep = r;
+}
+
 }  // namespace
+
+void lanczos(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
+  if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "Lanczos needs tables and diagonal");
+  SBDGB_REQUIRE(o.nroots == 1, SBDGB_E_UNSUPPORTED, "Lanczos solves one root");
+  SBDGB_REQUIRE(o.precision == SBDGB_FP64, SBDGB_E_UNSUPPORTED, "Lanczos runs in FP64");
+  lanczos_fp64(p, o, E, Xout, rep);
+}
 
 void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
   if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "Davidson needs tables and diagonal");

@@ -104,6 +104,13 @@ void string_norms(Problem &p, const double *W, double *r, double *c, cudaStream_
 }
 
 void occupation_density(Problem &p, const double *W, double *density_host, cudaStream_t s) {
+  cudaPointerAttributes at{};
+  SBDGB_CUDA(cudaPointerGetAttributes(&at, W));
+  if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) {  // host vector: stage it
+    double *Wd = (double *)workspace(p, WS_RES64, sizeof(double) * p.N);
+    SBDGB_CUDA(cudaMemcpyAsync(Wd, W, sizeof(double) * p.N, cudaMemcpyHostToDevice, s));
+    W = Wd;
+  }
   double *r = (double *)workspace(p, WS_NORM_A, sizeof(double) * p.na);
   double *c = (double *)workspace(p, WS_NORM_B, sizeof(double) * p.nb);
   double *out = (double *)workspace(p, WS_OCC, sizeof(double) * 2 * (size_t)p.norb);

@@ -25,7 +25,7 @@ SYMBOLS = [
     "sbdgb_ctx_launch_count", "sbdgb_ctx_set_stream", "sbdgb_ctx_enable_timing", "sbdgb_ctx_sigma_timing", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
     "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
     "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_noalloc", "sbdgb_occupation_density", "sbdgb_problem_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
-    "sbdgb_davidson", "sbdgb_server_create", "sbdgb_server_submit", "sbdgb_server_poll", "sbdgb_server_wait",
+    "sbdgb_davidson", "sbdgb_lanczos", "sbdgb_server_create", "sbdgb_server_submit", "sbdgb_server_poll", "sbdgb_server_wait",
     "sbdgb_server_stats", "sbdgb_server_last_error", "sbdgb_server_destroy",
 ]
 
@@ -121,6 +121,7 @@ def load(path: str = LIB_PATH):
     L.sbdgb_davidson_default_opts.argtypes = [C.POINTER(DavidsonOpts)]
     L.sbdgb_davidson_default_opts.restype = None
     L.sbdgb_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _f64p, vp, C.POINTER(Report)]
+    L.sbdgb_lanczos.argtypes = [vp, C.POINTER(DavidsonOpts), _f64p, vp, C.POINTER(Report)]
     L.sbdgb_server_create.argtypes = [C.c_int, C.c_int, C.c_size_t, C.POINTER(vp)]
     L.sbdgb_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]
     L.sbdgb_server_poll.argtypes = [vp, C.c_uint64, C.POINTER(C.c_int)]
@@ -304,15 +305,33 @@ class TPBProblem:
     def sigma_mixed_device(self, c_ptr: int, s_ptr: int, stream: int | None = None):
         self.engine.check(self.lib.sbdgb_sigma_mixed(self.h, c_ptr, s_ptr, self._stream_arg(stream)))
 
+    def lanczos(self, max_it: int = 20, num_block: int = 40, eps: float = 1e-12, init: int = 0,
+                want_vector: bool = True, W0: np.ndarray | None = None, max_time: float = 0.0,
+                verbose: bool = False) -> DavidsonResult:
+        """The reference's --method 2 solver (restarted Lanczos, one root)."""
+        o = DavidsonOpts()
+        self.lib.sbdgb_davidson_default_opts(C.byref(o))
+        o.nroots, o.max_nb, o.eps, o.max_it, o.max_time, o.verbose = 1, num_block, eps, max_it, max_time, int(verbose)
+        o.init = 2 if W0 is not None else init
+        E = np.zeros(1)
+        X = None
+        if want_vector or W0 is not None:
+            X = np.zeros(self.N) if W0 is None else np.ascontiguousarray(W0, dtype=np.float64).copy()
+        rep = Report()
+        self.engine.check(self.lib.sbdgb_lanczos(self.h, C.byref(o), E, X.ctypes.data if X is not None else None,
+                                                 C.byref(rep)))
+        return DavidsonResult(E, X, rep.as_dict(1))
+
     def occupation_density(self, W) -> np.ndarray:
         """Occupation density [2*norb] of W (a host array or a device pointer)."""
         out = np.zeros(2 * self.norb)
         if isinstance(W, int):
             self.engine.check(self.lib.sbdgb_occupation_density(self.h, W, out, None))
             return out
-        import torch
-        w = torch.as_tensor(np.ascontiguousarray(W, dtype=np.float64).ravel(), device="cuda")
-        self.engine.check(self.lib.sbdgb_occupation_density(self.h, w.data_ptr(), out, CUDA_STREAM_LEGACY))
+        w = np.ascontiguousarray(W, dtype=np.float64).ravel()
+        if w.size != self.N:
+            raise ValueError("vector size mismatch")
+        self.engine.check(self.lib.sbdgb_occupation_density(self.h, w.ctypes.data, out, None))
         return out
 
     def davidson(self, nroots: int = 1, max_nb: int = 20, eps: float = 1e-8, max_it: int = 100,

@@ -1,7 +1,8 @@
 // Drop-in use of the C++ mirror: the same call sequence as the reference's TPB
 // app (apps/chemistry_tpb_selected_basis_diagonalization/main.cc:127-191):
 // load FCIDUMP, load and sort the alpha/beta string files, run diag.
-//   tpb_drop_in --fcidump F --adetfile A [--bdetfile B] --block NB --iteration IT --tolerance EPS
+//   tpb_drop_in --fcidump F --adetfile A [--bdetfile B] [--method 0|2] --block NB --iteration IT
+//               --tolerance EPS
 #include <cstdio>
 #include <iostream>
 #include <string>
@@ -24,8 +25,8 @@ int main(int argc, char **argv) {
   auto adet = sbdgb::LoadAlphaDets(adetfile, L);
   auto bdet = bdetfile.empty() ? adet : sbdgb::LoadAlphaDets(bdetfile, L);
   double energy = 0.0;
-  std::vector<double> W;
-  sbdgb::tpb::diag(1, sbd_data, fcidump, adet, bdet, energy, &W);
+  std::vector<double> W, density;
+  sbdgb::tpb::diag(1, sbd_data, fcidump, adet, bdet, energy, &W, nullptr, &density);
   // <W|H|W> through the mult entry point, as the reference reports it (sbdiag.h:488-526)
   sbdgb::Context ctx(sbd_data.device);
   sbdgb::Problem p(ctx, sbdgb::SetupIntegrals(fcidump), adet, bdet);
@@ -36,6 +37,12 @@ int main(int argc, char **argv) {
   for (size_t i = 0; i < W.size(); ++i) e += W[i] * HW[i];
   std::cout.precision(16);
   std::cout << " Energy = " << e << std::endl;
-  std::cout << " Davidson energy = " << energy << std::endl;
+  std::cout << " Solver energy = " << energy << std::endl;
+  double na = 0.0, nb = 0.0;
+  for (int io = 0; io < L; ++io) {
+    na += density[2 * io];
+    nb += density[2 * io + 1];
+  }
+  std::cout << " Density sums = " << na << " " << nb << std::endl;
   return 0;
 }

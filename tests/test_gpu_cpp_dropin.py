@@ -38,3 +38,22 @@ def test_cpp_drop_in_matches_reference_energy(exe, tmp_path, name):
                         "--tolerance", "1e-10"], capture_output=True, text=True, check=True)
     e = float(re.search(r"Energy = ([-0-9.eE+]+)", r.stdout).group(1))
     assert abs(e - c.energy) < 1e-8
+
+    na_e, nb_e = bin(int(c.astr[0])).count("1"), bin(int(c.bstr[0])).count("1")
+    dens = [float(x) for x in re.search(r"Density sums = (\S+) (\S+)", r.stdout).groups()]
+    assert abs(dens[0] - na_e) < 1e-8 and abs(dens[1] - nb_e) < 1e-8
+
+
+@pytest.mark.parametrize("name", ["fci_L8", "wide_L58"])
+def test_cpp_drop_in_lanczos_method(exe, tmp_path, name):
+    """--method 2 runs the Lanczos solver, like the reference app."""
+    c = load(name)
+    ints = Integrals(norb=c.norb, nelec=0, ecore=c.ecore, h1=c.h1, eri=c.eri)
+    write_fcidump(str(tmp_path / "fcidump.txt"), ints)
+    write_strings(str(tmp_path / "a.txt"), c.astr, c.norb)
+    write_strings(str(tmp_path / "b.txt"), c.bstr, c.norb)
+    r = subprocess.run([exe, "--fcidump", str(tmp_path / "fcidump.txt"), "--adetfile", str(tmp_path / "a.txt"),
+                        "--bdetfile", str(tmp_path / "b.txt"), "--method", "2", "--block", "40", "--iteration", "20",
+                        "--tolerance", "1e-12"], capture_output=True, text=True, check=True)
+    e = float(re.search(r"Solver energy = ([-0-9.eE+]+)", r.stdout).group(1))
+    assert abs(e - c.lanczos_energy) < 1e-8

@@ -87,3 +87,15 @@ def test_occupation_density(gcase):
     c, p = gcase
     p.diag_terms()
     assert max_rel(p.occupation_density(c.C), c.density_c) <= 1e-12
+
+
+def test_lanczos_matches_reference_lanczos(gcase):
+    """The reference's --method 2 solver from its init-0 vector, same Krylov size and tolerance."""
+    c, p = gcase
+    p.diag_terms()
+    r = p.lanczos(max_it=20, num_block=40, eps=1e-12, init=0)
+    assert abs(r.energies[0] - c.lanczos_energy) < 1e-8
+    # the Ritz vector is normalised and its Rayleigh quotient is the energy
+    W = r.vectors
+    assert abs(np.dot(W, W) - 1.0) < 1e-8
+    assert abs(np.dot(W, p.mult(W)) - r.energies[0]) < 1e-7

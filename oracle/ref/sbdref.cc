@@ -18,6 +18,10 @@
 //          [--davidson 1 --block NB --iteration IT --tolerance EPS]
 //          [--time_mult K] [--density 1] [--rdm 1]
 //          [--lanczos 1 --lanczos_block NB --lanczos_iteration IT --lanczos_tolerance EPS]
+//          [--save NAME] [--load NAME]
+// --save writes the Davidson vector with SaveWavefunction (chemistry/tpb/
+// restart.h:21-67, file NAME000000); --load maps a saved wavefunction onto the
+// current strings with LoadWavefunction (restart.h:415-660) and outputs it.
 // --density and --rdm evaluate OccupationDensity (chemistry/tpb/occupation.h)
 // and Correlation (chemistry/tpb/correlation.h) on the --cvec vector; --lanczos
 // runs the matrix-free Lanczos (chemistry/tpb/lanczos.h:169) from the init-0
@@ -84,6 +88,8 @@ int main(int argc, char **argv) {
   const int want_density = std::stoi(arg(argc, argv, "--density", "0"));
   const int want_rdm = std::stoi(arg(argc, argv, "--rdm", "0"));
   const int want_lanczos = std::stoi(arg(argc, argv, "--lanczos", "0"));
+  const std::string savename = arg(argc, argv, "--save", "");
+  const std::string loadname = arg(argc, argv, "--load", "");
   const int lz_nb = std::stoi(arg(argc, argv, "--lanczos_block", "40"));
   const int lz_it = std::stoi(arg(argc, argv, "--lanczos_iteration", "20"));
   const double lz_eps = std::stod(arg(argc, argv, "--lanczos_tolerance", "1e-12"));
@@ -221,6 +227,13 @@ int main(int argc, char **argv) {
     out.scalar("t_davidson", std::chrono::duration<double>(td1 - td0).count());
     out.scalar("energy", E);
     out.f64("W", W);
+    if (!savename.empty()) sbd::SaveWavefunction(savename, adet, bdet, 1, 1, h_comm, b_comm, t_comm, W);
+  }
+
+  if (!loadname.empty()) {
+    std::vector<double> W;
+    sbd::LoadWavefunction(loadname, adet, bdet, 1, 1, h_comm, b_comm, t_comm, W);
+    out.f64("loaded_W", W);
   }
   MPI_Finalize();
   return 0;

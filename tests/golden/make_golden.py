@@ -11,7 +11,10 @@ oracle/Makefile -- and the reference's results are stored:
     matrix-vector product is checked here against the reference's sigma;
   * the occupation density of C (OccupationDensity), for norb <= 12 the one-
     and two-particle RDMs of C (Correlation), and the ground energy of the
-    reference's matrix-free Lanczos (the --method 2 solver).
+    reference's matrix-free Lanczos (the --method 2 solver);
+  * for norb <= 10 the bytes of the reference's SaveWavefunction file of its
+    Davidson vector, and that file mapped by LoadWavefunction onto sub-lists
+    of the strings (every third alpha and every fourth beta string dropped).
 Integrals are stored as h1 plus pair factors (the ERI is rebuilt with
 sbd_gb300.generators.eri_from_factors, an order-fixed elementwise sum).
 
@@ -111,8 +114,22 @@ def run_case(name, spec, outdir):
                 "--lanczos_block", "40", "--lanczos_iteration", "20", "--lanczos_tolerance", "1e-12"]
         if norb <= 12:
             args += ["--rdm", "1"]
+        if norb <= 10:
+            args += ["--save", f"{d}/wf"]
         subprocess.run(args, check=True, capture_output=True, env=dict(os.environ, OMP_NUM_THREADS="4"))
         r = parse_sbdref(f"{d}/o.bin")
+        wf = None
+        if norb <= 10:
+            wf = {"wf_saved": np.fromfile(f"{d}/wf000000", dtype=np.uint8)}
+            la = np.delete(astr, np.arange(0, astr.size, 3))
+            lb = np.delete(bstr, np.arange(0, bstr.size, 4))
+            write_strings(f"{d}/la.txt", la, norb)
+            write_strings(f"{d}/lb.txt", lb, norb)
+            largs = [REF_BIN, "--fcidump", f"{d}/fcidump.txt", "--adet", f"{d}/la.txt", "--bdet", f"{d}/lb.txt",
+                     "--out", f"{d}/l.bin", "--tables", "0", "--hii", "0", "--load", f"{d}/wf"]
+            subprocess.run(largs, check=True, capture_output=True, env=dict(os.environ, OMP_NUM_THREADS="4"))
+            lr = parse_sbdref(f"{d}/l.bin")
+            wf.update({"load_astr": la, "load_bstr": lb, "loaded_W": lr["loaded_W"]})
     types = {int(r[f"task{k}.type"][0]): k for k in range(3)}
     ka, kb = types[2], types[1]
     out = {
@@ -121,6 +138,8 @@ def run_case(name, spec, outdir):
         "energy": np.float64(r["energy"][0]), "density_c": r["density_c"],
         "lanczos_energy": np.float64(r["lanczos_energy"][0]),
     }
+    if wf is not None:
+        out.update(wf)
     if norb <= 12:
         out["rdm1"] = np.stack([r["rdm1_0"], r["rdm1_1"]])
         out["rdm2"] = np.stack([r[f"rdm2_{k}"] for k in range(4)])

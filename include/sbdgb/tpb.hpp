@@ -22,6 +22,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstdlib>
 #include <fstream>
@@ -171,6 +172,17 @@ std::vector<uint64_t> pack_strings(const DetVec &dets, size_t bit_length, int L)
   return v;
 }
 
+// The reverse: uint64 strings to rows of `bit_length`-bit words (row-major,
+// ceil(L / bit_length) words per string).
+inline std::vector<size_t> to_words(const std::vector<uint64_t> &v, int L, size_t bit_length) {
+  const size_t words = ((size_t)L + bit_length - 1) / bit_length;
+  const uint64_t mask = bit_length >= 64 ? ~0ull : ((1ull << bit_length) - 1ull);
+  std::vector<size_t> out(v.size() * words, 0);
+  for (size_t i = 0; i < v.size(); ++i)
+    for (size_t w = 0; w < words; ++w) out[i * words + w] = (size_t)((v[i] >> (w * bit_length)) & mask);
+  return out;
+}
+
 // ---- engine objects ------------------------------------------------------------
 
 class Context {
@@ -243,6 +255,71 @@ inline double Davidson(Problem &p, std::vector<double> &W, int max_iteration, in
   sbdgb_report rep;
   check(sbdgb_davidson(p.get(), &o, &E, W.data(), &rep), p.ctx(), "Davidson");
   return E;
+}
+
+// SaveWavefunction (restart.h:21-67) at communicator size 1: file + "000000"
+// holding na, nb, det_length, the strings in bit_length-bit words, and W.
+inline void SaveWavefunction(const std::string &file, const std::vector<uint64_t> &adet,
+                             const std::vector<uint64_t> &bdet, int L, const std::vector<double> &W,
+                             size_t bit_length = 20) {
+  if (W.size() != adet.size() * bdet.size()) throw std::invalid_argument("SaveWavefunction: size mismatch");
+  std::ofstream f(file + "000000", std::ios::binary);
+  if (!f) throw std::runtime_error("SaveWavefunction: cannot open " + file + "000000");
+  const size_t na = adet.size(), nb = bdet.size(), dl = ((size_t)L + bit_length - 1) / bit_length;
+  f.write((const char *)&na, sizeof(size_t));
+  f.write((const char *)&nb, sizeof(size_t));
+  f.write((const char *)&dl, sizeof(size_t));
+  auto put = [&](const std::vector<uint64_t> &v) {
+    std::vector<size_t> w = to_words(v, L, bit_length);
+    f.write((const char *)w.data(), (std::streamsize)(sizeof(size_t) * w.size()));
+  };
+  put(adet);
+  put(bdet);
+  f.write((const char *)W.data(), (std::streamsize)(sizeof(double) * W.size()));
+}
+
+// LoadWavefunction (restart.h:415-660) at communicator size 1: the saved
+// coefficients of the (alpha, beta) pairs whose strings are in adet x bdet,
+// placed at those determinants, the rest zero, normalised.
+inline void LoadWavefunction(const std::string &file, const std::vector<uint64_t> &adet,
+                             const std::vector<uint64_t> &bdet, std::vector<double> &W, size_t bit_length = 20) {
+  std::ifstream f(file + "000000", std::ios::binary);
+  if (!f) throw std::runtime_error("LoadWavefunction: cannot open " + file + "000000");
+  size_t na = 0, nb = 0, dl = 0;
+  f.read((char *)&na, sizeof(size_t));
+  f.read((char *)&nb, sizeof(size_t));
+  f.read((char *)&dl, sizeof(size_t));
+  auto get = [&](size_t n) {
+    std::vector<size_t> w(n * dl);
+    f.read((char *)w.data(), (std::streamsize)(sizeof(size_t) * w.size()));
+    std::vector<uint64_t> v(n, 0);
+    for (size_t i = 0; i < n; ++i)
+      for (size_t k = 0; k < dl; ++k) v[i] |= (uint64_t)w[i * dl + k] << (k * bit_length);
+    return v;
+  };
+  const std::vector<uint64_t> la = get(na), lb = get(nb);
+  std::vector<double> lw(na * nb);
+  f.read((char *)lw.data(), (std::streamsize)(sizeof(double) * lw.size()));
+  if (!f) throw std::runtime_error("LoadWavefunction: truncated file");
+  auto index = [](const std::vector<uint64_t> &list, uint64_t x) -> long {
+    auto it = std::lower_bound(list.begin(), list.end(), x);
+    return (it != list.end() && *it == x) ? (long)(it - list.begin()) : -1;
+  };
+  W.assign(adet.size() * bdet.size(), 0.0);
+  std::vector<long> jb(nb);
+  for (size_t ib = 0; ib < nb; ++ib) jb[ib] = index(bdet, lb[ib]);
+  for (size_t ia = 0; ia < na; ++ia) {
+    const long ja = index(adet, la[ia]);
+    if (ja < 0) continue;
+    for (size_t ib = 0; ib < nb; ++ib)
+      if (jb[ib] >= 0) W[(size_t)ja * bdet.size() + (size_t)jb[ib]] += lw[ia * nb + ib];
+  }
+  double n2 = 0.0;
+  for (double x : W) n2 += x * x;
+  if (n2 > 0.0) {
+    const double inv = 1.0 / std::sqrt(n2);
+    for (double &x : W) x *= inv;
+  }
 }
 
 // Lanczos (lanczos.h:169-320): W in = starting vector (or empty for the

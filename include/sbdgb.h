@@ -156,6 +156,26 @@ int sbdgb_sigma_noalloc(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, 
  * memory (the call waits for it). */
 int sbdgb_occupation_density(sbdgb_problem *p, const double *W, double *density, void *stream);
 
+/* String weights of a vector, the diagonal of the half-determinant reduced
+ * density matrices (DiagonalAdetReducedDensityMatrix / ...Bdet..., chemistry/
+ * tpb/rdmat.h:13-60, 137-187) that carry-over selection ranks strings by:
+ * wa[ia] = sum_ib |W[ia][ib]|^2 (na doubles), wb[ib] = sum_ia |W[ia][ib]|^2
+ * (nb doubles), host outputs.  W: N doubles, device or host memory. */
+int sbdgb_string_weights(sbdgb_problem *p, const double *W, double *wa, double *wb, void *stream);
+/* For the amplitude-based basis extension (SinglesExtendHalfdets,
+ * chemistry/tpb/extend.h:13-60): ca[ia] / cb[ib] = number of determinants of
+ * that string with |W|^2 > cutoff, *total_weight = their summed weight. */
+int sbdgb_string_cut_counts(sbdgb_problem *p, const double *W, double cutoff, uint64_t *ca, uint64_t *cb,
+                            double *total_weight, void *stream);
+
+/* One- and two-particle reduced density matrices of W (Correlation,
+ * chemistry/tpb/correlation.h:379-640, as sbd::tpb::diag computes them with
+ * do_rdm != 0), in the reference's layout: one = 2 blocks of norb^2 doubles
+ * (spin s at s*norb^2, element i + norb*j), two = 4 blocks of norb^4 doubles
+ * (spin pair s1 + 2*s2, element a + norb*b + norb^2*c + norb^3*d).  Host
+ * outputs; two may be NULL (one-particle part only).  W: device or host. */
+int sbdgb_rdm(sbdgb_problem *p, const double *W, double *one, double *two, void *stream);
+
 /* Host-buffer form of sbd::mult: Wb += H*Wk with host vectors (copies
  * inside).  hii is ignored when NULL (the problem's own diagonal is used). */
 int sbdgb_mult_host(sbdgb_problem *p, const double *hii, const double *Wk, double *Wb);

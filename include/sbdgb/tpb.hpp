@@ -347,6 +347,99 @@ inline void OccupationDensity(Problem &p, int norb, const std::vector<double> &W
   check(sbdgb_occupation_density(p.get(), W.data(), res.data(), nullptr), p.ctx(), "OccupationDensity");
 }
 
+// Correlation (correlation.h:379-640): one-particle (2 x L^2) and
+// two-particle (4 x L^4) reduced density matrices of W in the reference layout.
+inline void Correlation(Problem &p, int norb, const std::vector<double> &W, std::vector<std::vector<double>> &onebody,
+                        std::vector<std::vector<double>> &twobody) {
+  if (W.size() != p.size()) throw std::invalid_argument("vector size mismatch");
+  const size_t L2 = (size_t)norb * norb, L4 = L2 * L2;
+  std::vector<double> one(2 * L2), two(4 * L4);
+  check(sbdgb_rdm(p.get(), W.data(), one.data(), two.data(), nullptr), p.ctx(), "Correlation");
+  onebody.assign(2, std::vector<double>());
+  twobody.assign(4, std::vector<double>());
+  for (int k = 0; k < 2; ++k) onebody[k].assign(one.begin() + k * L2, one.begin() + (k + 1) * L2);
+  for (int k = 0; k < 4; ++k) twobody[k].assign(two.begin() + k * L4, two.begin() + (k + 1) * L4);
+}
+
+// Carry-over selection (CarryOverAdet/Bdet, rdmat.h:62-135, 189-261): the
+// strings ranked by weight sum |W|^2 (ties by index), either up to the one
+// whose cumulative weight exceeds 1 - threshold or the `kept` heaviest.
+inline std::vector<uint64_t> carry_over_select(const std::vector<uint64_t> &strs, const std::vector<double> &w,
+                                               double threshold, size_t kept, double *discarded) {
+  std::vector<size_t> order(strs.size());
+  for (size_t i = 0; i < order.size(); ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return w[x] > w[y]; });
+  size_t n = 0;
+  double acc = 0.0;
+  if (kept == (size_t)-1) {
+    for (; n < order.size(); ++n) {
+      acc += w[order[n]];
+      if (acc > 1.0 - threshold) {
+        ++n;
+        break;
+      }
+    }
+  } else {
+    n = std::min(kept, order.size());
+    for (size_t k = 0; k < n; ++k) acc += w[order[k]];
+    if (discarded) *discarded = 1.0 - acc;
+  }
+  std::vector<uint64_t> out(n);
+  for (size_t k = 0; k < n; ++k) out[k] = strs[order[k]];
+  return out;
+}
+
+// SinglesExtendHalfdets (extend.h:186-318): the strings and all their single
+// excitations within norb orbitals, sorted, duplicates removed.
+inline std::vector<uint64_t> SinglesExtend(const std::vector<uint64_t> &strs, int norb) {
+  std::vector<uint64_t> out(strs);
+  for (uint64_t v : strs)
+    for (int i = 0; i < norb; ++i)
+      if ((v >> i) & 1u)
+        for (int a = 0; a < norb; ++a)
+          if (!((v >> a) & 1u)) out.push_back(v ^ (1ull << i) ^ (1ull << a));
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+  return out;
+}
+
+// The carry-over branch of diag (sbdiag.h:749-796) for a solved problem.
+inline void CarryOver(Problem &p, int norb, const std::vector<uint64_t> &adet, const std::vector<uint64_t> &bdet,
+                      const std::vector<double> &W, int carryover_type, double ratio, double threshold,
+                      std::vector<uint64_t> &co_adet, std::vector<uint64_t> &co_bdet) {
+  if (carryover_type == 1 || carryover_type == 2) {
+    std::vector<double> wa(adet.size()), wb(bdet.size());
+    check(sbdgb_string_weights(p.get(), W.data(), wa.data(), wb.data(), nullptr), p.ctx(), "CarryOver");
+    if (ratio == 0.0) {
+      co_adet = carry_over_select(adet, wa, threshold, (size_t)-1, nullptr);
+      co_bdet = carry_over_select(bdet, wb, threshold, (size_t)-1, nullptr);
+    } else {
+      double t = 0.0;
+      co_adet = carry_over_select(adet, wa, 0.0, (size_t)(ratio * adet.size()), &t);
+      co_bdet = carry_over_select(bdet, wb, 0.0, (size_t)(ratio * bdet.size()), &t);
+    }
+    if (carryover_type == 2) {
+      co_adet = SinglesExtend(co_adet, norb);
+      co_bdet = SinglesExtend(co_bdet, norb);
+    }
+  } else if (carryover_type == 3) {
+    std::vector<uint64_t> ca(adet.size()), cb(bdet.size());
+    double total = 0.0;
+    check(sbdgb_string_cut_counts(p.get(), W.data(), threshold, ca.data(), cb.data(), &total, nullptr), p.ctx(),
+          "CarryOver");
+    std::vector<uint64_t> a, b;
+    for (size_t i = 0; i < adet.size(); ++i)
+      if (ca[i]) a.push_back(adet[i]);
+    for (size_t i = 0; i < bdet.size(); ++i)
+      if (cb[i]) b.push_back(bdet[i]);
+    co_adet = SinglesExtend(a, norb);
+    co_bdet = SinglesExtend(b, norb);
+  } else {
+    co_adet.clear();
+    co_bdet.clear();
+  }
+}
+
 // Device operator with the reference's MultBase::run shape (chemistry/basic/
 // mult.h:19-103) over raw device pointers: Wb = hii o Wk + H_offdiag Wk.
 class MultTPBGB300 {
@@ -411,6 +504,9 @@ inline SBD generate_sbd_data(int argc, char *argv[]) {
     else if (a == "--tolerance") d.eps = std::atof(v);
     else if (a == "--max_time") d.max_time = std::atof(v);
     else if (a == "--rdm") d.do_rdm = std::atoi(v);
+    else if (a == "--carryover_type") d.carryover_type = std::atoi(v);
+    else if (a == "--carryover_ratio") d.ratio = std::atof(v);
+    else if (a == "--carryover_threshold") d.threshold = std::atof(v);
     else if (a == "--bit_length") d.bit_length = std::atoi(v);
     else if (a == "--nroots") d.nroots = std::atoi(v);
     else if (a == "--precision") d.precision = std::atoi(v);
@@ -435,7 +531,7 @@ inline void diag(int comm_size, const SBD &sbd_data, const FCIDump &fcidump, con
                                sbd_data.adet_comm_size * sbd_data.bdet_comm_size, sbd_data.task_comm_size),
         ctx.get(), "diag");
   if (sbd_data.method < 0 || sbd_data.method > 3) throw std::invalid_argument("--method must be 0..3");
-  if (sbd_data.do_rdm != 0) throw std::invalid_argument("RDM output is not provided by this engine");
+  if (sbd_data.do_rdm != 0) throw std::invalid_argument("use the overload with RDM outputs for do_rdm != 0");
   const bool use_lanczos = (sbd_data.method & 2) != 0;
   Integrals ints = SetupIntegrals(fcidump);
   Problem p(ctx, ints, adet, bdet);
@@ -465,6 +561,66 @@ inline void diag(int comm_size, const SBD &sbd_data, const FCIDump &fcidump, con
     check(sbdgb_occupation_density(p.get(), X.data(), density->data(), nullptr), ctx.get(), "diag density");
   }
   if (W) W->assign(X.begin(), X.begin() + p.size());
+}
+
+// diag with the reference's argument list (sbdiag.h:151-163) at communicator
+// size 1: loadname / savename name wavefunction files (LoadWavefunction gives
+// the starting vector, SaveWavefunction stores the result); density is the
+// occupation density (from the one-particle RDM when do_rdm != 0); co_adet /
+// co_bdet are the carry-over strings of carryover_type 1..3; one_p_rdm /
+// two_p_rdm are filled when do_rdm != 0.
+inline void diag(int comm_size, const SBD &sbd_data, const FCIDump &fcidump, const std::vector<uint64_t> &adet,
+                 const std::vector<uint64_t> &bdet, const std::string &loadname, const std::string &savename,
+                 double &energy, std::vector<double> &density, std::vector<uint64_t> &co_adet,
+                 std::vector<uint64_t> &co_bdet, std::vector<std::vector<double>> &one_p_rdm,
+                 std::vector<std::vector<double>> &two_p_rdm) {
+  Context ctx(sbd_data.device);
+  check(sbdgb_check_comm_sizes(ctx.get(), comm_size / std::max(1, sbd_data.task_comm_size * sbd_data.adet_comm_size *
+                                                                      sbd_data.bdet_comm_size),
+                               sbd_data.adet_comm_size * sbd_data.bdet_comm_size, sbd_data.task_comm_size),
+        ctx.get(), "diag");
+  if (sbd_data.method < 0 || sbd_data.method > 3) throw std::invalid_argument("--method must be 0..3");
+  const bool use_lanczos = (sbd_data.method & 2) != 0;
+  Integrals ints = SetupIntegrals(fcidump);
+  const int L = ints.L;
+  Problem p(ctx, ints, adet, bdet);
+  sbdgb_davidson_opts o;
+  sbdgb_davidson_default_opts(&o);
+  o.max_it = sbd_data.max_it;
+  o.max_nb = sbd_data.max_nb;
+  o.eps = sbd_data.eps;
+  o.max_time = sbd_data.max_time;
+  o.nroots = use_lanczos ? 1 : sbd_data.nroots;
+  o.init = sbd_data.init == 0 ? 0 : 1;
+  o.precision = sbd_data.precision;
+  o.refine_every = sbd_data.refine_every;
+  std::vector<double> E(o.nroots), X(p.size() * o.nroots);
+  if (!loadname.empty()) {
+    std::vector<double> W0;
+    LoadWavefunction(loadname, adet, bdet, W0, sbd_data.bit_length);
+    std::copy(W0.begin(), W0.end(), X.begin());
+    o.init = 2;
+    if (o.nroots > 1) throw std::invalid_argument("a loaded wavefunction starts one root");
+  }
+  sbdgb_report rep;
+  if (use_lanczos)
+    check(sbdgb_lanczos(p.get(), &o, E.data(), X.data(), &rep), ctx.get(), "diag");
+  else
+    check(sbdgb_davidson(p.get(), &o, E.data(), X.data(), &rep), ctx.get(), "diag");
+  energy = E[0];
+  std::vector<double> W(X.begin(), X.begin() + p.size());
+  density.assign(2 * (size_t)L, 0.0);
+  if (sbd_data.do_rdm == 0) {
+    check(sbdgb_occupation_density(p.get(), W.data(), density.data(), nullptr), ctx.get(), "diag density");
+  } else {
+    Correlation(p, L, W, one_p_rdm, two_p_rdm);
+    for (int io = 0; io < L; ++io) {
+      density[2 * io] = one_p_rdm[0][io + (size_t)L * io];
+      density[2 * io + 1] = one_p_rdm[1][io + (size_t)L * io];
+    }
+  }
+  CarryOver(p, L, adet, bdet, W, sbd_data.carryover_type, sbd_data.ratio, sbd_data.threshold, co_adet, co_bdet);
+  if (!savename.empty()) SaveWavefunction(savename, adet, bdet, L, W, sbd_data.bit_length);
 }
 
 }  // namespace tpb

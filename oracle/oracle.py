@@ -256,6 +256,72 @@ class Oracle:
                 break
         return float(E[0]), W
 
+    def carry_over(self, W: np.ndarray, carryover_type: int, ratio: float = 0.0, threshold: float = 0.01) -> dict:
+        """The carry-over branch of sbd::tpb::diag (chemistry/tpb/sbdiag.h:749-796):
+        CarryOverAdet/Bdet (rdmat.h:62-135, 189-261) and SinglesExtendHalfdets
+        (extend.h:13-318), restated with plain loops."""
+        M = np.asarray(W, dtype=np.float64).reshape(self.na, self.nb)
+        L = self.norb
+
+        def weights(rows):  # D[i] = sum_j |W|^2, accumulated in order
+            out = []
+            for r in rows:
+                acc = 0.0
+                for x in r:
+                    acc += x * x
+                out.append(acc)
+            return out
+
+        def ranked(D):
+            return sorted(range(len(D)), key=lambda i: (-D[i], i))
+
+        def by_threshold(strs, D):
+            order, acc, kept = ranked(D), 0.0, []
+            for i in order:
+                kept.append(int(strs[i]))
+                if acc + D[i] > 1.0 - threshold:
+                    break
+                acc += D[i]
+            return kept
+
+        def by_count(strs, D, n):
+            order = ranked(D)[:n]
+            acc = 0.0
+            for i in order:
+                acc += D[i]
+            return [int(strs[i]) for i in order], 1.0 - acc
+
+        def extend(strs):
+            out = set()
+            for v in strs:
+                out.add(v)
+                for i in range(L):
+                    if v >> i & 1:
+                        for a in range(L):
+                            if not v >> a & 1:
+                                out.add(v ^ (1 << i) ^ (1 << a))
+            return sorted(out)
+
+        res = {}
+        if carryover_type in (1, 2):
+            Da, Db = weights(M), weights(M.T)
+            if ratio == 0.0:
+                a, b = by_threshold(self.astr, Da), by_threshold(self.bstr, Db)
+            else:
+                a, res["truncated_a"] = by_count(self.astr, Da, int(ratio * self.na))
+                b, res["truncated_b"] = by_count(self.bstr, Db, int(ratio * self.nb))
+            if carryover_type == 2:
+                a, b = extend(a), extend(b)
+        else:
+            W2 = M * M
+            sel = W2 > threshold
+            res["total_weight"] = float(sum(W2[sel].tolist()))
+            a = extend([int(self.astr[i]) for i in range(self.na) if sel[i].any()])
+            b = extend([int(self.bstr[j]) for j in range(self.nb) if sel[:, j].any()])
+        res["alpha"] = np.array(a, dtype=np.uint64)
+        res["beta"] = np.array(b, dtype=np.uint64)
+        return res
+
     def energy(self, W: np.ndarray) -> float:
         """<W|H|W> as the reference reports it after the solve (sbdiag.h:488-526)."""
         HW = self.mult(W)

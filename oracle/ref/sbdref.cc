@@ -19,6 +19,9 @@
 //          [--time_mult K] [--density 1] [--rdm 1]
 //          [--lanczos 1 --lanczos_block NB --lanczos_iteration IT --lanczos_tolerance EPS]
 //          [--save NAME] [--load NAME]
+//          [--carryover TYPE --carryover_ratio R --carryover_threshold T]
+// --carryover runs the carry-over branch of sbd::tpb::diag (chemistry/tpb/
+// sbdiag.h:749-796) on the Davidson vector and outputs the selected strings.
 // --save writes the Davidson vector with SaveWavefunction (chemistry/tpb/
 // restart.h:21-67, file NAME000000); --load maps a saved wavefunction onto the
 // current strings with LoadWavefunction (restart.h:415-660) and outputs it.
@@ -89,6 +92,9 @@ int main(int argc, char **argv) {
   const int want_rdm = std::stoi(arg(argc, argv, "--rdm", "0"));
   const int want_lanczos = std::stoi(arg(argc, argv, "--lanczos", "0"));
   const std::string savename = arg(argc, argv, "--save", "");
+  const int co_type = std::stoi(arg(argc, argv, "--carryover", "0"));
+  const double co_ratio = std::stod(arg(argc, argv, "--carryover_ratio", "0"));
+  const double co_threshold = std::stod(arg(argc, argv, "--carryover_threshold", "0.01"));
   const std::string loadname = arg(argc, argv, "--load", "");
   const int lz_nb = std::stoi(arg(argc, argv, "--lanczos_block", "40"));
   const int lz_it = std::stoi(arg(argc, argv, "--lanczos_iteration", "20"));
@@ -228,6 +234,39 @@ int main(int argc, char **argv) {
     out.scalar("energy", E);
     out.f64("W", W);
     if (!savename.empty()) sbd::SaveWavefunction(savename, adet, bdet, 1, 1, h_comm, b_comm, t_comm, W);
+    if (co_type != 0) {
+      sbd::det_vector<size_t, sbd::det_kind::half> co_adet, co_bdet;
+      if (co_type == 1 || co_type == 2) {
+        if (co_ratio == 0.0) {
+          sbd::CarryOverAdet(W, adet, bdet, 1, 1, b_comm, co_adet, co_threshold);
+          sbd::CarryOverBdet(W, adet, bdet, 1, 1, b_comm, co_bdet, co_threshold);
+        } else {
+          double tw = 0.0;
+          sbd::CarryOverAdet(W, adet, bdet, 1, 1, b_comm, static_cast<size_t>(co_ratio * adet.size()), co_adet, tw);
+          out.scalar("truncated_a", tw);
+          sbd::CarryOverBdet(W, adet, bdet, 1, 1, b_comm, static_cast<size_t>(co_ratio * bdet.size()), co_bdet, tw);
+          out.scalar("truncated_b", tw);
+        }
+        if (co_type == 2) {
+          sbd::det_vector<size_t, sbd::det_kind::half> ra, rb;
+          sbd::SinglesExtendHalfdets(co_adet, co_bdet, bit_length, (size_t)L, 1, 1, b_comm, ra, rb);
+          co_adet = ra;
+          co_bdet = rb;
+        }
+      } else if (co_type == 3) {
+        double total = 0.0;
+        sbd::SinglesExtendHalfdets(W, adet, bdet, bit_length, (size_t)L, 1, 1, b_comm, co_threshold, co_adet, co_bdet,
+                                   total);
+        out.scalar("total_weight", total);
+      }
+      std::vector<size_t> a(co_adet.size() * co_adet.elem_size()), b(co_bdet.size() * co_bdet.elem_size());
+      for (size_t i = 0; i < co_adet.size(); ++i)
+        for (size_t w = 0; w < co_adet.elem_size(); ++w) a[i * co_adet.elem_size() + w] = co_adet[i][w];
+      for (size_t i = 0; i < co_bdet.size(); ++i)
+        for (size_t w = 0; w < co_bdet.elem_size(); ++w) b[i * co_bdet.elem_size() + w] = co_bdet[i][w];
+      out.u64("co_adet_words", a);
+      out.u64("co_bdet_words", b);
+    }
   }
 
   if (!loadname.empty()) {

@@ -109,10 +109,10 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
   // FP64 sigma transpose scratch (also used by the mixed refinement)
   b += 8 * N;
   // solver reductions (partial sums of at most 4 blocks per SM of 64 values, staging)
-  b += 8 * (size_t)(1024 * 64 * 4 + 64) + 8 * 4096 + 8 * 8192;
+  b += 8 * (size_t)(1024 * 32 * 16 + 64) + 8 * 4096 + 8 * 8192;
   if (!mixed) {
     const size_t max_nb = std::min<size_t>((size_t)std::max(o.max_nb, 2 * (int)k), std::max<size_t>(N, 1));
-    b += 16 * N * max_nb + 32 * N * k;
+    b += 16 * N * max_nb + 48 * N * k;  // basis and sigma; 2k restart vectors and their sigma; T; U
   } else {
     const size_t mmax = (size_t)std::max(std::min(o.max_nb, 64) - (int)k, 2 * (int)k);
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;  // FP32 tables
@@ -120,6 +120,11 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
     b += 32 * N * k + 4 * N * (k + mmax) + 4 * N * mmax + 12 * N * k + 4 * (8 * 3 * 64 + 64);
   }
   return b;
+}
+
+double *pinned_buffer(Ctx *c) {
+  if (!c->pinned) SBDGB_CUDA(cudaMallocHost(&c->pinned, sizeof(double) * kPinnedDoubles));
+  return c->pinned;
 }
 
 cudaEvent_t timing_event(Ctx *c) {
@@ -194,6 +199,7 @@ void sbdgb_ctx_destroy(sbdgb_ctx *ctx) {
     cudaEventDestroy(pr.second);
   }
   for (auto e : ctx->c.event_pool) cudaEventDestroy(e);
+  if (ctx->c.pinned) cudaFreeHost(ctx->c.pinned);
   if (ctx->c.own_stream) cudaStreamDestroy(ctx->c.own_stream);
   delete ctx;
 }

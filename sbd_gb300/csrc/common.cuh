@@ -109,7 +109,7 @@ enum WsSlot {
   WS_V, WS_HV, WS_X, WS_HX, WS_T, WS_PARTIAL, WS_RED, WS_COEF,
   WS_DIAG0, WS_DIAG1, WS_DIAG2,
   WS_VF, WS_HVF, WS_CF, WS_SF, WS_RES64, WS_C64, WS_TUNE,
-  WS_U, WS_UF, WS_RED2, WS_NORM_A, WS_NORM_B, WS_OCC,
+  WS_U, WS_UF, WS_RED2, WS_NORM_A, WS_NORM_B, WS_OCC, WS_RDM1, WS_RDM2, WS_RDMAB,
   WS_COUNT
 };
 
@@ -166,7 +166,11 @@ struct Ctx {
   // its tile shapes from the problem size instead of timing candidates.
   cudaMemPool_t pool = nullptr;
   bool autotune = true;
+  double *pinned = nullptr;  // page-locked read-back buffer (kPinnedDoubles), made on first use
 };
+
+constexpr size_t kPinnedDoubles = 8192;
+double *pinned_buffer(Ctx *c);
 
 // sigma timing hooks (api.cu)
 cudaEvent_t timing_event(Ctx *c);

@@ -30,6 +30,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <numeric>
 #include <type_traits>
 
 #include "common.cuh"
@@ -44,6 +45,18 @@ constexpr int kMaxV = 8;   // basis columns per dots pass
 constexpr int kMaxW = 4;   // right-hand columns per dots pass
 constexpr int kMaxCoef = 64 * 16;
 constexpr int kMaxBlock = 8;  // new directions per step
+constexpr int kMaxChunks = 16;  // dots passes batched behind one host read-back
+
+// Small coefficient sets travel as kernel parameters (no host-to-device copy,
+// no staging buffer to protect between launches).
+template <int M>
+struct Vals {
+  double v[M];
+};
+template <int M>
+struct FVals {
+  float v[M];
+};
 
 template <typename T, int M>
 struct Ptrs {
@@ -119,14 +132,14 @@ struct CombineArgs {
   size_t N;
   int nv;
   int k;
-  const double *coef;   // nv x k column-major (coef[j + nv*r])
-  const double *theta;  // k
   const double *hii;
   double *X;        // k x N or null
   double *HX;       // k x N or null
   double *T;        // k x N or null: preconditioned residual
   double *U;        // k x N or null: X / (theta - d), for the Olsen correction of T
   double *partial;  // blocks x k residual norm^2 partials (x 3k with U: norm^2, x.T, x.U)
+  Vals<kMaxCoef> coef;  // nv x k column-major (coef[j + nv*r])
+  Vals<16> theta;       // k
 };
 
 // X_r = V c_r, HX_r = HV c_r, R_r = HX_r - theta_r X_r, T_r = R_r / (theta_r - d)
@@ -140,8 +153,8 @@ template <int K>
 __global__ void __launch_bounds__(kRed) k_combine(CombineArgs a) {
   __shared__ double cs[kMaxCoef];
   __shared__ double th[16];
-  for (int t = threadIdx.x; t < a.nv * K; t += kRed) cs[t] = a.coef[t];
-  if (threadIdx.x < K) th[threadIdx.x] = a.theta[threadIdx.x];
+  for (int t = threadIdx.x; t < a.nv * K; t += kRed) cs[t] = a.coef.v[t];
+  if (threadIdx.x < K) th[threadIdx.x] = a.theta.v[threadIdx.x];
   __syncthreads();
   double rn[K], xt[K], xu[K];
 #pragma unroll
@@ -203,11 +216,11 @@ __global__ void __launch_bounds__(kRed) k_combine(CombineArgs a) {
 
 // T_r -= eps_r U_r (Olsen's correction, eps on the device).
 template <typename T>
-__global__ void __launch_bounds__(kRed) k_olsen(T *__restrict__ Tv, const T *__restrict__ U,
-                                                 const double *__restrict__ eps, int k, size_t N) {
+__global__ void __launch_bounds__(kRed) k_olsen(T *__restrict__ Tv, const T *__restrict__ U, const Vals<kMaxBlock> eps,
+                                                 int k, size_t N) {
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed)
     for (int r = 0; r < k; ++r) {
-      const T ep = (T)eps[r];
+      const T ep = (T)eps.v[r];
       Tv[(size_t)r * N + e] = fma(-ep, U[(size_t)r * N + e], Tv[(size_t)r * N + e]);
     }
 }
@@ -215,9 +228,9 @@ __global__ void __launch_bounds__(kRed) k_olsen(T *__restrict__ Tv, const T *__r
 // T_r -= sum_j V_j G[j][r]  (G column-major, ld = nv), in the vectors' precision.
 template <typename T, int K>
 __global__ void __launch_bounds__(kRed) k_project_out(const T *__restrict__ V, int nv, size_t N,
-                                                       const double *__restrict__ G, T *__restrict__ Tv) {
+                                                       const Vals<kMaxCoef> G, T *__restrict__ Tv) {
   __shared__ T gs[kMaxCoef];
-  for (int t = threadIdx.x; t < nv * K; t += kRed) gs[t] = (T)G[t];
+  for (int t = threadIdx.x; t < nv * K; t += kRed) gs[t] = (T)G.v[t];
   __syncthreads();
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     T t[K];
@@ -236,9 +249,9 @@ __global__ void __launch_bounds__(kRed) k_project_out(const T *__restrict__ V, i
 // Y_q = sum_j X_j M[j + nx*q], q < ny (a small basis change, written to Y).
 template <typename T>
 __global__ void __launch_bounds__(kRed) k_lincomb(const T *__restrict__ X, int nx, size_t N,
-                                                   const double *__restrict__ M, int ny, T *__restrict__ Y) {
+                                                   const Vals<kMaxBlock * kMaxBlock> M, int ny, T *__restrict__ Y) {
   __shared__ T ms[kMaxBlock * kMaxBlock];
-  for (int t = threadIdx.x; t < nx * ny; t += kRed) ms[t] = (T)M[t];
+  for (int t = threadIdx.x; t < nx * ny; t += kRed) ms[t] = (T)M.v[t];
   __syncthreads();
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     T x[kMaxBlock];
@@ -314,13 +327,13 @@ __global__ void k_argmin(const double *__restrict__ h, size_t N, const unsigned 
 // residuals rounded once per refinement (the residual is small, so its FP32
 // copy keeps FP32 relative accuracy of a small vector).
 __global__ void k_make_anchor_f32(const double *__restrict__ X, const double *__restrict__ S,
-                                  const double *__restrict__ theta, int k, size_t N, float *__restrict__ Xf,
+                                  const Vals<kMaxBlock> theta, int k, size_t N, float *__restrict__ Xf,
                                   float *__restrict__ Rf) {
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
     for (int j = 0; j < k; ++j) {
       const double x = X[(size_t)j * N + e];
       Xf[(size_t)j * N + e] = (float)x;
-      Rf[(size_t)j * N + e] = (float)fma(-theta[j], x, S[(size_t)j * N + e]);
+      Rf[(size_t)j * N + e] = (float)fma(-theta.v[j], x, S[(size_t)j * N + e]);
     }
 }
 
@@ -328,12 +341,12 @@ struct MixedResArgs {
   const float *Xf, *Rf, *W, *HW;
   int k, m, nq;
   size_t N;
-  const float *coef;   // per root q: [k cx | k dth | m cw], stride 3*64
-  const float *theta;  // nq current Ritz values
   const double *hii;
   float *T;            // out: nq preconditioned residuals
   float *U;            // out: nq Ritz vectors / (theta - d), for Olsen's correction
   double *partial;     // blocks x 3nq: residual norm^2, x.T, x.U
+  FVals<kMaxBlock * 3 * 64> coef;  // per root q: [k cx | k dth | m cw], stride 3*64
+  FVals<kMaxBlock> theta;          // nq current Ritz values
 };
 
 // For each root q of the block:
@@ -353,8 +366,8 @@ template <int K>
 __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
   __shared__ float c[K][3 * 64];
   __shared__ float th[K];
-  for (int t = threadIdx.x; t < K * 3 * 64; t += kRed) c[t / (3 * 64)][t % (3 * 64)] = a.coef[t];
-  if (threadIdx.x < K) th[threadIdx.x] = a.theta[threadIdx.x];
+  for (int t = threadIdx.x; t < K * 3 * 64; t += kRed) c[t / (3 * 64)][t % (3 * 64)] = a.coef.v[t];
+  if (threadIdx.x < K) th[threadIdx.x] = a.theta.v[threadIdx.x];
   __syncthreads();
   float s[3 * K], comp[3 * K];
 #pragma unroll
@@ -413,12 +426,12 @@ __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
 
 // y = sum_j X_j cx_j (FP64) + fp64(sum_l W_l cw_l) (FP32): the refined Ritz vector.
 __global__ void __launch_bounds__(kRed) k_mixed_assemble(const double *__restrict__ X, int k, const float *__restrict__ W,
-                                                         int m, size_t N, const double *__restrict__ cx,
-                                                         const float *__restrict__ cw, double *__restrict__ y) {
+                                                         int m, size_t N, const Vals<64> cx, const FVals<64> cw,
+                                                         double *__restrict__ y) {
   __shared__ double sx[64];
   __shared__ float sw[64];
-  for (int t = threadIdx.x; t < k; t += kRed) sx[t] = cx[t];
-  for (int t = threadIdx.x; t < m; t += kRed) sw[t] = cw[t];
+  for (int t = threadIdx.x; t < k; t += kRed) sx[t] = cx.v[t];
+  for (int t = threadIdx.x; t < m; t += kRed) sw[t] = cw.v[t];
   __syncthreads();
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     double v = 0.0;
@@ -434,9 +447,8 @@ __global__ void __launch_bounds__(kRed) k_mixed_assemble(const double *__restric
 // HC -= alpha C; next = HC; partial sums of |HC|^2 (one Lanczos step's
 // three-term update, lanczos.h:244-261).
 __global__ void __launch_bounds__(kRed) k_lz_update(double *__restrict__ HC, const double *__restrict__ Cb,
-                                                     double *__restrict__ next, const double *__restrict__ alpha,
-                                                     size_t N, double *__restrict__ partial) {
-  const double a = *alpha;
+                                                     double *__restrict__ next, const double a, size_t N,
+                                                     double *__restrict__ partial) {
   double s = 0.0;
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     const double h = fma(-a, __ldg(Cb + e), HC[e]);
@@ -457,9 +469,8 @@ __global__ void __launch_bounds__(kRed) k_lz_update(double *__restrict__ HC, con
 
 // next /= beta; HC = -beta * C (lanczos.h:263, 281-291 at communicator size 1).
 __global__ void __launch_bounds__(kRed) k_lz_scale(double *__restrict__ next, double *__restrict__ HC,
-                                                    const double *__restrict__ Cb, const double *__restrict__ beta,
-                                                    size_t N) {
-  const double b = *beta, ib = 1.0 / b;
+                                                    const double *__restrict__ Cb, const double b, size_t N) {
+  const double ib = 1.0 / b;
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     next[e] *= ib;
     HC[e] = -b * __ldg(Cb + e);
@@ -467,10 +478,10 @@ __global__ void __launch_bounds__(kRed) k_lz_scale(double *__restrict__ next, do
 }
 
 // W = sum_j u_j C_j over the n Krylov vectors (lanczos.h:300-312).
-__global__ void __launch_bounds__(kRed) k_lz_ritz(const double *__restrict__ C, int n, size_t N,
-                                                   const double *__restrict__ u, double *__restrict__ W) {
+__global__ void __launch_bounds__(kRed) k_lz_ritz(const double *__restrict__ C, int n, size_t N, const Vals<64> u,
+                                                   double *__restrict__ W) {
   __shared__ double us[64];
-  for (int t = threadIdx.x; t < n; t += kRed) us[t] = u[t];
+  for (int t = threadIdx.x; t < n; t += kRed) us[t] = u.v[t];
   __syncthreads();
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     double w = 0.0;
@@ -486,25 +497,47 @@ struct Solver {
   cudaStream_t s;
   size_t N;
   int blocks;
-  double *partial = nullptr;  // blocks * kMaxV*kMaxW
+  double *partial = nullptr;  // blocks * kMaxV*kMaxW per batched dots pass
   double *red = nullptr;      // reduced results (device)
-  double *coef = nullptr;     // device coefficient staging
-  std::vector<double> hbuf;
+  double *host = nullptr;     // pinned read-back buffer of the context
 
   Solver(Problem &pp, cudaStream_t ss) : p(pp), s(ss), N(pp.N) {
     int dev = p.ctx->device, sms = 0;
     SBDGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     size_t want = (N + kRed - 1) / kRed;
     blocks = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 4));
-    partial = (double *)workspace(p, WS_PARTIAL, sizeof(double) * ((size_t)blocks * kMaxV * kMaxW + 64));
+    partial = (double *)workspace(p, WS_PARTIAL,
+                                  sizeof(double) * ((size_t)blocks * kMaxV * kMaxW * kMaxChunks + 64));
     red = (double *)workspace(p, WS_RED, sizeof(double) * 4096);
-    coef = (double *)workspace(p, WS_COEF, sizeof(double) * (kMaxCoef + 64));
+    host = pinned_buffer(p.ctx);
   }
 
-  // G (column-major nv x nw) = V^T W, V columns at V0 + j*N.
+  // Copies n reduced values from red to the pinned buffer and waits for them.
+  const double *read_back(int n) {
+    SBDGB_CUDA(cudaMemcpyAsync(host, red, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+    SBDGB_CUDA(cudaStreamSynchronize(s));
+    return host;
+  }
+
+  // G (column-major nv x nw) = V^T W, V columns at V0 + j*N.  All passes
+  // (at most kMaxV x kMaxW each) are launched first and read back together.
   template <typename TV, typename TW>
   void dots(const TV *V0, int nv, const TW *const *W, int nw, std::vector<double> &G) {
     G.assign((size_t)nv * nw, 0.0);
+    struct Pass {
+      int i0, j0, mv, mw, off;
+    };
+    std::vector<Pass> batch;
+    int width = 0;
+    auto flush = [&]() {
+      if (batch.empty()) return;
+      const double *h = read_back(width);
+      for (const Pass &q : batch)
+        for (int i = 0; i < q.mv; ++i)
+          for (int j = 0; j < q.mw; ++j) G[(size_t)(q.i0 + i) + (size_t)nv * (q.j0 + j)] = h[q.off + i * q.mw + j];
+      batch.clear();
+      width = 0;
+    };
     for (int j0 = 0; j0 < nw; j0 += kMaxW) {
       const int mw = std::min(kMaxW, nw - j0);
       Ptrs<TW, kMaxW> wp{};
@@ -513,17 +546,16 @@ struct Solver {
         const int mv = std::min(kMaxV, nv - i0);
         Ptrs<TV, kMaxV> vp{};
         for (int i = 0; i < kMaxV; ++i) vp.p[i] = V0 + (size_t)(i0 + std::min(i, mv - 1)) * N;
-        launch_dots<TV, TW>(vp, wp, mv, mw);
-        const int width = mv * mw;
-        k_sum_partials<<<(width + 63) / 64, 64, 0, s>>>(partial, blocks, width, red);
+        double *part = partial + (size_t)batch.size() * blocks * kMaxV * kMaxW;
+        launch_dots<TV, TW>(vp, wp, mv, mw, part);
+        k_sum_partials<<<(mv * mw + 63) / 64, 64, 0, s>>>(part, blocks, mv * mw, red + width);
         count_launch(p.ctx);
-        hbuf.resize(width);
-        SBDGB_CUDA(cudaMemcpyAsync(hbuf.data(), red, sizeof(double) * width, cudaMemcpyDeviceToHost, s));
-        SBDGB_CUDA(cudaStreamSynchronize(s));
-        for (int i = 0; i < mv; ++i)
-          for (int j = 0; j < mw; ++j) G[(size_t)(i0 + i) + (size_t)nv * (j0 + j)] = hbuf[i * mw + j];
+        batch.push_back({i0, j0, mv, mw, width});
+        width += mv * mw;
+        if ((int)batch.size() == kMaxChunks) flush();
       }
     }
+    flush();
   }
   // G = V^T W for W contiguous too.
   template <typename TV, typename TW>
@@ -534,25 +566,25 @@ struct Solver {
   }
 
   template <typename TV, typename TW, int NV>
-  void launch_dots_w(Ptrs<TV, kMaxV> vp, Ptrs<TW, kMaxW> wp, int mw) {
+  void launch_dots_w(Ptrs<TV, kMaxV> vp, Ptrs<TW, kMaxW> wp, int mw, double *part) {
     switch (mw) {
-      case 1: k_dots<TV, TW, NV, 1><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
-      case 2: k_dots<TV, TW, NV, 2><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
-      case 3: k_dots<TV, TW, NV, 3><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
-      default: k_dots<TV, TW, NV, 4><<<blocks, kRed, 0, s>>>(vp, wp, N, partial); break;
+      case 1: k_dots<TV, TW, NV, 1><<<blocks, kRed, 0, s>>>(vp, wp, N, part); break;
+      case 2: k_dots<TV, TW, NV, 2><<<blocks, kRed, 0, s>>>(vp, wp, N, part); break;
+      case 3: k_dots<TV, TW, NV, 3><<<blocks, kRed, 0, s>>>(vp, wp, N, part); break;
+      default: k_dots<TV, TW, NV, 4><<<blocks, kRed, 0, s>>>(vp, wp, N, part); break;
     }
   }
   template <typename TV, typename TW>
-  void launch_dots(Ptrs<TV, kMaxV> vp, Ptrs<TW, kMaxW> wp, int mv, int mw) {
+  void launch_dots(Ptrs<TV, kMaxV> vp, Ptrs<TW, kMaxW> wp, int mv, int mw, double *part) {
     switch (mv) {
-      case 1: launch_dots_w<TV, TW, 1>(vp, wp, mw); break;
-      case 2: launch_dots_w<TV, TW, 2>(vp, wp, mw); break;
-      case 3: launch_dots_w<TV, TW, 3>(vp, wp, mw); break;
-      case 4: launch_dots_w<TV, TW, 4>(vp, wp, mw); break;
-      case 5: launch_dots_w<TV, TW, 5>(vp, wp, mw); break;
-      case 6: launch_dots_w<TV, TW, 6>(vp, wp, mw); break;
-      case 7: launch_dots_w<TV, TW, 7>(vp, wp, mw); break;
-      default: launch_dots_w<TV, TW, 8>(vp, wp, mw); break;
+      case 1: launch_dots_w<TV, TW, 1>(vp, wp, mw, part); break;
+      case 2: launch_dots_w<TV, TW, 2>(vp, wp, mw, part); break;
+      case 3: launch_dots_w<TV, TW, 3>(vp, wp, mw, part); break;
+      case 4: launch_dots_w<TV, TW, 4>(vp, wp, mw, part); break;
+      case 5: launch_dots_w<TV, TW, 5>(vp, wp, mw, part); break;
+      case 6: launch_dots_w<TV, TW, 6>(vp, wp, mw, part); break;
+      case 7: launch_dots_w<TV, TW, 7>(vp, wp, mw, part); break;
+      default: launch_dots_w<TV, TW, 8>(vp, wp, mw, part); break;
     }
     count_launch(p.ctx);
     SBDGB_CUDA(cudaGetLastError());
@@ -563,12 +595,11 @@ struct Solver {
   std::vector<double> combine(const double *V, const double *HV, int nv, int k, const std::vector<double> &c,
                               const std::vector<double> &theta, double *X, double *HX, double *T,
                               double *U = nullptr) {
-    std::vector<double> hc((size_t)nv * k + 16, 0.0);
-    std::copy(c.begin(), c.end(), hc.begin());
-    SBDGB_CUDA(cudaMemcpyAsync(coef, hc.data(), sizeof(double) * nv * k, cudaMemcpyHostToDevice, s));
-    SBDGB_CUDA(cudaMemcpyAsync(red + 2048, theta.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
+    SBDGB_REQUIRE((size_t)nv * k <= (size_t)kMaxCoef && k <= 16, SBDGB_E_UNSUPPORTED, "subspace too large");
     if (!T) U = nullptr;
-    CombineArgs a{V, HV, N, nv, k, coef, red + 2048, p.hii, X, HX, T, U, partial};
+    CombineArgs a{V, HV, N, nv, k, p.hii, X, HX, T, U, partial, {}, {}};
+    std::copy(c.begin(), c.begin() + (size_t)nv * k, a.coef.v);
+    for (int r = 0; r < k; ++r) a.theta.v[r] = r < (int)theta.size() ? theta[r] : 0.0;
     switch (k) {
 #define SBDGB_K(KK) \
   case KK: k_combine<KK><<<blocks, kRed, 0, s>>>(a); break;
@@ -581,9 +612,8 @@ struct Solver {
     k_sum_partials<<<1, 64, 0, s>>>(partial, blocks, width, red);
     count_launch(p.ctx, 2);
     SBDGB_CUDA(cudaGetLastError());
-    std::vector<double> v(width);
-    SBDGB_CUDA(cudaMemcpyAsync(v.data(), red, sizeof(double) * width, cudaMemcpyDeviceToHost, s));
-    SBDGB_CUDA(cudaStreamSynchronize(s));
+    const double *h = read_back(width);
+    std::vector<double> v(h, h + width);
     std::vector<double> rn(v.begin(), v.begin() + k);
     for (auto &x : rn) x = std::sqrt(std::max(0.0, x));
     if (U) olsen<double>(T, U, k, std::vector<double>(v.begin() + k, v.begin() + 2 * k),
@@ -594,18 +624,17 @@ struct Solver {
   // T_r -= (x.T_r / x.U_r) U_r for every root whose ratio is finite.
   template <typename T>
   void olsen(T *Tv, const T *U, int k, const std::vector<double> &xt, const std::vector<double> &xu) {
-    std::vector<double> e(k, 0.0);
+    Vals<kMaxBlock> e{};
     bool any = false;
-    for (int r = 0; r < k; ++r) {
+    for (int r = 0; r < k && r < kMaxBlock; ++r) {
       const double q = xt[r] / xu[r];
       if (std::isfinite(q) && xu[r] != 0.0) {
-        e[r] = q;
+        e.v[r] = q;
         any = true;
       }
     }
     if (!any) return;
-    SBDGB_CUDA(cudaMemcpyAsync(red + 2200, e.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
-    k_olsen<T><<<blocks, kRed, 0, s>>>(Tv, U, red + 2200, k, N);
+    k_olsen<T><<<blocks, kRed, 0, s>>>(Tv, U, e, k, N);
     count_launch(p.ctx);
     SBDGB_CUDA(cudaGetLastError());
   }
@@ -615,14 +644,13 @@ struct Solver {
     if (nv == 0) return;
     for (int j0 = 0; j0 < nv; j0 += kMaxCoef / std::max(k, 1)) {
       const int mv = std::min(nv - j0, kMaxCoef / std::max(k, 1));
-      std::vector<double> g((size_t)mv * k);
+      Vals<kMaxCoef> g;
       for (int r = 0; r < k; ++r)
-        for (int j = 0; j < mv; ++j) g[j + (size_t)mv * r] = G[(j0 + j) + (size_t)nv * r];
-      SBDGB_CUDA(cudaMemcpyAsync(coef, g.data(), sizeof(double) * mv * k, cudaMemcpyHostToDevice, s));
+        for (int j = 0; j < mv; ++j) g.v[j + (size_t)mv * r] = G[(j0 + j) + (size_t)nv * r];
       const T *Vj = V + (size_t)j0 * N;
       switch (k) {
 #define SBDGB_K(KK) \
-  case KK: k_project_out<T, KK><<<blocks, kRed, 0, s>>>(Vj, mv, N, coef, Tv); break;
+  case KK: k_project_out<T, KK><<<blocks, kRed, 0, s>>>(Vj, mv, N, g, Tv); break;
         SBDGB_K(1) SBDGB_K(2) SBDGB_K(3) SBDGB_K(4) SBDGB_K(5) SBDGB_K(6) SBDGB_K(7) SBDGB_K(8)
 #undef SBDGB_K
         default: throw Error(SBDGB_E_UNSUPPORTED, "at most 8 vectors per projection");
@@ -635,8 +663,9 @@ struct Solver {
   template <typename T>
   void lincomb(const T *X, int nx, const std::vector<double> &M, int ny, T *Y) {
     SBDGB_REQUIRE(nx <= kMaxBlock && ny <= kMaxBlock, SBDGB_E_UNSUPPORTED, "block too large");
-    SBDGB_CUDA(cudaMemcpyAsync(coef, M.data(), sizeof(double) * nx * ny, cudaMemcpyHostToDevice, s));
-    k_lincomb<T><<<blocks, kRed, 0, s>>>(X, nx, N, coef, ny, Y);
+    Vals<kMaxBlock * kMaxBlock> m;
+    std::copy(M.begin(), M.begin() + (size_t)nx * ny, m.v);
+    k_lincomb<T><<<blocks, kRed, 0, s>>>(X, nx, N, m, ny, Y);
     count_launch(p.ctx);
     SBDGB_CUDA(cudaGetLastError());
   }
@@ -644,11 +673,9 @@ struct Solver {
   double reduce_partials(int width, std::vector<double> *out = nullptr) {
     k_sum_partials<<<1, 64, 0, s>>>(partial, blocks, width, red);
     count_launch(p.ctx);
-    std::vector<double> v(width);
-    SBDGB_CUDA(cudaMemcpyAsync(v.data(), red, sizeof(double) * width, cudaMemcpyDeviceToHost, s));
-    SBDGB_CUDA(cudaStreamSynchronize(s));
-    if (out) *out = v;
-    return v[0];
+    const double *h = read_back(width);
+    if (out) out->assign(h, h + width);
+    return h[0];
   }
 
   // Orthonormalises the nt vectors Tb against the first nv columns of V and
@@ -787,8 +814,8 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
   Solver sv(p, s);
   double *V = (double *)workspace(p, WS_V, sizeof(double) * N * max_nb);
   double *HV = (double *)workspace(p, WS_HV, sizeof(double) * N * max_nb);
-  double *X = (double *)workspace(p, WS_X, sizeof(double) * N * k);
-  double *HX = (double *)workspace(p, WS_HX, sizeof(double) * N * k);
+  double *X = (double *)workspace(p, WS_X, sizeof(double) * N * 2 * k);  // restart basis (<= 2k)
+  double *HX = (double *)workspace(p, WS_HX, sizeof(double) * N * 2 * k);
   double *T = (double *)workspace(p, WS_T, sizeof(double) * N * k);
   double *U = (double *)workspace(p, WS_U, sizeof(double) * N * k);
 
@@ -816,6 +843,8 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
   extend(0, nv);
 
   std::vector<double> theta, Y, resid(k, 0.0), c, th;
+  std::vector<double> cprev;  // previous step's Ritz coefficients in the current basis (nvprev x kk)
+  int nvprev = 0, kprev = 0;
   bool converged = false;
   int iter = 0, kk = 0;
   const int max_steps = std::max(1, o.max_it) * max_nb;
@@ -843,16 +872,62 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
     int nnew = 0;
     for (int q = 0; q < kk; ++q) nnew += (resid[q] >= o.eps);
     if (nv + nnew > max_nb) {
-      // thick restart with the Ritz vectors and their sigma vectors
-      sv.combine(V, HV, nv, kk, c, th, X, HX, nullptr);
-      SBDGB_CUDA(cudaMemcpyAsync(V, X, sizeof(double) * N * kk, cudaMemcpyDeviceToDevice, s));
-      SBDGB_CUDA(cudaMemcpyAsync(HV, HX, sizeof(double) * N * kk, cudaMemcpyDeviceToDevice, s));
-      nv = kk;
+      // Thick restart on span{Ritz vectors, previous step's Ritz vectors}
+      // (the second set keeps the search direction, as in locally optimal
+      // methods).  The new basis is V Q for Q orthonormal in coefficient
+      // space, so its sigma vectors are HV Q and its projected matrix
+      // Q^T A Q: no sigma product and no dot product is needed.
+      std::vector<std::vector<double>> cols;
+      for (int q = 0; q < kk; ++q) cols.emplace_back(c.begin() + (size_t)nv * q, c.begin() + (size_t)nv * (q + 1));
+      const int nkeep = std::min(kprev, max_nb - kk - nnew);
+      for (int q = 0; q < nkeep; ++q) {
+        std::vector<double> v(nv, 0.0);
+        for (int i = 0; i < nvprev && i < nv; ++i) v[i] = cprev[i + (size_t)nvprev * q];
+        cols.push_back(v);
+      }
+      std::vector<double> Q;  // nv x m, orthonormal columns
+      int m = 0;
+      for (auto &v : cols) {
+        const double n0 = std::sqrt(std::inner_product(v.begin(), v.end(), v.begin(), 0.0));
+        for (int pass = 0; pass < 2; ++pass)
+          for (int j = 0; j < m; ++j) {
+            double pr = 0.0;
+            for (int i = 0; i < nv; ++i) pr += Q[i + (size_t)nv * j] * v[i];
+            for (int i = 0; i < nv; ++i) v[i] -= pr * Q[i + (size_t)nv * j];
+          }
+        const double nn = std::sqrt(std::inner_product(v.begin(), v.end(), v.begin(), 0.0));
+        if (!(nn > 1e-8 * n0)) continue;
+        for (double &x : v) x /= nn;
+        Q.insert(Q.end(), v.begin(), v.end());
+        ++m;
+      }
+      sv.combine(V, HV, nv, m, Q, th, X, HX, nullptr);
+      SBDGB_CUDA(cudaMemcpyAsync(V, X, sizeof(double) * N * m, cudaMemcpyDeviceToDevice, s));
+      SBDGB_CUDA(cudaMemcpyAsync(HV, HX, sizeof(double) * N * m, cudaMemcpyDeviceToDevice, s));
+      std::vector<double> A((size_t)nv * nv), AQ((size_t)nv * m, 0.0), Hn((size_t)m * m, 0.0), cn((size_t)m * kk, 0.0);
+      for (int j = 0; j < nv; ++j)
+        for (int i = 0; i < nv; ++i)
+          A[i + (size_t)nv * j] = 0.5 * (Hs[i + (size_t)max_nb * j] + Hs[j + (size_t)max_nb * i]);
+      for (int b = 0; b < m; ++b)
+        for (int j = 0; j < nv; ++j)
+          for (int i = 0; i < nv; ++i) AQ[i + (size_t)nv * b] += A[i + (size_t)nv * j] * Q[j + (size_t)nv * b];
+      for (int b = 0; b < m; ++b)
+        for (int a2 = 0; a2 < m; ++a2)
+          for (int i = 0; i < nv; ++i) Hn[a2 + (size_t)m * b] += Q[i + (size_t)nv * a2] * AQ[i + (size_t)nv * b];
+      for (int q = 0; q < kk; ++q)
+        for (int a2 = 0; a2 < m; ++a2)
+          for (int i = 0; i < nv; ++i) cn[a2 + (size_t)m * q] += Q[i + (size_t)nv * a2] * c[i + (size_t)nv * q];
       std::fill(Hs.begin(), Hs.end(), 0.0);
-      for (int q = 0; q < kk; ++q) Hs[q + (size_t)max_nb * q] = th[q];
+      for (int b = 0; b < m; ++b)
+        for (int a2 = 0; a2 < m; ++a2) Hs[a2 + (size_t)max_nb * b] = Hn[a2 + (size_t)m * b];
+      c = cn;
+      nv = m;
       r.restarts++;
       // T still holds the preconditioned residuals of these Ritz vectors
     }
+    cprev = c;
+    nvprev = nv;
+    kprev = kk;
     // corrections of the unconverged roots, packed at the front of T
     int nt = 0;
     for (int q = 0; q < kk; ++q)
@@ -905,7 +980,6 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
   float *Rf = (float *)workspace(p, WS_SF, sizeof(float) * N * k);
   float *Tf = (float *)workspace(p, WS_CF, sizeof(float) * N * k);
   float *Uf = (float *)workspace(p, WS_UF, sizeof(float) * N * k);
-  float *dcoef = (float *)workspace(p, WS_DIAG1, sizeof(float) * (kMaxBlock * 3 * 64 + 64));
 
   sbdgb_report r{};
   // anchors: starting vectors orthonormalised in FP64
@@ -989,8 +1063,11 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
     double elapsed = std::chrono::duration<double>(clock::now() - t0).count();
     if (converged || iter >= max_steps || (o.max_time > 0 && elapsed > o.max_time)) break;
     // rounded anchors and residuals for the FP32 inner steps
-    SBDGB_CUDA(cudaMemcpyAsync(sv.red + 2048, theta.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
-    k_make_anchor_f32<<<sv.blocks, kRed, 0, s>>>(X, S, sv.red + 2048, k, N, Xf, Rf);
+    {
+      Vals<kMaxBlock> th{};
+      for (int j = 0; j < k; ++j) th.v[j] = theta[j];
+      k_make_anchor_f32<<<sv.blocks, kRed, 0, s>>>(X, S, th, k, N, Xf, Rf);
+    }
     count_launch(p.ctx);
     couple(0, m);
     bool stalled = false;
@@ -1010,19 +1087,16 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       const int nq = (int)roots.size();
       if (nq == 0 || m + nq > mmax) break;
       // preconditioned residuals of the unconverged roots, FP32, one pass
-      std::vector<float> hc((size_t)kMaxBlock * 3 * 64, 0.f), hth(kMaxBlock, 0.f);
+      MixedResArgs ma{Xf, Rf, W, HW, k, m, nq, N, p.hii, Tf, Uf, sv.partial, {}, {}};
       for (int i = 0; i < nq; ++i) {
         const int q = roots[i];
         for (int j = 0; j < k; ++j) {
-          hc[(size_t)i * 192 + j] = (float)cX[j + (size_t)k * q];
-          hc[(size_t)i * 192 + 64 + j] = (float)(theta[j] - thc[q]);
+          ma.coef.v[(size_t)i * 192 + j] = (float)cX[j + (size_t)k * q];
+          ma.coef.v[(size_t)i * 192 + 64 + j] = (float)(theta[j] - thc[q]);
         }
-        for (int l = 0; l < m; ++l) hc[(size_t)i * 192 + 128 + l] = (float)cW[l + (size_t)m * q];
-        hth[i] = (float)thc[q];
+        for (int l = 0; l < m; ++l) ma.coef.v[(size_t)i * 192 + 128 + l] = (float)cW[l + (size_t)m * q];
+        ma.theta.v[i] = (float)thc[q];
       }
-      SBDGB_CUDA(cudaMemcpyAsync(dcoef, hc.data(), sizeof(float) * hc.size(), cudaMemcpyHostToDevice, s));
-      SBDGB_CUDA(cudaMemcpyAsync(dcoef + hc.size(), hth.data(), sizeof(float) * kMaxBlock, cudaMemcpyHostToDevice, s));
-      MixedResArgs ma{Xf, Rf, W, HW, k, m, nq, N, dcoef, dcoef + hc.size(), p.hii, Tf, Uf, sv.partial};
       switch (nq) {
 #define SBDGB_K(KK) \
   case KK: k_mixed_residual<KK><<<sv.blocks, kRed, 0, s>>>(ma); break;
@@ -1072,13 +1146,11 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
     }
     // refinement: assemble the Ritz vectors in FP64, orthonormalise, FP64 sigma
     for (int q = 0; q < k; ++q) {
-      std::vector<double> cx(k);
-      std::vector<float> cw(m);
-      for (int j = 0; j < k; ++j) cx[j] = cX[j + (size_t)k * q];
-      for (int l = 0; l < m; ++l) cw[l] = (float)cW[l + (size_t)m * q];
-      SBDGB_CUDA(cudaMemcpyAsync(sv.red + 3000, cx.data(), sizeof(double) * k, cudaMemcpyHostToDevice, s));
-      if (m) SBDGB_CUDA(cudaMemcpyAsync(dcoef, cw.data(), sizeof(float) * m, cudaMemcpyHostToDevice, s));
-      k_mixed_assemble<<<sv.blocks, kRed, 0, s>>>(X, k, W, m, N, sv.red + 3000, dcoef, T + (size_t)q * N);
+      Vals<64> cx{};
+      FVals<64> cw{};
+      for (int j = 0; j < k; ++j) cx.v[j] = cX[j + (size_t)k * q];
+      for (int l = 0; l < m; ++l) cw.v[l] = (float)cW[l + (size_t)m * q];
+      k_mixed_assemble<<<sv.blocks, kRed, 0, s>>>(X, k, W, m, N, cx, cw, T + (size_t)q * N);
       count_launch(p.ctx);
     }
     SBDGB_REQUIRE(sv.orthonormalize_block<double>(T, k, X, 0, X, 1e-8) == k, SBDGB_E_STATE,
@@ -1141,7 +1213,6 @@ void lanczos_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X
       SBDGB_CUDA(cudaMemcpyAsync(W, Cv, sizeof(double) * N, cudaMemcpyDeviceToDevice, s));
     }
   }
-  double *dval = sv.red + 2400;  // device scalars alpha (0), beta (1), Ritz coefficients (8..)
   sbdgb_report r{};
   double E0 = 0.0, change = 0.0;
   bool stop = false;
@@ -1176,14 +1247,12 @@ void lanczos_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X
       E_old = theta[0];
       if (ib + 1 == nb) break;
       double *next = Cv + (size_t)(ib + 1) * N;
-      SBDGB_CUDA(cudaMemcpyAsync(dval, &alpha, sizeof(double), cudaMemcpyHostToDevice, s));
-      k_lz_update<<<sv.blocks, kRed, 0, s>>>(HC, Cb, next, dval, N, sv.partial);
+      k_lz_update<<<sv.blocks, kRed, 0, s>>>(HC, Cb, next, alpha, N, sv.partial);
       count_launch(p.ctx);
       const double beta = std::sqrt(std::max(0.0, sv.reduce_partials(1)));
       A[ib + (size_t)nb * (ib + 1)] = A[(ib + 1) + (size_t)nb * ib] = beta;
       if (std::fabs(beta) < o.eps) break;  // invariant subspace (the new vector is not used)
-      SBDGB_CUDA(cudaMemcpyAsync(dval + 1, &beta, sizeof(double), cudaMemcpyHostToDevice, s));
-      k_lz_scale<<<sv.blocks, kRed, 0, s>>>(next, HC, Cb, dval + 1, N);
+      k_lz_scale<<<sv.blocks, kRed, 0, s>>>(next, HC, Cb, beta, N);
       count_launch(p.ctx);
       SBDGB_CUDA(cudaGetLastError());
     }
@@ -1192,9 +1261,9 @@ void lanczos_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X
       for (int i = 0; i < n; ++i) T[i + (size_t)n * j] = A[i + (size_t)nb * j];
     jacobi_eig(n, T, theta, Y);
     E0 = theta[0];
-    std::vector<double> u(Y.begin(), Y.begin() + n);
-    SBDGB_CUDA(cudaMemcpyAsync(dval + 8, u.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s));
-    k_lz_ritz<<<sv.blocks, kRed, 0, s>>>(Cv, n, N, dval + 8, W);
+    Vals<64> u{};
+    std::copy(Y.begin(), Y.begin() + n, u.v);
+    k_lz_ritz<<<sv.blocks, kRed, 0, s>>>(Cv, n, N, u, W);
     count_launch(p.ctx);
     SBDGB_CUDA(cudaGetLastError());
     r.restarts++;

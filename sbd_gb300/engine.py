@@ -24,7 +24,7 @@ SYMBOLS = [
     "sbdgb_abi_version", "sbdgb_ctx_create", "sbdgb_ctx_destroy", "sbdgb_last_error", "sbdgb_ctx_bytes_in_use",
     "sbdgb_ctx_launch_count", "sbdgb_ctx_set_stream", "sbdgb_ctx_enable_timing", "sbdgb_ctx_sigma_timing", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
     "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
-    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_noalloc", "sbdgb_occupation_density", "sbdgb_problem_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
+    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_noalloc", "sbdgb_occupation_density", "sbdgb_string_weights", "sbdgb_string_cut_counts", "sbdgb_rdm", "sbdgb_problem_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
     "sbdgb_davidson", "sbdgb_lanczos", "sbdgb_server_create", "sbdgb_server_submit", "sbdgb_server_poll", "sbdgb_server_wait",
     "sbdgb_server_stats", "sbdgb_server_last_error", "sbdgb_server_destroy",
 ]
@@ -115,6 +115,9 @@ def load(path: str = LIB_PATH):
     L.sbdgb_sigma_mixed.argtypes = [vp, vp, vp, vp]
     L.sbdgb_sigma_noalloc.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_occupation_density.argtypes = [vp, vp, _f64p, vp]
+    L.sbdgb_string_weights.argtypes = [vp, vp, _f64p, _f64p, vp]
+    L.sbdgb_rdm.argtypes = [vp, vp, _f64p, vp, vp]
+    L.sbdgb_string_cut_counts.argtypes = [vp, vp, C.c_double, _u64p, _u64p, C.POINTER(C.c_double), vp]
     L.sbdgb_mult_host.argtypes = [vp, vp, _f64p, _f64p]
     L.sbdgb_problem_tuning.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
@@ -321,6 +324,38 @@ class TPBProblem:
         self.engine.check(self.lib.sbdgb_lanczos(self.h, C.byref(o), E, X.ctypes.data if X is not None else None,
                                                  C.byref(rep)))
         return DavidsonResult(E, X, rep.as_dict(1))
+
+    def _vec(self, W):
+        if isinstance(W, int):
+            return W, None
+        w = np.ascontiguousarray(W, dtype=np.float64).ravel()
+        if w.size != self.N:
+            raise ValueError("vector size mismatch")
+        return w.ctypes.data, w
+
+    def string_weights(self, W) -> tuple[np.ndarray, np.ndarray]:
+        """Alpha and beta string weights sum |W|^2 (the carry-over ranking)."""
+        ptr, keep = self._vec(W)
+        wa, wb = np.zeros(self.na), np.zeros(self.nb)
+        self.engine.check(self.lib.sbdgb_string_weights(self.h, ptr, wa, wb, None))
+        return wa, wb
+
+    def string_cut_counts(self, W, cutoff: float) -> tuple[np.ndarray, np.ndarray, float]:
+        """Per string, the number of determinants with |W|^2 > cutoff; and their total weight."""
+        ptr, keep = self._vec(W)
+        ca, cb = np.zeros(self.na, dtype=np.uint64), np.zeros(self.nb, dtype=np.uint64)
+        tot = C.c_double(0.0)
+        self.engine.check(self.lib.sbdgb_string_cut_counts(self.h, ptr, float(cutoff), ca, cb, C.byref(tot), None))
+        return ca, cb, tot.value
+
+    def rdm(self, W, two_body: bool = True) -> tuple[np.ndarray, np.ndarray | None]:
+        """One-particle (2, L*L) and two-particle (4, L^4) RDMs in the reference's layout."""
+        ptr, keep = self._vec(W)
+        L = self.norb
+        one = np.zeros((2, L * L))
+        two = np.zeros((4, L ** 4)) if two_body else None
+        self.engine.check(self.lib.sbdgb_rdm(self.h, ptr, one, two.ctypes.data if two is not None else None, None))
+        return one, two
 
     def occupation_density(self, W) -> np.ndarray:
         """Occupation density [2*norb] of W (a host array or a device pointer)."""

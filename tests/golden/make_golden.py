@@ -14,7 +14,10 @@ oracle/Makefile -- and the reference's results are stored:
     reference's matrix-free Lanczos (the --method 2 solver);
   * for norb <= 10 the bytes of the reference's SaveWavefunction file of its
     Davidson vector, and that file mapped by LoadWavefunction onto sub-lists
-    of the strings (every third alpha and every fourth beta string dropped).
+    of the strings (every third alpha and every fourth beta string dropped);
+  * for norb <= 16 with equal alpha and beta electron counts, the reference's
+    Davidson vector W and the carry-over strings sbd::tpb::diag selects from
+    it (types 1 by threshold and by ratio, 2 and 3; sbdiag.h:749-796).
 Integrals are stored as h1 plus pair factors (the ERI is rebuilt with
 sbd_gb300.generators.eri_from_factors, an order-fixed elementwise sum).
 
@@ -36,7 +39,7 @@ sys.path.insert(0, ROOT)
 from oracle.oracle import REF_BIN, Oracle, build_reference, parse_sbdref  # noqa: E402
 from sbd_gb300.fcidump import Integrals, write_fcidump  # noqa: E402
 from sbd_gb300.generators import draw_strings, eri_from_factors, make_factors, make_h1  # noqa: E402
-from sbd_gb300.strings import write_strings  # noqa: E402
+from sbd_gb300.strings import from_words, write_strings  # noqa: E402
 
 # name: (norb, n_alpha_elec, n_beta_elec, n_alpha_strings, n_beta_strings (None = same list), nchol, seed)
 CASES = {
@@ -118,6 +121,25 @@ def run_case(name, spec, outdir):
             args += ["--save", f"{d}/wf"]
         subprocess.run(args, check=True, capture_output=True, env=dict(os.environ, OMP_NUM_THREADS="4"))
         r = parse_sbdref(f"{d}/o.bin")
+        co = None
+        if norb <= 16 and na_e == nb_e:
+            co = {"W": r["W"]}
+            runs = {"co1t": ["--carryover", "1", "--carryover_threshold", "0.05"],
+                    "co1r": ["--carryover", "1", "--carryover_ratio", "0.5"],
+                    "co2": ["--carryover", "2", "--carryover_threshold", "0.2"],
+                    "co3": ["--carryover", "3", "--carryover_threshold", "1e-4"]}
+            base = args[:args.index("--density")]
+            for tag, extra in runs.items():
+                cargs = [x if x != f"{d}/o.bin" else f"{d}/c_{tag}.bin" for x in base] + extra
+                subprocess.run(cargs, check=True, capture_output=True, env=dict(os.environ, OMP_NUM_THREADS="4"))
+                cr = parse_sbdref(f"{d}/c_{tag}.bin")
+                assert np.array_equal(cr["W"], r["W"]), (name, tag, "Davidson vector differs between runs")
+                words = (norb + 19) // 20
+                co[f"{tag}_a"] = from_words(cr["co_adet_words"].reshape(-1, words))
+                co[f"{tag}_b"] = from_words(cr["co_bdet_words"].reshape(-1, words))
+                for key in ("truncated_a", "truncated_b", "total_weight"):
+                    if key in cr:
+                        co[f"{tag}_{key}"] = np.float64(cr[key][0])
         wf = None
         if norb <= 10:
             wf = {"wf_saved": np.fromfile(f"{d}/wf000000", dtype=np.uint8)}
@@ -140,6 +162,8 @@ def run_case(name, spec, outdir):
     }
     if wf is not None:
         out.update(wf)
+    if co is not None:
+        out.update(co)
     if norb <= 12:
         out["rdm1"] = np.stack([r["rdm1_0"], r["rdm1_1"]])
         out["rdm2"] = np.stack([r[f"rdm2_{k}"] for k in range(4)])

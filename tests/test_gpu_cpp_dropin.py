@@ -57,3 +57,41 @@ def test_cpp_drop_in_lanczos_method(exe, tmp_path, name):
                         "--tolerance", "1e-12"], capture_output=True, text=True, check=True)
     e = float(re.search(r"Solver energy = ([-0-9.eE+]+)", r.stdout).group(1))
     assert abs(e - c.lanczos_energy) < 1e-8
+
+
+@pytest.fixture(scope="module")
+def exe_full(tmp_path_factory):
+    lib = build.build()
+    out = str(tmp_path_factory.mktemp("cppfull") / "tpb_diag_full")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "tpb_diag_full.cpp"), "-L" + os.path.dirname(lib), "-lsbdgb",
+                    "-Wl,-rpath," + os.path.dirname(lib), "-o", out], check=True)
+    return out
+
+
+@pytest.mark.parametrize("name", ["fci_L8", "open_L10"])
+def test_cpp_full_diag_carry_over_rdm_and_files(exe_full, tmp_path, name):
+    """The reference-shaped diag: carry-over type 2 strings as the reference
+    selected them, RDM traces = electron counts, and a saved wavefunction that
+    restarts the next solve at the same energy."""
+    c = load(name)
+    ints = Integrals(norb=c.norb, nelec=0, ecore=c.ecore, h1=c.h1, eri=c.eri)
+    write_fcidump(str(tmp_path / "fcidump.txt"), ints)
+    write_strings(str(tmp_path / "a.txt"), c.astr, c.norb)
+    write_strings(str(tmp_path / "b.txt"), c.bstr, c.norb)
+    args = [exe_full, "--fcidump", str(tmp_path / "fcidump.txt"), "--adetfile", str(tmp_path / "a.txt"),
+            "--bdetfile", str(tmp_path / "b.txt"), "--block", "12", "--iteration", "200", "--tolerance", "1e-10",
+            "--rdm", "1", "--carryover_type", "2", "--carryover_threshold", "0.2"]
+    r = subprocess.run(args + ["--savename", str(tmp_path / "wf")], capture_output=True, text=True, check=True)
+    e = float(re.search(r"Energy = ([-0-9.eE+]+)", r.stdout).group(1))
+    assert abs(e - c.energy) < 1e-8
+    co_a = [int(x) for x in re.search(r"CarryOver alpha =(.*)", r.stdout).group(1).split()]
+    co_b = [int(x) for x in re.search(r"CarryOver beta =(.*)", r.stdout).group(1).split()]
+    assert co_a == [int(x) for x in c.d["co2_a"]] and co_b == [int(x) for x in c.d["co2_b"]]
+    na_e, nb_e = bin(int(c.astr[0])).count("1"), bin(int(c.bstr[0])).count("1")
+    tr = [float(x) for x in re.search(r"RDM1 traces = (\S+) (\S+)", r.stdout).groups()]
+    assert abs(tr[0] - na_e) < 1e-8 and abs(tr[1] - nb_e) < 1e-8
+    assert os.path.exists(str(tmp_path / "wf000000"))
+    r2 = subprocess.run(args + ["--loadname", str(tmp_path / "wf")], capture_output=True, text=True, check=True)
+    e2 = float(re.search(r"Energy = ([-0-9.eE+]+)", r2.stdout).group(1))
+    assert abs(e2 - c.energy) < 1e-8

@@ -90,3 +90,17 @@ def test_device_pointer_sigma(engine):
     p.sigma_device(c_dev.data_ptr(), s_dev.data_ptr(), accumulate=False, stream=stream.cuda_stream)
     torch.cuda.synchronize()
     assert max_rel(s_dev.cpu().numpy(), ref) <= 1e-14
+
+
+def test_rdms_against_oracle_norb16(engine):
+    """RDMs at norb 16 (beyond the fixtures) against the oracle's restatement."""
+    prob = make_problem(16, 5, 5, 150, 120, seed=21)
+    p = TPBProblem.from_problem(engine, prob)
+    p.build_tables()
+    o = Oracle.from_problem(prob)
+    W = np.random.default_rng(4).uniform(-1, 1, prob.ndet)
+    one, two = p.rdm(W)
+    ro, rt = o.correlation(W)
+    assert np.abs(one - ro).max() <= 1e-12 * np.abs(ro).max()
+    assert np.abs(two - rt).max() <= 1e-12 * np.abs(rt).max()
+    p.close()

@@ -99,3 +99,15 @@ def test_lanczos_matches_reference_lanczos(gcase):
     W = r.vectors
     assert abs(np.dot(W, W) - 1.0) < 1e-8
     assert abs(np.dot(W, p.mult(W)) - r.energies[0]) < 1e-7
+
+
+def test_rdms_match_reference(gcase):
+    """One- and two-particle RDMs of C against the reference's Correlation (norb <= 12 fixtures)."""
+    c, p = gcase
+    if c.rdm1 is None:
+        pytest.skip("RDM fixtures are stored for norb <= 12")
+    one, two = p.rdm(c.C)
+    assert np.abs(one - c.rdm1).max() <= 1e-12 * np.abs(c.rdm1).max()
+    assert np.abs(two - c.rdm2).max() <= 1e-12 * np.abs(c.rdm2).max()
+    one_only, none = p.rdm(c.C, two_body=False)
+    assert none is None and np.abs(one_only - c.rdm1).max() <= 1e-12 * np.abs(c.rdm1).max()

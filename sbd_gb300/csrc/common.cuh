@@ -200,7 +200,9 @@ void build_diag(Problem &p, cudaStream_t s);
 void build_row_tiles(Problem &p, cudaStream_t s);
 void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s);
 void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, double *CT, cudaStream_t s);
-void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s);
+// (H - shift) C in the mixed form: the diagonal term is formed in FP64 before
+// the result is rounded, so a shift near the spectrum keeps FP32 outputs small.
+void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double shift = 0.0);
 void prepare_mixed(Problem &p, cudaStream_t s);
 // davidson.cu
 void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X, sbdgb_report *rep);

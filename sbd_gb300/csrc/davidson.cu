@@ -346,7 +346,8 @@ struct MixedResArgs {
   float *U;            // out: nq Ritz vectors / (theta - d), for Olsen's correction
   double *partial;     // blocks x 3nq: residual norm^2, x.T, x.U
   FVals<kMaxBlock * 3 * 64> coef;  // per root q: [k cx | k dth | m cw], stride 3*64
-  FVals<kMaxBlock> theta;          // nq current Ritz values
+  FVals<kMaxBlock> thw;            // nq Ritz values minus the shift of HW
+  Vals<kMaxBlock> theta;           // nq Ritz values (preconditioner)
 };
 
 // For each root q of the block:
@@ -367,7 +368,7 @@ __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
   __shared__ float c[K][3 * 64];
   __shared__ float th[K];
   for (int t = threadIdx.x; t < K * 3 * 64; t += kRed) c[t / (3 * 64)][t % (3 * 64)] = a.coef.v[t];
-  if (threadIdx.x < K) th[threadIdx.x] = a.theta.v[threadIdx.x];
+  if (threadIdx.x < K) th[threadIdx.x] = a.thw.v[threadIdx.x];
   __syncthreads();
   float s[3 * K], comp[3 * K];
 #pragma unroll
@@ -399,7 +400,7 @@ __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
 #pragma unroll
     for (int q = 0; q < K; ++q) {
       kahan_add(s[q], comp[q], r[q] * r[q]);
-      double den = (double)th[q] - d;
+      double den = a.theta.v[q] - d;
       if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
       const float t = (float)((double)r[q] / den), u = (float)((double)x[q] / den);
       a.T[(size_t)q * a.N + e] = t;
@@ -422,6 +423,14 @@ __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
     for (int w2 = 0; w2 < kRed / 32; ++w2) t += red[w2][threadIdx.x];
     a.partial[(size_t)blockIdx.x * 3 * K + threadIdx.x] = t;
   }
+}
+
+// D_j = fp32(X_j) - Xf_j: the step of the anchors over one refinement (the
+// search direction kept when the FP32 subspace is dropped).
+__global__ void k_anchor_step_f32(const double *__restrict__ X, const float *__restrict__ Xf, int k, size_t N,
+                                  float *__restrict__ D) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < N; e += (size_t)gridDim.x * blockDim.x)
+    for (int j = 0; j < k; ++j) D[(size_t)j * N + e] = (float)X[(size_t)j * N + e] - Xf[(size_t)j * N + e];
 }
 
 // y = sum_j X_j cx_j (FP64) + fp64(sum_l W_l cw_l) (FP32): the refined Ritz vector.
@@ -1006,12 +1015,16 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
     theta = th;
   };
   refine_rr();
+  // FP32 sigma products are taken of H - shift with the first Ritz value as
+  // the shift: H W is then of the size of the spread of the spectrum rather
+  // than of the energy, and HW - theta W loses no FP32 digits to cancellation
+  const double shift = theta[0];
 
   // projected quantities of the basis [anchors, W]
   std::vector<double> Sxw((size_t)k * mmax), Hxw((size_t)k * mmax), Sww((size_t)mmax * mmax),
       Hww((size_t)mmax * mmax);
   std::vector<double> cX((size_t)k * k, 0.0), cW, thc(k);  // current Ritz vectors: cX[j + k*q], cW[l + m*q]
-  int m = 0;
+  int m = 0, seed = 0;
   // Rayleigh-Ritz on span{anchors, W}: generalised problem with the exact overlaps
   auto rayleigh_ritz = [&]() -> bool {
     const int n = k + m;
@@ -1069,6 +1082,28 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       k_make_anchor_f32<<<sv.blocks, kRed, 0, s>>>(X, S, th, k, N, Xf, Rf);
     }
     count_launch(p.ctx);
+    if (seed > 0) {
+      // the FP32 subspace was dropped: restart it with the anchors' last step
+      // (locally optimal restart), orthonormalised against the new anchors
+      const int added = sv.orthonormalize_block<float>(Tf, seed, XW, k, W, 1e-3);
+      for (int j = 0; j < added; ++j) {
+        sigma_mixed(p, W + (size_t)j * N, HW + (size_t)j * N, s, shift);
+        r.sigma_calls++;
+      }
+      if (added > 0) {
+        std::vector<double> g3, g4;
+        sv.dots_c<float, float>(W, added, W, added, g3);
+        sv.dots_c<float, float>(W, added, HW, added, g4);
+        for (int c2 = 0; c2 < added; ++c2)
+          for (int l = 0; l < added; ++l) {
+            Sww[l + (size_t)mmax * c2] = g3[l + (size_t)added * c2];
+            Hww[l + (size_t)mmax * c2] = 0.5 * (g4[l + (size_t)added * c2] + g4[c2 + (size_t)added * l]) +
+                                         shift * g3[l + (size_t)added * c2];
+          }
+      }
+      m = added;
+      seed = 0;
+    }
     couple(0, m);
     bool stalled = false;
     if (m > 0) {
@@ -1095,7 +1130,8 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
           ma.coef.v[(size_t)i * 192 + 64 + j] = (float)(theta[j] - thc[q]);
         }
         for (int l = 0; l < m; ++l) ma.coef.v[(size_t)i * 192 + 128 + l] = (float)cW[l + (size_t)m * q];
-        ma.theta.v[i] = (float)thc[q];
+        ma.thw.v[i] = (float)(thc[q] - shift);
+        ma.theta.v[i] = thc[q];
       }
       switch (nq) {
 #define SBDGB_K(KK) \
@@ -1118,7 +1154,7 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
         break;
       }
       for (int j = m; j < m + added; ++j) {
-        sigma_mixed(p, W + (size_t)j * N, HW + (size_t)j * N, s);
+        sigma_mixed(p, W + (size_t)j * N, HW + (size_t)j * N, s, shift);
         r.sigma_calls++;
       }
       // projected quantities of the new columns
@@ -1129,7 +1165,8 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       for (int jj = 0; jj < added; ++jj)
         for (int l = 0; l < m + added; ++l) {
           const int c2 = m + jj;
-          const double sw = g3[l + (size_t)(m + added) * jj], hw = g4[l + (size_t)(m + added) * jj];
+          const double sw = g3[l + (size_t)(m + added) * jj];
+          const double hw = g4[l + (size_t)(m + added) * jj] + shift * sw;  // W^T H W from W^T (H - shift) W
           Sww[l + (size_t)mmax * c2] = Sww[c2 + (size_t)mmax * l] = sw;
           if (l < c2 || l == c2) {
             Hww[l + (size_t)mmax * c2] = Hww[c2 + (size_t)mmax * l] = hw;
@@ -1158,7 +1195,14 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
     r.restarts++;
     refine_rr();
     bool full = m + k > mmax;
-    if (full) m = 0;  // subspace full: the anchors carry its information on
+    if (full) {
+      // subspace full: the anchors carry its information on, together with
+      // their step over this refinement (Xf still holds the previous anchors)
+      k_anchor_step_f32<<<sv.blocks, kRed, 0, s>>>(X, Xf, k, N, Tf);
+      count_launch(p.ctx);
+      seed = k;
+      m = 0;
+    }
     if (stalled) {
       bool ok = true;
       for (int q = 0; q < k; ++q) ok = ok && resid[q] < o.eps;

@@ -69,7 +69,20 @@ struct Args {
   const T *Kp;  // [npair][npair]
   int npair;
   const uint32_t *tile_start, *tile_order;  // row tiles of the kernel's row spin
+  double shift;  // sigma = (H - shift) C; 0 except in the mixed solver's inner products
 };
+
+// Strings and phase masks as 32-bit words when norb <= 32 (half the integer
+// work per element: one AND and one POPC instead of two each), 64-bit otherwise.
+template <typename Wd>
+__device__ __forceinline__ Wd word(const uint64_t *a, size_t i) {
+  if constexpr (sizeof(Wd) == 4)
+    return __ldg(reinterpret_cast<const uint32_t *>(a) + 2 * i);  // low half (little endian)
+  else
+    return __ldg(a + i);
+}
+__device__ __forceinline__ uint32_t parity(uint32_t x) { return __popc(x) & 1u; }
+__device__ __forceinline__ uint32_t parity(unsigned long long x) { return __popcll(x) & 1u; }
 
 template <typename T>
 __device__ __forceinline__ void madd(double &acc, T &part, T v, T x) {
@@ -82,12 +95,12 @@ __device__ __forceinline__ void madd(double &acc, T &part, T v, T x) {
 // Same-spin excitations of one row applied to this thread's CPT columns.
 // In: ket-major input rows (ld = ldin); Jo: opposite-spin Coulomb table
 // [npair][ldj] for the single excitations.
-template <int CPT, typename T>
+template <int CPT, typename T, typename Wd>
 __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__restrict__ vs,
                                               const T *__restrict__ vd, const T *__restrict__ Jo, size_t ldj,
                                               const T *__restrict__ In, size_t ldin, uint32_t row,
                                               const uint32_t (&col)[CPT], const bool (&ok)[CPT],
-                                              const uint64_t (&opp)[CPT], double (&acc)[CPT]) {
+                                              const Wd (&opp)[CPT], double (&acc)[CPT]) {
   T part[CPT];
 #pragma unroll
   for (int c = 0; c < CPT; ++c) part[c] = T(0);
@@ -97,13 +110,13 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
   for (; p + 2 <= p1; p += 2) {
     uint32_t ket[2], code[2];
     T v[2];
-    uint64_t m[2];
+    Wd m[2];
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
       ket[u] = __ldg(Tb.ket_s + p + u);
       code[u] = __ldg(Tb.code_s + p + u);
       v[u] = __ldg(vs + p + u);
-      m[u] = __ldg(Tb.mask_s + p + u);
+      m[u] = word<Wd>(Tb.mask_s, p + u);
     }
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
@@ -116,7 +129,7 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
         }
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          const uint32_t ph = (__popcll(opp[c] & m[u]) ^ (code[u] >> 31)) & 1u;
+          const uint32_t ph = parity(opp[c] & m[u]) ^ (code[u] >> 31);
           madd<T>(acc[c], part[c], flip(v[u] + j[u], ph), x[u]);
         }
       }
@@ -124,11 +137,11 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
   if (p < p1) {
     const uint32_t ket = __ldg(Tb.ket_s + p), code = __ldg(Tb.code_s + p);
     const T v = __ldg(vs + p);
-    const uint64_t m = __ldg(Tb.mask_s + p);
+    const Wd m = word<Wd>(Tb.mask_s, p);
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
       if (ok[c]) {
-        const uint32_t ph = (__popcll(opp[c] & m) ^ (code >> 31)) & 1u;
+        const uint32_t ph = parity(opp[c] & m) ^ (code >> 31);
         const T j = __ldg(Jo + (size_t)((code >> 16) & 0x7fffu) * ldj + col[c]);
         madd<T>(acc[c], part[c], flip(v + j, ph), __ldg(In + (size_t)ket * ldin + col[c]));
       }
@@ -139,12 +152,12 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
   for (; p + 4 <= d1; p += 4) {
     uint32_t ket[4];
     T v[4];
-    uint64_t m[4];
+    Wd m[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       ket[u] = __ldg(Tb.ket_d + p + u);
       v[u] = __ldg(vd + p + u);
-      m[u] = __ldg(Tb.mask_d + p + u);
+      m[u] = word<Wd>(Tb.mask_d, p + u);
     }
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
@@ -153,16 +166,16 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
 #pragma unroll
         for (int u = 0; u < 4; ++u) x[u] = __ldg(In + (size_t)ket[u] * ldin + col[c]);
 #pragma unroll
-        for (int u = 0; u < 4; ++u) madd<T>(acc[c], part[c], flip(v[u], __popcll(opp[c] & m[u]) & 1u), x[u]);
+        for (int u = 0; u < 4; ++u) madd<T>(acc[c], part[c], flip(v[u], parity(opp[c] & m[u])), x[u]);
       }
   }
   for (; p < d1; ++p) {
     const uint32_t ket = __ldg(Tb.ket_d + p);
     const T v = __ldg(vd + p);
-    const uint64_t m = __ldg(Tb.mask_d + p);
+    const Wd m = word<Wd>(Tb.mask_d, p);
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
-      if (ok[c]) madd<T>(acc[c], part[c], flip(v, __popcll(opp[c] & m) & 1u), __ldg(In + (size_t)ket * ldin + col[c]));
+      if (ok[c]) madd<T>(acc[c], part[c], flip(v, parity(opp[c] & m)), __ldg(In + (size_t)ket * ldin + col[c]));
   }
   if constexpr (!std::is_same<T, double>::value) {
 #pragma unroll
@@ -170,7 +183,7 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
   }
 }
 
-template <int TA, int CPT, typename T>
+template <int TA, int CPT, typename T, typename Wd>
 __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
   constexpr int TB = kThreads * CPT;
   const uint32_t tile = __ldg(a.tile_order + blockIdx.x);
@@ -179,12 +192,12 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
   const uint32_t ib0 = blockIdx.y * TB;
   uint32_t col[CPT], q0[CPT], q1[CPT];
   bool ok[CPT];
-  uint64_t beta[CPT];
+  Wd beta[CPT];
 #pragma unroll
   for (int c = 0; c < CPT; ++c) {
     col[c] = ib0 + threadIdx.x + kThreads * c;
     ok[c] = col[c] < a.nb;
-    beta[c] = ok[c] ? __ldg(a.bstr + col[c]) : 0ull;
+    beta[c] = ok[c] ? word<Wd>(a.bstr, col[c]) : Wd(0);
     q0[c] = ok[c] ? __ldg(a.B.off_s + col[c]) : 0u;
     q1[c] = ok[c] ? __ldg(a.B.off_s + col[c] + 1) : 0u;
   }
@@ -196,10 +209,10 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       const size_t k = (size_t)ia * a.nb + col[c];
-      acc[c] = ok[c] ? __ldg(a.hii + k) * (double)__ldg(a.C + k) : 0.0;
+      acc[c] = ok[c] ? (__ldg(a.hii + k) - a.shift) * (double)__ldg(a.C + k) : 0.0;
     }
     // alpha singles and doubles (task type 2, mult.h:450-488)
-    same_spin_row<CPT, T>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, a.C, a.nb, ia, col, ok, beta, acc);
+    same_spin_row<CPT, T, Wd>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, a.C, a.nb, ia, col, ok, beta, acc);
     // alpha single x beta single (task type 0, mult.h:527-557)
     T part[CPT];
 #pragma unroll
@@ -207,17 +220,17 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
     const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
     for (uint32_t p = p0; p < p1; ++p) {
       const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
-      const uint64_t ma = __ldg(a.A.mask_s + p);
-      const uint64_t alpha_ket = __ldg(a.astr + ja);
+      const Wd ma = word<Wd>(a.A.mask_s, p);
+      const Wd alpha_ket = word<Wd>(a.astr, ja);
       const T *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
       const T *crow = a.C + (size_t)ja * a.nb;
 #pragma unroll
       for (int c = 0; c < CPT; ++c) {
-        const uint32_t pa = (__popcll(beta[c] & ma) ^ (ca >> 31)) & 1u;
+        const uint32_t pa = parity(beta[c] & ma) ^ (ca >> 31);
         for (uint32_t q = q0[c]; q < q1[c]; ++q) {
           const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-          const uint64_t mb = __ldg(a.B.mask_s + q);
-          const uint32_t ph = (pa ^ __popcll(alpha_ket & mb) ^ (cb >> 31)) & 1u;
+          const Wd mb = word<Wd>(a.B.mask_s, q);
+          const uint32_t ph = (pa ^ parity(alpha_ket & mb) ^ (cb >> 31)) & 1u;
           madd<T>(acc[c], part[c], flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph), __ldg(crow + jb));
         }
       }
@@ -236,7 +249,7 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
 // beta singles and doubles (task type 1, mult.h:489-525) on the transposed
 // vector.  Row results are staged in shared memory; each thread then adds the
 // TA consecutive beta entries of its alpha rows into sigma.
-template <int TA, int CPT, typename T>
+template <int TA, int CPT, typename T, typename Wd>
 __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
   constexpr int TB = kThreads * CPT;
   __shared__ double tile[TA][TB];
@@ -246,19 +259,19 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
   const uint32_t ia0 = blockIdx.y * TB;
   uint32_t col[CPT];
   bool ok[CPT];
-  uint64_t alpha[CPT];
+  Wd alpha[CPT];
 #pragma unroll
   for (int c = 0; c < CPT; ++c) {
     col[c] = ia0 + threadIdx.x + kThreads * c;
     ok[c] = col[c] < a.na;
-    alpha[c] = ok[c] ? __ldg(a.astr + col[c]) : 0ull;
+    alpha[c] = ok[c] ? word<Wd>(a.astr, col[c]) : Wd(0);
   }
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
     double acc[CPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) acc[c] = 0.0;
-    same_spin_row<CPT, T>(a.B, a.val_sb, a.val_db, a.Ja, a.na, a.CT, a.na, ib0 + r, col, ok, alpha, acc);
+    same_spin_row<CPT, T, Wd>(a.B, a.val_sb, a.val_db, a.Ja, a.na, a.CT, a.na, ib0 + r, col, ok, alpha, acc);
 #pragma unroll
     for (int c = 0; c < CPT; ++c) tile[r][threadIdx.x + kThreads * c] = acc[c];
   }
@@ -305,7 +318,10 @@ void launch_a_shape(const Problem &p, Args<T> a, cudaStream_t s) {
   a.tile_start = p.tile_start[0][v];
   a.tile_order = p.tile_order[0][v];
   dim3 g(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
-  k_sigma_alpha<TA, CPT, T><<<g, kThreads, 0, s>>>(a);
+  if (p.norb <= 32)
+    k_sigma_alpha<TA, CPT, T, uint32_t><<<g, kThreads, 0, s>>>(a);
+  else
+    k_sigma_alpha<TA, CPT, T, unsigned long long><<<g, kThreads, 0, s>>>(a);
 }
 template <typename T, int TA, int CPT>
 void launch_b_shape(const Problem &p, Args<T> a, cudaStream_t s) {
@@ -314,7 +330,10 @@ void launch_b_shape(const Problem &p, Args<T> a, cudaStream_t s) {
   a.tile_start = p.tile_start[1][v];
   a.tile_order = p.tile_order[1][v];
   dim3 g(p.n_tiles[1][v], (p.na + TB - 1) / TB);
-  k_sigma_beta<TA, CPT, T><<<g, kThreads, 0, s>>>(a);
+  if (p.norb <= 32)
+    k_sigma_beta<TA, CPT, T, uint32_t><<<g, kThreads, 0, s>>>(a);
+  else
+    k_sigma_beta<TA, CPT, T, unsigned long long><<<g, kThreads, 0, s>>>(a);
 }
 
 template <typename T>
@@ -439,6 +458,7 @@ Args<T> base_args(Problem &p, const T *C, T *S, int accumulate) {
   a.C = C;
   a.S = S;
   a.accumulate = accumulate;
+  a.shift = 0.0;
   a.A = p.A;
   a.B = p.B;
   a.npair = p.npair;
@@ -585,11 +605,12 @@ void prepare_mixed(Problem &p, cudaStream_t s) {
   p.mixed_ready = true;
 }
 
-void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s) {
+void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double shift) {
   prepare_mixed(p, s);
   if (!p.CTf) p.CTf = (float *)dev_alloc(p, sizeof(float) * p.N);
   if (p.N == 0) return;
   Args<float> a = base_args<float>(p, C, S, 0);
+  a.shift = shift;
   a.CT = p.CTf;
   a.val_sa = p.val_sf[0];
   a.val_da = p.val_df[0];

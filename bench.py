@@ -286,6 +286,26 @@ def run_gpu(args):
         except Exception:
             traffic = None
 
+    # serving: a bounded sample of the config-4 request mix through the request
+    # loop (all submitted at once), against the plain FP64 path one solve at a time
+    serving = None
+    if rank == 0 and args.serve_requests > 0:
+        from sbd_gb300 import serve_bench as sb
+        reqs = sb.generate(4, args.serve_requests, min(16, os.cpu_count() or 1))
+        slat, sE = sb.run_serial(reqs, 4)
+        serving = {"workload": f"config4: first {len(reqs)} requests of the seeded mix (norb 24-48, "
+                               "200-4000 strings per spin, 1-3 roots, tol 1e-7), all submitted at once",
+                   "plain_fp64_one_at_a_time": {"solves_per_s": len(reqs) / sum(slat),
+                                                "p50_s": float(np.percentile(slat, 50)),
+                                                "p99_s": float(np.percentile(slat, 99))}}
+        for prec, name in ((0, "fp64"), (1, "mixed")):
+            res, wall_s, st = sb.run_serving(reqs, 4, prec, float("inf"), args.serve_workers, 7)
+            summ = sb.summarize(res, wall_s, st, sE, prec, float("inf"))
+            serving[f"loop_{name}"] = {k: summ[k] for k in ("solves_per_s", "p50_s", "p99_s", "max_abs_dE",
+                                                             "failed", "not_converged", "peak_running")}
+            serving[f"loop_{name}"]["vs_plain_fp64"] = summ["solves_per_s"] / serving["plain_fp64_one_at_a_time"][
+                "solves_per_s"]
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -310,9 +330,11 @@ def run_gpu(args):
             "sigma_tiles": tiles,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "sigma operator (k_transpose + k_sigma_alpha + k_sigma_beta)",
+                         "kernel": ("sigma operator (fused k_sigma_alpha)" if tiles.get("beta_shape") == "fused"
+                                    else "sigma operator (k_transpose + k_sigma_alpha + k_sigma_beta)"),
                          "algorithmic_bytes": bytes_sigma, "peak_kind": f"{peak_kind} hbm_gbs"},
             "mixed_precision": mixed,
+            "serving": serving,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
@@ -337,6 +359,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mixed-steps", type=int, default=2)
+    ap.add_argument("--serve-requests", type=int, default=48, help="config-4 requests for the serving block (0: skip)")
+    ap.add_argument("--serve-workers", type=int, default=16)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -128,11 +128,17 @@ int sbdgb_sigma_mixed(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, void
 /* The sigma tile shapes the autotuner picked on this problem's first product
  * (precision 0 = FP64, 1 = mixed; -1 = not tuned yet) and the time it measured
  * for each of the n_shapes candidates of kernel A (alpha sweep) and B (beta
- * sweep).  Shapes: 0 = 8x128, 1 = 8x256, 2 = 8x512, 3 = 16x256 rows x columns.
+ * sweep).  Shapes: 0 = 8x128, 1 = 8x256, 2 = 8x512, 3 = 16x256 rows x columns;
+ * shape_b = 4 means the beta sweep is fused into kernel A (one kernel, no
+ * transposed copy; chosen when that is faster, typically for short beta lists).
  * The first product of each precision tunes (and synchronises), so make it
  * before any stream capture. */
 int sbdgb_problem_tuning(const sbdgb_problem *p, int precision, int *shape_a, int *shape_b, float *ms_a,
                          float *ms_b, int n_shapes);
+/* Sets the sigma tile shapes of one precision instead of the autotuner's
+ * choice (shape_a 0..3, shape_b 0..4 as above); results do not depend on it
+ * beyond the order of floating-point sums. */
+int sbdgb_problem_set_tuning(sbdgb_problem *p, int precision, int shape_a, int shape_b);
 
 /* sigma that makes no device allocation.  No counterpart in the reference:
  * it is for callers that cannot call cudaMalloc once they run (a host

@@ -398,6 +398,14 @@ int sbdgb_problem_tuning(const sbdgb_problem *pr, int precision, int *shape_a, i
   return SBDGB_OK;
 }
 
+int sbdgb_problem_set_tuning(sbdgb_problem *pr, int precision, int shape_a, int shape_b) {
+  if (!pr || (precision != 0 && precision != 1)) return SBDGB_E_INPUT;
+  if (shape_a < 0 || shape_a > 3 || shape_b < 0 || shape_b > 4) return SBDGB_E_INPUT;
+  pr->p.tune_a[precision] = shape_a;
+  pr->p.tune_b[precision] = shape_b;
+  return SBDGB_OK;
+}
+
 int sbdgb_mult_host(sbdgb_problem *pr, const double *hii, const double *Wk, double *Wb) {
   if (!pr || !Wk || !Wb) return SBDGB_E_INPUT;
   return guarded(pr->p.ctx, [&] {

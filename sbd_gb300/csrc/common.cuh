@@ -142,7 +142,7 @@ struct Problem {
   uint32_t *tile_start[2][2] = {}, *tile_order[2][2] = {};
   uint32_t n_tiles[2][2] = {};
   int tune_a[2] = {-1, -1}, tune_b[2] = {-1, -1};  // autotuned sigma tile shapes (FP64, mixed)
-  float tune_ms[2][2][8] = {};                       // timings the autotuner saw
+  float tune_ms[2][3][8] = {};                       // timings the autotuner saw (A, B, fused)
   size_t bytes = 0;
   std::vector<void *> allocs;
   // host copies of strings

@@ -183,7 +183,11 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
   }
 }
 
-template <int TA, int CPT, typename T, typename Wd>
+// kFused: the beta singles and doubles (task type 1) of each column are
+// added here too, reading row ia of C directly (per-thread pair lists, no
+// transposed copy); for sparse beta lists this replaces the transpose and the
+// beta sweep.
+template <int TA, int CPT, typename T, typename Wd, bool kFused>
 __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
   constexpr int TB = kThreads * CPT;
   const uint32_t tile = __ldg(a.tile_order + blockIdx.x);
@@ -200,6 +204,14 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
     beta[c] = ok[c] ? word<Wd>(a.bstr, col[c]) : Wd(0);
     q0[c] = ok[c] ? __ldg(a.B.off_s + col[c]) : 0u;
     q1[c] = ok[c] ? __ldg(a.B.off_s + col[c] + 1) : 0u;
+  }
+  uint32_t d0[kFused ? CPT : 1], d1[kFused ? CPT : 1];
+  if constexpr (kFused) {
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) {
+      d0[c] = ok[c] ? __ldg(a.B.off_d + col[c]) : 0u;
+      d1[c] = ok[c] ? __ldg(a.B.off_d + col[c] + 1) : 0u;
+    }
   }
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
@@ -232,6 +244,25 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
           const Wd mb = word<Wd>(a.B.mask_s, q);
           const uint32_t ph = (pa ^ parity(alpha_ket & mb) ^ (cb >> 31)) & 1u;
           madd<T>(acc[c], part[c], flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph), __ldg(crow + jb));
+        }
+      }
+    }
+    if constexpr (kFused) {
+      // beta singles and doubles (task type 1, mult.h:489-525) on row ia
+      const Wd arow = word<Wd>(a.astr, ia);
+      const T *crow_a = a.C + (size_t)ia * a.nb;
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) {
+        for (uint32_t q = q0[c]; q < q1[c]; ++q) {
+          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+          const uint32_t ph = parity(arow & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31);
+          const T j = __ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia);
+          madd<T>(acc[c], part[c], flip(__ldg(a.val_sb + q) + j, ph), __ldg(crow_a + jb));
+        }
+        for (uint32_t q = d0[c]; q < d1[c]; ++q) {
+          const uint32_t jb = __ldg(a.B.ket_d + q);
+          madd<T>(acc[c], part[c], flip(__ldg(a.val_db + q), parity(arow & word<Wd>(a.B.mask_d, q))),
+                  __ldg(crow_a + jb));
         }
       }
     }
@@ -308,10 +339,11 @@ __global__ void k_to_float(const double *__restrict__ x, float *__restrict__ y, 
 // ---- tile shapes and the autotuner ---------------------------------------------
 
 constexpr int kNumShapes = 4;
+constexpr int kFusedShape = 4;  // tune_b value meaning "beta sweep fused into kernel A"
 constexpr int kShapeTA[kNumShapes] = {8, 8, 8, 16};
 constexpr int kShapeCPT[kNumShapes] = {1, 2, 4, 2};
 
-template <typename T, int TA, int CPT>
+template <typename T, int TA, int CPT, bool F>
 void launch_a_shape(const Problem &p, Args<T> a, cudaStream_t s) {
   constexpr int TB = kThreads * CPT;
   constexpr int v = TA == 8 ? 0 : 1;
@@ -319,9 +351,9 @@ void launch_a_shape(const Problem &p, Args<T> a, cudaStream_t s) {
   a.tile_order = p.tile_order[0][v];
   dim3 g(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
   if (p.norb <= 32)
-    k_sigma_alpha<TA, CPT, T, uint32_t><<<g, kThreads, 0, s>>>(a);
+    k_sigma_alpha<TA, CPT, T, uint32_t, F><<<g, kThreads, 0, s>>>(a);
   else
-    k_sigma_alpha<TA, CPT, T, unsigned long long><<<g, kThreads, 0, s>>>(a);
+    k_sigma_alpha<TA, CPT, T, unsigned long long, F><<<g, kThreads, 0, s>>>(a);
 }
 template <typename T, int TA, int CPT>
 void launch_b_shape(const Problem &p, Args<T> a, cudaStream_t s) {
@@ -336,14 +368,19 @@ void launch_b_shape(const Problem &p, Args<T> a, cudaStream_t s) {
     k_sigma_beta<TA, CPT, T, unsigned long long><<<g, kThreads, 0, s>>>(a);
 }
 
-template <typename T>
+template <typename T, bool F = false>
 void launch_a(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
   switch (shape) {
-    case 0: launch_a_shape<T, 8, 1>(p, a, s); break;
-    case 1: launch_a_shape<T, 8, 2>(p, a, s); break;
-    case 2: launch_a_shape<T, 8, 4>(p, a, s); break;
-    default: launch_a_shape<T, 16, 2>(p, a, s); break;
+    case 0: launch_a_shape<T, 8, 1, F>(p, a, s); break;
+    case 1: launch_a_shape<T, 8, 2, F>(p, a, s); break;
+    case 2: launch_a_shape<T, 8, 4, F>(p, a, s); break;
+    default: launch_a_shape<T, 16, 2, F>(p, a, s); break;
   }
+}
+// The fused single-kernel product (no transposed copy), in shape `shape`.
+template <typename T>
+void launch_fused(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
+  launch_a<T, true>(p, a, shape, s);
 }
 template <typename T>
 void launch_b(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
@@ -354,6 +391,9 @@ void launch_b(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
     default: launch_b_shape<T, 16, 2>(p, a, s); break;
   }
 }
+
+template <typename T>
+void transpose(Problem &p, const T *in, T *out, uint32_t R, uint32_t Cn, cudaStream_t s);
 
 // Times every tile shape of both kernels once (after one untimed run) on the
 // problem's own vectors, writing into scratch, and keeps the fastest.
@@ -391,6 +431,37 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
     }
     (kern == 0 ? p.tune_a : p.tune_b)[prec] = best_shape;
   }
+  // the fused single kernel against transpose + both sweeps
+  float t_tr = 0.f;
+  SBDGB_CUDA(cudaEventRecord(e0, s));
+  transpose<T>(p, a.C, const_cast<T *>(a.CT), p.na, p.nb, s);
+  SBDGB_CUDA(cudaEventRecord(e1, s));
+  SBDGB_CUDA(cudaEventSynchronize(e1));
+  SBDGB_CUDA(cudaEventElapsedTime(&t_tr, e0, e1));
+  const float two_kernels = t_tr + p.tune_ms[prec][0][p.tune_a[prec]] + p.tune_ms[prec][1][p.tune_b[prec]];
+  float best_f = 1e30f;
+  int best_fs = 0;
+  for (int sh = 0; sh < kNumShapes; ++sh) {
+    for (int rep = 0; rep < 2; ++rep) {
+      SBDGB_CUDA(cudaEventRecord(e0, s));
+      launch_fused<T>(p, a, sh, s);
+      SBDGB_CUDA(cudaEventRecord(e1, s));
+      count_launch(p.ctx);
+    }
+    SBDGB_CUDA(cudaGetLastError());
+    SBDGB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    SBDGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    p.tune_ms[prec][2][sh] = ms;
+    if (ms < best_f) {
+      best_f = ms;
+      best_fs = sh;
+    }
+  }
+  if (best_f < two_kernels) {
+    p.tune_a[prec] = best_fs;
+    p.tune_b[prec] = kFusedShape;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   release_workspace(p, WS_TUNE);
@@ -398,6 +469,8 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
 
 // Shape taken without timing (serving contexts): 128-column tiles when the
 // swept dimension is short, so that small problems still spread over the SMs.
+// The fused single kernel is taken when the beta lists are short (at most 8
+// pairs per string on average), where its per-thread lists diverge little.
 inline int size_shape(uint32_t columns) { return columns <= 1024 ? 0 : 1; }
 
 template <typename T>
@@ -406,7 +479,7 @@ bool needs_tuning(Problem &p) {
   if (p.tune_a[prec] >= 0 && p.tune_b[prec] >= 0) return false;
   if (p.ctx->autotune) return true;
   p.tune_a[prec] = size_shape(p.nb);
-  p.tune_b[prec] = size_shape(p.na);
+  p.tune_b[prec] = (p.B.ns + p.B.nd) <= 8ull * p.nb ? kFusedShape : size_shape(p.na);
   return false;
 }
 
@@ -414,6 +487,12 @@ template <typename T>
 void launch(Problem &p, const Args<T> &a, cudaStream_t s) {
   const int prec = std::is_same<T, double>::value ? 0 : 1;
   if (p.tune_a[prec] < 0 || p.tune_b[prec] < 0) autotune<T>(p, a, s);
+  if (p.tune_b[prec] == kFusedShape) {
+    launch_fused<T>(p, a, p.tune_a[prec], s);
+    count_launch(p.ctx, 1);
+    SBDGB_CUDA(cudaGetLastError());
+    return;
+  }
   launch_a<T>(p, a, p.tune_a[prec], s);
   launch_b<T>(p, a, p.tune_b[prec], s);
   count_launch(p.ctx, 2);
@@ -550,10 +629,14 @@ void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, 
   a.Jb = p.Jb;
   a.Ja = p.Ja;
   a.Kp = p.Kp;
-  transpose<double>(p, C, CT, p.na, p.nb, s);
   const int sa = p.tune_a[0] >= 0 ? p.tune_a[0] : 1, sb = p.tune_b[0] >= 0 ? p.tune_b[0] : 1;
-  launch_a<double>(p, a, sa, s);
-  launch_b<double>(p, a, sb, s);
+  if (sb == kFusedShape) {
+    launch_fused<double>(p, a, sa, s);
+  } else {
+    transpose<double>(p, C, CT, p.na, p.nb, s);
+    launch_a<double>(p, a, sa, s);
+    launch_b<double>(p, a, sb, s);
+  }
   count_launch(p.ctx, 2);
   SBDGB_CUDA(cudaGetLastError());
 }
@@ -577,7 +660,7 @@ void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStre
   }
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   begin_timing(p, s, ev0, ev1);
-  transpose<double>(p, C, p.CT, p.na, p.nb, s);
+  if (p.tune_b[0] != kFusedShape) transpose<double>(p, C, p.CT, p.na, p.nb, s);
   launch<double>(p, a, s);
   end_timing(p, s, ev0, ev1);
 }
@@ -625,7 +708,7 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double sh
   }
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   begin_timing(p, s, ev0, ev1);
-  transpose<float>(p, C, p.CTf, p.na, p.nb, s);
+  if (p.tune_b[1] != kFusedShape) transpose<float>(p, C, p.CTf, p.na, p.nb, s);
   launch<float>(p, a, s);
   end_timing(p, s, ev0, ev1);
 }

@@ -111,3 +111,20 @@ def test_rdms_match_reference(gcase):
     assert np.abs(two - c.rdm2).max() <= 1e-12 * np.abs(c.rdm2).max()
     one_only, none = p.rdm(c.C, two_body=False)
     assert none is None and np.abs(one_only - c.rdm1).max() <= 1e-12 * np.abs(c.rdm1).max()
+
+
+@pytest.mark.parametrize("shapes", [(0, 0), (1, 2), (3, 3), (0, 4), (2, 4), (3, 4)])
+def test_sigma_every_tile_shape(gcase, shapes):
+    """Every tile shape, and the fused single kernel (shape_b 4), gives the reference sigma,
+    in both precisions."""
+    c, p = gcase
+    p.diag_terms()
+    p.set_tuning(0, *shapes)
+    assert max_rel(p.sigma(c.C), c.sigma) <= 1e-12
+    import torch
+    p.set_tuning(1, *shapes)
+    C32 = torch.tensor(c.C, dtype=torch.float32, device="cuda")
+    S32 = torch.empty_like(C32)
+    p.sigma_mixed_device(C32.data_ptr(), S32.data_ptr(), stream=0)
+    torch.cuda.synchronize()
+    assert max_rel(S32.double().cpu().numpy(), c.sigma) <= 1e-5

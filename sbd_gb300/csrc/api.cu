@@ -274,6 +274,10 @@ int sbdgb_problem_create(sbdgb_ctx *ctx, int norb, const uint64_t *astr, size_t 
     SBDGB_REQUIRE(norb >= 1 && norb <= 64, SBDGB_E_UNSUPPORTED, "norb must be in [1, 64]");
     SBDGB_REQUIRE(na >= 1 && nb >= 1, SBDGB_E_INPUT, "empty string list");
     SBDGB_REQUIRE(na < (1ull << 31) && nb < (1ull << 31), SBDGB_E_UNSUPPORTED, "too many strings");
+    SBDGB_REQUIRE((uint64_t)na * nb < (1ull << 32), SBDGB_E_UNSUPPORTED,
+                  "more than 2^32 determinants (one vector alone would exceed 34 GB)");
+    SBDGB_REQUIRE((uint64_t)(norb * (norb + 1) / 2) * std::max(na, nb) < (1ull << 32), SBDGB_E_UNSUPPORTED,
+                  "orbital pairs x strings >= 2^32 (the Coulomb tables would exceed 34 GB)");
     SBDGB_REQUIRE(astr && bstr && h1 && eri_packed, SBDGB_E_INPUT, "null input pointer");
     const uint64_t lim = norb == 64 ? ~0ull : ((1ull << norb) - 1ull);
     auto check = [&](const uint64_t *s, size_t n, const char *name, int &nocc) {

@@ -94,11 +94,13 @@ __device__ __forceinline__ void madd(double &acc, T &part, T v, T x) {
 
 // Same-spin excitations of one row applied to this thread's CPT columns.
 // In: ket-major input rows (ld = ldin); Jo: opposite-spin Coulomb table
-// [npair][ldj] for the single excitations.
+// [npair][ldj] for the single excitations.  Element offsets are 32-bit
+// (problems have fewer than 2^32 determinants): the address of a gather is
+// one 32-bit multiply-add and one widening add.
 template <int CPT, typename T, typename Wd>
 __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__restrict__ vs,
-                                              const T *__restrict__ vd, const T *__restrict__ Jo, size_t ldj,
-                                              const T *__restrict__ In, size_t ldin, uint32_t row,
+                                              const T *__restrict__ vd, const T *__restrict__ Jo, uint32_t ldj,
+                                              const T *__restrict__ In, uint32_t ldin, uint32_t row,
                                               const uint32_t (&col)[CPT], const bool (&ok)[CPT],
                                               const Wd (&opp)[CPT], double (&acc)[CPT]) {
   T part[CPT];
@@ -124,8 +126,8 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
         T x[2], j[2];
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          x[u] = __ldg(In + (size_t)ket[u] * ldin + col[c]);
-          j[u] = __ldg(Jo + (size_t)((code[u] >> 16) & 0x7fffu) * ldj + col[c]);
+          x[u] = __ldg(In + (ket[u] * ldin + col[c]));
+          j[u] = __ldg(Jo + (((code[u] >> 16) & 0x7fffu) * ldj + col[c]));
         }
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
@@ -142,8 +144,8 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
     for (int c = 0; c < CPT; ++c)
       if (ok[c]) {
         const uint32_t ph = parity(opp[c] & m) ^ (code >> 31);
-        const T j = __ldg(Jo + (size_t)((code >> 16) & 0x7fffu) * ldj + col[c]);
-        madd<T>(acc[c], part[c], flip(v + j, ph), __ldg(In + (size_t)ket * ldin + col[c]));
+        const T j = __ldg(Jo + (((code >> 16) & 0x7fffu) * ldj + col[c]));
+        madd<T>(acc[c], part[c], flip(v + j, ph), __ldg(In + (ket * ldin + col[c])));
       }
   }
   // doubles, four at a time
@@ -164,7 +166,7 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
       if (ok[c]) {
         T x[4];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) x[u] = __ldg(In + (size_t)ket[u] * ldin + col[c]);
+        for (int u = 0; u < 4; ++u) x[u] = __ldg(In + (ket[u] * ldin + col[c]));
 #pragma unroll
         for (int u = 0; u < 4; ++u) madd<T>(acc[c], part[c], flip(v[u], parity(opp[c] & m[u])), x[u]);
       }
@@ -175,7 +177,7 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
     const Wd m = word<Wd>(Tb.mask_d, p);
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
-      if (ok[c]) madd<T>(acc[c], part[c], flip(v, parity(opp[c] & m)), __ldg(In + (size_t)ket * ldin + col[c]));
+      if (ok[c]) madd<T>(acc[c], part[c], flip(v, parity(opp[c] & m)), __ldg(In + (ket * ldin + col[c])));
   }
   if constexpr (!std::is_same<T, double>::value) {
 #pragma unroll

@@ -125,6 +125,10 @@ int sbdgb_sigma(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accu
 /* Mixed-precision sigma: FP32 vectors, FP32 products, FP64 accumulation of
  * each element's sum, FP32 result. */
 int sbdgb_sigma_mixed(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, void *stream);
+/* sbdgb_sigma_mixed for nvec vectors stored one after another (nvec*N floats
+ * in and out).  Up to four vectors share each element's phase and address,
+ * which is most of the FP32 kernels' work; results equal nvec single calls. */
+int sbdgb_sigma_mixed_block(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, int nvec, void *stream);
 /* The sigma tile shapes the autotuner picked on this problem's first product
  * (precision 0 = FP64, 1 = mixed; -1 = not tuned yet) and the time it measured
  * for each of the n_shapes candidates of kernel A (alpha sweep) and B (beta
@@ -226,6 +230,18 @@ int sbdgb_davidson(sbdgb_problem *p, const sbdgb_davidson_opts *o, double *E, do
  * lowest Ritz value, X (may be NULL) the Ritz vector; rep->resid[0] is the
  * last change of the Ritz value and rep->restarts the cycles run. */
 int sbdgb_lanczos(sbdgb_problem *p, const sbdgb_davidson_opts *o, double *E, double *X, sbdgb_report *rep);
+
+/* Many small problems of one context solved in one launch: each problem's
+ * whole FP64 Davidson (the algorithm of sbdgb_davidson, init 1) runs inside
+ * one thread block, so a batch of thousands of tiny problems costs one kernel
+ * launch instead of tens of launches and synchronisations per iteration each.
+ * No counterpart in the reference.  Options as for sbdgb_davidson with
+ * nroots 1..8, precision FP64, init 1; the subspace is capped at 32.
+ * E: count*nroots energies; reps (may be NULL): count reports; X (may be
+ * NULL, entries may be NULL): count host buffers of nroots*N for the Ritz
+ * vectors.  Meant for problems of up to a few hundred thousand determinants. */
+int sbdgb_batch_davidson(sbdgb_ctx *ctx, sbdgb_problem **problems, int count, const sbdgb_davidson_opts *o,
+                         double *E, sbdgb_report *reps, double **X);
 
 /* ---- serving: many solves at once, admitted by HBM footprint -------------
  * No single counterpart in the reference, whose app solves one problem per

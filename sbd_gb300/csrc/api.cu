@@ -117,6 +117,7 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
     const size_t mmax = (size_t)std::max(std::min(o.max_nb, 64) - (int)k, 2 * (int)k);
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;  // FP32 tables
     b += 4 * N;                                                                          // FP32 transpose
+    b += 4 * N * std::min<size_t>(4, k);  // transposed copies of the vectors of one multi-vector product
     b += 32 * N * k + 4 * N * (k + mmax) + 4 * N * mmax + 12 * N * k + 4 * (8 * 3 * 64 + 64);
   }
   return b;
@@ -386,6 +387,17 @@ int sbdgb_sigma_mixed(sbdgb_problem *pr, const float *Wk_dev, float *Wb_dev, voi
     SBDGB_REQUIRE(p.tables && p.diag, SBDGB_E_STATE, "build tables and diagonal first");
     cudaStream_t s = stream ? (cudaStream_t)stream : p.ctx->stream;
     sbdgb::sigma_mixed(p, Wk_dev, Wb_dev, s);
+  });
+}
+
+int sbdgb_sigma_mixed_block(sbdgb_problem *pr, const float *Wk_dev, float *Wb_dev, int nvec, void *stream) {
+  if (!pr || !Wk_dev || !Wb_dev || nvec < 1) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    sbdgb::Problem &p = pr->p;
+    SBDGB_REQUIRE(p.tables && p.diag, SBDGB_E_STATE, "build tables and diagonal first");
+    cudaStream_t s = stream ? (cudaStream_t)stream : p.ctx->stream;
+    for (int j = 0; j < nvec; j += 4)
+      sbdgb::sigma_mixed_multi(p, Wk_dev + (size_t)j * p.N, Wb_dev + (size_t)j * p.N, std::min(4, nvec - j), s);
   });
 }
 

@@ -109,7 +109,7 @@ enum WsSlot {
   WS_V, WS_HV, WS_X, WS_HX, WS_T, WS_PARTIAL, WS_RED, WS_COEF,
   WS_DIAG0, WS_DIAG1, WS_DIAG2,
   WS_VF, WS_HVF, WS_CF, WS_SF, WS_RES64, WS_C64, WS_TUNE,
-  WS_U, WS_UF, WS_RED2, WS_NORM_A, WS_NORM_B, WS_OCC, WS_RDM1, WS_RDM2, WS_RDMAB,
+  WS_U, WS_UF, WS_RED2, WS_NORM_A, WS_NORM_B, WS_OCC, WS_RDM1, WS_RDM2, WS_RDMAB, WS_CTMV,
   WS_COUNT
 };
 
@@ -203,10 +203,15 @@ void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, 
 // (H - shift) C in the mixed form: the diagonal term is formed in FP64 before
 // the result is rounded, so a shift near the spectrum keeps FP32 outputs small.
 void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double shift = 0.0);
+// The same for nvec <= 4 vectors at once (inputs and outputs at stride N).
+void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStream_t s, double shift = 0.0);
 void prepare_mixed(Problem &p, cudaStream_t s);
 // davidson.cu
 void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X, sbdgb_report *rep);
 void lanczos(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X, sbdgb_report *rep);
+// batch.cu
+void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &o, double *E, sbdgb_report *reps,
+                    double **X);
 
 }  // namespace sbdgb
 

@@ -1086,9 +1086,10 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       // the FP32 subspace was dropped: restart it with the anchors' last step
       // (locally optimal restart), orthonormalised against the new anchors
       const int added = sv.orthonormalize_block<float>(Tf, seed, XW, k, W, 1e-3);
-      for (int j = 0; j < added; ++j) {
-        sigma_mixed(p, W + (size_t)j * N, HW + (size_t)j * N, s, shift);
-        r.sigma_calls++;
+      for (int j = 0; j < added; j += 4) {
+        const int nv = std::min(4, added - j);
+        sigma_mixed_multi(p, W + (size_t)j * N, HW + (size_t)j * N, nv, s, shift);
+        r.sigma_calls += nv;
       }
       if (added > 0) {
         std::vector<double> g3, g4;
@@ -1153,9 +1154,10 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
         stalled = true;
         break;
       }
-      for (int j = m; j < m + added; ++j) {
-        sigma_mixed(p, W + (size_t)j * N, HW + (size_t)j * N, s, shift);
-        r.sigma_calls++;
+      for (int j = m; j < m + added; j += 4) {
+        const int nv = std::min(4, m + added - j);
+        sigma_mixed_multi(p, W + (size_t)j * N, HW + (size_t)j * N, nv, s, shift);
+        r.sigma_calls += nv;
       }
       // projected quantities of the new columns
       couple(m, m + added);

@@ -39,151 +39,14 @@
 #include <type_traits>
 
 #include "common.cuh"
+#include "sigma_dev.cuh"
 
 namespace sbdgb {
 
 namespace {
 
+using namespace sdev;
 constexpr int kThreads = 128;
-
-__device__ __forceinline__ double flip(double x, uint32_t ph) {
-  return __longlong_as_double(__double_as_longlong(x) ^ ((unsigned long long)ph << 63));
-}
-__device__ __forceinline__ float flip(float x, uint32_t ph) {
-  return __int_as_float(__float_as_int(x) ^ (int)(ph << 31));
-}
-
-template <typename T>
-struct Args {
-  const uint64_t *astr, *bstr;
-  uint32_t na, nb;
-  const double *hii;
-  const T *C;   // N, row-major [ia][ib]
-  const T *CT;  // N, transposed [ib][ia]
-  T *S;
-  int accumulate;
-  SpinTables A, B;
-  const T *val_sa, *val_da, *val_sb, *val_db;  // table values in storage precision
-  const T *Jb;  // [npair][nb]
-  const T *Ja;  // [npair][na]
-  const T *Kp;  // [npair][npair]
-  int npair;
-  const uint32_t *tile_start, *tile_order;  // row tiles of the kernel's row spin
-  double shift;  // sigma = (H - shift) C; 0 except in the mixed solver's inner products
-};
-
-// Strings and phase masks as 32-bit words when norb <= 32 (half the integer
-// work per element: one AND and one POPC instead of two each), 64-bit otherwise.
-template <typename Wd>
-__device__ __forceinline__ Wd word(const uint64_t *a, size_t i) {
-  if constexpr (sizeof(Wd) == 4)
-    return __ldg(reinterpret_cast<const uint32_t *>(a) + 2 * i);  // low half (little endian)
-  else
-    return __ldg(a + i);
-}
-__device__ __forceinline__ uint32_t parity(uint32_t x) { return __popc(x) & 1u; }
-__device__ __forceinline__ uint32_t parity(unsigned long long x) { return __popcll(x) & 1u; }
-
-template <typename T>
-__device__ __forceinline__ void madd(double &acc, T &part, T v, T x) {
-  if constexpr (std::is_same<T, double>::value)
-    acc = fma(v, x, acc);
-  else
-    part = fmaf(v, x, part);
-}
-
-// Same-spin excitations of one row applied to this thread's CPT columns.
-// In: ket-major input rows (ld = ldin); Jo: opposite-spin Coulomb table
-// [npair][ldj] for the single excitations.  Element offsets are 32-bit
-// (problems have fewer than 2^32 determinants): the address of a gather is
-// one 32-bit multiply-add and one widening add.
-template <int CPT, typename T, typename Wd>
-__device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__restrict__ vs,
-                                              const T *__restrict__ vd, const T *__restrict__ Jo, uint32_t ldj,
-                                              const T *__restrict__ In, uint32_t ldin, uint32_t row,
-                                              const uint32_t (&col)[CPT], const bool (&ok)[CPT],
-                                              const Wd (&opp)[CPT], double (&acc)[CPT]) {
-  T part[CPT];
-#pragma unroll
-  for (int c = 0; c < CPT; ++c) part[c] = T(0);
-  // singles, two at a time
-  const uint32_t p0 = __ldg(Tb.off_s + row), p1 = __ldg(Tb.off_s + row + 1);
-  uint32_t p = p0;
-  for (; p + 2 <= p1; p += 2) {
-    uint32_t ket[2], code[2];
-    T v[2];
-    Wd m[2];
-#pragma unroll
-    for (int u = 0; u < 2; ++u) {
-      ket[u] = __ldg(Tb.ket_s + p + u);
-      code[u] = __ldg(Tb.code_s + p + u);
-      v[u] = __ldg(vs + p + u);
-      m[u] = word<Wd>(Tb.mask_s, p + u);
-    }
-#pragma unroll
-    for (int c = 0; c < CPT; ++c)
-      if (ok[c]) {
-        T x[2], j[2];
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          x[u] = __ldg(In + (ket[u] * ldin + col[c]));
-          j[u] = __ldg(Jo + (((code[u] >> 16) & 0x7fffu) * ldj + col[c]));
-        }
-#pragma unroll
-        for (int u = 0; u < 2; ++u) {
-          const uint32_t ph = parity(opp[c] & m[u]) ^ (code[u] >> 31);
-          madd<T>(acc[c], part[c], flip(v[u] + j[u], ph), x[u]);
-        }
-      }
-  }
-  if (p < p1) {
-    const uint32_t ket = __ldg(Tb.ket_s + p), code = __ldg(Tb.code_s + p);
-    const T v = __ldg(vs + p);
-    const Wd m = word<Wd>(Tb.mask_s, p);
-#pragma unroll
-    for (int c = 0; c < CPT; ++c)
-      if (ok[c]) {
-        const uint32_t ph = parity(opp[c] & m) ^ (code >> 31);
-        const T j = __ldg(Jo + (((code >> 16) & 0x7fffu) * ldj + col[c]));
-        madd<T>(acc[c], part[c], flip(v + j, ph), __ldg(In + (ket * ldin + col[c])));
-      }
-  }
-  // doubles, four at a time
-  const uint32_t d0 = __ldg(Tb.off_d + row), d1 = __ldg(Tb.off_d + row + 1);
-  p = d0;
-  for (; p + 4 <= d1; p += 4) {
-    uint32_t ket[4];
-    T v[4];
-    Wd m[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      ket[u] = __ldg(Tb.ket_d + p + u);
-      v[u] = __ldg(vd + p + u);
-      m[u] = word<Wd>(Tb.mask_d, p + u);
-    }
-#pragma unroll
-    for (int c = 0; c < CPT; ++c)
-      if (ok[c]) {
-        T x[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u) x[u] = __ldg(In + (ket[u] * ldin + col[c]));
-#pragma unroll
-        for (int u = 0; u < 4; ++u) madd<T>(acc[c], part[c], flip(v[u], parity(opp[c] & m[u])), x[u]);
-      }
-  }
-  for (; p < d1; ++p) {
-    const uint32_t ket = __ldg(Tb.ket_d + p);
-    const T v = __ldg(vd + p);
-    const Wd m = word<Wd>(Tb.mask_d, p);
-#pragma unroll
-    for (int c = 0; c < CPT; ++c)
-      if (ok[c]) madd<T>(acc[c], part[c], flip(v, parity(opp[c] & m)), __ldg(In + (ket * ldin + col[c])));
-  }
-  if constexpr (!std::is_same<T, double>::value) {
-#pragma unroll
-    for (int c = 0; c < CPT; ++c) acc[c] += (double)part[c];
-  }
-}
 
 // kFused: the beta singles and doubles (task type 1) of each column are
 // added here too, reading row ia of C directly (per-thread pair lists, no
@@ -501,6 +364,293 @@ void launch(Problem &p, const Args<T> &a, cudaStream_t s) {
   SBDGB_CUDA(cudaGetLastError());
 }
 
+// ---- multi-vector FP32 products (mixed form) --------------------------------------
+//
+// The FP32 kernels are bound by integer work per element (phase popcount,
+// sign flip, gather address), not by FP32 arithmetic.  These variants apply
+// one element to NV vectors at once: the phase, the signed value and the
+// offset are formed once, then NV loads and NV FMAs follow.  Same sums in the
+// same order per vector as the single-vector kernels.
+
+constexpr int kMaxNV = 4;
+
+struct ArgsMV {
+  Args<float> a;  // tables, strings and integrals as in the single-vector form
+  const float *Cv[kMaxNV];
+  const float *CTv[kMaxNV];
+  float *Sv[kMaxNV];
+};
+
+template <int CPT, int NV, typename Wd>
+__device__ __forceinline__ void same_spin_row_mv(const SpinTables &Tb, const float *__restrict__ vs,
+                                                 const float *__restrict__ vd, const float *__restrict__ Jo,
+                                                 uint32_t ldj, const float *const (&In)[kMaxNV], uint32_t ldin,
+                                                 uint32_t row, const uint32_t (&col)[CPT], const bool (&ok)[CPT],
+                                                 const Wd (&opp)[CPT], double (&acc)[NV][CPT]) {
+  float part[NV][CPT];
+#pragma unroll
+  for (int n = 0; n < NV; ++n)
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) part[n][c] = 0.f;
+  const uint32_t p0 = __ldg(Tb.off_s + row), p1 = __ldg(Tb.off_s + row + 1);
+  for (uint32_t p = p0; p < p1; ++p) {
+    const uint32_t ket = __ldg(Tb.ket_s + p), code = __ldg(Tb.code_s + p);
+    const float v = __ldg(vs + p);
+    const Wd m = word<Wd>(Tb.mask_s, p);
+#pragma unroll
+    for (int c = 0; c < CPT; ++c)
+      if (ok[c]) {
+        const uint32_t off = ket * ldin + col[c];
+        const float sv = flip(v + __ldg(Jo + (((code >> 16) & 0x7fffu) * ldj + col[c])),
+                              parity(opp[c] & m) ^ (code >> 31));
+#pragma unroll
+        for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, __ldg(In[n] + off), part[n][c]);
+      }
+  }
+  const uint32_t d0 = __ldg(Tb.off_d + row), d1 = __ldg(Tb.off_d + row + 1);
+  uint32_t p = d0;
+  for (; p + 2 <= d1; p += 2) {
+    uint32_t ket[2];
+    float v[2];
+    Wd m[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      ket[u] = __ldg(Tb.ket_d + p + u);
+      v[u] = __ldg(vd + p + u);
+      m[u] = word<Wd>(Tb.mask_d, p + u);
+    }
+#pragma unroll
+    for (int c = 0; c < CPT; ++c)
+      if (ok[c]) {
+        float x[2][NV];
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+          for (int n = 0; n < NV; ++n) x[u][n] = __ldg(In[n] + (ket[u] * ldin + col[c]));
+#pragma unroll
+        for (int u = 0; u < 2; ++u) {
+          const float sv = flip(v[u], parity(opp[c] & m[u]));
+#pragma unroll
+          for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, x[u][n], part[n][c]);
+        }
+      }
+  }
+  if (p < d1) {
+    const uint32_t ket = __ldg(Tb.ket_d + p);
+    const float v = __ldg(vd + p);
+    const Wd m = word<Wd>(Tb.mask_d, p);
+#pragma unroll
+    for (int c = 0; c < CPT; ++c)
+      if (ok[c]) {
+        const float sv = flip(v, parity(opp[c] & m));
+#pragma unroll
+        for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, __ldg(In[n] + (ket * ldin + col[c])), part[n][c]);
+      }
+  }
+#pragma unroll
+  for (int n = 0; n < NV; ++n)
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) acc[n][c] += (double)part[n][c];
+}
+
+template <int TA, int CPT, int NV, typename Wd, bool kFused>
+__global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
+  const Args<float> &a = m.a;
+  constexpr int TB = kThreads * CPT;
+  const uint32_t tile = __ldg(a.tile_order + blockIdx.x);
+  const uint32_t ia0 = __ldg(a.tile_start + tile);
+  const uint32_t rend = __ldg(a.tile_start + tile + 1) - ia0;
+  const uint32_t ib0 = blockIdx.y * TB;
+  uint32_t col[CPT], q0[CPT], q1[CPT], d0[CPT], d1[CPT];
+  bool ok[CPT];
+  Wd beta[CPT];
+#pragma unroll
+  for (int c = 0; c < CPT; ++c) {
+    col[c] = ib0 + threadIdx.x + kThreads * c;
+    ok[c] = col[c] < a.nb;
+    beta[c] = ok[c] ? word<Wd>(a.bstr, col[c]) : Wd(0);
+    q0[c] = ok[c] ? __ldg(a.B.off_s + col[c]) : 0u;
+    q1[c] = ok[c] ? __ldg(a.B.off_s + col[c] + 1) : 0u;
+    d0[c] = (kFused && ok[c]) ? __ldg(a.B.off_d + col[c]) : 0u;
+    d1[c] = (kFused && ok[c]) ? __ldg(a.B.off_d + col[c] + 1) : 0u;
+  }
+#pragma unroll 1
+  for (uint32_t r = 0; r < rend; ++r) {
+    const uint32_t ia = ia0 + r;
+    double acc[NV][CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) {
+      const uint32_t k = ia * a.nb + col[c];
+      const double h = ok[c] ? __ldg(a.hii + k) - a.shift : 0.0;
+#pragma unroll
+      for (int n = 0; n < NV; ++n) acc[n][c] = ok[c] ? h * (double)__ldg(m.Cv[n] + k) : 0.0;
+    }
+    same_spin_row_mv<CPT, NV, Wd>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, m.Cv, a.nb, ia, col, ok, beta, acc);
+    float part[NV][CPT];
+#pragma unroll
+    for (int n = 0; n < NV; ++n)
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) part[n][c] = 0.f;
+    const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
+    for (uint32_t p = p0; p < p1; ++p) {
+      const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
+      const Wd ma = word<Wd>(a.A.mask_s, p);
+      const Wd alpha_ket = word<Wd>(a.astr, ja);
+      const float *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
+      const uint32_t rowoff = ja * a.nb;
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) {
+        const uint32_t pa = parity(beta[c] & ma) ^ (ca >> 31);
+        for (uint32_t q = q0[c]; q < q1[c]; ++q) {
+          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+          const uint32_t ph = (pa ^ parity(alpha_ket & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31)) & 1u;
+          const float kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
+#pragma unroll
+          for (int n = 0; n < NV; ++n) part[n][c] = fmaf(kv, __ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
+        }
+      }
+    }
+    if constexpr (kFused) {
+      const Wd arow = word<Wd>(a.astr, ia);
+      const uint32_t rowoff = ia * a.nb;
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) {
+        for (uint32_t q = q0[c]; q < q1[c]; ++q) {
+          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+          const uint32_t ph = parity(arow & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31);
+          const float sv = flip(__ldg(a.val_sb + q) + __ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia), ph);
+#pragma unroll
+          for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, __ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
+        }
+        for (uint32_t q = d0[c]; q < d1[c]; ++q) {
+          const uint32_t jb = __ldg(a.B.ket_d + q);
+          const float sv = flip(__ldg(a.val_db + q), parity(arow & word<Wd>(a.B.mask_d, q)));
+#pragma unroll
+          for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, __ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
+        }
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < CPT; ++c)
+      if (ok[c]) {
+        const uint32_t k = ia * a.nb + col[c];
+#pragma unroll
+        for (int n = 0; n < NV; ++n) m.Sv[n][k] = (float)(acc[n][c] + (double)part[n][c]);
+      }
+  }
+}
+
+template <int TA, int CPT, int NV, typename Wd>
+__global__ void __launch_bounds__(kThreads) k_sigma_beta_mv(ArgsMV m) {
+  const Args<float> &a = m.a;
+  constexpr int TB = kThreads * CPT;
+  extern __shared__ double tile_mv[];  // [NV][TA][TB]
+  const uint32_t t = __ldg(a.tile_order + blockIdx.x);
+  const uint32_t ib0 = __ldg(a.tile_start + t);
+  const uint32_t rend = __ldg(a.tile_start + t + 1) - ib0;
+  const uint32_t ia0 = blockIdx.y * TB;
+  uint32_t col[CPT];
+  bool ok[CPT];
+  Wd alpha[CPT];
+#pragma unroll
+  for (int c = 0; c < CPT; ++c) {
+    col[c] = ia0 + threadIdx.x + kThreads * c;
+    ok[c] = col[c] < a.na;
+    alpha[c] = ok[c] ? word<Wd>(a.astr, col[c]) : Wd(0);
+  }
+#pragma unroll 1
+  for (uint32_t r = 0; r < rend; ++r) {
+    double acc[NV][CPT];
+#pragma unroll
+    for (int n = 0; n < NV; ++n)
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) acc[n][c] = 0.0;
+    same_spin_row_mv<CPT, NV, Wd>(a.B, a.val_sb, a.val_db, a.Ja, a.na, m.CTv, a.na, ib0 + r, col, ok, alpha, acc);
+#pragma unroll
+    for (int n = 0; n < NV; ++n)
+#pragma unroll
+      for (int c = 0; c < CPT; ++c) tile_mv[((size_t)n * TA + r) * TB + threadIdx.x + kThreads * c] = acc[n][c];
+  }
+#pragma unroll
+  for (int c = 0; c < CPT; ++c)
+    if (ok[c])
+#pragma unroll
+      for (int n = 0; n < NV; ++n) {
+        float *srow = m.Sv[n] + (size_t)col[c] * a.nb + ib0;
+        for (uint32_t r = 0; r < rend; ++r)
+          srow[r] = (float)((double)srow[r] + tile_mv[((size_t)n * TA + r) * TB + threadIdx.x + kThreads * c]);
+      }
+}
+
+template <int TA, int CPT, int NV, bool F>
+void launch_a_mv_shape(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
+  ArgsMV m = mv;
+  constexpr int TB = kThreads * CPT;
+  constexpr int v = TA == 8 ? 0 : 1;
+  m.a.tile_start = p.tile_start[0][v];
+  m.a.tile_order = p.tile_order[0][v];
+  dim3 g(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
+  if (p.norb <= 32)
+    k_sigma_alpha_mv<TA, CPT, NV, uint32_t, F><<<g, kThreads, 0, s>>>(m);
+  else
+    k_sigma_alpha_mv<TA, CPT, NV, unsigned long long, F><<<g, kThreads, 0, s>>>(m);
+}
+template <int TA, int CPT, int NV>
+void launch_b_mv_shape(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
+  ArgsMV m = mv;
+  constexpr int TB = kThreads * CPT;
+  constexpr int v = TA == 8 ? 0 : 1;
+  m.a.tile_start = p.tile_start[1][v];
+  m.a.tile_order = p.tile_order[1][v];
+  dim3 g(p.n_tiles[1][v], (p.na + TB - 1) / TB);
+  const size_t smem = sizeof(double) * NV * TA * TB;
+  if (p.norb <= 32) {
+    auto k = k_sigma_beta_mv<TA, CPT, NV, uint32_t>;
+    SBDGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<g, kThreads, smem, s>>>(m);
+  } else {
+    auto k = k_sigma_beta_mv<TA, CPT, NV, unsigned long long>;
+    SBDGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k<<<g, kThreads, smem, s>>>(m);
+  }
+}
+template <int NV, bool F>
+void launch_a_mv(const Problem &p, const ArgsMV &m, int shape, cudaStream_t s) {
+  switch (shape) {
+    case 0: launch_a_mv_shape<8, 1, NV, F>(p, m, s); break;
+    case 1: launch_a_mv_shape<8, 2, NV, F>(p, m, s); break;
+    case 2: launch_a_mv_shape<8, 4, NV, F>(p, m, s); break;
+    default: launch_a_mv_shape<16, 2, NV, F>(p, m, s); break;
+  }
+}
+template <int NV>
+void launch_b_mv(const Problem &p, const ArgsMV &m, int shape, cudaStream_t s) {
+  switch (shape) {
+    case 0: launch_b_mv_shape<8, 1, NV>(p, m, s); break;
+    case 1: launch_b_mv_shape<8, 2, NV>(p, m, s); break;
+    case 2: launch_b_mv_shape<8, 4, NV>(p, m, s); break;
+    default: launch_b_mv_shape<16, 2, NV>(p, m, s); break;
+  }
+}
+// Kernel B stages NV x TA x TB doubles; shapes whose staging would exceed
+// 48 KB (and cut the CTAs per SM) fall back to narrower tiles.
+template <int NV>
+int shape_b_mv(int tuned) {
+  auto fits = [](int sh) { return (size_t)NV * kShapeTA[sh] * kThreads * kShapeCPT[sh] * 8 <= 49152; };
+  if (fits(tuned)) return tuned;
+  return fits(1) ? 1 : 0;
+}
+
+template <int NV>
+void launch_mv(const Problem &p, const ArgsMV &m, cudaStream_t s) {
+  if (p.tune_b[1] == kFusedShape) {
+    launch_a_mv<NV, true>(p, m, p.tune_a[1], s);
+  } else {
+    launch_a_mv<NV, false>(p, m, p.tune_a[1], s);
+    launch_b_mv<NV>(p, m, shape_b_mv<NV>(p.tune_b[1]), s);
+  }
+}
+
 template <typename T>
 void transpose(Problem &p, const T *in, T *out, uint32_t R, uint32_t Cn, cudaStream_t s) {
   dim3 grid((Cn + 31) / 32, (R + 31) / 32), block(32, 8);
@@ -713,6 +863,48 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double sh
   if (p.tune_b[1] != kFusedShape) transpose<float>(p, C, p.CTf, p.na, p.nb, s);
   launch<float>(p, a, s);
   end_timing(p, s, ev0, ev1);
+}
+
+// (H - shift) C_j for nvec FP32 vectors at once (nvec <= 4; vectors and
+// results at stride N), through the multi-vector kernels.
+void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStream_t s, double shift) {
+  if (nvec <= 0) return;
+  if (nvec == 1) {
+    sigma_mixed(p, C, S, s, shift);
+    return;
+  }
+  SBDGB_REQUIRE(nvec <= kMaxNV, SBDGB_E_UNSUPPORTED, "at most 4 vectors per multi-vector sigma");
+  prepare_mixed(p, s);
+  if (p.N == 0) return;
+  if (needs_tuning<float>(p)) sigma_mixed(p, C, S, s, shift);  // tunes the FP32 shapes on the first vector
+  ArgsMV m{};
+  m.a = base_args<float>(p, C, S, 0);
+  m.a.shift = shift;
+  m.a.val_sa = p.val_sf[0];
+  m.a.val_da = p.val_df[0];
+  m.a.val_sb = p.val_sf[1];
+  m.a.val_db = p.val_df[1];
+  m.a.Jb = p.Jbf;
+  m.a.Ja = p.Jaf;
+  m.a.Kp = p.Kpf;
+  const bool fused = p.tune_b[1] == kFusedShape;
+  float *CT = fused ? nullptr : (float *)workspace(p, WS_CTMV, sizeof(float) * p.N * (size_t)nvec);
+  for (int n = 0; n < nvec; ++n) {
+    m.Cv[n] = C + (size_t)n * p.N;
+    m.Sv[n] = S + (size_t)n * p.N;
+    m.CTv[n] = fused ? nullptr : CT + (size_t)n * p.N;
+    if (!fused) transpose<float>(p, m.Cv[n], CT + (size_t)n * p.N, p.na, p.nb, s);
+  }
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  begin_timing(p, s, ev0, ev1);
+  switch (nvec) {
+    case 2: launch_mv<2>(p, m, s); break;
+    case 3: launch_mv<3>(p, m, s); break;
+    default: launch_mv<4>(p, m, s); break;
+  }
+  end_timing(p, s, ev0, ev1);
+  count_launch(p.ctx, fused ? 1 : 2);
+  SBDGB_CUDA(cudaGetLastError());
 }
 
 }  // namespace sbdgb

@@ -24,8 +24,8 @@ SYMBOLS = [
     "sbdgb_abi_version", "sbdgb_ctx_create", "sbdgb_ctx_destroy", "sbdgb_last_error", "sbdgb_ctx_bytes_in_use",
     "sbdgb_ctx_launch_count", "sbdgb_ctx_set_stream", "sbdgb_ctx_enable_timing", "sbdgb_ctx_sigma_timing", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
     "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
-    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_noalloc", "sbdgb_occupation_density", "sbdgb_string_weights", "sbdgb_string_cut_counts", "sbdgb_rdm", "sbdgb_problem_tuning", "sbdgb_problem_set_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
-    "sbdgb_davidson", "sbdgb_lanczos", "sbdgb_server_create", "sbdgb_server_submit", "sbdgb_server_poll", "sbdgb_server_wait",
+    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_mixed_block", "sbdgb_sigma_noalloc", "sbdgb_occupation_density", "sbdgb_string_weights", "sbdgb_string_cut_counts", "sbdgb_rdm", "sbdgb_problem_tuning", "sbdgb_problem_set_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
+    "sbdgb_davidson", "sbdgb_lanczos", "sbdgb_batch_davidson", "sbdgb_server_create", "sbdgb_server_submit", "sbdgb_server_poll", "sbdgb_server_wait",
     "sbdgb_server_stats", "sbdgb_server_last_error", "sbdgb_server_destroy",
 ]
 
@@ -113,6 +113,7 @@ def load(path: str = LIB_PATH):
     L.sbdgb_diag_terms.argtypes = [vp, vp]
     L.sbdgb_sigma.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_sigma_mixed.argtypes = [vp, vp, vp, vp]
+    L.sbdgb_sigma_mixed_block.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_sigma_noalloc.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_occupation_density.argtypes = [vp, vp, _f64p, vp]
     L.sbdgb_string_weights.argtypes = [vp, vp, _f64p, _f64p, vp]
@@ -126,6 +127,7 @@ def load(path: str = LIB_PATH):
     L.sbdgb_davidson_default_opts.restype = None
     L.sbdgb_davidson.argtypes = [vp, C.POINTER(DavidsonOpts), _f64p, vp, C.POINTER(Report)]
     L.sbdgb_lanczos.argtypes = [vp, C.POINTER(DavidsonOpts), _f64p, vp, C.POINTER(Report)]
+    L.sbdgb_batch_davidson.argtypes = [vp, C.POINTER(vp), C.c_int, C.POINTER(DavidsonOpts), _f64p, vp, vp]
     L.sbdgb_server_create.argtypes = [C.c_int, C.c_int, C.c_size_t, C.POINTER(vp)]
     L.sbdgb_server_submit.argtypes = [vp, C.POINTER(Request), C.POINTER(C.c_uint64)]
     L.sbdgb_server_poll.argtypes = [vp, C.c_uint64, C.POINTER(C.c_int)]
@@ -190,6 +192,24 @@ class Engine:
 
     def check_comm_sizes(self, h: int, b: int, t: int):
         self.check(self.lib.sbdgb_check_comm_sizes(self.h, h, b, t))
+
+
+def batch_davidson(engine: Engine, problems: list, nroots: int = 1, max_nb: int = 20, eps: float = 1e-8,
+                   max_it: int = 100, want_vectors: bool = False) -> list:
+    """Solves every TPBProblem of the list (all on `engine`) in one launch, one thread
+    block per problem; returns one DavidsonResult per problem."""
+    n = len(problems)
+    o = DavidsonOpts()
+    load().sbdgb_davidson_default_opts(C.byref(o))
+    o.nroots, o.max_nb, o.eps, o.max_it, o.init = nroots, max_nb, eps, max_it, 1
+    hs = (C.c_void_p * max(n, 1))(*[p.h.value for p in problems])
+    E = np.zeros(max(n * nroots, 1))
+    reps = (Report * max(n, 1))()
+    xs = [np.zeros((nroots, p.N)) for p in problems] if want_vectors else None
+    xp = (C.c_void_p * max(n, 1))(*[x.ctypes.data for x in xs]) if want_vectors else None
+    engine.check(engine.lib.sbdgb_batch_davidson(engine.h, hs, n, C.byref(o), E, reps, xp))
+    return [DavidsonResult(E[i * nroots:(i + 1) * nroots].copy(), xs[i] if xs else None, reps[i].as_dict(nroots))
+            for i in range(n)]
 
 
 def footprint(norb: int, na: int, nb: int, max_nb: int, nroots: int, precision: int = FP64) -> int:
@@ -312,6 +332,9 @@ class TPBProblem:
 
     def sigma_mixed_device(self, c_ptr: int, s_ptr: int, stream: int | None = None):
         self.engine.check(self.lib.sbdgb_sigma_mixed(self.h, c_ptr, s_ptr, self._stream_arg(stream)))
+
+    def sigma_mixed_block_device(self, c_ptr: int, s_ptr: int, nvec: int, stream: int | None = None):
+        self.engine.check(self.lib.sbdgb_sigma_mixed_block(self.h, c_ptr, s_ptr, nvec, self._stream_arg(stream)))
 
     def lanczos(self, max_it: int = 20, num_block: int = 40, eps: float = 1e-12, init: int = 0,
                 want_vector: bool = True, W0: np.ndarray | None = None, max_time: float = 0.0,

@@ -5,8 +5,9 @@
 Prints one JSON line: problem sizes and nonzero counts, table/diagonal build
 times, the FP64 and mixed sigma times (CUDA events on the launch stream, after
 two untimed products) with their model bandwidth (24N + 8 nnz bytes FP64,
-16N + 4 nnz mixed), the autotuner's tile choice, and optionally one Davidson
-solve in each precision.
+16N + 4 nnz mixed), the mixed product of 2-4 vectors at once (time per
+vector), the autotuner's tile choice, and optionally one Davidson solve in
+each precision.
 """
 from __future__ import annotations
 
@@ -77,6 +78,12 @@ def main(argv=None) -> int:
         out["sigma_mixed_GBs_model"] = (16 * N + 4 * nnz) / (msm * 1e-3) / 1e9
         out["sigma_mixed_relerr"] = float((S32.double() - S).abs().max() / S.abs().max())
         out["tuning_mixed"] = p.tuning(MIXED)
+        # several FP32 vectors per product: time per vector
+        for nv in (2, 3, 4):
+            X = torch.rand(nv, N, dtype=torch.float32, device="cuda") * 2 - 1
+            Y = torch.empty_like(X)
+            ms_b = timed(lambda: p.sigma_mixed_block_device(X.data_ptr(), Y.data_ptr(), nv, stream=st.cuda_stream))
+            out[f"sigma_mixed_block{nv}_ms_per_vector"] = ms_b / nv
     if a.davidson:
         for prec, name in ((0, "fp64"), (MIXED, "mixed")):
             r = p.davidson(nroots=a.nroots, max_nb=24, eps=1e-8, init=1, precision=prec, want_vectors=False)

@@ -109,6 +109,37 @@ def run_serving(reqs, cfg: int, precision: int, rate: float, workers: int, seed:
     return results, wall, st
 
 
+def run_batch(reqs, cfg: int, chunk: int):
+    """The batched solver: upload and tables per problem, then one launch per
+    chunk of problems (one thread block each, the whole Davidson on the device).
+    Returns (energies, wall seconds of the whole batch, launch seconds, reports)."""
+    import torch
+
+    from .engine import Engine, TPBProblem, batch_davidson
+    o = solver_opts(cfg)
+    eng = Engine(0)
+    t0 = time.perf_counter()
+    E, reps, t_launch = [], [], 0.0
+    for c0 in range(0, len(reqs), chunk):
+        part = reqs[c0:c0 + chunk]
+        tps = [TPBProblem(eng, norb, a, b, h1, eri, ecore) for (norb, a, b, h1, eri, ecore, k) in part]
+        for t in tps:
+            t.build_tables()
+            t.diag_terms()
+        k = part[0][6]
+        tl = time.perf_counter()
+        res = batch_davidson(eng, tps, nroots=k, max_nb=o["max_nb"], eps=o["eps"])
+        t_launch += time.perf_counter() - tl
+        E += [r.energies.copy() for r in res]
+        reps += [r.report for r in res]
+        for t in tps:
+            t.close()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    eng.close()
+    return E, wall, t_launch, reps
+
+
 def summarize(results, wall, st, ref_E, precision, rate):
     lat = [r["total_seconds"] for r in results]
     failed = [r for r in results if r["status"] != 0]
@@ -138,6 +169,8 @@ def main(argv=None) -> int:
     ap.add_argument("--jobs", type=int, default=min(16, os.cpu_count() or 1))
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--records", default=None, help="write per-request results (JSON lines) to this file")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="also time the batched solver with this many problems per launch (0: skip)")
     a = ap.parse_args(argv)
     n = a.requests or (512 if a.config == 4 else 4096)
     rates = [float(x) for x in (a.rates or ("20,200,inf" if a.config == 4 else "inf")).split(",")]
@@ -181,6 +214,14 @@ def main(argv=None) -> int:
             for i in range(ns):
                 f.write(json.dumps({"precision": "serial_fp64", "index": i, "seconds": lat[i]}) + "\n")
     out["serving"] = runs
+    if a.batch > 0:
+        Eb, wall_b, t_launch, reps = run_batch(reqs, a.config, a.batch)
+        dE = max(float(np.max(np.abs(e - r))) for e, r in zip(Eb, ref_E) if r is not None)
+        out["batched"] = {"requests": n, "problems_per_launch": a.batch, "wall_s": wall_b,
+                          "solves_per_s": n / wall_b, "solver_launch_s": t_launch,
+                          "solves_per_s_solver_only": n / t_launch, "max_abs_dE": dE,
+                          "not_converged": sum(1 for r in reps if not r["converged"]),
+                          "vs_plain_fp64": (n / wall_b) / out["serial_fp64"]["solves_per_s"]}
     best = {p: max((r["solves_per_s"] for r in runs if r["precision"] == p and r["rate"] == "inf"), default=None)
             for p in ("fp64", "mixed")}
     out["capacity_solves_per_s"] = best

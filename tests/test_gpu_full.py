@@ -104,3 +104,38 @@ def test_rdms_against_oracle_norb16(engine):
     assert np.abs(one - ro).max() <= 1e-12 * np.abs(ro).max()
     assert np.abs(two - rt).max() <= 1e-12 * np.abs(rt).max()
     p.close()
+
+
+@pytest.mark.parametrize("na,nb", [(1, 1), (1, 7), (9, 1), (2, 2)])
+def test_degenerate_lists_against_dense(engine, na, nb):
+    """Lists of one or two strings (no same-spin excitations on one side, N as small
+    as 1): sigma equals the assembled H, and every solver finds its lowest eigenvalue."""
+    from sbd_gb300.engine import MIXED
+    prob = make_problem(8, 3, 3, na, nb, seed=40 + na + nb)
+    p = TPBProblem.from_problem(engine, prob)
+    p.build_tables()
+    p.diag_terms()
+    o = Oracle.from_problem(prob)
+    H = o.hamiltonian().toarray()
+    C = np.random.default_rng(1).uniform(-1, 1, prob.ndet)
+    assert max_rel(p.mult(C), H @ C) <= 1e-12
+    w = np.linalg.eigvalsh(H)
+    k = min(2, prob.ndet)
+    r = p.davidson(nroots=k, eps=1e-10, max_nb=8, init=1)
+    assert np.allclose(r.energies, w[:k], atol=1e-8)
+    rm = p.davidson(nroots=1, eps=1e-9, max_nb=8, init=1, precision=MIXED)
+    assert abs(rm.energies[0] - w[0]) < 1e-6
+    rl = p.lanczos(max_it=20, num_block=min(10, max(2, prob.ndet)), eps=1e-12, init=1)
+    assert abs(rl.energies[0] - w[0]) < 1e-8
+    p.close()
+
+
+def test_more_roots_than_determinants_is_an_error(engine):
+    prob = make_problem(8, 3, 3, 1, 2, seed=3)
+    p = TPBProblem.from_problem(engine, prob)
+    p.build_tables()
+    p.diag_terms()
+    with pytest.raises(SbdgbError) as e:
+        p.davidson(nroots=3)
+    assert e.value.status == 1
+    p.close()

@@ -128,3 +128,23 @@ def test_sigma_every_tile_shape(gcase, shapes):
     p.sigma_mixed_device(C32.data_ptr(), S32.data_ptr(), stream=0)
     torch.cuda.synchronize()
     assert max_rel(S32.double().cpu().numpy(), c.sigma) <= 1e-5
+
+
+@pytest.mark.parametrize("shapes", [(0, 0), (1, 2), (3, 3), (0, 4), (3, 4)])
+@pytest.mark.parametrize("nvec", [2, 3, 4, 5])
+def test_mixed_block_sigma_equals_single(gcase, shapes, nvec):
+    """The multi-vector FP32 product gives each vector's single-vector product bit for bit."""
+    import torch
+    c, p = gcase
+    p.diag_terms()
+    p.set_tuning(1, *shapes)
+    N = c.C.size
+    rng = np.random.default_rng(nvec)
+    X = torch.tensor(rng.uniform(-1, 1, (nvec, N)), dtype=torch.float32, device="cuda")
+    Y = torch.empty_like(X)
+    p.sigma_mixed_block_device(X.data_ptr(), Y.data_ptr(), nvec, stream=0)
+    for j in range(nvec):
+        y = torch.empty(N, dtype=torch.float32, device="cuda")
+        p.sigma_mixed_device(X[j].data_ptr(), y.data_ptr(), stream=0)
+        torch.cuda.synchronize()
+        assert torch.equal(Y[j], y), (j, shapes)

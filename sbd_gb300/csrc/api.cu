@@ -112,7 +112,7 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
   b += 8 * (size_t)(1024 * 32 * 16 + 64) + 8 * 4096 + 8 * 8192;
   if (!mixed) {
     const size_t max_nb = std::min<size_t>((size_t)std::max(o.max_nb, 2 * (int)k), std::max<size_t>(N, 1));
-    b += 16 * N * max_nb + 48 * N * k;  // basis and sigma; 2k restart vectors and their sigma; T; U
+    b += 16 * N * max_nb + 64 * N * k;  // basis and sigma; 3k restart vectors and their sigma; T; U
   } else {
     const size_t mmax = (size_t)std::max(std::min(o.max_nb, 64) - (int)k, 2 * (int)k);
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;  // FP32 tables

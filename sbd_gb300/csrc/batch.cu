@@ -1,23 +1,31 @@
-// Many small Davidson solves in one launch: one CTA runs the whole FP64 solve
-// of one problem (sigma products, projections, Rayleigh-Ritz, corrections and
-// restarts) with no host round trip, so thousands of tiny problems cost one
-// kernel launch instead of tens of launches and synchronisations per
-// iteration each.
+// Many small Davidson solves advanced in lock step: every step of the solver
+// is one kernel launch over ALL problems of the batch, and one whole Davidson
+// iteration (twelve launches) is captured once in a CUDA graph and replayed,
+// so thousands of small problems cost a few graph launches per iteration
+// instead of tens of launches and host synchronisations per problem.
 //
 // The algorithm is the device solver's (davidson.cu, the reference's
 // chemistry/tpb/davidson.h:707-970 generalised to nroots): lowest-diagonal
-// start vectors with the deterministic perturbation, Olsen-corrected diagonal
+// start vectors with a deterministic perturbation, Olsen-corrected diagonal
 // preconditioner with the reference's 1e-12 guard, classical Gram-Schmidt
-// with a second pass, thick restart on the Ritz vectors and the previous
-// step's Ritz vectors, convergence on every residual norm below eps.
+// (two passes) with coefficient-space dropping, thick restart on the lowest
+// 2k Ritz vectors and the previous step's Ritz vectors, convergence on every
+// residual norm below eps.  Each problem stops on its own; its blocks then
+// return at once.
 //
-// Inside a CTA:
-//   - sigma: one element per thread at a time, the fused form (diagonal,
-//     alpha pairs of the row with the sigma kernels' same-spin sweep, alpha x
-//     beta singles, beta pairs of the column read from the same row);
-//   - dot products: up to 8 x 4 per pass in registers, one block reduction;
-//   - the projected eigenproblem (n <= 32): cyclic Jacobi by one warp in
-//     shared memory; coefficient-space Gram-Schmidt by one thread.
+// Work decomposition:
+//   - element work runs on chunks of kCH consecutive elements of one problem;
+//     the chunks of every problem form one grid.  Kernels that leave partial
+//     sums (dots, residuals) take one 256-thread block per chunk; the others
+//     (sigma, projections, restart and correction updates) take kSubPer
+//     blocks per chunk, so that the last few problems still fill the GPU;
+//   - dot products leave one partial per chunk (no atomics) that a
+//     per-problem warp sums in chunk order, so results are deterministic;
+//   - the projected eigenproblem (n <= 32) is cyclic Jacobi by one warp per
+//     problem, which also does the small coefficient-space work;
+//   - sigma is the fused per-element form (diagonal, alpha pairs of the row,
+//     alpha x beta singles, beta pairs of the column) for up to 8 vectors at
+//     once, sharing the index, value and phase work between the vectors.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -31,72 +39,96 @@ namespace {
 
 using namespace sdev;
 
-constexpr int kBT = 256;      // threads per problem
-constexpr int kBMaxNb = 32;   // subspace cap of the batched solver
-constexpr int kBMaxK = 8;     // roots
+constexpr int kNB = 32;    // subspace cap of the batched solver
+constexpr int kK = 8;      // roots
+constexpr int kR = 3 * kK; // restart basis: 2k Ritz vectors and k previous directions
+constexpr int kCH = 4096;  // elements per chunk (the unit of the partial sums)
+constexpr int kSub = 512;  // elements per block of the kernels without partial sums
+constexpr int kSubPer = kCH / kSub;
+constexpr int kT = 256;    // threads per element block
+constexpr int kStepLaunches = 12;
 
-struct SmallProb {
-  Args<double> a;  // strings, tables, integrals, diagonal (C, CT, S unused)
-  uint32_t N;
-  int norb;
-  double *V, *HV, *X, *HX, *T, *U;  // N x kBMaxNb, N x kBMaxNb, N x 2k, N x 2k, N x k, N x k
-  double *Xout;                      // N x k Ritz vectors, or null
-  double *out;                       // k energies, k residuals, then [iterations, sigma calls, converged, restarts]
+struct Chunk {
+  uint32_t prob, e0, e1;
 };
 
-struct SmallOpts {
-  int k, max_nb, max_steps;
+struct BProb {
+  Args<double> a;  // strings, tables, integrals, diagonal (C, CT, S unused)
+  uint32_t N;
+  int norb, max_nb, max_steps;
+  double *V, *HV, *T, *U;  // nb, nb, k, k columns at stride N
+  uint32_t c0, c1;         // chunk range of the problem
+};
+
+// Control state of one problem (device).
+struct BState {
+  int active, converged, iter, sigma_calls, restarts;
+  int nv, kk, kc, nvprev, kprev, restart, nv_old, m, nt, from, to;
+  int roots[kK];
+  double th[kK], res[kK], eo[kK], n0[kK];
+  double A[kNB * kNB];     // projected matrix, ld kNB (its symmetric part is used)
+  double c[kNB * 2 * kK];  // coefficients of the lowest kc = min(2k, nv) Ritz vectors (ld nv)
+  double cprev[kNB * kK];  // previous step's Ritz coefficients (nvprev x kprev)
+  double Q[kNB * kR];      // restart basis in coefficient space (nv_old x m, ld nv_old)
+  double G[kNB * kK];      // V^T T (nv x nt, ld nv)
+  double M[kK * kK];       // orthonormal combinations of the corrections (nt x kept, ld nt)
+};
+
+struct BCommon {
+  const BProb *P;
+  BState *S;
+  const Chunk *ch;
+  double *part;  // per-chunk partial sums, pstride doubles each
+  int pstride;
+  int k;
   double eps;
 };
 
-struct Smem {
-  double A[kBMaxNb * kBMaxNb];   // projected matrix (column-major, ld kBMaxNb)
-  double W[kBMaxNb * kBMaxNb];   // scratch matrix (eigenvectors, Q, Gram)
-  double E[kBMaxNb];             // eigenvalues
-  double c[kBMaxNb * kBMaxK];    // Ritz coefficients (nv x kk)
-  double cprev[kBMaxNb * kBMaxK];
-  double G[kBMaxNb * kBMaxK];    // dots
-  double red[kBT / 32][32];
-  double th[kBMaxK], res[kBMaxK], eo[kBMaxK];
-  double M[kBMaxK * kBMaxK];
-  double dv[kBT / 32];
-  unsigned long long di[kBT / 32];
-  unsigned long long pos[kBMaxK];
-  int ival[8];
-};
+// ---- block and warp primitives ----------------------------------------------------
 
-// ---- block primitives ------------------------------------------------------------
-
-// Sum of one value over the block; every thread gets it.
-__device__ double block_sum(double v, Smem &sm) {
+__device__ __forceinline__ double warp_sum(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) sm.dv[threadIdx.x >> 5] = v;
-  __syncthreads();
-  double t = 0.0;
-  for (int w = 0; w < kBT / 32; ++w) t += sm.dv[w];
-  return t;
+  return v;
 }
 
-// G[i + ldg*j] = V_i . W_j for i < nv, j < nw (columns at stride N).
-__device__ void block_dots(const double *V, int nv, const double *W, int nw, uint32_t N, double *G, int ldg,
-                           Smem &sm) {
-  for (int j0 = 0; j0 < nw; j0 += 4)
-    for (int i0 = 0; i0 < nv; i0 += 8) {
-      const int mw = min(4, nw - j0), mv = min(8, nv - i0);
+// Sums NV <= 32 per-thread values over the block into out[0, NV).
+template <int NV>
+__device__ void block_reduce(const double (&v)[NV], double (*red)[32], double *out) {
+  static_assert(NV <= 32, "at most 32 values");
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < NV; ++i) {
+    const double x = warp_sum(v[i]);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][i] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double t = 0.0;
+    for (int w = 0; w < kT / 32; ++w) t += red[w][threadIdx.x];
+    out[threadIdx.x] = t;
+  }
+  __syncthreads();
+}
+
+// out[i + ldo * j] = L_i . R_j over the elements [e0, e1), columns at stride N.
+__device__ void chunk_dots(const double *__restrict__ L, int nl, const double *__restrict__ R, int nr, uint32_t N,
+                           uint32_t e0, uint32_t e1, double *out, int ldo, double (*red)[32]) {
+  for (int j0 = 0; j0 < nr; j0 += 4)
+    for (int i0 = 0; i0 < nl; i0 += 8) {
+      const int mw = min(4, nr - j0), mv = min(8, nl - i0);
       double acc[8][4];
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
-      for (uint32_t e = threadIdx.x; e < N; e += kBT) {
+      for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
         double w[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) w[j] = j < mw ? W[(size_t)(j0 + j) * N + e] : 0.0;
+        for (int j = 0; j < 4; ++j) w[j] = j < mw ? R[(size_t)(j0 + j) * N + e] : 0.0;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           if (i >= mv) break;
-          const double v = V[(size_t)(i0 + i) * N + e];
+          const double v = L[(size_t)(i0 + i) * N + e];
 #pragma unroll
           for (int j = 0; j < 4; ++j) acc[i][j] = fma(v, w[j], acc[i][j]);
         }
@@ -106,212 +138,208 @@ __device__ void block_dots(const double *V, int nv, const double *W, int nw, uin
       for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          double x = acc[i][j];
-          for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-          if ((threadIdx.x & 31) == 0) sm.red[threadIdx.x >> 5][i * 4 + j] = x;
+          const double x = warp_sum(acc[i][j]);
+          if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][i * 4 + j] = x;
         }
       __syncthreads();
       if (threadIdx.x < 32) {
         const int i = threadIdx.x / 4, j = threadIdx.x % 4;
         if (i < mv && j < mw) {
           double t = 0.0;
-          for (int w2 = 0; w2 < kBT / 32; ++w2) t += sm.red[w2][threadIdx.x];
-          G[(i0 + i) + (size_t)ldg * (j0 + j)] = t;
-        }
-      }
-      __syncthreads();
-    }
-}
-
-// Symmetric eigenproblem of the n x n leading block of sm.A (ld kBMaxNb), by
-// warp 0: eigenvalues ascending in sm.E, eigenvectors in the columns of sm.W.
-__device__ void block_eig(int n, Smem &sm, double *Aw) {
-  // Aw: a working copy (shared), ld kBMaxNb
-  for (int t = threadIdx.x; t < kBMaxNb * kBMaxNb; t += kBT) {
-    const int i = t % kBMaxNb, j = t / kBMaxNb;
-    Aw[t] = (i < n && j < n) ? 0.5 * (sm.A[i + kBMaxNb * j] + sm.A[j + kBMaxNb * i]) : 0.0;
-    sm.W[t] = (i == j) ? 1.0 : 0.0;
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    const int l = threadIdx.x;
-    for (int sweep = 0; sweep < 60; ++sweep) {
-      double off = 0.0, dg = 0.0;
-      for (int j = 0; j < n; ++j)
-        if (l < n) {
-          const double x = Aw[l + kBMaxNb * j];
-          if (l == j) dg += x * x; else off += x * x;
-        }
-      for (int o = 16; o > 0; o >>= 1) {
-        off += __shfl_xor_sync(0xffffffffu, off, o);
-        dg += __shfl_xor_sync(0xffffffffu, dg, o);
-      }
-      if (off <= 1e-30 * (dg + 1e-300)) break;
-      for (int p = 0; p < n - 1; ++p)
-        for (int q = p + 1; q < n; ++q) {
-          const double apq = Aw[p + kBMaxNb * q];
-          if (fabs(apq) < 1e-300) continue;
-          const double theta = (Aw[q + kBMaxNb * q] - Aw[p + kBMaxNb * p]) / (2.0 * apq);
-          const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-          const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-          __syncwarp();
-          if (l < n) {  // columns p, q
-            const double akp = Aw[l + kBMaxNb * p], akq = Aw[l + kBMaxNb * q];
-            Aw[l + kBMaxNb * p] = c * akp - s * akq;
-            Aw[l + kBMaxNb * q] = s * akp + c * akq;
-          }
-          __syncwarp();
-          if (l < n) {  // rows p, q
-            const double apk = Aw[p + kBMaxNb * l], aqk = Aw[q + kBMaxNb * l];
-            Aw[p + kBMaxNb * l] = c * apk - s * aqk;
-            Aw[q + kBMaxNb * l] = s * apk + c * aqk;
-            const double vkp = sm.W[l + kBMaxNb * p], vkq = sm.W[l + kBMaxNb * q];
-            sm.W[l + kBMaxNb * p] = c * vkp - s * vkq;
-            sm.W[l + kBMaxNb * q] = s * vkp + c * vkq;
-          }
-          __syncwarp();
-        }
-    }
-    if (l == 0) {  // sort ascending (selection), permuting the eigenvector columns
-      for (int i = 0; i < n; ++i) sm.E[i] = Aw[i + kBMaxNb * i];
-      for (int i = 0; i < n; ++i) {
-        int b = i;
-        for (int j = i + 1; j < n; ++j)
-          if (sm.E[j] < sm.E[b]) b = j;
-        if (b != i) {
-          const double e = sm.E[i];
-          sm.E[i] = sm.E[b];
-          sm.E[b] = e;
-          for (int r = 0; r < n; ++r) {
-            const double x = sm.W[r + kBMaxNb * i];
-            sm.W[r + kBMaxNb * i] = sm.W[r + kBMaxNb * b];
-            sm.W[r + kBMaxNb * b] = x;
-          }
+          for (int w2 = 0; w2 < kT / 32; ++w2) t += red[w2][threadIdx.x];
+          out[(i0 + i) + (size_t)ldo * (j0 + j)] = t;
         }
       }
     }
-  }
   __syncthreads();
 }
 
-// One sigma element, fused form (as k_sigma_alpha<..., kFused>).
-template <typename Wd>
-__device__ double sigma_element(const Args<double> &a, const double *__restrict__ x, uint32_t ia, uint32_t ib) {
-  const uint32_t col[1] = {ib};
-  const bool ok[1] = {true};
-  const Wd beta[1] = {word<Wd>(a.bstr, ib)};
-  double acc[1] = {a.hii[(size_t)ia * a.nb + ib] * x[(size_t)ia * a.nb + ib]};
-  same_spin_row<1, double, Wd>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, x, a.nb, ia, col, ok, beta, acc);
-  double part = 0.0;
-  const uint32_t q0 = a.B.off_s[ib], q1 = a.B.off_s[ib + 1];
-  for (uint32_t p = a.A.off_s[ia]; p < a.A.off_s[ia + 1]; ++p) {
-    const uint32_t ja = a.A.ket_s[p], ca = a.A.code_s[p];
+// Sum over the problem's chunks (in chunk order) of partial value v.
+__device__ __forceinline__ double chunk_total(const BCommon &g, const BProb &P, int v) {
+  double t = 0.0;
+  for (uint32_t c = P.c0; c < P.c1; ++c) t += g.part[(size_t)c * g.pstride + v];
+  return t;
+}
+
+// The element range of this block in a kernel launched with kSubPer blocks per
+// chunk; false when the range is empty (the last chunk of a problem).
+__device__ __forceinline__ bool sub_range(const BCommon &g, Chunk &ch, uint32_t &e0, uint32_t &e1) {
+  ch = g.ch[blockIdx.x / kSubPer];
+  e0 = ch.e0 + (blockIdx.x % kSubPer) * kSub;
+  e1 = min(ch.e1, e0 + kSub);
+  return e0 < e1;
+}
+
+// Symmetric eigenproblem of the n x n leading block of A (ld kNB, symmetric
+// part) by one warp: eigenvalues ascending in E, eigenvectors in the columns
+// of Wv (ld kNB).  Aw, Wv, E: shared.
+__device__ void warp_eig(int n, const double *A, double *Aw, double *Wv, double *E) {
+  const int l = threadIdx.x & 31;
+  for (int t = l; t < kNB * kNB; t += 32) {
+    const int i = t % kNB, j = t / kNB;
+    Aw[t] = (i < n && j < n) ? 0.5 * (A[i + kNB * j] + A[j + kNB * i]) : 0.0;
+    Wv[t] = (i == j) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0, dg = 0.0;
+    if (l < n)
+      for (int j = 0; j < n; ++j) {
+        const double x = Aw[l + kNB * j];
+        if (l == j) dg += x * x; else off += x * x;
+      }
+    off = warp_sum(off);
+    dg = warp_sum(dg);
+    if (off <= 1e-30 * (dg + 1e-300)) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        const double apq = Aw[p + kNB * q];
+        if (fabs(apq) < 1e-300) continue;
+        const double theta = (Aw[q + kNB * q] - Aw[p + kNB * p]) / (2.0 * apq);
+        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
+        __syncwarp();
+        if (l < n) {  // columns p, q
+          const double akp = Aw[l + kNB * p], akq = Aw[l + kNB * q];
+          Aw[l + kNB * p] = c * akp - s * akq;
+          Aw[l + kNB * q] = s * akp + c * akq;
+        }
+        __syncwarp();
+        if (l < n) {  // rows p, q and the eigenvectors
+          const double apk = Aw[p + kNB * l], aqk = Aw[q + kNB * l];
+          Aw[p + kNB * l] = c * apk - s * aqk;
+          Aw[q + kNB * l] = s * apk + c * aqk;
+          const double vkp = Wv[l + kNB * p], vkq = Wv[l + kNB * q];
+          Wv[l + kNB * p] = c * vkp - s * vkq;
+          Wv[l + kNB * q] = s * vkp + c * vkq;
+        }
+        __syncwarp();
+      }
+  }
+  if (l == 0) {  // ascending order (selection sort), permuting the eigenvector columns
+    for (int i = 0; i < n; ++i) E[i] = Aw[i + kNB * i];
+    for (int i = 0; i < n; ++i) {
+      int b = i;
+      for (int j = i + 1; j < n; ++j)
+        if (E[j] < E[b]) b = j;
+      if (b != i) {
+        const double e = E[i];
+        E[i] = E[b];
+        E[b] = e;
+        for (int r = 0; r < n; ++r) {
+          const double x = Wv[r + kNB * i];
+          Wv[r + kNB * i] = Wv[r + kNB * b];
+          Wv[r + kNB * b] = x;
+        }
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// ---- sigma ---------------------------------------------------------------------------
+
+// sigma of NV vectors (columns of x at stride N) at element (ia, ib), fused form.
+template <int NV, typename Wd>
+__device__ __forceinline__ void sigma_element_mv(const Args<double> &a, const double *__restrict__ x, uint32_t N,
+                                                 uint32_t ia, uint32_t ib, double (&acc)[NV]) {
+  const uint32_t nb = a.nb, e = ia * nb + ib;
+  const double h = __ldg(a.hii + e);
+#pragma unroll
+  for (int n = 0; n < NV; ++n) acc[n] = h * __ldg(x + (size_t)n * N + e);
+  const Wd beta = word<Wd>(a.bstr, ib);
+  // alpha singles and doubles of row ia, this column
+  for (uint32_t p = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1); p < p1; ++p) {
+    const uint32_t ja = __ldg(a.A.ket_s + p), code = __ldg(a.A.code_s + p);
+    const double v = __ldg(a.val_sa + p) + __ldg(a.Jb + ((code >> 16) & 0x7fffu) * nb + ib);
+    const double sv = flip(v, parity(beta & word<Wd>(a.A.mask_s, p)) ^ (code >> 31));
+    const uint32_t off = ja * nb + ib;
+#pragma unroll
+    for (int n = 0; n < NV; ++n) acc[n] = fma(sv, __ldg(x + (size_t)n * N + off), acc[n]);
+  }
+  for (uint32_t p = __ldg(a.A.off_d + ia), p1 = __ldg(a.A.off_d + ia + 1); p < p1; ++p) {
+    const uint32_t off = __ldg(a.A.ket_d + p) * nb + ib;
+    const double sv = flip(__ldg(a.val_da + p), parity(beta & word<Wd>(a.A.mask_d, p)));
+#pragma unroll
+    for (int n = 0; n < NV; ++n) acc[n] = fma(sv, __ldg(x + (size_t)n * N + off), acc[n]);
+  }
+  // alpha x beta singles
+  const uint32_t q0 = __ldg(a.B.off_s + ib), q1 = __ldg(a.B.off_s + ib + 1);
+  for (uint32_t p = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1); p < p1; ++p) {
+    const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
     const Wd alpha_ket = word<Wd>(a.astr, ja);
     const double *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
-    const uint32_t pa = parity(beta[0] & word<Wd>(a.A.mask_s, p)) ^ (ca >> 31);
+    const uint32_t pa = parity(beta & word<Wd>(a.A.mask_s, p)) ^ (ca >> 31);
+    const uint32_t rowoff = ja * nb;
     for (uint32_t q = q0; q < q1; ++q) {
-      const uint32_t jb = a.B.ket_s[q], cb = a.B.code_s[q];
+      const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
       const uint32_t ph = (pa ^ parity(alpha_ket & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31)) & 1u;
-      part = fma(flip(krow[(cb >> 16) & 0x7fffu], ph), x[(size_t)ja * a.nb + jb], part);
+      const double kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
+#pragma unroll
+      for (int n = 0; n < NV; ++n) acc[n] = fma(kv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
     }
   }
+  // beta singles and doubles of column ib, this row
   const Wd arow = word<Wd>(a.astr, ia);
-  const double *row = x + (size_t)ia * a.nb;
+  const uint32_t rowoff = ia * nb;
   for (uint32_t q = q0; q < q1; ++q) {
-    const uint32_t jb = a.B.ket_s[q], cb = a.B.code_s[q];
-    const uint32_t ph = parity(arow & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31);
-    part = fma(flip(a.val_sb[q] + a.Ja[(size_t)((cb >> 16) & 0x7fffu) * a.na + ia], ph), row[jb], part);
+    const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+    const double sv = flip(__ldg(a.val_sb + q) + __ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia),
+                           parity(arow & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31));
+#pragma unroll
+    for (int n = 0; n < NV; ++n) acc[n] = fma(sv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
   }
-  for (uint32_t q = a.B.off_d[ib]; q < a.B.off_d[ib + 1]; ++q)
-    part = fma(flip(a.val_db[q], parity(arow & word<Wd>(a.B.mask_d, q))), row[a.B.ket_d[q]], part);
-  return acc[0] + part;
+  for (uint32_t q = __ldg(a.B.off_d + ib), q1d = __ldg(a.B.off_d + ib + 1); q < q1d; ++q) {
+    const uint32_t jb = __ldg(a.B.ket_d + q);
+    const double sv = flip(__ldg(a.val_db + q), parity(arow & word<Wd>(a.B.mask_d, q)));
+#pragma unroll
+    for (int n = 0; n < NV; ++n) acc[n] = fma(sv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
+  }
+}
+
+template <int NV, typename Wd>
+__device__ void chunk_sigma(const BProb &P, const double *x, double *y, uint32_t e0, uint32_t e1) {
+  const uint32_t nb = P.a.nb;
+  for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
+    double acc[NV];
+    sigma_element_mv<NV, Wd>(P.a, x, P.N, e / nb, e % nb, acc);
+#pragma unroll
+    for (int n = 0; n < NV; ++n) y[(size_t)n * P.N + e] = acc[n];
+  }
 }
 
 template <typename Wd>
-__device__ void block_sigma(const SmallProb &P, const double *x, double *y) {
-  for (uint32_t e = threadIdx.x; e < P.N; e += kBT) y[e] = sigma_element<Wd>(P.a, x, e / P.a.nb, e % P.a.nb);
-  __syncthreads();
+__device__ void chunk_sigma_any(const BProb &P, int nvec, const double *x, double *y, uint32_t e0, uint32_t e1) {
+  switch (nvec) {
+    case 1: chunk_sigma<1, Wd>(P, x, y, e0, e1); break;
+    case 2: chunk_sigma<2, Wd>(P, x, y, e0, e1); break;
+    case 3: chunk_sigma<3, Wd>(P, x, y, e0, e1); break;
+    case 4: chunk_sigma<4, Wd>(P, x, y, e0, e1); break;
+    case 5: chunk_sigma<5, Wd>(P, x, y, e0, e1); break;
+    case 6: chunk_sigma<6, Wd>(P, x, y, e0, e1); break;
+    case 7: chunk_sigma<7, Wd>(P, x, y, e0, e1); break;
+    default: chunk_sigma<8, Wd>(P, x, y, e0, e1); break;
+  }
 }
 
-// Orthonormalises the nt columns of T (stride N) against V[0, nv) and among
-// themselves (CGS with a second pass when a norm falls below half, then
-// coefficient-space Gram-Schmidt with dropping below `drop` of the original
-// norm); writes the kept directions to V[nv, nv + kept).  Returns kept.
-__device__ int block_orthonormalize(double *T, int nt, double *V, int nv, uint32_t N, double drop, Smem &sm) {
-  double n0[kBMaxK], prev[kBMaxK];
-  block_dots(T, nt, T, nt, N, sm.W, kBMaxNb, sm);
-  for (int q = 0; q < nt; ++q) n0[q] = prev[q] = sm.W[q + kBMaxNb * q];
-  for (int pass = 0; pass < 2 && nv > 0; ++pass) {
-    block_dots(V, nv, T, nt, N, sm.G, kBMaxNb, sm);
-    for (uint32_t e = threadIdx.x; e < N; e += kBT)
-      for (int q = 0; q < nt; ++q) {
-        double t = T[(size_t)q * N + e];
-        for (int j = 0; j < nv; ++j) t = fma(-V[(size_t)j * N + e], sm.G[j + kBMaxNb * q], t);
-        T[(size_t)q * N + e] = t;
-      }
-    __syncthreads();
-    block_dots(T, nt, T, nt, N, sm.W, kBMaxNb, sm);
-    bool again = false;
-    for (int q = 0; q < nt; ++q) {
-      const double g = sm.W[q + kBMaxNb * q];
-      again = again || (g < 0.5 * prev[q]);
-      prev[q] = g;
-    }
-    if (!again) break;
-  }
-  // coefficient-space Gram-Schmidt on the Gram matrix sm.W (thread 0)
-  if (threadIdx.x == 0) {
-    int kept = 0;
-    for (int q = 0; q < nt; ++q) {
-      if (!(n0[q] > 0.0)) continue;
-      double v[kBMaxK];
-      for (int i = 0; i < nt; ++i) v[i] = (i == q) ? 1.0 : 0.0;
-      for (int pass = 0; pass < 2; ++pass)
-        for (int u = 0; u < kept; ++u) {
-          double pr = 0.0;
-          for (int i = 0; i < nt; ++i)
-            for (int j = 0; j < nt; ++j) pr += sm.M[i + kBMaxK * u] * sm.W[i + kBMaxNb * j] * v[j];
-          for (int i = 0; i < nt; ++i) v[i] -= pr * sm.M[i + kBMaxK * u];
-        }
-      double nn = 0.0;
-      for (int i = 0; i < nt; ++i)
-        for (int j = 0; j < nt; ++j) nn += v[i] * sm.W[i + kBMaxNb * j] * v[j];
-      if (!(nn > drop * drop * n0[q])) continue;
-      const double f = 1.0 / sqrt(nn);
-      for (int i = 0; i < nt; ++i) sm.M[i + kBMaxK * kept] = v[i] * f;
-      ++kept;
-    }
-    sm.ival[0] = kept;
-  }
-  __syncthreads();
-  const int kept = sm.ival[0];
-  for (uint32_t e = threadIdx.x; e < N; e += kBT) {
-    double t[kBMaxK];
-    for (int q = 0; q < nt; ++q) t[q] = T[(size_t)q * N + e];
-    for (int c = 0; c < kept; ++c) {
-      double y = 0.0;
-      for (int q = 0; q < nt; ++q) y = fma(t[q], sm.M[q + kBMaxK * c], y);
-      V[(size_t)(nv + c) * N + e] = y;
-    }
-  }
-  __syncthreads();
-  return kept;
-}
+// ---- kernels ---------------------------------------------------------------------------
 
-template <typename Wd>
-__device__ void solve_one(const SmallProb &P, const SmallOpts o, Smem &sm, double *Aw) {
+// Start vectors (one block per problem): unit vectors on the k lowest diagonal
+// entries (ties by index) plus a deterministic splitmix64 component of total
+// size 1e-3, in T; the state is set for the first orthonormalisation.
+__global__ void __launch_bounds__(kT) k_b_init(BCommon g) {
+  __shared__ double dv[kT / 32];
+  __shared__ unsigned long long di[kT / 32], pos[kK];
+  const BProb &P = g.P[blockIdx.x];
+  BState &S = g.S[blockIdx.x];
   const uint32_t N = P.N;
-  const int k = min(o.k, (int)N);
-  const int max_nb = min(min(max(o.max_nb, 2 * k), kBMaxNb), (int)N);
-  double *V = P.V, *HV = P.HV, *T = P.T, *U = P.U;
-  // start vectors: unit vectors on the k lowest diagonal entries (ties by
-  // index) plus a deterministic splitmix64 component of total size 1e-3
+  const int k = g.k;
   for (int q = 0; q < k; ++q) {
     double best = INFINITY;
     unsigned long long bi = ~0ull;
-    for (uint32_t e = threadIdx.x; e < N; e += kBT) {
+    for (uint32_t e = threadIdx.x; e < N; e += kT) {
       bool skip = false;
-      for (int r = 0; r < q; ++r) skip |= (sm.pos[r] == e);
+      for (int r = 0; r < q; ++r) skip |= (pos[r] == e);
       const double h = P.a.hii[e];
       if (!skip && (h < best || (h == best && e < bi))) {
         best = h;
@@ -327,24 +355,24 @@ __device__ void solve_one(const SmallProb &P, const SmallOpts o, Smem &sm, doubl
       }
     }
     if ((threadIdx.x & 31) == 0) {
-      sm.dv[threadIdx.x >> 5] = best;
-      sm.di[threadIdx.x >> 5] = bi;
+      dv[threadIdx.x >> 5] = best;
+      di[threadIdx.x >> 5] = bi;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
       double b = INFINITY;
       unsigned long long ix = ~0ull;
-      for (int w = 0; w < kBT / 32; ++w)
-        if (sm.dv[w] < b || (sm.dv[w] == b && sm.di[w] < ix)) {
-          b = sm.dv[w];
-          ix = sm.di[w];
+      for (int w = 0; w < kT / 32; ++w)
+        if (dv[w] < b || (dv[w] == b && di[w] < ix)) {
+          b = dv[w];
+          ix = di[w];
         }
-      sm.pos[q] = ix;
+      pos[q] = ix;
     }
     __syncthreads();
   }
   const double amp = 1e-3 * sqrt(3.0 / (double)N);
-  for (uint32_t e = threadIdx.x; e < N; e += kBT)
+  for (uint32_t e = threadIdx.x; e < N; e += kT)
     for (int q = 0; q < k; ++q) {
       uint64_t z = (uint64_t)e * 0x9E3779B97F4A7C15ull + 0x5BD1E995ull * (uint64_t)(q + 1);
       z ^= z >> 30;
@@ -352,229 +380,530 @@ __device__ void solve_one(const SmallProb &P, const SmallOpts o, Smem &sm, doubl
       z ^= z >> 27;
       z *= 0x94D049BB133111EBull;
       z ^= z >> 31;
-      T[(size_t)q * N + e] = (e == sm.pos[q] ? 1.0 : 0.0) + amp * ((double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0);
+      P.T[(size_t)q * N + e] = (e == pos[q] ? 1.0 : 0.0) + amp * ((double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0);
     }
-  __syncthreads();
-  int nv = block_orthonormalize(T, k, V, 0, N, 1e-8, sm);
-  int sigma_calls = 0, restarts = 0, iter = 0, kk = 0, nvprev = 0, kprev = 0;
-  for (int j = 0; j < nv; ++j) block_sigma<Wd>(P, V + (size_t)j * N, HV + (size_t)j * N);
-  sigma_calls += nv;
-  block_dots(V, nv, HV, nv, N, sm.A, kBMaxNb, sm);
-  bool converged = false;
-  while (true) {
-    block_eig(nv, sm, Aw);
-    kk = min(k, nv);
-    for (int t = threadIdx.x; t < nv * kk; t += kBT) sm.c[t] = sm.W[(t % nv) + kBMaxNb * (t / nv)];
-    if (threadIdx.x < kk) sm.th[threadIdx.x] = sm.E[threadIdx.x];
-    __syncthreads();
-    // residuals and Olsen-corrected preconditioned corrections
-    double rn[kBMaxK], xt[kBMaxK], xu[kBMaxK];
-    for (int q = 0; q < kk; ++q) rn[q] = xt[q] = xu[q] = 0.0;
-    for (uint32_t e = threadIdx.x; e < N; e += kBT) {
-      const double d = P.a.hii[e];
-      for (int q = 0; q < kk; ++q) {
-        double xv = 0.0, hv = 0.0;
-        for (int j = 0; j < nv; ++j) {
-          const double cq = sm.c[j + nv * q];
-          xv = fma(V[(size_t)j * N + e], cq, xv);
-          hv = fma(HV[(size_t)j * N + e], cq, hv);
-        }
-        const double r = hv - sm.th[q] * xv;
-        rn[q] = fma(r, r, rn[q]);
-        double den = sm.th[q] - d;
-        if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
-        const double t = r / den, u = xv / den;
-        T[(size_t)q * N + e] = t;
-        U[(size_t)q * N + e] = u;
-        xt[q] = fma(xv, t, xt[q]);
-        xu[q] = fma(xv, u, xu[q]);
-      }
-    }
-    for (int q = 0; q < kk; ++q) {
-      const double rq = sqrt(fmax(0.0, block_sum(rn[q], sm)));
-      const double a1 = block_sum(xt[q], sm), a2 = block_sum(xu[q], sm);
-      if (threadIdx.x == 0) {
-        sm.res[q] = rq;
-        sm.eo[q] = (a2 != 0.0 && isfinite(a1 / a2)) ? a1 / a2 : 0.0;
-      }
-    }
-    __syncthreads();
-    for (uint32_t e = threadIdx.x; e < N; e += kBT)
-      for (int q = 0; q < kk; ++q) T[(size_t)q * N + e] = fma(-sm.eo[q], U[(size_t)q * N + e], T[(size_t)q * N + e]);
-    __syncthreads();
-    ++iter;
-    converged = kk == k;
-    int nnew = 0;
-    for (int q = 0; q < kk; ++q) {
-      converged = converged && (sm.res[q] < o.eps);
-      nnew += (sm.res[q] >= o.eps);
-    }
-    if (converged || iter >= o.max_steps) break;
-    if (nv + nnew > max_nb) {
-      // thick restart on span{Ritz vectors, previous Ritz vectors}: V Q, HV Q, Q^T A Q
-      if (threadIdx.x == 0) {
-        int m = 0;
-        const int nkeep = min(kprev, max_nb - kk - nnew);
-        for (int col = 0; col < kk + nkeep; ++col) {
-          double v[kBMaxNb];
-          for (int i = 0; i < nv; ++i)
-            v[i] = col < kk ? sm.c[i + nv * col] : (i < nvprev ? sm.cprev[i + nvprev * (col - kk)] : 0.0);
-          double n0 = 0.0;
-          for (int i = 0; i < nv; ++i) n0 += v[i] * v[i];
-          n0 = sqrt(n0);
-          for (int pass = 0; pass < 2; ++pass)
-            for (int j = 0; j < m; ++j) {
-              double pr = 0.0;
-              for (int i = 0; i < nv; ++i) pr += sm.W[i + kBMaxNb * j] * v[i];
-              for (int i = 0; i < nv; ++i) v[i] -= pr * sm.W[i + kBMaxNb * j];
-            }
-          double nn = 0.0;
-          for (int i = 0; i < nv; ++i) nn += v[i] * v[i];
-          nn = sqrt(nn);
-          if (!(nn > 1e-8 * n0)) continue;
-          for (int i = 0; i < nv; ++i) sm.W[i + kBMaxNb * m] = v[i] / nn;
-          ++m;
-        }
-        sm.ival[1] = m;
-      }
-      __syncthreads();
-      const int m = sm.ival[1];
-      for (uint32_t e = threadIdx.x; e < N; e += kBT)
-        for (int b = 0; b < m; ++b) {
-          double xv = 0.0, hv = 0.0;
-          for (int j = 0; j < nv; ++j) {
-            xv = fma(V[(size_t)j * N + e], sm.W[j + kBMaxNb * b], xv);
-            hv = fma(HV[(size_t)j * N + e], sm.W[j + kBMaxNb * b], hv);
-          }
-          P.X[(size_t)b * N + e] = xv;
-          P.HX[(size_t)b * N + e] = hv;
-        }
-      __syncthreads();
-      for (uint32_t e = threadIdx.x; e < N; e += kBT)
-        for (int b = 0; b < m; ++b) {
-          V[(size_t)b * N + e] = P.X[(size_t)b * N + e];
-          HV[(size_t)b * N + e] = P.HX[(size_t)b * N + e];
-        }
-      // projected matrix Q^T A Q and the Ritz coefficients Q^T c (thread 0)
-      if (threadIdx.x == 0) {
-        // A Q into Aw (nv x m), then Q^T (A Q) (m x m) into a local block
-        for (int b = 0; b < m; ++b)
-          for (int j = 0; j < nv; ++j) {
-            double aq = 0.0;
-            for (int i = 0; i < nv; ++i)
-              aq += 0.5 * (sm.A[j + kBMaxNb * i] + sm.A[i + kBMaxNb * j]) * sm.W[i + kBMaxNb * b];
-            Aw[j + kBMaxNb * b] = aq;
-          }
-        double hn[2 * kBMaxK * 2 * kBMaxK];
-        for (int b = 0; b < m; ++b)
-          for (int a2 = 0; a2 < m; ++a2) {
-            double t = 0.0;
-            for (int j = 0; j < nv; ++j) t += sm.W[j + kBMaxNb * a2] * Aw[j + kBMaxNb * b];
-            hn[a2 + m * b] = t;
-          }
-        for (int t = 0; t < kBMaxNb * kBMaxNb; ++t) sm.A[t] = 0.0;
-        for (int b = 0; b < m; ++b)
-          for (int a2 = 0; a2 < m; ++a2) sm.A[a2 + kBMaxNb * b] = hn[a2 + m * b];
-        double cn[kBMaxNb * kBMaxK];
-        for (int q = 0; q < kk; ++q)
-          for (int a2 = 0; a2 < m; ++a2) {
-            double t = 0.0;
-            for (int i = 0; i < nv; ++i) t += sm.W[i + kBMaxNb * a2] * sm.c[i + nv * q];
-            cn[a2 + m * q] = t;
-          }
-        for (int t = 0; t < m * kk; ++t) sm.c[t] = cn[t];
-      }
-      __syncthreads();
-      nv = m;
-      ++restarts;
-    }
-    for (int t = threadIdx.x; t < nv * kk; t += kBT) sm.cprev[t] = sm.c[t];
-    nvprev = nv;
-    kprev = kk;
-    __syncthreads();
-    // corrections of the unconverged roots, packed at the front of T
-    int nt = 0;
-    for (int q = 0; q < kk; ++q)
-      if (sm.res[q] >= o.eps) {
-        if (nt != q)
-          for (uint32_t e = threadIdx.x; e < N; e += kBT) T[(size_t)nt * N + e] = T[(size_t)q * N + e];
-        ++nt;
-      }
-    __syncthreads();
-    const int added = block_orthonormalize(T, nt, V, nv, N, 1e-8, sm);
-    if (added == 0) break;
-    for (int j = nv; j < nv + added; ++j) block_sigma<Wd>(P, V + (size_t)j * N, HV + (size_t)j * N);
-    sigma_calls += added;
-    // new columns of the projected matrix
-    block_dots(V, nv + added, HV + (size_t)nv * N, added, N, sm.G, kBMaxNb, sm);
-    for (int t = threadIdx.x; t < (nv + added) * added; t += kBT) {
-      const int i = t % (nv + added), jj = t / (nv + added);
-      const double g = sm.G[i + kBMaxNb * jj];
-      sm.A[i + kBMaxNb * (nv + jj)] = g;
-      sm.A[(nv + jj) + kBMaxNb * i] = g;
-    }
-    __syncthreads();
-    nv += added;
-  }
-  // outputs
-  if (P.Xout)
-    for (uint32_t e = threadIdx.x; e < N; e += kBT)
-      for (int q = 0; q < kk; ++q) {
-        double xv = 0.0;
-        for (int j = 0; j < nv; ++j) xv = fma(V[(size_t)j * N + e], sm.c[j + nv * q], xv);
-        P.Xout[(size_t)q * N + e] = xv;
-      }
   if (threadIdx.x == 0) {
-    for (int q = 0; q < o.k; ++q) {
-      P.out[q] = q < kk ? sm.th[q] : NAN;
-      P.out[o.k + q] = q < kk ? sm.res[q] : NAN;
+    S.active = 1;
+    S.converged = S.iter = S.sigma_calls = S.restarts = 0;
+    S.nv = S.kk = S.kc = S.nvprev = S.kprev = S.restart = S.nv_old = S.m = S.from = S.to = 0;
+    S.nt = k;
+    for (int q = 0; q < kK; ++q) {
+      S.roots[q] = q;
+      S.th[q] = S.res[q] = S.eo[q] = S.n0[q] = 0.0;
     }
-    P.out[2 * o.k + 0] = iter;
-    P.out[2 * o.k + 1] = sigma_calls;
-    P.out[2 * o.k + 2] = converged ? 1.0 : 0.0;
-    P.out[2 * o.k + 3] = restarts;
   }
 }
 
-__global__ void __launch_bounds__(kBT) k_batch_davidson(const SmallProb *__restrict__ probs, SmallOpts o) {
-  extern __shared__ double smem_raw[];
-  Smem &sm = *reinterpret_cast<Smem *>(smem_raw);
-  double *Aw = smem_raw + (sizeof(Smem) + 7) / 8;  // kBMaxNb^2 working copy for the eigensolver
-  const SmallProb &P = probs[blockIdx.x];
+// Partial dot products of one chunk.  mode 0: V[0, to)^T HV[from, to) (the new
+// columns of the projected matrix); mode 1: V[0, nv)^T T[0, nt) followed by the
+// Gram matrix T^T T.
+__global__ void __launch_bounds__(kT) k_b_dots(BCommon g, int mode) {
+  __shared__ double red[kT / 32][32];
+  const Chunk ch = g.ch[blockIdx.x];
+  const BState &S = g.S[ch.prob];
+  if (!S.active) return;
+  const BProb &P = g.P[ch.prob];
+  double *out = g.part + (size_t)blockIdx.x * g.pstride;
+  if (mode == 0) {
+    const int nl = S.to, nr = S.to - S.from;
+    chunk_dots(P.V, nl, P.HV + (size_t)S.from * P.N, nr, P.N, ch.e0, ch.e1, out, nl, red);
+  } else {
+    const int nl = S.nv, nr = S.nt;
+    chunk_dots(P.V, nl, P.T, nr, P.N, ch.e0, ch.e1, out, nl, red);
+    chunk_dots(P.T, nr, P.T, nr, P.N, ch.e0, ch.e1, out + nl * nr, nr, red);
+  }
+}
+
+// Rayleigh-Ritz (one warp per problem): the new columns of the projected
+// matrix from the mode-0 partials, then its lowest kk eigenpairs.
+__global__ void __launch_bounds__(32) k_b_rr(BCommon g) {
+  __shared__ double Aw[kNB * kNB], Wv[kNB * kNB], E[kNB];
+  const BProb &P = g.P[blockIdx.x];
+  BState &S = g.S[blockIdx.x];
+  if (!S.active) return;
+  const int l = threadIdx.x, from = S.from, to = S.to, nr = to - from;
+  for (int v = l; v < to * nr; v += 32) {
+    const double t = chunk_total(g, P, v);
+    const int i = v % to, j = from + v / to;
+    S.A[i + kNB * j] = t;
+    if (i < from) S.A[j + kNB * i] = t;
+  }
+  __syncwarp();
+  const int nv = to, kk = min(g.k, nv), kc = min(2 * g.k, nv);
+  warp_eig(nv, S.A, Aw, Wv, E);
+  for (int t = l; t < nv * kc; t += 32) S.c[t] = Wv[(t % nv) + kNB * (t / nv)];
+  if (l < kk) S.th[l] = E[l];
+  if (l == 0) {
+    S.nv = nv;
+    S.kk = kk;
+    S.kc = kc;
+    S.iter++;
+  }
+}
+
+// Residuals and Olsen-corrected preconditioned corrections of the kk Ritz
+// pairs: T = r / (theta - d), U = x / (theta - d); partials of |r|^2, x.T, x.U.
+__global__ void __launch_bounds__(kT) k_b_combine(BCommon g) {
+  __shared__ double red[kT / 32][32];
+  __shared__ double cs[kNB * kK], th[kK];
+  const Chunk ch = g.ch[blockIdx.x];
+  const BState &S = g.S[ch.prob];
+  if (!S.active) return;
+  const BProb &P = g.P[ch.prob];
+  const int nv = S.nv, kk = S.kk;
+  const uint32_t N = P.N;
+  for (int t = threadIdx.x; t < nv * kk; t += kT) cs[t] = S.c[t];
+  if (threadIdx.x < kk) th[threadIdx.x] = S.th[threadIdx.x];
+  __syncthreads();
+  double acc[3 * kK];
+#pragma unroll
+  for (int i = 0; i < 3 * kK; ++i) acc[i] = 0.0;
+  for (uint32_t e = ch.e0 + threadIdx.x; e < ch.e1; e += kT) {
+    double xv[kK], hv[kK];
+#pragma unroll
+    for (int q = 0; q < kK; ++q) xv[q] = hv[q] = 0.0;
+    for (int j = 0; j < nv; ++j) {
+      const double vj = P.V[(size_t)j * N + e], hj = P.HV[(size_t)j * N + e];
+#pragma unroll
+      for (int q = 0; q < kK; ++q)
+        if (q < kk) {
+          xv[q] = fma(vj, cs[j + nv * q], xv[q]);
+          hv[q] = fma(hj, cs[j + nv * q], hv[q]);
+        }
+    }
+    const double d = P.a.hii[e];
+#pragma unroll
+    for (int q = 0; q < kK; ++q)
+      if (q < kk) {
+        const double r = hv[q] - th[q] * xv[q];
+        double den = th[q] - d;
+        if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
+        const double t = r / den, u = xv[q] / den;
+        P.T[(size_t)q * N + e] = t;
+        P.U[(size_t)q * N + e] = u;
+        acc[q] = fma(r, r, acc[q]);
+        acc[kK + q] = fma(xv[q], t, acc[kK + q]);
+        acc[2 * kK + q] = fma(xv[q], u, acc[2 * kK + q]);
+      }
+  }
+  block_reduce<3 * kK>(acc, red, g.part + (size_t)blockIdx.x * g.pstride);
+}
+
+// Control after the residuals (one warp per problem): residual norms, Olsen
+// coefficients, convergence, and the thick restart in coefficient space.
+__global__ void __launch_bounds__(32) k_b_ctl(BCommon g) {
+  __shared__ double sums[3 * kK];
+  __shared__ double Aw[kNB * kR];
+  __shared__ int flag[2];
+  const BProb &P = g.P[blockIdx.x];
+  BState &S = g.S[blockIdx.x];
+  if (!S.active) return;
+  const int l = threadIdx.x, kk = S.kk, nv = S.nv;
+  if (l < 3 * kK) sums[l] = chunk_total(g, P, l);
+  __syncwarp();
+  if (l == 0) {
+    int nnew = 0;
+    bool conv = kk == g.k;
+    for (int q = 0; q < kk; ++q) {
+      const double a1 = sums[kK + q], a2 = sums[2 * kK + q];
+      S.res[q] = sqrt(fmax(0.0, sums[q]));
+      S.eo[q] = (a2 != 0.0 && isfinite(a1 / a2)) ? a1 / a2 : 0.0;
+      conv = conv && (S.res[q] < g.eps);
+      nnew += (S.res[q] >= g.eps);
+    }
+    S.restart = 0;
+    flag[0] = 0;
+    if (conv || S.iter >= P.max_steps) {
+      S.converged = conv;
+      S.active = 0;
+      flag[0] = 1;
+    } else if (nv + nnew > P.max_nb) {
+      // orthonormal Q (nv x m) spanning the lowest 2k Ritz coefficient
+      // vectors (room permitting) and the previous step's Ritz coefficients
+      const int keep = max(kk, min(S.kc, P.max_nb - nnew));
+      const int nkeep = max(0, min(S.kprev, P.max_nb - keep - nnew));
+      int m = 0;
+      for (int col = 0; col < keep + nkeep; ++col) {
+        double v[kNB];
+        for (int i = 0; i < nv; ++i)
+          v[i] = col < keep ? S.c[i + nv * col] : (i < S.nvprev ? S.cprev[i + S.nvprev * (col - keep)] : 0.0);
+        double n0 = 0.0;
+        for (int i = 0; i < nv; ++i) n0 += v[i] * v[i];
+        n0 = sqrt(n0);
+        for (int pass = 0; pass < 2; ++pass)
+          for (int j = 0; j < m; ++j) {
+            double pr = 0.0;
+            for (int i = 0; i < nv; ++i) pr += S.Q[i + nv * j] * v[i];
+            for (int i = 0; i < nv; ++i) v[i] -= pr * S.Q[i + nv * j];
+          }
+        double nn = 0.0;
+        for (int i = 0; i < nv; ++i) nn += v[i] * v[i];
+        nn = sqrt(nn);
+        if (!(nn > 1e-8 * n0)) continue;
+        for (int i = 0; i < nv; ++i) S.Q[i + nv * m] = v[i] / nn;
+        ++m;
+      }
+      S.m = m;
+      S.restart = 1;
+    }
+    if (!flag[0]) {
+      int nt = 0;
+      for (int q = 0; q < kk; ++q)
+        if (S.res[q] >= g.eps) S.roots[nt++] = q;
+      nt = min(nt, P.max_nb - (S.restart ? S.m : nv));
+      if (nt <= 0) {  // no room for a new direction: the subspace is the whole space
+        S.converged = 0;
+        S.active = 0;
+        S.restart = 0;
+        flag[0] = 1;
+      }
+      S.nt = nt;
+    }
+    flag[1] = S.restart;
+  }
+  __syncwarp();
+  if (flag[0]) return;
+  if (flag[1]) {
+    // A <- Q^T A Q, c <- Q^T c (lanes over the columns of Q; m <= 24)
+    const int m = S.m;
+    for (int b = l; b < m; b += 32)
+      for (int j = 0; j < nv; ++j) {
+        double aq = 0.0;
+        for (int i = 0; i < nv; ++i) aq += 0.5 * (S.A[j + kNB * i] + S.A[i + kNB * j]) * S.Q[i + nv * b];
+        Aw[j + kNB * b] = aq;
+      }
+    __syncwarp();
+    double hn[kR], cn[kK];
+    if (l < m) {
+      for (int a2 = 0; a2 < m; ++a2) {
+        double t = 0.0;
+        for (int j = 0; j < nv; ++j) t += S.Q[j + nv * a2] * Aw[j + kNB * l];
+        hn[a2] = t;
+      }
+      for (int q = 0; q < kk; ++q) {
+        double t = 0.0;
+        for (int i = 0; i < nv; ++i) t += S.Q[i + nv * l] * S.c[i + nv * q];
+        cn[q] = t;
+      }
+    }
+    __syncwarp();
+    if (l < m) {
+      for (int a2 = 0; a2 < m; ++a2) S.A[a2 + kNB * l] = hn[a2];
+      for (int q = 0; q < kk; ++q) S.c[l + m * q] = cn[q];
+    }
+    __syncwarp();
+    if (l == 0) {
+      S.nv_old = nv;
+      S.nv = m;
+      S.restarts++;
+    }
+    __syncwarp();
+  }
+  const int nvn = flag[1] ? S.m : nv;
+  for (int t = l; t < nvn * kk; t += 32) S.cprev[t] = S.c[t];
+  if (l == 0) {
+    S.nvprev = nvn;
+    S.kprev = kk;
+  }
+}
+
+// Element updates after the control step: the restart V <- V Q, HV <- HV Q
+// (per element, in registers), then the Olsen update T - eo U of the
+// unconverged roots, packed at the front of T.
+__global__ void __launch_bounds__(kT) k_b_apply(BCommon g) {
+  __shared__ double Qs[kNB * kR], eo[kK];
+  __shared__ int roots[kK];
+  Chunk ch;
+  uint32_t e0, e1;
+  if (!sub_range(g, ch, e0, e1)) return;
+  const BState &S = g.S[ch.prob];
+  if (!S.active) return;
+  const BProb &P = g.P[ch.prob];
+  const uint32_t N = P.N;
+  const int restart = S.restart, nvo = S.nv_old, m = S.m, nt = S.nt;
+  if (restart)
+    for (int t = threadIdx.x; t < nvo * m; t += kT) Qs[t] = S.Q[t];
+  if (threadIdx.x < kK) {
+    eo[threadIdx.x] = S.eo[threadIdx.x];
+    roots[threadIdx.x] = S.roots[threadIdx.x];
+  }
+  __syncthreads();
+  for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
+    if (restart) {
+      for (int pass = 0; pass < 2; ++pass) {
+        double *B = pass == 0 ? P.V : P.HV;
+        double vin[kNB];
+#pragma unroll
+        for (int j = 0; j < kNB; ++j) vin[j] = j < nvo ? B[(size_t)j * N + e] : 0.0;
+        for (int b = 0; b < m; ++b) {
+          double y = 0.0;
+#pragma unroll
+          for (int j = 0; j < kNB; ++j)
+            if (j < nvo) y = fma(vin[j], Qs[j + nvo * b], y);
+          B[(size_t)b * N + e] = y;
+        }
+      }
+    }
+    double t[kK];
+#pragma unroll
+    for (int i = 0; i < kK; ++i)
+      if (i < nt) {
+        const int r = roots[i];
+        t[i] = fma(-eo[r], P.U[(size_t)r * N + e], P.T[(size_t)r * N + e]);
+      }
+#pragma unroll
+    for (int i = 0; i < kK; ++i)
+      if (i < nt) P.T[(size_t)i * N + e] = t[i];
+  }
+}
+
+// First Gram-Schmidt pass, control (one warp per problem): G = V^T T and the
+// original correction norms.
+__global__ void __launch_bounds__(32) k_b_gs1(BCommon g) {
+  const BProb &P = g.P[blockIdx.x];
+  BState &S = g.S[blockIdx.x];
+  if (!S.active) return;
+  const int nv = S.nv, nt = S.nt;
+  for (int v = threadIdx.x; v < nv * nt; v += 32) S.G[v] = chunk_total(g, P, v);
+  if ((int)threadIdx.x < nt) S.n0[threadIdx.x] = chunk_total(g, P, nv * nt + threadIdx.x * (nt + 1));
+}
+
+// T <- T - V G.
+__global__ void __launch_bounds__(kT) k_b_project(BCommon g) {
+  __shared__ double Gs[kNB * kK];
+  Chunk ch;
+  uint32_t e0, e1;
+  if (!sub_range(g, ch, e0, e1)) return;
+  const BState &S = g.S[ch.prob];
+  if (!S.active) return;
+  const BProb &P = g.P[ch.prob];
+  const uint32_t N = P.N;
+  const int nv = S.nv, nt = S.nt;
+  if (nv == 0) return;
+  for (int t = threadIdx.x; t < nv * nt; t += kT) Gs[t] = S.G[t];
+  __syncthreads();
+  for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
+    double t[kK];
+#pragma unroll
+    for (int q = 0; q < kK; ++q) t[q] = q < nt ? P.T[(size_t)q * N + e] : 0.0;
+    for (int j = 0; j < nv; ++j) {
+      const double vj = P.V[(size_t)j * N + e];
+#pragma unroll
+      for (int q = 0; q < kK; ++q)
+        if (q < nt) t[q] = fma(-vj, Gs[j + nv * q], t[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < kK; ++q)
+      if (q < nt) P.T[(size_t)q * N + e] = t[q];
+  }
+}
+
+// Second Gram-Schmidt pass, control (one warp per problem): G = V^T T (the
+// second projection, applied with the new columns), the Gram matrix of the
+// projected block (T^T T - G^T G) and its coefficient-space Gram-Schmidt with
+// dropping below 1e-8 of the original norm.
+__global__ void __launch_bounds__(32) k_b_gs2(BCommon g) {
+  __shared__ double Gm[kK * kK];
+  const BProb &P = g.P[blockIdx.x];
+  BState &S = g.S[blockIdx.x];
+  if (!S.active) return;
+  const int nv = S.nv, nt = S.nt, l = threadIdx.x;
+  for (int v = l; v < nv * nt; v += 32) S.G[v] = chunk_total(g, P, v);
+  for (int v = l; v < nt * nt; v += 32) Gm[v] = chunk_total(g, P, nv * nt + v);
+  __syncwarp();
+  for (int v = l; v < nt * nt; v += 32) {
+    const int i = v % nt, j = v / nt;
+    double s = Gm[v];
+    for (int r = 0; r < nv; ++r) s -= S.G[r + nv * i] * S.G[r + nv * j];
+    Gm[v] = s;
+  }
+  __syncwarp();
+  if (l == 0) {
+    int kept = 0;
+    for (int q = 0; q < nt; ++q) {
+      const double n0 = S.n0[q];
+      if (!(n0 > 0.0) || !isfinite(n0)) continue;
+      double v[kK];
+      for (int i = 0; i < nt; ++i) v[i] = (i == q) ? 1.0 : 0.0;
+      for (int pass = 0; pass < 2; ++pass)
+        for (int u = 0; u < kept; ++u) {
+          double pr = 0.0;
+          for (int i = 0; i < nt; ++i)
+            for (int j = 0; j < nt; ++j) pr += S.M[i + nt * u] * Gm[i + nt * j] * v[j];
+          for (int i = 0; i < nt; ++i) v[i] -= pr * S.M[i + nt * u];
+        }
+      double nn = 0.0;
+      for (int i = 0; i < nt; ++i)
+        for (int j = 0; j < nt; ++j) nn += v[i] * Gm[i + nt * j] * v[j];
+      if (!(nn > 1e-16 * n0)) continue;
+      const double f = 1.0 / sqrt(nn);
+      for (int i = 0; i < nt; ++i) S.M[i + nt * kept] = v[i] * f;
+      ++kept;
+    }
+    if (kept == 0) {  // no new direction: the subspace is invariant
+      S.active = 0;
+      S.converged = 0;
+    } else {
+      S.from = nv;
+      S.to = nv + kept;
+      S.sigma_calls += kept;
+    }
+  }
+}
+
+// New basis columns V[nv + c] = (T - V G) M.
+__global__ void __launch_bounds__(kT) k_b_newcols(BCommon g) {
+  __shared__ double Gs[kNB * kK], Ms[kK * kK];
+  Chunk ch;
+  uint32_t e0, e1;
+  if (!sub_range(g, ch, e0, e1)) return;
+  const BState &S = g.S[ch.prob];
+  if (!S.active) return;
+  const BProb &P = g.P[ch.prob];
+  const uint32_t N = P.N;
+  const int nv = S.nv, nt = S.nt, kept = S.to - S.from;
+  for (int t = threadIdx.x; t < nv * nt; t += kT) Gs[t] = S.G[t];
+  for (int t = threadIdx.x; t < nt * kept; t += kT) Ms[t] = S.M[t];
+  __syncthreads();
+  for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
+    double t[kK];
+#pragma unroll
+    for (int q = 0; q < kK; ++q) t[q] = q < nt ? P.T[(size_t)q * N + e] : 0.0;
+    for (int j = 0; j < nv; ++j) {
+      const double vj = P.V[(size_t)j * N + e];
+#pragma unroll
+      for (int q = 0; q < kK; ++q)
+        if (q < nt) t[q] = fma(-vj, Gs[j + nv * q], t[q]);
+    }
+    for (int c = 0; c < kept; ++c) {
+      double y = 0.0;
+#pragma unroll
+      for (int q = 0; q < kK; ++q)
+        if (q < nt) y = fma(t[q], Ms[q + nt * c], y);
+      P.V[(size_t)(nv + c) * N + e] = y;
+    }
+  }
+}
+
+// HV[from, to) = H V[from, to).
+__global__ void __launch_bounds__(kT) k_b_sigma(BCommon g) {
+  Chunk ch;
+  uint32_t e0, e1;
+  if (!sub_range(g, ch, e0, e1)) return;
+  const BState &S = g.S[ch.prob];
+  if (!S.active) return;
+  const BProb &P = g.P[ch.prob];
+  const int from = S.from, nvec = S.to - S.from;
+  const double *x = P.V + (size_t)from * P.N;
+  double *y = P.HV + (size_t)from * P.N;
   if (P.norb <= 32)
-    solve_one<uint32_t>(P, o, sm, Aw);
+    chunk_sigma_any<uint32_t>(P, nvec, x, y, e0, e1);
   else
-    solve_one<unsigned long long>(P, o, sm, Aw);
+    chunk_sigma_any<unsigned long long>(P, nvec, x, y, e0, e1);
+}
+
+// Ritz vectors V c into T (every problem, stopped or not).
+__global__ void __launch_bounds__(kT) k_b_ritz(BCommon g) {
+  __shared__ double cs[kNB * kK];
+  Chunk ch;
+  uint32_t e0, e1;
+  if (!sub_range(g, ch, e0, e1)) return;
+  const BState &S = g.S[ch.prob];
+  const BProb &P = g.P[ch.prob];
+  const uint32_t N = P.N;
+  const int nv = S.nv, kk = S.kk;
+  for (int t = threadIdx.x; t < nv * kk; t += kT) cs[t] = S.c[t];
+  __syncthreads();
+  for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
+    double xv[kK];
+#pragma unroll
+    for (int q = 0; q < kK; ++q) xv[q] = 0.0;
+    for (int j = 0; j < nv; ++j) {
+      const double vj = P.V[(size_t)j * N + e];
+#pragma unroll
+      for (int q = 0; q < kK; ++q)
+        if (q < kk) xv[q] = fma(vj, cs[j + nv * q], xv[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < kK; ++q)
+      if (q < kk) P.T[(size_t)q * N + e] = xv[q];
+  }
+}
+
+// Number of problems still iterating (one block of 1024 threads).
+__global__ void k_b_count(const BState *S, int count, int *out) {
+  __shared__ int w[32];
+  int n = 0;
+  for (int i = threadIdx.x; i < count; i += blockDim.x) n += S[i].active;
+  for (int o = 16; o > 0; o >>= 1) n += __shfl_xor_sync(0xffffffffu, n, o);
+  if ((threadIdx.x & 31) == 0) w[threadIdx.x >> 5] = n;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int t = 0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += w[i];
+    *out = t;
+  }
+}
+
+// Results: k energies, k residuals, iterations, sigma calls, converged, restarts.
+__global__ void k_b_results(const BState *S, int count, int k, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const BState &s = S[i];
+  double *o = out + (size_t)i * (2 * k + 4);
+  for (int q = 0; q < k; ++q) {
+    o[q] = q < s.kk ? s.th[q] : NAN;
+    o[k + q] = q < s.kk ? s.res[q] : NAN;
+  }
+  o[2 * k + 0] = s.iter;
+  o[2 * k + 1] = s.sigma_calls;
+  o[2 * k + 2] = s.converged;
+  o[2 * k + 3] = s.restarts;
 }
 
 }  // namespace
 
-// Solves every problem of the batch with the same options in one launch.
-// Problems must belong to one context; tables and diagonals are built here if
-// missing.  E: count x nroots energies; reps: count reports (may be null);
-// X: count pointers to host buffers of nroots x N (entries may be null).
+// Solves every problem of the batch with the same options, all problems in
+// lock step.  Problems must belong to one context; tables and diagonals are
+// built here if missing.  E: count x nroots energies; reps: count reports (may
+// be null); X: count pointers to host buffers of nroots x N (entries may be
+// null).
 void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &o, double *E, sbdgb_report *reps,
                     double **X) {
   using clock = std::chrono::steady_clock;
   const auto t0 = clock::now();
   SBDGB_REQUIRE(count >= 0, SBDGB_E_INPUT, "negative batch size");
   if (count == 0) return;
-  SBDGB_REQUIRE(o.nroots >= 1 && o.nroots <= kBMaxK, SBDGB_E_UNSUPPORTED, "the batched solver takes 1..8 roots");
+  SBDGB_REQUIRE(o.nroots >= 1 && o.nroots <= kK, SBDGB_E_UNSUPPORTED, "the batched solver takes 1..8 roots");
   SBDGB_REQUIRE(o.precision == SBDGB_FP64, SBDGB_E_UNSUPPORTED, "the batched solver runs in FP64");
   SBDGB_REQUIRE(o.init == 1, SBDGB_E_UNSUPPORTED, "the batched solver starts on the lowest diagonal (init 1)");
   cudaStream_t s = c.stream;
-  const int k = o.nroots, nb = std::min(std::max(o.max_nb, 2 * k), kBMaxNb);
-  std::vector<SmallProb> hp(count);
+  const int k = o.nroots, nb = std::min(std::max(o.max_nb, 2 * k), kNB);
+  size_t total = 0;
   for (int i = 0; i < count; ++i) {
     Problem &p = *ps[i];
     SBDGB_REQUIRE(p.ctx == &c, SBDGB_E_INPUT, "batch problems must belong to the context");
     SBDGB_REQUIRE(p.N >= (uint64_t)k, SBDGB_E_INPUT, "more roots than determinants");
+    total += p.N;
+  }
+  const size_t per_elem = (size_t)2 * nb + 2 * k;  // V, HV, T, U
+  const size_t bytes = sizeof(double) * total * per_elem;
+  SBDGB_REQUIRE(!c.budget || c.in_use + bytes <= c.budget, SBDGB_E_NOMEM,
+                "HBM budget exceeded by the batched solver's vectors");
+  for (int i = 0; i < count; ++i) {
+    Problem &p = *ps[i];
     if (!p.tables) build_tables(p, s);
     if (!p.diag) build_diag(p, s);
+  }
+  std::vector<BProb> hp(count);
+  std::vector<Chunk> chunks;
+  double *arena = (double *)tmp_alloc(&c, bytes);
+  size_t off = 0;
+  for (int i = 0; i < count; ++i) {
+    Problem &p = *ps[i];
     const size_t N = p.N;
-    double *w = (double *)workspace(p, WS_V, sizeof(double) * N * ((size_t)2 * nb + 6 * k) + 8 * (3 * k + 8));
-    SmallProb &q = hp[i];
-    q = SmallProb{};
+    BProb &q = hp[i];
+    q = BProb{};
     q.a.astr = p.astr;
     q.a.bstr = p.bstr;
     q.a.na = p.na;
@@ -592,43 +921,130 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
     q.a.npair = p.npair;
     q.N = (uint32_t)N;
     q.norb = p.norb;
-    q.V = w;
+    q.max_nb = (int)std::min<size_t>((size_t)nb, N);
+    q.max_steps = std::max(1, o.max_it) * q.max_nb;
+    q.V = arena + off;
     q.HV = q.V + N * nb;
-    q.X = q.HV + N * nb;
-    q.HX = q.X + N * 2 * k;
-    q.T = q.HX + N * 2 * k;
+    q.T = q.HV + N * nb;
     q.U = q.T + N * k;
-    q.out = q.U + N * k;
-    q.Xout = (X && X[i]) ? (double *)workspace(p, WS_C64, sizeof(double) * N * k) : nullptr;
+    off += N * per_elem;
+    q.c0 = (uint32_t)chunks.size();
+    for (size_t e0 = 0; e0 < N; e0 += kCH)
+      chunks.push_back(Chunk{(uint32_t)i, (uint32_t)e0, (uint32_t)std::min(N, e0 + kCH)});
+    q.c1 = (uint32_t)chunks.size();
   }
-  SmallProb *dp = (SmallProb *)tmp_alloc(&c, sizeof(SmallProb) * count);
-  SBDGB_CUDA(cudaMemcpyAsync(dp, hp.data(), sizeof(SmallProb) * count, cudaMemcpyHostToDevice, s));
-  SmallOpts so{k, nb, std::max(1, o.max_it) * nb, o.eps};
-  const size_t smem = sizeof(Smem) + 8 * kBMaxNb * kBMaxNb + 8;
-  SBDGB_CUDA(cudaFuncSetAttribute(k_batch_davidson, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  k_batch_davidson<<<count, kBT, smem, s>>>(dp, so);
-  count_launch(&c);
-  SBDGB_CUDA(cudaGetLastError());
-  std::vector<double> out(3 * k + 8);
-  for (int i = 0; i < count; ++i) {
-    SBDGB_CUDA(cudaMemcpyAsync(out.data(), hp[i].out, sizeof(double) * (2 * k + 4), cudaMemcpyDeviceToHost, s));
-    if (hp[i].Xout) SBDGB_CUDA(cudaMemcpyAsync(X[i], hp[i].Xout, sizeof(double) * hp[i].N * k, cudaMemcpyDeviceToHost, s));
-    SBDGB_CUDA(cudaStreamSynchronize(s));
-    for (int q = 0; q < k; ++q) E[(size_t)i * k + q] = out[q];
-    if (reps) {
-      sbdgb_report &r = reps[i];
-      r = sbdgb_report{};
-      for (int q = 0; q < k && q < 16; ++q) r.resid[q] = out[k + q];
-      r.iterations = (int)out[2 * k];
-      r.sigma_calls = r.sigma_fp64 = (int)out[2 * k + 1];
-      r.converged = (int)out[2 * k + 2];
-      r.restarts = (int)out[2 * k + 3];
+  const int nch = (int)chunks.size(), nsub = nch * kSubPer;
+  const int pstride = std::max(nb * k + k * k, 3 * kK);
+  const size_t nres = (size_t)count * (2 * k + 4);
+  const size_t meta = sizeof(BProb) * count + sizeof(BState) * count + sizeof(double) * ((size_t)nch * pstride + nres) +
+                      sizeof(Chunk) * nch + 64;
+  char *mb = nullptr;
+  try {
+    mb = (char *)tmp_alloc(&c, meta);
+  } catch (...) {
+    tmp_free(&c, arena);
+    throw;
+  }
+  BProb *dP = (BProb *)mb;
+  BState *dS = (BState *)(dP + count);
+  double *dpart = (double *)(dS + count);
+  double *dres = dpart + (size_t)nch * pstride;
+  Chunk *dch = (Chunk *)(dres + nres);
+  int *dcount = (int *)(((uintptr_t)(dch + nch) + 7) & ~(uintptr_t)7);
+  cudaGraphExec_t exec = nullptr;
+  try {
+    SBDGB_CUDA(cudaMemcpyAsync(dP, hp.data(), sizeof(BProb) * count, cudaMemcpyHostToDevice, s));
+    SBDGB_CUDA(cudaMemcpyAsync(dch, chunks.data(), sizeof(Chunk) * nch, cudaMemcpyHostToDevice, s));
+    const BCommon g{dP, dS, dch, dpart, pstride, k, o.eps};
+    auto ortho_sigma = [&] {
+      k_b_dots<<<nch, kT, 0, s>>>(g, 1);
+      k_b_gs1<<<count, 32, 0, s>>>(g);
+      k_b_project<<<nsub, kT, 0, s>>>(g);
+      k_b_dots<<<nch, kT, 0, s>>>(g, 1);
+      k_b_gs2<<<count, 32, 0, s>>>(g);
+      k_b_newcols<<<nsub, kT, 0, s>>>(g);
+      k_b_sigma<<<nsub, kT, 0, s>>>(g);
+    };
+    auto iteration = [&] {
+      k_b_dots<<<nch, kT, 0, s>>>(g, 0);
+      k_b_rr<<<count, 32, 0, s>>>(g);
+      k_b_combine<<<nch, kT, 0, s>>>(g);
+      k_b_ctl<<<count, 32, 0, s>>>(g);
+      k_b_apply<<<nsub, kT, 0, s>>>(g);
+      ortho_sigma();
+    };
+    // start vectors, their orthonormalisation and sigma
+    k_b_init<<<count, kT, 0, s>>>(g);
+    ortho_sigma();
+    count_launch(&c, 8);
+    SBDGB_CUDA(cudaGetLastError());
+    // one Davidson iteration of every problem, captured once (not on the
+    // legacy default stream, which cannot be captured)
+    if (s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread) {
+      cudaGraph_t graph = nullptr;
+      SBDGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      iteration();
+      SBDGB_CUDA(cudaStreamEndCapture(s, &graph));
+      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      SBDGB_CUDA(ie);
     }
+    int *pin = (int *)pinned_buffer(&c);
+    int max_steps = 0;
+    for (const BProb &q : hp) max_steps = std::max(max_steps, q.max_steps);
+    for (int it = 0; it <= max_steps;) {
+      const int per_check = it < 8 ? 4 : 2;
+      for (int r = 0; r < per_check; ++r, ++it) {
+        if (exec)
+          SBDGB_CUDA(cudaGraphLaunch(exec, s));
+        else
+          iteration();
+        count_launch(&c, kStepLaunches);
+      }
+      SBDGB_CUDA(cudaGetLastError());
+      k_b_count<<<1, 1024, 0, s>>>(dS, count, dcount);
+      count_launch(&c);
+      SBDGB_CUDA(cudaMemcpyAsync(pin, dcount, sizeof(int), cudaMemcpyDeviceToHost, s));
+      SBDGB_CUDA(cudaStreamSynchronize(s));
+      if (pin[0] == 0) break;
+    }
+    k_b_results<<<(count + 127) / 128, 128, 0, s>>>(dS, count, k, dres);
+    count_launch(&c);
+    if (X) {
+      k_b_ritz<<<nsub, kT, 0, s>>>(g);
+      count_launch(&c);
+    }
+    SBDGB_CUDA(cudaGetLastError());
+    std::vector<double> out(nres);
+    SBDGB_CUDA(cudaMemcpyAsync(out.data(), dres, sizeof(double) * nres, cudaMemcpyDeviceToHost, s));
+    if (X)
+      for (int i = 0; i < count; ++i)
+        if (X[i]) SBDGB_CUDA(cudaMemcpyAsync(X[i], hp[i].T, sizeof(double) * hp[i].N * k, cudaMemcpyDeviceToHost, s));
+    SBDGB_CUDA(cudaStreamSynchronize(s));
+    const double secs = std::chrono::duration<double>(clock::now() - t0).count();
+    for (int i = 0; i < count; ++i) {
+      const double *r = out.data() + (size_t)i * (2 * k + 4);
+      for (int q = 0; q < k; ++q) E[(size_t)i * k + q] = r[q];
+      if (reps) {
+        sbdgb_report &rp = reps[i];
+        rp = sbdgb_report{};
+        for (int q = 0; q < k && q < 16; ++q) rp.resid[q] = r[k + q];
+        rp.iterations = (int)r[2 * k];
+        rp.sigma_calls = rp.sigma_fp64 = (int)r[2 * k + 1];
+        rp.converged = (int)r[2 * k + 2];
+        rp.restarts = (int)r[2 * k + 3];
+        rp.seconds = secs;
+      }
+    }
+  } catch (...) {
+    if (exec) cudaGraphExecDestroy(exec);
+    tmp_free(&c, mb);
+    tmp_free(&c, arena);
+    throw;
   }
-  tmp_free(&c, dp);
-  const double secs = std::chrono::duration<double>(clock::now() - t0).count();
-  if (reps)
-    for (int i = 0; i < count; ++i) reps[i].seconds = secs;
+  if (exec) cudaGraphExecDestroy(exec);
+  tmp_free(&c, mb);
+  tmp_free(&c, arena);
 }
 
 }  // namespace sbdgb

@@ -110,9 +110,10 @@ def run_serving(reqs, cfg: int, precision: int, rate: float, workers: int, seed:
 
 
 def run_batch(reqs, cfg: int, chunk: int):
-    """The batched solver: upload and tables per problem, then one launch per
-    chunk of problems (one thread block each, the whole Davidson on the device).
-    Returns (energies, wall seconds of the whole batch, launch seconds, reports)."""
+    """The batched solver: upload and tables per problem, then one solver call per
+    chunk of problems (all problems of the chunk advanced in lock step, one
+    graph launch per Davidson iteration).
+    Returns (energies, wall seconds of the whole batch, solver seconds, reports)."""
     import torch
 
     from .engine import Engine, TPBProblem, batch_davidson
@@ -189,7 +190,7 @@ def main(argv=None) -> int:
                           "p99_s": pct(lat, 99)}
     ref_E = list(E_serial) + [None] * (n - ns)
     runs = []
-    precs = [0 if p == "fp64" else 1 for p in a.precisions.split(",")]
+    precs = [0 if p == "fp64" else 1 for p in a.precisions.split(",") if p]
     for prec in precs:
         for rate in rates:
             m = n if math.isinf(rate) else max(16, min(n, int(rate * a.max_arrival_seconds)))

@@ -130,6 +130,25 @@ def test_degenerate_lists_against_dense(engine, na, nb):
     p.close()
 
 
+@pytest.mark.parametrize("na,nb,k", [(1, 5, 4), (2, 2, 3), (3, 3, 8)])
+def test_more_than_half_the_space_in_roots(engine, na, nb, k):
+    """2 * nroots > N: the subspace is capped at N and the solver still returns the
+    lowest eigenvalues (regular and batched solvers)."""
+    from sbd_gb300.engine import batch_davidson
+    prob = make_problem(8, 3, 3, na, nb, seed=60 + na + nb)
+    p = TPBProblem.from_problem(engine, prob)
+    try:
+        p.build_tables()
+        p.diag_terms()
+        w = np.linalg.eigvalsh(Oracle.from_problem(prob).hamiltonian().toarray())
+        r = p.davidson(nroots=k, eps=1e-9, max_nb=24, init=1)
+        assert np.allclose(r.energies, w[:k], atol=1e-8)
+        rb = batch_davidson(engine, [p], nroots=k, max_nb=24, eps=1e-9)[0]
+        assert np.allclose(rb.energies, w[:k], atol=1e-8)
+    finally:
+        p.close()
+
+
 def test_more_roots_than_determinants_is_an_error(engine):
     prob = make_problem(8, 3, 3, 1, 2, seed=3)
     p = TPBProblem.from_problem(engine, prob)

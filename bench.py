@@ -19,6 +19,11 @@ diagonal resident, starting from the lowest diagonal entries).
   cpu_baseline : the CPU oracle port of the reference's TRADMODE sigma (OpenMP,
           all host cores) timed on a bounded sample of alpha rows and scaled to
           the solve's sigma count
+  serving : a bounded sample of the config-4 request mix through the request
+          loop (FP64 and mixed), against the plain FP64 path one solve at a time
+  batched : a bounded sample of the config-2 batch (256 problems by default)
+          solved in lock step by the batched solver (FP64 and mixed), against
+          the plain FP64 path one solve at a time
 
 Multi-GPU: each rank solves its own replica (the path does not shard across
 GPUs in this build): scaling "weak", value = total solves / max rank time.
@@ -306,6 +311,32 @@ def run_gpu(args):
             serving[f"loop_{name}"]["vs_plain_fp64"] = summ["solves_per_s"] / serving["plain_fp64_one_at_a_time"][
                 "solves_per_s"]
 
+    # batching: a bounded sample of the config-2 batch (norb 12, 4+4, 4 roots,
+    # tol 1e-8) solved in lock step by the batched solver, against the plain
+    # FP64 path one solve at a time on its first problems
+    batched = None
+    if rank == 0 and args.batch_problems > 0:
+        from sbd_gb300 import serve_bench as sb
+        reqs = sb.generate(2, args.batch_problems, min(16, os.cpu_count() or 1))
+        nser = min(args.batch_serial, len(reqs))
+        slat, sE = sb.run_serial(reqs[:nser], 2)
+        batched = {"workload": f"config2: first {len(reqs)} problems of the seeded batch (norb 12, 4+4 electrons, "
+                               "50-495 strings per spin, 4 roots, tol 1e-8), one batched solver call",
+                   "plain_fp64_one_at_a_time": {"problems": nser, "solves_per_s": nser / sum(slat),
+                                                "p50_s": float(np.percentile(slat, 50)),
+                                                "p99_s": float(np.percentile(slat, 99))}}
+        for prec, name in ((0, "batched_fp64"), (1, "batched_mixed")):
+            Eb, wall_b, t_solver, reps = sb.run_batch(reqs, 2, len(reqs), prec)
+            batched[name] = {"problems": len(reqs), "solves_per_s": len(reqs) / wall_b,
+                             "solver_seconds": t_solver, "wall_seconds": wall_b,
+                             "iterations_mean": float(np.mean([r["iterations"] for r in reps])),
+                             "sigma_products_mean": float(np.mean([r["sigma_calls"] for r in reps])),
+                             "fp64_sigma_products_mean": float(np.mean([r["sigma_fp64"] for r in reps])),
+                             "not_converged": sum(1 for r in reps if not r["converged"]),
+                             "max_abs_dE_vs_plain": max(float(np.max(np.abs(e - r))) for e, r in zip(Eb, sE))}
+            batched[name]["vs_plain_fp64"] = (batched[name]["solves_per_s"] /
+                                              batched["plain_fp64_one_at_a_time"]["solves_per_s"])
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -335,6 +366,7 @@ def run_gpu(args):
                          "algorithmic_bytes": bytes_sigma, "peak_kind": f"{peak_kind} hbm_gbs"},
             "mixed_precision": mixed,
             "serving": serving,
+            "batched": batched,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
             "gpu_launches": int(launches),
@@ -361,6 +393,10 @@ def main():
     ap.add_argument("--mixed-steps", type=int, default=2)
     ap.add_argument("--serve-requests", type=int, default=48, help="config-4 requests for the serving block (0: skip)")
     ap.add_argument("--serve-workers", type=int, default=16)
+    ap.add_argument("--batch-problems", type=int, default=256,
+                    help="config-2 problems for the batched block (0: skip)")
+    ap.add_argument("--batch-serial", type=int, default=32,
+                    help="of which solved one at a time on the plain FP64 path")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

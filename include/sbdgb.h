@@ -231,15 +231,20 @@ int sbdgb_davidson(sbdgb_problem *p, const sbdgb_davidson_opts *o, double *E, do
  * last change of the Ritz value and rep->restarts the cycles run. */
 int sbdgb_lanczos(sbdgb_problem *p, const sbdgb_davidson_opts *o, double *E, double *X, sbdgb_report *rep);
 
-/* Many small problems of one context solved in one launch: each problem's
- * whole FP64 Davidson (the algorithm of sbdgb_davidson, init 1) runs inside
- * one thread block, so a batch of thousands of tiny problems costs one kernel
- * launch instead of tens of launches and synchronisations per iteration each.
- * No counterpart in the reference.  Options as for sbdgb_davidson with
- * nroots 1..8, precision FP64, init 1; the subspace is capped at 32.
- * E: count*nroots energies; reps (may be NULL): count reports; X (may be
- * NULL, entries may be NULL): count host buffers of nroots*N for the Ritz
- * vectors.  Meant for problems of up to a few hundred thousand determinants. */
+/* Many small problems of one context solved together: every problem runs
+ * the Davidson of sbdgb_davidson (init 1), all of them in lock step, each step
+ * one kernel launch over all problems and each iteration one replay of a
+ * captured CUDA graph, so a batch of thousands of small problems costs a few
+ * launches per iteration instead of tens of launches and synchronisations per
+ * iteration each.  No counterpart in the reference.  Options as for
+ * sbdgb_davidson with nroots 1..8 and init 1; the subspace is capped at 32.
+ * precision MIXED runs the iteration on FP32 vectors and an FP32 sigma until
+ * every residual is below 2e-6 |E|, then in FP64 from the lowest Ritz vectors
+ * of that phase to the full tolerance (rep->sigma_fp64 counts the FP64
+ * products).  E: count*nroots energies; reps (may be NULL): count reports; X
+ * (may be NULL, entries may be NULL): count host buffers of nroots*N for the
+ * Ritz vectors.  Meant for problems of up to a few hundred thousand
+ * determinants each. */
 int sbdgb_batch_davidson(sbdgb_ctx *ctx, sbdgb_problem **problems, int count, const sbdgb_davidson_opts *o,
                          double *E, sbdgb_report *reps, double **X);
 

@@ -26,7 +26,19 @@
 //   - sigma is the fused per-element form (diagonal, alpha pairs of the row,
 //     alpha x beta singles, beta pairs of the column) for up to 8 vectors at
 //     once, sharing the index, value and phase work between the vectors.
+//
+// Mixed form (precision MIXED): FP64 arithmetic runs at 1/64 of the FP32 rate
+// on this GPU and the FP64 sigma above keeps the FP64 pipe ~97% busy, so the
+// mixed form runs the same iteration first on FP32 vectors (FP32 sigma from
+// FP32 table values, FP32 vector algebra; partial sums, projected matrix,
+// Rayleigh-Ritz and control stay FP64) until every residual is below
+// kMixedRel * |theta|, then polishes in FP64 from the lowest 2k Ritz vectors
+// of that phase (at most 8).  The FP64 phase applies the full tolerance, so
+// the energies and vectors are those of the FP64 solver; the FP32 phase only
+// removes FP64 iterations (about 60% of the FP64 sigma products on the
+// norb-12 batch).
 #include <algorithm>
+#include <type_traits>
 #include <chrono>
 #include <cmath>
 
@@ -47,6 +59,7 @@ constexpr int kSub = 512;  // elements per block of the kernels without partial 
 constexpr int kSubPer = kCH / kSub;
 constexpr int kT = 256;    // threads per element block
 constexpr int kStepLaunches = 12;
+constexpr double kMixedRel = 2e-6;  // FP32 phase: residual below this times |theta|
 
 struct Chunk {
   uint32_t prob, e0, e1;
@@ -54,15 +67,18 @@ struct Chunk {
 
 struct BProb {
   Args<double> a;  // strings, tables, integrals, diagonal (C, CT, S unused)
+  Args<float> af;  // the same with FP32 table values (mixed form)
   uint32_t N;
   int norb, max_nb, max_steps;
   double *V, *HV, *T, *U;  // nb, nb, k, k columns at stride N
+  float *Vf, *HVf, *Tf, *Uf;  // FP32 phase: the same shapes, in the first half of the region
   uint32_t c0, c1;         // chunk range of the problem
 };
 
 // Control state of one problem (device).
 struct BState {
   int active, converged, iter, sigma_calls, restarts;
+  int iter32, sigma32;  // FP32-phase iterations and sigma products (mixed form)
   int nv, kk, kc, nvprev, kprev, restart, nv_old, m, nt, from, to;
   int roots[kK];
   double th[kK], res[kK], eo[kK], n0[kK];
@@ -81,8 +97,31 @@ struct BCommon {
   double *part;  // per-chunk partial sums, pstride doubles each
   int pstride;
   int k;
-  double eps;
+  double eps;      // convergence: every residual below max(eps, eps_rel * |theta|)
+  double eps_rel;
+  int step_cap;    // iteration cap of the phase (0: the problem's max_steps)
 };
+
+template <typename T>
+struct Buf {
+  T *V, *HV, *T_, *U;
+};
+template <typename T>
+__device__ __forceinline__ Buf<T> buf(const BProb &P) {
+  if constexpr (std::is_same<T, float>::value)
+    return Buf<float>{P.Vf, P.HVf, P.Tf, P.Uf};
+  else
+    return Buf<double>{P.V, P.HV, P.T, P.U};
+}
+template <typename T>
+__device__ __forceinline__ const Args<T> &args_of(const BProb &P) {
+  if constexpr (std::is_same<T, float>::value)
+    return P.af;
+  else
+    return P.a;
+}
+__device__ __forceinline__ float fmx(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmx(double a, double b, double c) { return fma(a, b, c); }
 
 // ---- block and warp primitives ----------------------------------------------------
 
@@ -110,27 +149,29 @@ __device__ void block_reduce(const double (&v)[NV], double (*red)[32], double *o
   __syncthreads();
 }
 
-// out[i + ldo * j] = L_i . R_j over the elements [e0, e1), columns at stride N.
-__device__ void chunk_dots(const double *__restrict__ L, int nl, const double *__restrict__ R, int nr, uint32_t N,
+// out[i + ldo * j] = L_i . R_j over the elements [e0, e1), columns at stride N
+// (per-thread sums in the storage precision, block sums in FP64).
+template <typename T>
+__device__ void chunk_dots(const T *__restrict__ L, int nl, const T *__restrict__ R, int nr, uint32_t N,
                            uint32_t e0, uint32_t e1, double *out, int ldo, double (*red)[32]) {
   for (int j0 = 0; j0 < nr; j0 += 4)
     for (int i0 = 0; i0 < nl; i0 += 8) {
       const int mw = min(4, nr - j0), mv = min(8, nl - i0);
-      double acc[8][4];
+      T acc[8][4];
 #pragma unroll
       for (int i = 0; i < 8; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = 0.0;
+        for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
       for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
-        double w[4];
+        T w[4];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) w[j] = j < mw ? R[(size_t)(j0 + j) * N + e] : 0.0;
+        for (int j = 0; j < 4; ++j) w[j] = j < mw ? R[(size_t)(j0 + j) * N + e] : T(0);
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           if (i >= mv) break;
-          const double v = L[(size_t)(i0 + i) * N + e];
+          const T v = L[(size_t)(i0 + i) * N + e];
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = fma(v, w[j], acc[i][j]);
+          for (int j = 0; j < 4; ++j) acc[i][j] = fmx(v, w[j], acc[i][j]);
         }
       }
       __syncthreads();
@@ -138,7 +179,7 @@ __device__ void chunk_dots(const double *__restrict__ L, int nl, const double *_
       for (int i = 0; i < 8; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const double x = warp_sum(acc[i][j]);
+          const double x = warp_sum((double)acc[i][j]);
           if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][i * 4 + j] = x;
         }
       __syncthreads();
@@ -239,44 +280,45 @@ __device__ void warp_eig(int n, const double *A, double *Aw, double *Wv, double 
 
 // ---- sigma ---------------------------------------------------------------------------
 
-// sigma of NV vectors (columns of x at stride N) at element (ia, ib), fused form.
-template <int NV, typename Wd>
-__device__ __forceinline__ void sigma_element_mv(const Args<double> &a, const double *__restrict__ x, uint32_t N,
-                                                 uint32_t ia, uint32_t ib, double (&acc)[NV]) {
+// sigma of NV vectors (columns of x at stride N) at element (ia, ib), fused
+// form, in the storage precision T (table values of that precision).
+template <int NV, typename Wd, typename T>
+__device__ __forceinline__ void sigma_element_mv(const Args<T> &a, const T *__restrict__ x, uint32_t N, uint32_t ia,
+                                                 uint32_t ib, T (&acc)[NV]) {
   const uint32_t nb = a.nb, e = ia * nb + ib;
-  const double h = __ldg(a.hii + e);
+  const T h = (T)__ldg(a.hii + e);
 #pragma unroll
   for (int n = 0; n < NV; ++n) acc[n] = h * __ldg(x + (size_t)n * N + e);
   const Wd beta = word<Wd>(a.bstr, ib);
   // alpha singles and doubles of row ia, this column
   for (uint32_t p = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1); p < p1; ++p) {
     const uint32_t ja = __ldg(a.A.ket_s + p), code = __ldg(a.A.code_s + p);
-    const double v = __ldg(a.val_sa + p) + __ldg(a.Jb + ((code >> 16) & 0x7fffu) * nb + ib);
-    const double sv = flip(v, parity(beta & word<Wd>(a.A.mask_s, p)) ^ (code >> 31));
+    const T v = __ldg(a.val_sa + p) + __ldg(a.Jb + ((code >> 16) & 0x7fffu) * nb + ib);
+    const T sv = flip(v, parity(beta & word<Wd>(a.A.mask_s, p)) ^ (code >> 31));
     const uint32_t off = ja * nb + ib;
 #pragma unroll
-    for (int n = 0; n < NV; ++n) acc[n] = fma(sv, __ldg(x + (size_t)n * N + off), acc[n]);
+    for (int n = 0; n < NV; ++n) acc[n] = fmx(sv, __ldg(x + (size_t)n * N + off), acc[n]);
   }
   for (uint32_t p = __ldg(a.A.off_d + ia), p1 = __ldg(a.A.off_d + ia + 1); p < p1; ++p) {
     const uint32_t off = __ldg(a.A.ket_d + p) * nb + ib;
-    const double sv = flip(__ldg(a.val_da + p), parity(beta & word<Wd>(a.A.mask_d, p)));
+    const T sv = flip(__ldg(a.val_da + p), parity(beta & word<Wd>(a.A.mask_d, p)));
 #pragma unroll
-    for (int n = 0; n < NV; ++n) acc[n] = fma(sv, __ldg(x + (size_t)n * N + off), acc[n]);
+    for (int n = 0; n < NV; ++n) acc[n] = fmx(sv, __ldg(x + (size_t)n * N + off), acc[n]);
   }
   // alpha x beta singles
   const uint32_t q0 = __ldg(a.B.off_s + ib), q1 = __ldg(a.B.off_s + ib + 1);
   for (uint32_t p = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1); p < p1; ++p) {
     const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
     const Wd alpha_ket = word<Wd>(a.astr, ja);
-    const double *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
+    const T *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
     const uint32_t pa = parity(beta & word<Wd>(a.A.mask_s, p)) ^ (ca >> 31);
     const uint32_t rowoff = ja * nb;
     for (uint32_t q = q0; q < q1; ++q) {
       const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
       const uint32_t ph = (pa ^ parity(alpha_ket & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31)) & 1u;
-      const double kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
+      const T kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
 #pragma unroll
-      for (int n = 0; n < NV; ++n) acc[n] = fma(kv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
+      for (int n = 0; n < NV; ++n) acc[n] = fmx(kv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
     }
   }
   // beta singles and doubles of column ib, this row
@@ -284,41 +326,42 @@ __device__ __forceinline__ void sigma_element_mv(const Args<double> &a, const do
   const uint32_t rowoff = ia * nb;
   for (uint32_t q = q0; q < q1; ++q) {
     const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-    const double sv = flip(__ldg(a.val_sb + q) + __ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia),
-                           parity(arow & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31));
+    const T sv = flip(__ldg(a.val_sb + q) + __ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia),
+                      parity(arow & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31));
 #pragma unroll
-    for (int n = 0; n < NV; ++n) acc[n] = fma(sv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
+    for (int n = 0; n < NV; ++n) acc[n] = fmx(sv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
   }
   for (uint32_t q = __ldg(a.B.off_d + ib), q1d = __ldg(a.B.off_d + ib + 1); q < q1d; ++q) {
     const uint32_t jb = __ldg(a.B.ket_d + q);
-    const double sv = flip(__ldg(a.val_db + q), parity(arow & word<Wd>(a.B.mask_d, q)));
+    const T sv = flip(__ldg(a.val_db + q), parity(arow & word<Wd>(a.B.mask_d, q)));
 #pragma unroll
-    for (int n = 0; n < NV; ++n) acc[n] = fma(sv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
+    for (int n = 0; n < NV; ++n) acc[n] = fmx(sv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
   }
 }
 
-template <int NV, typename Wd>
-__device__ void chunk_sigma(const BProb &P, const double *x, double *y, uint32_t e0, uint32_t e1) {
-  const uint32_t nb = P.a.nb;
+template <int NV, typename Wd, typename T>
+__device__ void chunk_sigma(const BProb &P, const T *x, T *y, uint32_t e0, uint32_t e1) {
+  const Args<T> &a = args_of<T>(P);
+  const uint32_t nb = a.nb;
   for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
-    double acc[NV];
-    sigma_element_mv<NV, Wd>(P.a, x, P.N, e / nb, e % nb, acc);
+    T acc[NV];
+    sigma_element_mv<NV, Wd, T>(a, x, P.N, e / nb, e % nb, acc);
 #pragma unroll
     for (int n = 0; n < NV; ++n) y[(size_t)n * P.N + e] = acc[n];
   }
 }
 
-template <typename Wd>
-__device__ void chunk_sigma_any(const BProb &P, int nvec, const double *x, double *y, uint32_t e0, uint32_t e1) {
+template <typename Wd, typename T>
+__device__ void chunk_sigma_any(const BProb &P, int nvec, const T *x, T *y, uint32_t e0, uint32_t e1) {
   switch (nvec) {
-    case 1: chunk_sigma<1, Wd>(P, x, y, e0, e1); break;
-    case 2: chunk_sigma<2, Wd>(P, x, y, e0, e1); break;
-    case 3: chunk_sigma<3, Wd>(P, x, y, e0, e1); break;
-    case 4: chunk_sigma<4, Wd>(P, x, y, e0, e1); break;
-    case 5: chunk_sigma<5, Wd>(P, x, y, e0, e1); break;
-    case 6: chunk_sigma<6, Wd>(P, x, y, e0, e1); break;
-    case 7: chunk_sigma<7, Wd>(P, x, y, e0, e1); break;
-    default: chunk_sigma<8, Wd>(P, x, y, e0, e1); break;
+    case 1: chunk_sigma<1, Wd, T>(P, x, y, e0, e1); break;
+    case 2: chunk_sigma<2, Wd, T>(P, x, y, e0, e1); break;
+    case 3: chunk_sigma<3, Wd, T>(P, x, y, e0, e1); break;
+    case 4: chunk_sigma<4, Wd, T>(P, x, y, e0, e1); break;
+    case 5: chunk_sigma<5, Wd, T>(P, x, y, e0, e1); break;
+    case 6: chunk_sigma<6, Wd, T>(P, x, y, e0, e1); break;
+    case 7: chunk_sigma<7, Wd, T>(P, x, y, e0, e1); break;
+    default: chunk_sigma<8, Wd, T>(P, x, y, e0, e1); break;
   }
 }
 
@@ -327,11 +370,13 @@ __device__ void chunk_sigma_any(const BProb &P, int nvec, const double *x, doubl
 // Start vectors (one block per problem): unit vectors on the k lowest diagonal
 // entries (ties by index) plus a deterministic splitmix64 component of total
 // size 1e-3, in T; the state is set for the first orthonormalisation.
+template <typename T>
 __global__ void __launch_bounds__(kT) k_b_init(BCommon g) {
   __shared__ double dv[kT / 32];
   __shared__ unsigned long long di[kT / 32], pos[kK];
   const BProb &P = g.P[blockIdx.x];
   BState &S = g.S[blockIdx.x];
+  T *Tb = buf<T>(P).T_;
   const uint32_t N = P.N;
   const int k = g.k;
   for (int q = 0; q < k; ++q) {
@@ -380,11 +425,13 @@ __global__ void __launch_bounds__(kT) k_b_init(BCommon g) {
       z ^= z >> 27;
       z *= 0x94D049BB133111EBull;
       z ^= z >> 31;
-      P.T[(size_t)q * N + e] = (e == pos[q] ? 1.0 : 0.0) + amp * ((double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0);
+      Tb[(size_t)q * N + e] =
+          (T)((e == pos[q] ? 1.0 : 0.0) + amp * ((double)(z >> 11) * (2.0 / 9007199254740992.0) - 1.0));
     }
   if (threadIdx.x == 0) {
     S.active = 1;
     S.converged = S.iter = S.sigma_calls = S.restarts = 0;
+    S.iter32 = S.sigma32 = 0;
     S.nv = S.kk = S.kc = S.nvprev = S.kprev = S.restart = S.nv_old = S.m = S.from = S.to = 0;
     S.nt = k;
     for (int q = 0; q < kK; ++q) {
@@ -394,28 +441,52 @@ __global__ void __launch_bounds__(kT) k_b_init(BCommon g) {
   }
 }
 
+// Mixed form, between the phases (one thread per problem): the FP32 phase's
+// counters are kept aside and the state is set to orthonormalise the seed
+// vectors (the lowest kc Ritz vectors of the FP32 phase, at most 8, written to
+// the FP64 correction block by k_b_ritz) for the FP64 phase.
+__global__ void k_b_seed_state(BCommon g, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const BProb &P = g.P[i];
+  BState &S = g.S[i];
+  S.iter32 = S.iter;
+  S.sigma32 = S.sigma_calls;
+  S.active = 1;
+  S.converged = S.iter = S.sigma_calls = S.restarts = 0;
+  S.nt = min(min(S.kc, P.max_nb), kK);
+  S.nv = S.kk = S.kc = S.nvprev = S.kprev = S.restart = S.nv_old = S.m = S.from = S.to = 0;
+  for (int q = 0; q < kK; ++q) {
+    S.roots[q] = q;
+    S.th[q] = S.res[q] = S.eo[q] = S.n0[q] = 0.0;
+  }
+}
+
 // Partial dot products of one chunk.  mode 0: V[0, to)^T HV[from, to) (the new
 // columns of the projected matrix); mode 1: V[0, nv)^T T[0, nt) followed by the
 // Gram matrix T^T T.
+template <typename T>
 __global__ void __launch_bounds__(kT) k_b_dots(BCommon g, int mode) {
   __shared__ double red[kT / 32][32];
   const Chunk ch = g.ch[blockIdx.x];
   const BState &S = g.S[ch.prob];
   if (!S.active) return;
   const BProb &P = g.P[ch.prob];
+  const Buf<T> b = buf<T>(P);
   double *out = g.part + (size_t)blockIdx.x * g.pstride;
   if (mode == 0) {
     const int nl = S.to, nr = S.to - S.from;
-    chunk_dots(P.V, nl, P.HV + (size_t)S.from * P.N, nr, P.N, ch.e0, ch.e1, out, nl, red);
+    chunk_dots<T>(b.V, nl, b.HV + (size_t)S.from * P.N, nr, P.N, ch.e0, ch.e1, out, nl, red);
   } else {
     const int nl = S.nv, nr = S.nt;
-    chunk_dots(P.V, nl, P.T, nr, P.N, ch.e0, ch.e1, out, nl, red);
-    chunk_dots(P.T, nr, P.T, nr, P.N, ch.e0, ch.e1, out + nl * nr, nr, red);
+    chunk_dots<T>(b.V, nl, b.T_, nr, P.N, ch.e0, ch.e1, out, nl, red);
+    chunk_dots<T>(b.T_, nr, b.T_, nr, P.N, ch.e0, ch.e1, out + nl * nr, nr, red);
   }
 }
 
 // Rayleigh-Ritz (one warp per problem): the new columns of the projected
-// matrix from the mode-0 partials, then its lowest kk eigenpairs.
+// matrix from the mode-0 partials, then its eigenpairs; the coefficients of
+// the lowest kc = min(2k, nv) Ritz vectors are kept.
 __global__ void __launch_bounds__(32) k_b_rr(BCommon g) {
   __shared__ double Aw[kNB * kNB], Wv[kNB * kNB], E[kNB];
   const BProb &P = g.P[blockIdx.x];
@@ -443,50 +514,55 @@ __global__ void __launch_bounds__(32) k_b_rr(BCommon g) {
 
 // Residuals and Olsen-corrected preconditioned corrections of the kk Ritz
 // pairs: T = r / (theta - d), U = x / (theta - d); partials of |r|^2, x.T, x.U.
+template <typename T>
 __global__ void __launch_bounds__(kT) k_b_combine(BCommon g) {
   __shared__ double red[kT / 32][32];
-  __shared__ double cs[kNB * kK], th[kK];
+  __shared__ T cs[kNB * kK], th[kK];
   const Chunk ch = g.ch[blockIdx.x];
   const BState &S = g.S[ch.prob];
   if (!S.active) return;
   const BProb &P = g.P[ch.prob];
+  const Buf<T> b = buf<T>(P);
   const int nv = S.nv, kk = S.kk;
   const uint32_t N = P.N;
-  for (int t = threadIdx.x; t < nv * kk; t += kT) cs[t] = S.c[t];
-  if (threadIdx.x < kk) th[threadIdx.x] = S.th[threadIdx.x];
+  for (int t = threadIdx.x; t < nv * kk; t += kT) cs[t] = (T)S.c[t];
+  if (threadIdx.x < kk) th[threadIdx.x] = (T)S.th[threadIdx.x];
   __syncthreads();
-  double acc[3 * kK];
+  T acc[3 * kK];
 #pragma unroll
-  for (int i = 0; i < 3 * kK; ++i) acc[i] = 0.0;
+  for (int i = 0; i < 3 * kK; ++i) acc[i] = T(0);
   for (uint32_t e = ch.e0 + threadIdx.x; e < ch.e1; e += kT) {
-    double xv[kK], hv[kK];
+    T xv[kK], hv[kK];
 #pragma unroll
-    for (int q = 0; q < kK; ++q) xv[q] = hv[q] = 0.0;
+    for (int q = 0; q < kK; ++q) xv[q] = hv[q] = T(0);
     for (int j = 0; j < nv; ++j) {
-      const double vj = P.V[(size_t)j * N + e], hj = P.HV[(size_t)j * N + e];
+      const T vj = b.V[(size_t)j * N + e], hj = b.HV[(size_t)j * N + e];
 #pragma unroll
       for (int q = 0; q < kK; ++q)
         if (q < kk) {
-          xv[q] = fma(vj, cs[j + nv * q], xv[q]);
-          hv[q] = fma(hj, cs[j + nv * q], hv[q]);
+          xv[q] = fmx(vj, cs[j + nv * q], xv[q]);
+          hv[q] = fmx(hj, cs[j + nv * q], hv[q]);
         }
     }
-    const double d = P.a.hii[e];
+    const T d = (T)P.a.hii[e];
 #pragma unroll
     for (int q = 0; q < kK; ++q)
       if (q < kk) {
-        const double r = hv[q] - th[q] * xv[q];
-        double den = th[q] - d;
-        if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
-        const double t = r / den, u = xv[q] / den;
-        P.T[(size_t)q * N + e] = t;
-        P.U[(size_t)q * N + e] = u;
-        acc[q] = fma(r, r, acc[q]);
-        acc[kK + q] = fma(xv[q], t, acc[kK + q]);
-        acc[2 * kK + q] = fma(xv[q], u, acc[2 * kK + q]);
+        const T r = hv[q] - th[q] * xv[q];
+        T den = th[q] - d;
+        if (fabs(den) <= T(1.0e-12)) den -= T(1.0e-12);
+        const T t = r / den, u = xv[q] / den;
+        b.T_[(size_t)q * N + e] = t;
+        b.U[(size_t)q * N + e] = u;
+        acc[q] = fmx(r, r, acc[q]);
+        acc[kK + q] = fmx(xv[q], t, acc[kK + q]);
+        acc[2 * kK + q] = fmx(xv[q], u, acc[2 * kK + q]);
       }
   }
-  block_reduce<3 * kK>(acc, red, g.part + (size_t)blockIdx.x * g.pstride);
+  double accd[3 * kK];
+#pragma unroll
+  for (int i = 0; i < 3 * kK; ++i) accd[i] = (double)acc[i];
+  block_reduce<3 * kK>(accd, red, g.part + (size_t)blockIdx.x * g.pstride);
 }
 
 // Control after the residuals (one warp per problem): residual norms, Olsen
@@ -508,12 +584,14 @@ __global__ void __launch_bounds__(32) k_b_ctl(BCommon g) {
       const double a1 = sums[kK + q], a2 = sums[2 * kK + q];
       S.res[q] = sqrt(fmax(0.0, sums[q]));
       S.eo[q] = (a2 != 0.0 && isfinite(a1 / a2)) ? a1 / a2 : 0.0;
-      conv = conv && (S.res[q] < g.eps);
-      nnew += (S.res[q] >= g.eps);
+      const bool ok = S.res[q] < fmax(g.eps, g.eps_rel * fabs(S.th[q]));
+      conv = conv && ok;
+      nnew += !ok;
     }
     S.restart = 0;
     flag[0] = 0;
-    if (conv || S.iter >= P.max_steps) {
+    const int cap = g.step_cap > 0 ? min(g.step_cap, P.max_steps) : P.max_steps;
+    if (conv || S.iter >= cap) {
       S.converged = conv;
       S.active = 0;
       flag[0] = 1;
@@ -549,7 +627,7 @@ __global__ void __launch_bounds__(32) k_b_ctl(BCommon g) {
     if (!flag[0]) {
       int nt = 0;
       for (int q = 0; q < kk; ++q)
-        if (S.res[q] >= g.eps) S.roots[nt++] = q;
+        if (!(S.res[q] < fmax(g.eps, g.eps_rel * fabs(S.th[q])))) S.roots[nt++] = q;
       nt = min(nt, P.max_nb - (S.restart ? S.m : nv));
       if (nt <= 0) {  // no room for a new direction: the subspace is the whole space
         S.converged = 0;
@@ -595,6 +673,7 @@ __global__ void __launch_bounds__(32) k_b_ctl(BCommon g) {
     if (l == 0) {
       S.nv_old = nv;
       S.nv = m;
+      S.kc = kk;  // only the kk Ritz coefficient vectors follow the restart
       S.restarts++;
     }
     __syncwarp();
@@ -610,8 +689,9 @@ __global__ void __launch_bounds__(32) k_b_ctl(BCommon g) {
 // Element updates after the control step: the restart V <- V Q, HV <- HV Q
 // (per element, in registers), then the Olsen update T - eo U of the
 // unconverged roots, packed at the front of T.
+template <typename T>
 __global__ void __launch_bounds__(kT) k_b_apply(BCommon g) {
-  __shared__ double Qs[kNB * kR], eo[kK];
+  __shared__ T Qs[kNB * kR], eo[kK];
   __shared__ int roots[kK];
   Chunk ch;
   uint32_t e0, e1;
@@ -619,41 +699,42 @@ __global__ void __launch_bounds__(kT) k_b_apply(BCommon g) {
   const BState &S = g.S[ch.prob];
   if (!S.active) return;
   const BProb &P = g.P[ch.prob];
+  const Buf<T> bf = buf<T>(P);
   const uint32_t N = P.N;
   const int restart = S.restart, nvo = S.nv_old, m = S.m, nt = S.nt;
   if (restart)
-    for (int t = threadIdx.x; t < nvo * m; t += kT) Qs[t] = S.Q[t];
+    for (int t = threadIdx.x; t < nvo * m; t += kT) Qs[t] = (T)S.Q[t];
   if (threadIdx.x < kK) {
-    eo[threadIdx.x] = S.eo[threadIdx.x];
+    eo[threadIdx.x] = (T)S.eo[threadIdx.x];
     roots[threadIdx.x] = S.roots[threadIdx.x];
   }
   __syncthreads();
   for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
     if (restart) {
       for (int pass = 0; pass < 2; ++pass) {
-        double *B = pass == 0 ? P.V : P.HV;
-        double vin[kNB];
+        T *B = pass == 0 ? bf.V : bf.HV;
+        T vin[kNB];
 #pragma unroll
-        for (int j = 0; j < kNB; ++j) vin[j] = j < nvo ? B[(size_t)j * N + e] : 0.0;
+        for (int j = 0; j < kNB; ++j) vin[j] = j < nvo ? B[(size_t)j * N + e] : T(0);
         for (int b = 0; b < m; ++b) {
-          double y = 0.0;
+          T y = T(0);
 #pragma unroll
           for (int j = 0; j < kNB; ++j)
-            if (j < nvo) y = fma(vin[j], Qs[j + nvo * b], y);
+            if (j < nvo) y = fmx(vin[j], Qs[j + nvo * b], y);
           B[(size_t)b * N + e] = y;
         }
       }
     }
-    double t[kK];
+    T t[kK];
 #pragma unroll
     for (int i = 0; i < kK; ++i)
       if (i < nt) {
         const int r = roots[i];
-        t[i] = fma(-eo[r], P.U[(size_t)r * N + e], P.T[(size_t)r * N + e]);
+        t[i] = fmx(-eo[r], bf.U[(size_t)r * N + e], bf.T_[(size_t)r * N + e]);
       }
 #pragma unroll
     for (int i = 0; i < kK; ++i)
-      if (i < nt) P.T[(size_t)i * N + e] = t[i];
+      if (i < nt) bf.T_[(size_t)i * N + e] = t[i];
   }
 }
 
@@ -669,32 +750,34 @@ __global__ void __launch_bounds__(32) k_b_gs1(BCommon g) {
 }
 
 // T <- T - V G.
+template <typename T>
 __global__ void __launch_bounds__(kT) k_b_project(BCommon g) {
-  __shared__ double Gs[kNB * kK];
+  __shared__ T Gs[kNB * kK];
   Chunk ch;
   uint32_t e0, e1;
   if (!sub_range(g, ch, e0, e1)) return;
   const BState &S = g.S[ch.prob];
   if (!S.active) return;
   const BProb &P = g.P[ch.prob];
+  const Buf<T> bf = buf<T>(P);
   const uint32_t N = P.N;
   const int nv = S.nv, nt = S.nt;
   if (nv == 0) return;
-  for (int t = threadIdx.x; t < nv * nt; t += kT) Gs[t] = S.G[t];
+  for (int t = threadIdx.x; t < nv * nt; t += kT) Gs[t] = (T)S.G[t];
   __syncthreads();
   for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
-    double t[kK];
+    T t[kK];
 #pragma unroll
-    for (int q = 0; q < kK; ++q) t[q] = q < nt ? P.T[(size_t)q * N + e] : 0.0;
+    for (int q = 0; q < kK; ++q) t[q] = q < nt ? bf.T_[(size_t)q * N + e] : T(0);
     for (int j = 0; j < nv; ++j) {
-      const double vj = P.V[(size_t)j * N + e];
+      const T vj = bf.V[(size_t)j * N + e];
 #pragma unroll
       for (int q = 0; q < kK; ++q)
-        if (q < nt) t[q] = fma(-vj, Gs[j + nv * q], t[q]);
+        if (q < nt) t[q] = fmx(-vj, Gs[j + nv * q], t[q]);
     }
 #pragma unroll
     for (int q = 0; q < kK; ++q)
-      if (q < nt) P.T[(size_t)q * N + e] = t[q];
+      if (q < nt) bf.T_[(size_t)q * N + e] = t[q];
   }
 }
 
@@ -752,40 +835,43 @@ __global__ void __launch_bounds__(32) k_b_gs2(BCommon g) {
 }
 
 // New basis columns V[nv + c] = (T - V G) M.
+template <typename T>
 __global__ void __launch_bounds__(kT) k_b_newcols(BCommon g) {
-  __shared__ double Gs[kNB * kK], Ms[kK * kK];
+  __shared__ T Gs[kNB * kK], Ms[kK * kK];
   Chunk ch;
   uint32_t e0, e1;
   if (!sub_range(g, ch, e0, e1)) return;
   const BState &S = g.S[ch.prob];
   if (!S.active) return;
   const BProb &P = g.P[ch.prob];
+  const Buf<T> bf = buf<T>(P);
   const uint32_t N = P.N;
   const int nv = S.nv, nt = S.nt, kept = S.to - S.from;
-  for (int t = threadIdx.x; t < nv * nt; t += kT) Gs[t] = S.G[t];
-  for (int t = threadIdx.x; t < nt * kept; t += kT) Ms[t] = S.M[t];
+  for (int t = threadIdx.x; t < nv * nt; t += kT) Gs[t] = (T)S.G[t];
+  for (int t = threadIdx.x; t < nt * kept; t += kT) Ms[t] = (T)S.M[t];
   __syncthreads();
   for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
-    double t[kK];
+    T t[kK];
 #pragma unroll
-    for (int q = 0; q < kK; ++q) t[q] = q < nt ? P.T[(size_t)q * N + e] : 0.0;
+    for (int q = 0; q < kK; ++q) t[q] = q < nt ? bf.T_[(size_t)q * N + e] : T(0);
     for (int j = 0; j < nv; ++j) {
-      const double vj = P.V[(size_t)j * N + e];
+      const T vj = bf.V[(size_t)j * N + e];
 #pragma unroll
       for (int q = 0; q < kK; ++q)
-        if (q < nt) t[q] = fma(-vj, Gs[j + nv * q], t[q]);
+        if (q < nt) t[q] = fmx(-vj, Gs[j + nv * q], t[q]);
     }
     for (int c = 0; c < kept; ++c) {
-      double y = 0.0;
+      T y = T(0);
 #pragma unroll
       for (int q = 0; q < kK; ++q)
-        if (q < nt) y = fma(t[q], Ms[q + nt * c], y);
-      P.V[(size_t)(nv + c) * N + e] = y;
+        if (q < nt) y = fmx(t[q], Ms[q + nt * c], y);
+      bf.V[(size_t)(nv + c) * N + e] = y;
     }
   }
 }
 
 // HV[from, to) = H V[from, to).
+template <typename T>
 __global__ void __launch_bounds__(kT) k_b_sigma(BCommon g) {
   Chunk ch;
   uint32_t e0, e1;
@@ -793,40 +879,45 @@ __global__ void __launch_bounds__(kT) k_b_sigma(BCommon g) {
   const BState &S = g.S[ch.prob];
   if (!S.active) return;
   const BProb &P = g.P[ch.prob];
+  const Buf<T> bf = buf<T>(P);
   const int from = S.from, nvec = S.to - S.from;
-  const double *x = P.V + (size_t)from * P.N;
-  double *y = P.HV + (size_t)from * P.N;
+  const T *x = bf.V + (size_t)from * P.N;
+  T *y = bf.HV + (size_t)from * P.N;
   if (P.norb <= 32)
-    chunk_sigma_any<uint32_t>(P, nvec, x, y, e0, e1);
+    chunk_sigma_any<uint32_t, T>(P, nvec, x, y, e0, e1);
   else
-    chunk_sigma_any<unsigned long long>(P, nvec, x, y, e0, e1);
+    chunk_sigma_any<unsigned long long, T>(P, nvec, x, y, e0, e1);
 }
 
-// Ritz vectors V c into T (every problem, stopped or not).
-__global__ void __launch_bounds__(kT) k_b_ritz(BCommon g) {
-  __shared__ double cs[kNB * kK];
+// Ritz vectors V c, in FP64, into the FP64 correction block (T, then U): the
+// kk wanted ones (seed 0: the solver's output), or the lowest kc (seed 1: the
+// start of the FP64 phase of the mixed form).  Every problem, stopped or not.
+template <typename T>
+__global__ void __launch_bounds__(kT) k_b_ritz(BCommon g, int seed) {
+  __shared__ double cs[kNB * 2 * kK];
   Chunk ch;
   uint32_t e0, e1;
   if (!sub_range(g, ch, e0, e1)) return;
   const BState &S = g.S[ch.prob];
   const BProb &P = g.P[ch.prob];
+  const T *V = buf<T>(P).V;
   const uint32_t N = P.N;
-  const int nv = S.nv, kk = S.kk;
-  for (int t = threadIdx.x; t < nv * kk; t += kT) cs[t] = S.c[t];
+  const int nv = S.nv, nc = seed ? min(S.kc, kK) : S.kk;
+  for (int t = threadIdx.x; t < nv * nc; t += kT) cs[t] = S.c[t];
   __syncthreads();
   for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
     double xv[kK];
 #pragma unroll
     for (int q = 0; q < kK; ++q) xv[q] = 0.0;
     for (int j = 0; j < nv; ++j) {
-      const double vj = P.V[(size_t)j * N + e];
+      const double vj = (double)V[(size_t)j * N + e];
 #pragma unroll
       for (int q = 0; q < kK; ++q)
-        if (q < kk) xv[q] = fma(vj, cs[j + nv * q], xv[q]);
+        if (q < nc) xv[q] = fma(vj, cs[j + nv * q], xv[q]);
     }
 #pragma unroll
     for (int q = 0; q < kK; ++q)
-      if (q < kk) P.T[(size_t)q * N + e] = xv[q];
+      if (q < nc) P.T[(size_t)q * N + e] = xv[q];
   }
 }
 
@@ -845,29 +936,31 @@ __global__ void k_b_count(const BState *S, int count, int *out) {
   }
 }
 
-// Results: k energies, k residuals, iterations, sigma calls, converged, restarts.
+// Results: k energies, k residuals, iterations, sigma calls, converged,
+// restarts, FP64 sigma calls.
 __global__ void k_b_results(const BState *S, int count, int k, double *out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= count) return;
   const BState &s = S[i];
-  double *o = out + (size_t)i * (2 * k + 4);
+  double *o = out + (size_t)i * (2 * k + 5);
   for (int q = 0; q < k; ++q) {
     o[q] = q < s.kk ? s.th[q] : NAN;
     o[k + q] = q < s.kk ? s.res[q] : NAN;
   }
-  o[2 * k + 0] = s.iter;
-  o[2 * k + 1] = s.sigma_calls;
+  o[2 * k + 0] = s.iter + s.iter32;
+  o[2 * k + 1] = s.sigma_calls + s.sigma32;
   o[2 * k + 2] = s.converged;
   o[2 * k + 3] = s.restarts;
+  o[2 * k + 4] = s.sigma_calls;
 }
 
 }  // namespace
 
 // Solves every problem of the batch with the same options, all problems in
-// lock step.  Problems must belong to one context; tables and diagonals are
-// built here if missing.  E: count x nroots energies; reps: count reports (may
-// be null); X: count pointers to host buffers of nroots x N (entries may be
-// null).
+// lock step (precision FP64, or MIXED: an FP32 phase then the FP64 phase).
+// Problems must belong to one context; tables and diagonals are built here if
+// missing.  E: count x nroots energies; reps: count reports (may be null); X:
+// count pointers to host buffers of nroots x N (entries may be null).
 void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &o, double *E, sbdgb_report *reps,
                     double **X) {
   using clock = std::chrono::steady_clock;
@@ -875,8 +968,9 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
   SBDGB_REQUIRE(count >= 0, SBDGB_E_INPUT, "negative batch size");
   if (count == 0) return;
   SBDGB_REQUIRE(o.nroots >= 1 && o.nroots <= kK, SBDGB_E_UNSUPPORTED, "the batched solver takes 1..8 roots");
-  SBDGB_REQUIRE(o.precision == SBDGB_FP64, SBDGB_E_UNSUPPORTED, "the batched solver runs in FP64");
+  SBDGB_REQUIRE(o.precision == SBDGB_FP64 || o.precision == SBDGB_MIXED, SBDGB_E_INPUT, "unknown precision");
   SBDGB_REQUIRE(o.init == 1, SBDGB_E_UNSUPPORTED, "the batched solver starts on the lowest diagonal (init 1)");
+  const bool mixed = o.precision == SBDGB_MIXED;
   cudaStream_t s = c.stream;
   const int k = o.nroots, nb = std::min(std::max(o.max_nb, 2 * k), kNB);
   size_t total = 0;
@@ -886,7 +980,9 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
     SBDGB_REQUIRE(p.N >= (uint64_t)k, SBDGB_E_INPUT, "more roots than determinants");
     total += p.N;
   }
-  const size_t per_elem = (size_t)2 * nb + 2 * k;  // V, HV, T, U
+  // per problem: V, HV (nb columns each), T, U (k each) in FP64; the FP32
+  // phase uses the same shapes in the first half of the region
+  const size_t per_elem = (size_t)2 * nb + 2 * k;
   const size_t bytes = sizeof(double) * total * per_elem;
   SBDGB_REQUIRE(!c.budget || c.in_use + bytes <= c.budget, SBDGB_E_NOMEM,
                 "HBM budget exceeded by the batched solver's vectors");
@@ -894,6 +990,7 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
     Problem &p = *ps[i];
     if (!p.tables) build_tables(p, s);
     if (!p.diag) build_diag(p, s);
+    if (mixed) prepare_mixed(p, s);
   }
   std::vector<BProb> hp(count);
   std::vector<Chunk> chunks;
@@ -919,6 +1016,23 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
     q.a.Ja = p.Ja;
     q.a.Kp = p.Kp;
     q.a.npair = p.npair;
+    if (mixed) {
+      q.af.astr = p.astr;
+      q.af.bstr = p.bstr;
+      q.af.na = p.na;
+      q.af.nb = p.nb;
+      q.af.hii = p.hii;
+      q.af.A = p.A;
+      q.af.B = p.B;
+      q.af.val_sa = p.val_sf[0];
+      q.af.val_da = p.val_df[0];
+      q.af.val_sb = p.val_sf[1];
+      q.af.val_db = p.val_df[1];
+      q.af.Jb = p.Jbf;
+      q.af.Ja = p.Jaf;
+      q.af.Kp = p.Kpf;
+      q.af.npair = p.npair;
+    }
     q.N = (uint32_t)N;
     q.norb = p.norb;
     q.max_nb = (int)std::min<size_t>((size_t)nb, N);
@@ -927,6 +1041,10 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
     q.HV = q.V + N * nb;
     q.T = q.HV + N * nb;
     q.U = q.T + N * k;
+    q.Vf = (float *)q.V;
+    q.HVf = q.Vf + N * nb;
+    q.Tf = q.HVf + N * nb;
+    q.Uf = q.Tf + N * k;
     off += N * per_elem;
     q.c0 = (uint32_t)chunks.size();
     for (size_t e0 = 0; e0 < N; e0 += kCH)
@@ -934,8 +1052,10 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
     q.c1 = (uint32_t)chunks.size();
   }
   const int nch = (int)chunks.size(), nsub = nch * kSubPer;
-  const int pstride = std::max(nb * k + k * k, 3 * kK);
-  const size_t nres = (size_t)count * (2 * k + 4);
+  const int nseed = std::min(2 * k, kK);
+  const int pstride = std::max({nb * k + k * k, nseed * nseed, 3 * kK});
+  const int rstride = 2 * k + 5;
+  const size_t nres = (size_t)count * rstride;
   const size_t meta = sizeof(BProb) * count + sizeof(BState) * count + sizeof(double) * ((size_t)nch * pstride + nres) +
                       sizeof(Chunk) * nch + 64;
   char *mb = nullptr;
@@ -955,63 +1075,85 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
   try {
     SBDGB_CUDA(cudaMemcpyAsync(dP, hp.data(), sizeof(BProb) * count, cudaMemcpyHostToDevice, s));
     SBDGB_CUDA(cudaMemcpyAsync(dch, chunks.data(), sizeof(Chunk) * nch, cudaMemcpyHostToDevice, s));
-    const BCommon g{dP, dS, dch, dpart, pstride, k, o.eps};
-    auto ortho_sigma = [&] {
-      k_b_dots<<<nch, kT, 0, s>>>(g, 1);
-      k_b_gs1<<<count, 32, 0, s>>>(g);
-      k_b_project<<<nsub, kT, 0, s>>>(g);
-      k_b_dots<<<nch, kT, 0, s>>>(g, 1);
-      k_b_gs2<<<count, 32, 0, s>>>(g);
-      k_b_newcols<<<nsub, kT, 0, s>>>(g);
-      k_b_sigma<<<nsub, kT, 0, s>>>(g);
-    };
-    auto iteration = [&] {
-      k_b_dots<<<nch, kT, 0, s>>>(g, 0);
-      k_b_rr<<<count, 32, 0, s>>>(g);
-      k_b_combine<<<nch, kT, 0, s>>>(g);
-      k_b_ctl<<<count, 32, 0, s>>>(g);
-      k_b_apply<<<nsub, kT, 0, s>>>(g);
-      ortho_sigma();
-    };
-    // start vectors, their orthonormalisation and sigma
-    k_b_init<<<count, kT, 0, s>>>(g);
-    ortho_sigma();
-    count_launch(&c, 8);
-    SBDGB_CUDA(cudaGetLastError());
-    // one Davidson iteration of every problem, captured once (not on the
-    // legacy default stream, which cannot be captured)
-    if (s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread) {
-      cudaGraph_t graph = nullptr;
-      SBDGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      iteration();
-      SBDGB_CUDA(cudaStreamEndCapture(s, &graph));
-      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-      cudaGraphDestroy(graph);
-      SBDGB_CUDA(ie);
-    }
     int *pin = (int *)pinned_buffer(&c);
     int max_steps = 0;
     for (const BProb &q : hp) max_steps = std::max(max_steps, q.max_steps);
-    for (int it = 0; it <= max_steps;) {
-      const int per_check = it < 8 ? 4 : 2;
-      for (int r = 0; r < per_check; ++r, ++it) {
-        if (exec)
-          SBDGB_CUDA(cudaGraphLaunch(exec, s));
-        else
-          iteration();
-        count_launch(&c, kStepLaunches);
-      }
+    // One phase: orthonormalise the start block and take its sigma, then
+    // iterate (one captured graph per Davidson iteration of every problem)
+    // until no problem is active.
+    auto run_phase = [&](auto tag, const BCommon &g, int steps) {
+      using T = decltype(tag);
+      auto ortho_sigma = [&] {
+        k_b_dots<T><<<nch, kT, 0, s>>>(g, 1);
+        k_b_gs1<<<count, 32, 0, s>>>(g);
+        k_b_project<T><<<nsub, kT, 0, s>>>(g);
+        k_b_dots<T><<<nch, kT, 0, s>>>(g, 1);
+        k_b_gs2<<<count, 32, 0, s>>>(g);
+        k_b_newcols<T><<<nsub, kT, 0, s>>>(g);
+        k_b_sigma<T><<<nsub, kT, 0, s>>>(g);
+      };
+      auto iteration = [&] {
+        k_b_dots<T><<<nch, kT, 0, s>>>(g, 0);
+        k_b_rr<<<count, 32, 0, s>>>(g);
+        k_b_combine<T><<<nch, kT, 0, s>>>(g);
+        k_b_ctl<<<count, 32, 0, s>>>(g);
+        k_b_apply<T><<<nsub, kT, 0, s>>>(g);
+        ortho_sigma();
+      };
+      ortho_sigma();
+      count_launch(&c, 7);
       SBDGB_CUDA(cudaGetLastError());
-      k_b_count<<<1, 1024, 0, s>>>(dS, count, dcount);
+      // the legacy default stream cannot be captured: launch directly there
+      if (s != nullptr && s != cudaStreamLegacy && s != cudaStreamPerThread) {
+        cudaGraph_t graph = nullptr;
+        SBDGB_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        iteration();
+        SBDGB_CUDA(cudaStreamEndCapture(s, &graph));
+        const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        SBDGB_CUDA(ie);
+      }
+      for (int it = 0; it <= steps;) {
+        const int per_check = it < 8 ? 4 : 2;
+        for (int r = 0; r < per_check; ++r, ++it) {
+          if (exec)
+            SBDGB_CUDA(cudaGraphLaunch(exec, s));
+          else
+            iteration();
+          count_launch(&c, kStepLaunches);
+        }
+        SBDGB_CUDA(cudaGetLastError());
+        k_b_count<<<1, 1024, 0, s>>>(dS, count, dcount);
+        count_launch(&c);
+        SBDGB_CUDA(cudaMemcpyAsync(pin, dcount, sizeof(int), cudaMemcpyDeviceToHost, s));
+        SBDGB_CUDA(cudaStreamSynchronize(s));
+        if (pin[0] == 0) break;
+      }
+      if (exec) {
+        cudaGraphExecDestroy(exec);
+        exec = nullptr;
+      }
+    };
+    const BCommon g64{dP, dS, dch, dpart, pstride, k, o.eps, 0.0, 0};
+    if (mixed) {
+      // FP32 phase to a relative residual of kMixedRel (at most 4 max_nb
+      // iterations), then the FP64 phase from its lowest Ritz vectors
+      const BCommon g32{dP, dS, dch, dpart, pstride, k, o.eps, kMixedRel, 4 * nb};
+      k_b_init<float><<<count, kT, 0, s>>>(g32);
       count_launch(&c);
-      SBDGB_CUDA(cudaMemcpyAsync(pin, dcount, sizeof(int), cudaMemcpyDeviceToHost, s));
-      SBDGB_CUDA(cudaStreamSynchronize(s));
-      if (pin[0] == 0) break;
+      run_phase(float{}, g32, 4 * nb);
+      k_b_ritz<float><<<nsub, kT, 0, s>>>(g32, 1);
+      k_b_seed_state<<<(count + 127) / 128, 128, 0, s>>>(g64, count);
+      count_launch(&c, 2);
+    } else {
+      k_b_init<double><<<count, kT, 0, s>>>(g64);
+      count_launch(&c);
     }
+    run_phase(double{}, g64, max_steps);
     k_b_results<<<(count + 127) / 128, 128, 0, s>>>(dS, count, k, dres);
     count_launch(&c);
     if (X) {
-      k_b_ritz<<<nsub, kT, 0, s>>>(g);
+      k_b_ritz<double><<<nsub, kT, 0, s>>>(g64, 0);
       count_launch(&c);
     }
     SBDGB_CUDA(cudaGetLastError());
@@ -1023,16 +1165,17 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
     SBDGB_CUDA(cudaStreamSynchronize(s));
     const double secs = std::chrono::duration<double>(clock::now() - t0).count();
     for (int i = 0; i < count; ++i) {
-      const double *r = out.data() + (size_t)i * (2 * k + 4);
+      const double *r = out.data() + (size_t)i * rstride;
       for (int q = 0; q < k; ++q) E[(size_t)i * k + q] = r[q];
       if (reps) {
         sbdgb_report &rp = reps[i];
         rp = sbdgb_report{};
         for (int q = 0; q < k && q < 16; ++q) rp.resid[q] = r[k + q];
         rp.iterations = (int)r[2 * k];
-        rp.sigma_calls = rp.sigma_fp64 = (int)r[2 * k + 1];
+        rp.sigma_calls = (int)r[2 * k + 1];
         rp.converged = (int)r[2 * k + 2];
         rp.restarts = (int)r[2 * k + 3];
+        rp.sigma_fp64 = (int)r[2 * k + 4];
         rp.seconds = secs;
       }
     }
@@ -1042,7 +1185,6 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
     tmp_free(&c, arena);
     throw;
   }
-  if (exec) cudaGraphExecDestroy(exec);
   tmp_free(&c, mb);
   tmp_free(&c, arena);
 }

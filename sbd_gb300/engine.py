@@ -195,13 +195,15 @@ class Engine:
 
 
 def batch_davidson(engine: Engine, problems: list, nroots: int = 1, max_nb: int = 20, eps: float = 1e-8,
-                   max_it: int = 100, want_vectors: bool = False) -> list:
-    """Solves every TPBProblem of the list (all on `engine`) in one launch, one thread
-    block per problem; returns one DavidsonResult per problem."""
+                   max_it: int = 100, want_vectors: bool = False, precision: int = FP64) -> list:
+    """Solves every TPBProblem of the list (all on `engine`) with the batched solver:
+    all problems advanced in lock step, one captured graph launch per Davidson
+    iteration.  precision MIXED runs an FP32 phase first and then the FP64 phase
+    (same tolerance, same energies).  Returns one DavidsonResult per problem."""
     n = len(problems)
     o = DavidsonOpts()
     load().sbdgb_davidson_default_opts(C.byref(o))
-    o.nroots, o.max_nb, o.eps, o.max_it, o.init = nroots, max_nb, eps, max_it, 1
+    o.nroots, o.max_nb, o.eps, o.max_it, o.init, o.precision = nroots, max_nb, eps, max_it, 1, precision
     hs = (C.c_void_p * max(n, 1))(*[p.h.value for p in problems])
     E = np.zeros(max(n * nroots, 1))
     reps = (Report * max(n, 1))()

@@ -109,7 +109,7 @@ def run_serving(reqs, cfg: int, precision: int, rate: float, workers: int, seed:
     return results, wall, st
 
 
-def run_batch(reqs, cfg: int, chunk: int):
+def run_batch(reqs, cfg: int, chunk: int, precision: int = 0):
     """The batched solver: upload and tables per problem, then one solver call per
     chunk of problems (all problems of the chunk advanced in lock step, one
     graph launch per Davidson iteration).
@@ -129,7 +129,7 @@ def run_batch(reqs, cfg: int, chunk: int):
             t.diag_terms()
         k = part[0][6]
         tl = time.perf_counter()
-        res = batch_davidson(eng, tps, nroots=k, max_nb=o["max_nb"], eps=o["eps"])
+        res = batch_davidson(eng, tps, nroots=k, max_nb=o["max_nb"], eps=o["eps"], precision=precision)
         t_launch += time.perf_counter() - tl
         E += [r.energies.copy() for r in res]
         reps += [r.report for r in res]
@@ -171,7 +171,8 @@ def main(argv=None) -> int:
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--records", default=None, help="write per-request results (JSON lines) to this file")
     ap.add_argument("--batch", type=int, default=0,
-                    help="also time the batched solver with this many problems per launch (0: skip)")
+                    help="also time the batched solver with this many problems per call (0: skip)")
+    ap.add_argument("--batch-precisions", default="fp64,mixed")
     a = ap.parse_args(argv)
     n = a.requests or (512 if a.config == 4 else 4096)
     rates = [float(x) for x in (a.rates or ("20,200,inf" if a.config == 4 else "inf")).split(",")]
@@ -216,13 +217,17 @@ def main(argv=None) -> int:
                 f.write(json.dumps({"precision": "serial_fp64", "index": i, "seconds": lat[i]}) + "\n")
     out["serving"] = runs
     if a.batch > 0:
-        Eb, wall_b, t_launch, reps = run_batch(reqs, a.config, a.batch)
-        dE = max(float(np.max(np.abs(e - r))) for e, r in zip(Eb, ref_E) if r is not None)
-        out["batched"] = {"requests": n, "problems_per_launch": a.batch, "wall_s": wall_b,
-                          "solves_per_s": n / wall_b, "solver_launch_s": t_launch,
-                          "solves_per_s_solver_only": n / t_launch, "max_abs_dE": dE,
-                          "not_converged": sum(1 for r in reps if not r["converged"]),
-                          "vs_plain_fp64": (n / wall_b) / out["serial_fp64"]["solves_per_s"]}
+        for prec in [0 if p == "fp64" else 1 for p in a.batch_precisions.split(",") if p]:
+            Eb, wall_b, t_launch, reps = run_batch(reqs, a.config, a.batch, prec)
+            dE = max(float(np.max(np.abs(e - r))) for e, r in zip(Eb, ref_E) if r is not None)
+            out["batched" if prec == 0 else "batched_mixed"] = {
+                "requests": n, "problems_per_call": a.batch, "wall_s": wall_b,
+                "solves_per_s": n / wall_b, "solver_s": t_launch,
+                "solves_per_s_solver_only": n / t_launch, "max_abs_dE": dE,
+                "not_converged": sum(1 for r in reps if not r["converged"]),
+                "sigma_products_mean": float(np.mean([r["sigma_calls"] for r in reps])),
+                "fp64_sigma_products_mean": float(np.mean([r["sigma_fp64"] for r in reps])),
+                "vs_plain_fp64": (n / wall_b) / out["serial_fp64"]["solves_per_s"]}
     best = {p: max((r["solves_per_s"] for r in runs if r["precision"] == p and r["rate"] == "inf"), default=None)
             for p in ("fp64", "mixed")}
     out["capacity_solves_per_s"] = best

@@ -60,6 +60,7 @@ constexpr int kSubPer = kCH / kSub;
 constexpr int kT = 256;    // threads per element block
 constexpr int kStepLaunches = 12;
 constexpr double kMixedRel = 2e-6;  // FP32 phase: residual below this times |theta|
+constexpr size_t kKpSmem = 48 * 1024;  // largest (P|Q) table staged in shared memory by sigma
 
 struct Chunk {
   uint32_t prob, e0, e1;
@@ -100,6 +101,7 @@ struct BCommon {
   double eps;      // convergence: every residual below max(eps, eps_rel * |theta|)
   double eps_rel;
   int step_cap;    // iteration cap of the phase (0: the problem's max_steps)
+  int kp_smem;     // sigma reads (P|Q) from shared memory
 };
 
 template <typename T>
@@ -283,8 +285,8 @@ __device__ void warp_eig(int n, const double *A, double *Aw, double *Wv, double 
 // sigma of NV vectors (columns of x at stride N) at element (ia, ib), fused
 // form, in the storage precision T (table values of that precision).
 template <int NV, typename Wd, typename T>
-__device__ __forceinline__ void sigma_element_mv(const Args<T> &a, const T *__restrict__ x, uint32_t N, uint32_t ia,
-                                                 uint32_t ib, T (&acc)[NV]) {
+__device__ __forceinline__ void sigma_element_mv(const Args<T> &a, const T *__restrict__ Kp, const T *__restrict__ x,
+                                                 uint32_t N, uint32_t ia, uint32_t ib, T (&acc)[NV]) {
   const uint32_t nb = a.nb, e = ia * nb + ib;
   const T h = (T)__ldg(a.hii + e);
 #pragma unroll
@@ -305,20 +307,24 @@ __device__ __forceinline__ void sigma_element_mv(const Args<T> &a, const T *__re
 #pragma unroll
     for (int n = 0; n < NV; ++n) acc[n] = fmx(sv, __ldg(x + (size_t)n * N + off), acc[n]);
   }
-  // alpha x beta singles
+  // alpha x beta singles: the beta singles of this column outside (their
+  // table entries are read once per thread), the alpha singles of the row
+  // inside (the same entries for the threads of one row: broadcast loads);
+  // Kp is the (P|Q) table, in shared memory when it fits
   const uint32_t q0 = __ldg(a.B.off_s + ib), q1 = __ldg(a.B.off_s + ib + 1);
-  for (uint32_t p = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1); p < p1; ++p) {
-    const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
-    const Wd alpha_ket = word<Wd>(a.astr, ja);
-    const T *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
-    const uint32_t pa = parity(beta & word<Wd>(a.A.mask_s, p)) ^ (ca >> 31);
-    const uint32_t rowoff = ja * nb;
-    for (uint32_t q = q0; q < q1; ++q) {
-      const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-      const uint32_t ph = (pa ^ parity(alpha_ket & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31)) & 1u;
-      const T kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
+  const uint32_t pa0 = __ldg(a.A.off_s + ia), pa1 = __ldg(a.A.off_s + ia + 1);
+  for (uint32_t q = q0; q < q1; ++q) {
+    const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+    const Wd mb = word<Wd>(a.B.mask_s, q);
+    const uint32_t kb = (cb >> 16) & 0x7fffu, sb = cb >> 31;
+    for (uint32_t p = pa0; p < pa1; ++p) {
+      const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
+      const uint32_t ph =
+          (parity(beta & word<Wd>(a.A.mask_s, p)) ^ parity(word<Wd>(a.astr, ja) & mb) ^ (ca >> 31) ^ sb) & 1u;
+      const T kv = flip(Kp[((ca >> 16) & 0x7fffu) * a.npair + kb], ph);
+      const uint32_t off = ja * nb + jb;
 #pragma unroll
-      for (int n = 0; n < NV; ++n) acc[n] = fmx(kv, __ldg(x + (size_t)n * N + rowoff + jb), acc[n]);
+      for (int n = 0; n < NV; ++n) acc[n] = fmx(kv, __ldg(x + (size_t)n * N + off), acc[n]);
     }
   }
   // beta singles and doubles of column ib, this row
@@ -340,28 +346,28 @@ __device__ __forceinline__ void sigma_element_mv(const Args<T> &a, const T *__re
 }
 
 template <int NV, typename Wd, typename T>
-__device__ void chunk_sigma(const BProb &P, const T *x, T *y, uint32_t e0, uint32_t e1) {
+__device__ void chunk_sigma(const BProb &P, const T *Kp, const T *x, T *y, uint32_t e0, uint32_t e1) {
   const Args<T> &a = args_of<T>(P);
   const uint32_t nb = a.nb;
   for (uint32_t e = e0 + threadIdx.x; e < e1; e += kT) {
     T acc[NV];
-    sigma_element_mv<NV, Wd, T>(a, x, P.N, e / nb, e % nb, acc);
+    sigma_element_mv<NV, Wd, T>(a, Kp, x, P.N, e / nb, e % nb, acc);
 #pragma unroll
     for (int n = 0; n < NV; ++n) y[(size_t)n * P.N + e] = acc[n];
   }
 }
 
 template <typename Wd, typename T>
-__device__ void chunk_sigma_any(const BProb &P, int nvec, const T *x, T *y, uint32_t e0, uint32_t e1) {
+__device__ void chunk_sigma_any(const BProb &P, int nvec, const T *Kp, const T *x, T *y, uint32_t e0, uint32_t e1) {
   switch (nvec) {
-    case 1: chunk_sigma<1, Wd, T>(P, x, y, e0, e1); break;
-    case 2: chunk_sigma<2, Wd, T>(P, x, y, e0, e1); break;
-    case 3: chunk_sigma<3, Wd, T>(P, x, y, e0, e1); break;
-    case 4: chunk_sigma<4, Wd, T>(P, x, y, e0, e1); break;
-    case 5: chunk_sigma<5, Wd, T>(P, x, y, e0, e1); break;
-    case 6: chunk_sigma<6, Wd, T>(P, x, y, e0, e1); break;
-    case 7: chunk_sigma<7, Wd, T>(P, x, y, e0, e1); break;
-    default: chunk_sigma<8, Wd, T>(P, x, y, e0, e1); break;
+    case 1: chunk_sigma<1, Wd, T>(P, Kp, x, y, e0, e1); break;
+    case 2: chunk_sigma<2, Wd, T>(P, Kp, x, y, e0, e1); break;
+    case 3: chunk_sigma<3, Wd, T>(P, Kp, x, y, e0, e1); break;
+    case 4: chunk_sigma<4, Wd, T>(P, Kp, x, y, e0, e1); break;
+    case 5: chunk_sigma<5, Wd, T>(P, Kp, x, y, e0, e1); break;
+    case 6: chunk_sigma<6, Wd, T>(P, Kp, x, y, e0, e1); break;
+    case 7: chunk_sigma<7, Wd, T>(P, Kp, x, y, e0, e1); break;
+    default: chunk_sigma<8, Wd, T>(P, Kp, x, y, e0, e1); break;
   }
 }
 
@@ -870,23 +876,35 @@ __global__ void __launch_bounds__(kT) k_b_newcols(BCommon g) {
   }
 }
 
-// HV[from, to) = H V[from, to).
+// HV[from, to) = H V[from, to).  With g.kp_smem the block first copies the
+// problem's (P|Q) table into shared memory (launched with npair^2 elements of
+// dynamic shared memory for the largest npair of the batch).
 template <typename T>
 __global__ void __launch_bounds__(kT) k_b_sigma(BCommon g) {
+  extern __shared__ __align__(16) unsigned char kp_raw[];
   Chunk ch;
   uint32_t e0, e1;
   if (!sub_range(g, ch, e0, e1)) return;
   const BState &S = g.S[ch.prob];
   if (!S.active) return;
   const BProb &P = g.P[ch.prob];
+  const Args<T> &a = args_of<T>(P);
+  const T *Kp = a.Kp;
+  if (g.kp_smem) {
+    T *ks = reinterpret_cast<T *>(kp_raw);
+    const int npp = a.npair * a.npair;
+    for (int t = threadIdx.x; t < npp; t += kT) ks[t] = __ldg(a.Kp + t);
+    __syncthreads();
+    Kp = ks;
+  }
   const Buf<T> bf = buf<T>(P);
   const int from = S.from, nvec = S.to - S.from;
   const T *x = bf.V + (size_t)from * P.N;
   T *y = bf.HV + (size_t)from * P.N;
   if (P.norb <= 32)
-    chunk_sigma_any<uint32_t, T>(P, nvec, x, y, e0, e1);
+    chunk_sigma_any<uint32_t, T>(P, nvec, Kp, x, y, e0, e1);
   else
-    chunk_sigma_any<unsigned long long, T>(P, nvec, x, y, e0, e1);
+    chunk_sigma_any<unsigned long long, T>(P, nvec, Kp, x, y, e0, e1);
 }
 
 // Ritz vectors V c, in FP64, into the FP64 correction block (T, then U): the
@@ -1052,6 +1070,11 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
     q.c1 = (uint32_t)chunks.size();
   }
   const int nch = (int)chunks.size(), nsub = nch * kSubPer;
+  // (P|Q) in shared memory for sigma when the largest table of the batch fits
+  // in kKpSmem bytes (norb <= 12 in FP64, <= 16 in FP32)
+  size_t npp_max = 0;
+  for (int i = 0; i < count; ++i) npp_max = std::max(npp_max, (size_t)ps[i]->npair * ps[i]->npair);
+  const bool kp64 = sizeof(double) * npp_max <= kKpSmem, kp32 = sizeof(float) * npp_max <= kKpSmem;
   const int nseed = std::min(2 * k, kK);
   const int pstride = std::max({nb * k + k * k, nseed * nseed, 3 * kK});
   const int rstride = 2 * k + 5;
@@ -1090,7 +1113,7 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
         k_b_dots<T><<<nch, kT, 0, s>>>(g, 1);
         k_b_gs2<<<count, 32, 0, s>>>(g);
         k_b_newcols<T><<<nsub, kT, 0, s>>>(g);
-        k_b_sigma<T><<<nsub, kT, 0, s>>>(g);
+        k_b_sigma<T><<<nsub, kT, g.kp_smem ? sizeof(T) * npp_max : 0, s>>>(g);
       };
       auto iteration = [&] {
         k_b_dots<T><<<nch, kT, 0, s>>>(g, 0);
@@ -1134,11 +1157,11 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
         exec = nullptr;
       }
     };
-    const BCommon g64{dP, dS, dch, dpart, pstride, k, o.eps, 0.0, 0};
+    const BCommon g64{dP, dS, dch, dpart, pstride, k, o.eps, 0.0, 0, kp64 ? 1 : 0};
     if (mixed) {
       // FP32 phase to a relative residual of kMixedRel (at most 4 max_nb
       // iterations), then the FP64 phase from its lowest Ritz vectors
-      const BCommon g32{dP, dS, dch, dpart, pstride, k, o.eps, kMixedRel, 4 * nb};
+      const BCommon g32{dP, dS, dch, dpart, pstride, k, o.eps, kMixedRel, 4 * nb, kp32 ? 1 : 0};
       k_b_init<float><<<count, kT, 0, s>>>(g32);
       count_launch(&c);
       run_phase(float{}, g32, 4 * nb);

@@ -216,7 +216,16 @@ __device__ __forceinline__ bool sub_range(const BCommon &g, Chunk &ch, uint32_t 
 // Symmetric eigenproblem of the n x n leading block of A (ld kNB, symmetric
 // part) by one warp: eigenvalues ascending in E, eigenvectors in the columns
 // of Wv (ld kNB).  Aw, Wv, E: shared.
+//
+// Parallel-order Jacobi: each sweep is n' - 1 rounds (n' = n rounded up to
+// even) of the round-robin pairing, and the n'/2 rotations of a round act on
+// disjoint index pairs, so their parameters are computed by n'/2 lanes at once
+// and applied together (A <- J^T A J zeroes every pair of the round).  FP64
+// division and square root dominate a rotation on this GPU; the parallel
+// order takes them once per round instead of once per pair.
 __device__ void warp_eig(int n, const double *A, double *Aw, double *Wv, double *E) {
+  __shared__ double rc[kNB / 2], rs[kNB / 2];
+  __shared__ int rp[kNB / 2], rq[kNB / 2];
   const int l = threadIdx.x & 31;
   for (int t = l; t < kNB * kNB; t += 32) {
     const int i = t % kNB, j = t / kNB;
@@ -224,7 +233,10 @@ __device__ void warp_eig(int n, const double *A, double *Aw, double *Wv, double 
     Wv[t] = (i == j) ? 1.0 : 0.0;
   }
   __syncwarp();
-  for (int sweep = 0; sweep < 60; ++sweep) {
+  const int n2 = (n + 1) & ~1, np = n2 / 2;
+  // position -> index in round r of the circle method (position 0 fixed)
+  auto idx = [&](int pos, int r) { return pos == 0 ? 0 : 1 + (pos - 1 + r) % (n2 - 1); };
+  for (int sweep = 0; sweep < 60 && n > 1; ++sweep) {
     double off = 0.0, dg = 0.0;
     if (l < n)
       for (int j = 0; j < n; ++j) {
@@ -234,30 +246,50 @@ __device__ void warp_eig(int n, const double *A, double *Aw, double *Wv, double 
     off = warp_sum(off);
     dg = warp_sum(dg);
     if (off <= 1e-30 * (dg + 1e-300)) break;
-    for (int p = 0; p < n - 1; ++p)
-      for (int q = p + 1; q < n; ++q) {
-        const double apq = Aw[p + kNB * q];
-        if (fabs(apq) < 1e-300) continue;
-        const double theta = (Aw[q + kNB * q] - Aw[p + kNB * p]) / (2.0 * apq);
-        const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-        const double c = 1.0 / sqrt(t * t + 1.0), s = t * c;
-        __syncwarp();
-        if (l < n) {  // columns p, q
-          const double akp = Aw[l + kNB * p], akq = Aw[l + kNB * q];
-          Aw[l + kNB * p] = c * akp - s * akq;
-          Aw[l + kNB * q] = s * akp + c * akq;
+    for (int r = 0; r < n2 - 1; ++r) {
+      if (l < np) {
+        const int a = idx(l, r), b = idx(n2 - 1 - l, r);
+        const int p = min(a, b), q = max(a, b);
+        double c = 1.0, sn = 0.0;
+        if (q < n) {  // q == n is the padding index of odd n
+          const double apq = Aw[p + kNB * q];
+          if (fabs(apq) >= 1e-300) {
+            const double theta = (Aw[q + kNB * q] - Aw[p + kNB * p]) / (2.0 * apq);
+            const double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            sn = t * c;
+          }
         }
-        __syncwarp();
-        if (l < n) {  // rows p, q and the eigenvectors
-          const double apk = Aw[p + kNB * l], aqk = Aw[q + kNB * l];
-          Aw[p + kNB * l] = c * apk - s * aqk;
-          Aw[q + kNB * l] = s * apk + c * aqk;
-          const double vkp = Wv[l + kNB * p], vkq = Wv[l + kNB * q];
-          Wv[l + kNB * p] = c * vkp - s * vkq;
-          Wv[l + kNB * q] = s * vkp + c * vkq;
-        }
-        __syncwarp();
+        rp[l] = p;
+        rq[l] = q;
+        rc[l] = c;
+        rs[l] = sn;
       }
+      __syncwarp();
+      if (l < n)  // columns p, q of every pair: row l
+        for (int i = 0; i < np; ++i) {
+          const int p = rp[i], q = rq[i];
+          if (q >= n || rs[i] == 0.0) continue;
+          const double c = rc[i], sn = rs[i];
+          const double akp = Aw[l + kNB * p], akq = Aw[l + kNB * q];
+          Aw[l + kNB * p] = c * akp - sn * akq;
+          Aw[l + kNB * q] = sn * akp + c * akq;
+        }
+      __syncwarp();
+      if (l < n)  // rows p, q of every pair: column l; and the eigenvectors: row l
+        for (int i = 0; i < np; ++i) {
+          const int p = rp[i], q = rq[i];
+          if (q >= n || rs[i] == 0.0) continue;
+          const double c = rc[i], sn = rs[i];
+          const double apk = Aw[p + kNB * l], aqk = Aw[q + kNB * l];
+          Aw[p + kNB * l] = c * apk - sn * aqk;
+          Aw[q + kNB * l] = sn * apk + c * aqk;
+          const double vkp = Wv[l + kNB * p], vkq = Wv[l + kNB * q];
+          Wv[l + kNB * p] = c * vkp - sn * vkq;
+          Wv[l + kNB * q] = sn * vkp + c * vkq;
+        }
+      __syncwarp();
+    }
   }
   if (l == 0) {  // ascending order (selection sort), permuting the eigenvector columns
     for (int i = 0; i < n; ++i) E[i] = Aw[i + kNB * i];

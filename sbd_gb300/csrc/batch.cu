@@ -1103,7 +1103,7 @@ void batch_davidson(Ctx &c, Problem **ps, int count, const sbdgb_davidson_opts &
   }
   const int nch = (int)chunks.size(), nsub = nch * kSubPer;
   // (P|Q) in shared memory for sigma when the largest table of the batch fits
-  // in kKpSmem bytes (norb <= 12 in FP64, <= 16 in FP32)
+  // in kKpSmem bytes (norb <= 12 in FP64, <= 14 in FP32)
   size_t npp_max = 0;
   for (int i = 0; i < count; ++i) npp_max = std::max(npp_max, (size_t)ps[i]->npair * ps[i]->npair);
   const bool kp64 = sizeof(double) * npp_max <= kKpSmem, kp32 = sizeof(float) * npp_max <= kKpSmem;

@@ -339,6 +339,34 @@ inline double Lanczos(Problem &p, std::vector<double> &W, int max_iteration, int
   return E;
 }
 
+// Many small problems of one context solved in lock step (no reference
+// counterpart; sbdgb_batch_davidson).  Returns energies[i][r] for problem i and
+// root r; precision SBDGB_MIXED runs an FP32 phase before the FP64 phase.
+inline std::vector<std::vector<double>> BatchDavidson(std::vector<Problem *> &problems, int nroots, int num_block,
+                                                      double eps, int max_iteration = 100,
+                                                      int precision = SBDGB_FP64) {
+  std::vector<std::vector<double>> out(problems.size());
+  if (problems.empty()) return out;
+  sbdgb_davidson_opts o;
+  sbdgb_davidson_default_opts(&o);
+  o.max_it = max_iteration;
+  o.max_nb = num_block;
+  o.eps = eps;
+  o.nroots = nroots;
+  o.init = 1;
+  o.precision = precision;
+  std::vector<sbdgb_problem *> ps(problems.size());
+  for (size_t i = 0; i < problems.size(); ++i) {
+    if (problems[i]->ctx() != problems[0]->ctx()) throw std::invalid_argument("batch problems share one context");
+    ps[i] = problems[i]->get();
+  }
+  std::vector<double> E(problems.size() * nroots);
+  check(sbdgb_batch_davidson(problems[0]->ctx(), ps.data(), (int)ps.size(), &o, E.data(), nullptr, nullptr),
+        problems[0]->ctx(), "BatchDavidson");
+  for (size_t i = 0; i < problems.size(); ++i) out[i].assign(E.begin() + i * nroots, E.begin() + (i + 1) * nroots);
+  return out;
+}
+
 // OccupationDensity (occupation.h:11-95) over all orbitals: res[2p] alpha,
 // res[2p+1] beta occupation of orbital p in W.
 inline void OccupationDensity(Problem &p, int norb, const std::vector<double> &W, std::vector<double> &res) {

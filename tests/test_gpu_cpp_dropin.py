@@ -95,3 +95,28 @@ def test_cpp_full_diag_carry_over_rdm_and_files(exe_full, tmp_path, name):
     r2 = subprocess.run(args + ["--loadname", str(tmp_path / "wf")], capture_output=True, text=True, check=True)
     e2 = float(re.search(r"Energy = ([-0-9.eE+]+)", r2.stdout).group(1))
     assert abs(e2 - c.energy) < 1e-8
+
+
+def test_cpp_batch_davidson_matches_reference_energies(tmp_path):
+    """BatchDavidson of the C++ mirror: several fixture problems in one call,
+    FP64 and mixed, each at the reference's energy."""
+    lib = build.build()
+    exe = str(tmp_path / "batch_solve")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "batch_solve.cpp"), "-L" + os.path.dirname(lib), "-lsbdgb",
+                    "-Wl,-rpath," + os.path.dirname(lib), "-o", exe], check=True)
+    names = ["fci_L8", "open_L10", "wide_L36"]
+    args = []
+    for name in names:
+        c = load(name)
+        ints = Integrals(norb=c.norb, nelec=0, ecore=c.ecore, h1=c.h1, eri=c.eri)
+        write_fcidump(str(tmp_path / f"{name}.fcidump"), ints)
+        write_strings(str(tmp_path / f"{name}.a"), c.astr, c.norb)
+        write_strings(str(tmp_path / f"{name}.b"), c.bstr, c.norb)
+        args += [str(tmp_path / f"{name}.fcidump"), str(tmp_path / f"{name}.a"), str(tmp_path / f"{name}.b")]
+    r = subprocess.run([exe] + args, capture_output=True, text=True, check=True)
+    got = re.findall(r"problem (\d+) fp64 (\S+) mixed (\S+)", r.stdout)
+    assert len(got) == len(names)
+    for (i, e64, emx), name in zip(got, names):
+        ref = load(name).energy
+        assert abs(float(e64) - ref) < 1e-8 and abs(float(emx) - ref) < 1e-8, (name, e64, emx, ref)

@@ -257,7 +257,7 @@ def run_gpu(args):
         from sbd_gb300.engine import MIXED
         mlat, mE = [], None
         for i in range(1 + args.mixed_steps):
-            rm = p.davidson(precision=MIXED, refine_every=4, **kw)
+            rm = p.davidson(precision=MIXED, refine_every=0, **kw)
             if i > 0:
                 mlat.append(rm.report["seconds"])
             mE = rm.energies

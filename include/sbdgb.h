@@ -202,7 +202,8 @@ typedef struct {
                         1: unit vectors on the lowest diagonal entries,
                         2: caller-supplied vectors in X */
   int precision;     /* sbdgb_precision */
-  int refine_every;  /* MIXED: FP64 sigma and residual every k iterations */
+  int refine_every;  /* MIXED: 0 (default) = FP32 Davidson, then FP64 from its lowest Ritz vectors;
+                        k > 0 = FP64 anchors, FP32 subspace, FP64 sigma and residual every k steps */
   int verbose;       /* print one line per iteration like the reference */
 } sbdgb_davidson_opts;
 

@@ -511,7 +511,7 @@ struct SBD {
   // engine extensions
   int nroots = 1;
   int precision = SBDGB_FP64;
-  int refine_every = 4;
+  int refine_every = 0;
   int device = 0;
 };
 

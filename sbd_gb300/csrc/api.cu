@@ -110,9 +110,18 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
   b += 8 * N;
   // solver reductions (partial sums of at most 4 blocks per SM of 64 values, staging)
   b += 8 * (size_t)(1024 * 32 * 16 + 64) + 8 * 4096 + 8 * 8192;
+  const size_t max_nb = std::min<size_t>((size_t)std::max(o.max_nb, 2 * (int)k), std::max<size_t>(N, 1));
   if (!mixed) {
-    const size_t max_nb = std::min<size_t>((size_t)std::max(o.max_nb, 2 * (int)k), std::max<size_t>(N, 1));
     b += 16 * N * max_nb + 64 * N * k;  // basis and sigma; 3k restart vectors and their sigma; T; U
+  } else if (o.refine_every == 0) {
+    // two-phase form: the FP64 solver's buffers (its start block holds up to
+    // 2k seed vectors), the same shapes in FP32, 2k FP64 seed vectors, FP32
+    // tables, the FP32 transpose and multi-vector scratch
+    b += 16 * N * max_nb + 72 * N * k;
+    b += 8 * N * max_nb + 32 * N * k;
+    b += 16 * N * k;
+    b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;
+    b += 4 * N + 4 * N * std::min<size_t>(4, k);
   } else {
     const size_t mmax = (size_t)std::max(std::min(o.max_nb, 64) - (int)k, 2 * (int)k);
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;  // FP32 tables
@@ -460,7 +469,7 @@ void sbdgb_davidson_default_opts(sbdgb_davidson_opts *o) {
   o->nroots = 1;
   o->init = 0;
   o->precision = SBDGB_FP64;
-  o->refine_every = 4;
+  o->refine_every = 0;
   o->verbose = 0;
 }
 

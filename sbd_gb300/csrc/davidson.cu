@@ -126,17 +126,18 @@ __global__ void k_sum_partials(const double *__restrict__ partial, int nblocks, 
   out[t] = s;
 }
 
+template <typename F>
 struct CombineArgs {
-  const double *V;
-  const double *HV;
+  const F *V;
+  const F *HV;
   size_t N;
   int nv;
   int k;
   const double *hii;
-  double *X;        // k x N or null
-  double *HX;       // k x N or null
-  double *T;        // k x N or null: preconditioned residual
-  double *U;        // k x N or null: X / (theta - d), for the Olsen correction of T
+  F *X;             // k x N or null
+  F *HX;            // k x N or null
+  F *T;             // k x N or null: preconditioned residual
+  F *U;             // k x N or null: X / (theta - d), for the Olsen correction of T
   double *partial;  // blocks x k residual norm^2 partials (x 3k with U: norm^2, x.T, x.U)
   Vals<kMaxCoef> coef;  // nv x k column-major (coef[j + nv*r])
   Vals<16> theta;       // k
@@ -149,46 +150,48 @@ struct CombineArgs {
 // component of the preconditioned residual orthogonal to the Ritz vector.
 // Where the diagonal is nearly exact (weakly coupled determinants) the plain
 // correction is almost parallel to X and the subspace stops growing.
-template <int K>
-__global__ void __launch_bounds__(kRed) k_combine(CombineArgs a) {
-  __shared__ double cs[kMaxCoef];
-  __shared__ double th[16];
-  for (int t = threadIdx.x; t < a.nv * K; t += kRed) cs[t] = a.coef.v[t];
-  if (threadIdx.x < K) th[threadIdx.x] = a.theta.v[threadIdx.x];
+// F is the storage and arithmetic precision (FP64, or FP32 in the first phase
+// of the two-phase mixed form); the block sums are FP64.
+template <int K, typename F>
+__global__ void __launch_bounds__(kRed) k_combine(CombineArgs<F> a) {
+  __shared__ F cs[kMaxCoef];
+  __shared__ F th[16];
+  for (int t = threadIdx.x; t < a.nv * K; t += kRed) cs[t] = (F)a.coef.v[t];
+  if (threadIdx.x < K) th[threadIdx.x] = (F)a.theta.v[threadIdx.x];
   __syncthreads();
-  double rn[K], xt[K], xu[K];
+  F rn[K], xt[K], xu[K];
 #pragma unroll
-  for (int r = 0; r < K; ++r) rn[r] = xt[r] = xu[r] = 0.0;
+  for (int r = 0; r < K; ++r) rn[r] = xt[r] = xu[r] = F(0);
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < a.N; e += (size_t)gridDim.x * kRed) {
-    double x[K], h[K];
+    F x[K], h[K];
 #pragma unroll
     for (int r = 0; r < K; ++r) {
-      x[r] = 0.0;
-      h[r] = 0.0;
+      x[r] = F(0);
+      h[r] = F(0);
     }
     for (int j = 0; j < a.nv; ++j) {
-      const double v = __ldg(a.V + (size_t)j * a.N + e);
-      const double hv = __ldg(a.HV + (size_t)j * a.N + e);
+      const F v = __ldg(a.V + (size_t)j * a.N + e);
+      const F hv = __ldg(a.HV + (size_t)j * a.N + e);
 #pragma unroll
       for (int r = 0; r < K; ++r) {
         x[r] = fma(v, cs[j + a.nv * r], x[r]);
         h[r] = fma(hv, cs[j + a.nv * r], h[r]);
       }
     }
-    const double d = a.hii ? __ldg(a.hii + e) : 0.0;
+    const F d = a.hii ? (F)__ldg(a.hii + e) : F(0);
 #pragma unroll
     for (int r = 0; r < K; ++r) {
-      const double res = h[r] - th[r] * x[r];
+      const F res = h[r] - th[r] * x[r];
       rn[r] = fma(res, res, rn[r]);
       if (a.X) a.X[(size_t)r * a.N + e] = x[r];
       if (a.HX) a.HX[(size_t)r * a.N + e] = h[r];
       if (a.T) {
-        double den = th[r] - d;
-        if (fabs(den) <= 1.0e-12) den -= 1.0e-12;
-        const double t = res / den;
+        F den = th[r] - d;
+        if (fabs(den) <= F(1.0e-12)) den -= F(1.0e-12);
+        const F t = res / den;
         a.T[(size_t)r * a.N + e] = t;
         if (a.U) {
-          const double u = x[r] / den;
+          const F u = x[r] / den;
           a.U[(size_t)r * a.N + e] = u;
           xt[r] = fma(x[r], t, xt[r]);
           xu[r] = fma(x[r], u, xu[r]);
@@ -202,7 +205,7 @@ __global__ void __launch_bounds__(kRed) k_combine(CombineArgs a) {
   const int width = a.U ? W3 : K;
 #pragma unroll
   for (int r = 0; r < W3; ++r) {
-    double x = r < K ? rn[r] : (r < 2 * K ? xt[r - K] : xu[r - 2 * K]);
+    double x = (double)(r < K ? rn[r] : (r < 2 * K ? xt[r - K] : xu[r - 2 * K]));
     for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
     if (lane == 0) red[warp][r] = x;
   }
@@ -601,17 +604,17 @@ struct Solver {
 
   // Ritz vectors (optional), their sigma (optional) and the preconditioned
   // residuals (optional) of the combination c; returns the residual norms.
-  std::vector<double> combine(const double *V, const double *HV, int nv, int k, const std::vector<double> &c,
-                              const std::vector<double> &theta, double *X, double *HX, double *T,
-                              double *U = nullptr) {
+  template <typename F>
+  std::vector<double> combine(const F *V, const F *HV, int nv, int k, const std::vector<double> &c,
+                              const std::vector<double> &theta, F *X, F *HX, F *T, F *U = nullptr) {
     SBDGB_REQUIRE((size_t)nv * k <= (size_t)kMaxCoef && k <= 16, SBDGB_E_UNSUPPORTED, "subspace too large");
     if (!T) U = nullptr;
-    CombineArgs a{V, HV, N, nv, k, p.hii, X, HX, T, U, partial, {}, {}};
+    CombineArgs<F> a{V, HV, N, nv, k, p.hii, X, HX, T, U, partial, {}, {}};
     std::copy(c.begin(), c.begin() + (size_t)nv * k, a.coef.v);
     for (int r = 0; r < k; ++r) a.theta.v[r] = r < (int)theta.size() ? theta[r] : 0.0;
     switch (k) {
 #define SBDGB_K(KK) \
-  case KK: k_combine<KK><<<blocks, kRed, 0, s>>>(a); break;
+  case KK: k_combine<KK, F><<<blocks, kRed, 0, s>>>(a); break;
       SBDGB_K(1) SBDGB_K(2) SBDGB_K(3) SBDGB_K(4) SBDGB_K(5) SBDGB_K(6) SBDGB_K(7) SBDGB_K(8)
       SBDGB_K(9) SBDGB_K(10) SBDGB_K(11) SBDGB_K(12) SBDGB_K(13) SBDGB_K(14) SBDGB_K(15) SBDGB_K(16)
 #undef SBDGB_K
@@ -625,8 +628,8 @@ struct Solver {
     std::vector<double> v(h, h + width);
     std::vector<double> rn(v.begin(), v.begin() + k);
     for (auto &x : rn) x = std::sqrt(std::max(0.0, x));
-    if (U) olsen<double>(T, U, k, std::vector<double>(v.begin() + k, v.begin() + 2 * k),
-                         std::vector<double>(v.begin() + 2 * k, v.end()));
+    if (U) olsen<F>(T, U, k, std::vector<double>(v.begin() + k, v.begin() + 2 * k),
+                    std::vector<double>(v.begin() + 2 * k, v.end()));
     return rn;
   }
 
@@ -808,10 +811,37 @@ void print_iter(const char *tag, int iter, const std::vector<double> &resid, con
   fflush(stdout);
 }
 
-// ---- FP64 solver ------------------------------------------------------------------
+// ---- FP64 solver and the two-phase mixed form ----------------------------------------
 
-void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
+// y = (D)x for n elements (precision conversion of a vector block).
+template <typename S, typename D>
+__global__ void __launch_bounds__(kRed) k_convert(const S *__restrict__ x, D *__restrict__ y, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < n; e += (size_t)gridDim.x * kRed) y[e] = (D)x[e];
+}
+
+// What a run of the Davidson core does besides the options: its convergence
+// test (every residual below max(eps, eps_rel |theta|)), an iteration cap,
+// start vectors given on the device (FP64, replacing the options' init), and
+// the lowest Ritz vectors written out in FP64 at the end.
+struct CorePhase {
+  double eps_rel = 0.0;
+  int step_cap = 0;               // 0: max_it * max_nb
+  double *seed = nullptr;         // nseed FP64 start vectors (overwritten)
+  int nseed = 0;
+  double *seed_out = nullptr;     // the lowest min(nseed_out, available) Ritz vectors
+  int nseed_out = 0;
+  int *nseed_written = nullptr;
+};
+
+// The Davidson iteration in storage precision F: FP64 (the plain solver), or
+// FP32 (the first phase of the two-phase mixed form: FP32 vectors, the FP32
+// sigma of the mixed kernels, FP32 vector algebra with FP64 block sums; the
+// projected matrix and Rayleigh-Ritz stay FP64).
+template <typename F>
+void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph, double *E, double *Xout,
+                   sbdgb_report &r) {
   using clock = std::chrono::steady_clock;
+  constexpr bool kF64 = std::is_same<F, double>::value;
   const auto t0 = clock::now();
   const int k = o.nroots;
   const size_t N = p.N;
@@ -821,27 +851,45 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
   SBDGB_REQUIRE(max_nb <= 64, SBDGB_E_INPUT, "max_nb must be <= 64");
   cudaStream_t s = p.ctx->stream;
   Solver sv(p, s);
-  double *V = (double *)workspace(p, WS_V, sizeof(double) * N * max_nb);
-  double *HV = (double *)workspace(p, WS_HV, sizeof(double) * N * max_nb);
-  double *X = (double *)workspace(p, WS_X, sizeof(double) * N * 3 * k);  // restart basis (<= 3k)
-  double *HX = (double *)workspace(p, WS_HX, sizeof(double) * N * 3 * k);
-  double *T = (double *)workspace(p, WS_T, sizeof(double) * N * k);
-  double *U = (double *)workspace(p, WS_U, sizeof(double) * N * k);
+  const int nstart = ph.seed ? ph.nseed : k;
+  F *V = (F *)workspace(p, kF64 ? WS_V : WS_VF, sizeof(F) * N * max_nb);
+  F *HV = (F *)workspace(p, kF64 ? WS_HV : WS_HVF, sizeof(F) * N * max_nb);
+  F *X = (F *)workspace(p, kF64 ? WS_X : WS_CF, sizeof(F) * N * 3 * k);  // restart basis (<= 3k)
+  F *HX = (F *)workspace(p, kF64 ? WS_HX : WS_SF, sizeof(F) * N * 3 * k);
+  F *T = (F *)workspace(p, kF64 ? WS_T : WS_RES64, sizeof(F) * N * std::max(k, nstart));
+  F *U = (F *)workspace(p, kF64 ? WS_U : WS_UF, sizeof(F) * N * k);
+  const double drop = kF64 ? 1e-8 : 1e-5;  // relative norm below which a new direction is dropped
 
-  sbdgb_report r{};
-  sv.start_vectors(o, k, T, Xout);
-  int nv = sv.orthonormalize_block<double>(T, k, V, 0, V, 1e-8);
+  int nv = 0;
+  if (ph.seed) {
+    SBDGB_REQUIRE(kF64, SBDGB_E_STATE, "seed vectors start the FP64 core only");
+    nv = sv.orthonormalize_block<double>(ph.seed, ph.nseed, (const double *)V, 0, (double *)V, drop);
+  } else if (kF64) {
+    sv.start_vectors(o, k, (double *)T, Xout);
+    nv = sv.orthonormalize_block<double>((double *)T, k, (const double *)V, 0, (double *)V, drop);
+  } else {
+    double *T64 = (double *)workspace(p, WS_C64, sizeof(double) * N * k);
+    sv.start_vectors(o, k, T64, Xout);
+    k_convert<double, float><<<sv.blocks, kRed, 0, s>>>(T64, (float *)T, N * k);
+    count_launch(p.ctx);
+    nv = sv.orthonormalize_block<F>(T, k, V, 0, V, drop);
+  }
   SBDGB_REQUIRE(nv >= 1, SBDGB_E_INPUT, "starting vectors are zero");
   std::vector<double> Hs((size_t)max_nb * max_nb, 0.0);  // projected matrix, column-major ld max_nb
   // sigma of V[from, to) and the new columns of the projected matrix
   auto extend = [&](int from, int to) {
-    for (int j = from; j < to; ++j) {
-      sigma_fp64(p, V + (size_t)j * N, HV + (size_t)j * N, 0, s);
-      r.sigma_calls++;
-      r.sigma_fp64++;
+    if constexpr (kF64) {
+      for (int j = from; j < to; ++j) {
+        sigma_fp64(p, V + (size_t)j * N, HV + (size_t)j * N, 0, s);
+        r.sigma_fp64++;
+      }
+    } else {
+      for (int j = from; j < to; j += 4)
+        sigma_mixed_multi(p, V + (size_t)j * N, HV + (size_t)j * N, std::min(4, to - j), s, 0.0);
     }
+    r.sigma_calls += to - from;
     std::vector<double> G;
-    sv.dots_c<double, double>(V, to, HV + (size_t)from * N, to - from, G);
+    sv.dots_c<F, F>(V, to, HV + (size_t)from * N, to - from, G);
     for (int jj = 0; jj < to - from; ++jj)
       for (int i = 0; i < to; ++i) {
         const double g = G[(size_t)i + (size_t)to * jj];
@@ -854,9 +902,11 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
   std::vector<double> theta, Y, resid(k, 0.0), c, th;
   std::vector<double> cprev;  // previous step's Ritz coefficients in the current basis (nvprev x kk)
   int nvprev = 0, kprev = 0;
-  bool converged = false;
+  bool converged = false, rotated = false;  // rotated: the basis changed since the last Rayleigh-Ritz
   int iter = 0, kk = 0;
-  const int max_steps = std::max(1, o.max_it) * max_nb;
+  int max_steps = std::max(1, o.max_it) * max_nb;
+  if (ph.step_cap > 0) max_steps = std::min(max_steps, ph.step_cap);
+  auto tol = [&](int q) { return std::max(o.eps, ph.eps_rel * std::fabs(th[q])); };
   while (true) {
     // Rayleigh-Ritz on the projected matrix
     std::vector<double> A((size_t)nv * nv);
@@ -864,22 +914,23 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
       for (int i = 0; i < nv; ++i)
         A[i + (size_t)nv * j] = 0.5 * (Hs[i + (size_t)max_nb * j] + Hs[j + (size_t)max_nb * i]);
     jacobi_eig(nv, A, theta, Y);
+    rotated = false;
     kk = std::min(k, nv);
     c.assign((size_t)nv * kk, 0.0);
     for (int q = 0; q < kk; ++q)
       for (int i = 0; i < nv; ++i) c[i + (size_t)nv * q] = Y[i + (size_t)nv * q];
     th.assign(theta.begin(), theta.begin() + kk);
     // residual norms and preconditioned corrections; Ritz vectors not materialised
-    resid = sv.combine(V, HV, nv, kk, c, th, nullptr, nullptr, T, U);
+    resid = sv.combine<F>(V, HV, nv, kk, c, th, nullptr, nullptr, T, U);
     iter++;
-    r.iterations = iter;
-    if (o.verbose) print_iter("", iter, resid, th, kk);
+    r.iterations++;
+    if (o.verbose) print_iter(kF64 ? "" : " (FP32 phase)", iter, resid, th, kk);
     converged = kk == k;
-    for (int q = 0; q < kk; ++q) converged = converged && (resid[q] < o.eps);
+    for (int q = 0; q < kk; ++q) converged = converged && (resid[q] < tol(q));
     const double elapsed = std::chrono::duration<double>(clock::now() - t0).count();
     if (converged || iter >= max_steps || (o.max_time > 0 && elapsed > o.max_time)) break;
     int nnew = 0;
-    for (int q = 0; q < kk; ++q) nnew += (resid[q] >= o.eps);
+    for (int q = 0; q < kk; ++q) nnew += (resid[q] >= tol(q));
     if (nv + nnew > max_nb) {
       // Thick restart on span{Ritz vectors, previous step's Ritz vectors}
       // (the second set keeps the search direction, as in locally optimal
@@ -914,9 +965,9 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
         Q.insert(Q.end(), v.begin(), v.end());
         ++m;
       }
-      sv.combine(V, HV, nv, m, Q, th, X, HX, nullptr);
-      SBDGB_CUDA(cudaMemcpyAsync(V, X, sizeof(double) * N * m, cudaMemcpyDeviceToDevice, s));
-      SBDGB_CUDA(cudaMemcpyAsync(HV, HX, sizeof(double) * N * m, cudaMemcpyDeviceToDevice, s));
+      sv.combine<F>(V, HV, nv, m, Q, th, X, HX, nullptr);
+      SBDGB_CUDA(cudaMemcpyAsync(V, X, sizeof(F) * N * m, cudaMemcpyDeviceToDevice, s));
+      SBDGB_CUDA(cudaMemcpyAsync(HV, HX, sizeof(F) * N * m, cudaMemcpyDeviceToDevice, s));
       std::vector<double> A((size_t)nv * nv), AQ((size_t)nv * m, 0.0), Hn((size_t)m * m, 0.0), cn((size_t)m * kk, 0.0);
       for (int j = 0; j < nv; ++j)
         for (int i = 0; i < nv; ++i)
@@ -935,6 +986,7 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
         for (int a2 = 0; a2 < m; ++a2) Hs[a2 + (size_t)max_nb * b] = Hn[a2 + (size_t)m * b];
       c = cn;
       nv = m;
+      rotated = true;
       r.restarts++;
       // T still holds the preconditioned residuals of these Ritz vectors
     }
@@ -944,16 +996,15 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
     // corrections of the unconverged roots, packed at the front of T
     int nt = 0;
     for (int q = 0; q < kk; ++q)
-      if (resid[q] >= o.eps) {
+      if (resid[q] >= tol(q)) {
         if (nt != q)
-          SBDGB_CUDA(cudaMemcpyAsync(T + (size_t)nt * N, T + (size_t)q * N, sizeof(double) * N,
-                                     cudaMemcpyDeviceToDevice, s));
+          SBDGB_CUDA(cudaMemcpyAsync(T + (size_t)nt * N, T + (size_t)q * N, sizeof(F) * N, cudaMemcpyDeviceToDevice, s));
         nt++;
       }
     // the subspace never exceeds max_nb (= N when 2k > N, where the restart
     // keeps k Ritz vectors and only N - k directions are left)
     nt = std::min(nt, max_nb - nv);
-    const int added = nt > 0 ? sv.orthonormalize_block<double>(T, nt, V, nv, V + (size_t)nv * N, 1e-8) : 0;
+    const int added = nt > 0 ? sv.orthonormalize_block<F>(T, nt, V, nv, V + (size_t)nv * N, drop) : 0;
     if (added == 0) break;  // no new direction: the subspace is invariant
     extend(nv, nv + added);
     nv += added;
@@ -961,12 +1012,71 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
   r.converged = converged ? 1 : 0;
   for (int q = 0; q < k && q < 16; ++q) r.resid[q] = q < (int)resid.size() ? resid[q] : 0.0;
   for (int q = 0; q < k; ++q) E[q] = q < (int)theta.size() ? theta[q] : NAN;
-  if (Xout) {
-    sv.combine(V, HV, nv, kk, c, th, X, nullptr, nullptr);
+  if (Xout && kF64) {
+    sv.combine<F>(V, HV, nv, kk, c, th, X, nullptr, nullptr);
     SBDGB_CUDA(cudaMemcpyAsync(Xout, X, sizeof(double) * N * kk, cudaMemcpyDeviceToHost, s));
   }
+  if (ph.seed_out) {
+    // the lowest Ritz vectors of the last Rayleigh-Ritz (only the kk of c if
+    // the basis was rotated after it), in FP64
+    std::vector<double> cs;
+    int ns;
+    if (!rotated) {
+      ns = std::min(std::min(ph.nseed_out, nv), 3 * k);
+      cs.assign(Y.begin(), Y.begin() + (size_t)nv * ns);
+    } else {
+      ns = std::min(kk, ph.nseed_out);
+      cs.assign(c.begin(), c.begin() + (size_t)nv * ns);
+    }
+    sv.combine<F>(V, HV, nv, ns, cs, std::vector<double>(ns, 0.0), X, nullptr, nullptr);
+    k_convert<F, double><<<sv.blocks, kRed, 0, s>>>(X, ph.seed_out, N * (size_t)ns);
+    count_launch(p.ctx);
+    SBDGB_CUDA(cudaGetLastError());
+    if (ph.nseed_written) *ph.nseed_written = ns;
+  }
   SBDGB_CUDA(cudaStreamSynchronize(s));
-  r.seconds = std::chrono::duration<double>(clock::now() - t0).count();
+  r.seconds += std::chrono::duration<double>(clock::now() - t0).count();
+}
+
+void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
+  sbdgb_report r{};
+  davidson_core<double>(p, o, CorePhase{}, E, Xout, r);
+  if (rep) *rep = r;
+}
+
+// Two-phase mixed form (precision MIXED with refine_every 0): the Davidson
+// iteration first in FP32 until every residual is below 2e-6 |theta| (at most
+// 4 max_nb iterations), then in FP64 from the lowest 2k Ritz vectors of that
+// phase (at most 8) to the full tolerance.  FP64 runs at 1/64 of the FP32
+// rate on this GPU; the FP32 phase takes most of the iterations and the FP64
+// phase ends at the FP64 solver's answer.
+void davidson_two_phase(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
+  const int k = o.nroots;
+  const size_t N = p.N;
+  cudaStream_t s = p.ctx->stream;
+  prepare_mixed(p, s);
+  const int max_nb = (int)std::min<size_t>((size_t)std::max(o.max_nb, 2 * k), N);
+  const int nseed = std::max(k, std::min(std::min(2 * k, kMaxBlock), max_nb));
+  double *seeds = (double *)workspace(p, WS_C64, sizeof(double) * N * std::max(nseed, k));
+  int written = 0;
+  CorePhase p32;
+  p32.eps_rel = 2e-6;
+  p32.step_cap = 4 * max_nb;
+  p32.seed_out = seeds;
+  p32.nseed_out = nseed;
+  p32.nseed_written = &written;
+  sbdgb_report r32{};
+  std::vector<double> E32(k);
+  davidson_core<float>(p, o, p32, E32.data(), Xout, r32);  // Xout: start vectors of init 2 (not written)
+  CorePhase p64;
+  p64.seed = seeds;
+  p64.nseed = written;
+  sbdgb_report r{};
+  davidson_core<double>(p, o, p64, E, Xout, r);
+  r.iterations += r32.iterations;
+  r.sigma_calls += r32.sigma_calls;
+  r.restarts += r32.restarts;
+  r.seconds += r32.seconds;
   if (rep) *rep = r;
 }
 
@@ -1016,7 +1126,7 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       for (int i = 0; i < j; ++i)
         G[i + (size_t)k * j] = G[j + (size_t)k * i] = 0.5 * (G[i + (size_t)k * j] + G[j + (size_t)k * i]);
     jacobi_eig(k, G, th, Yv);
-    resid = sv.combine(X, S, k, k, Yv, th, T, Y, nullptr);
+    resid = sv.combine<double>(X, S, k, k, Yv, th, T, Y, nullptr);
     SBDGB_CUDA(cudaMemcpyAsync(X, T, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, s));
     SBDGB_CUDA(cudaMemcpyAsync(S, Y, sizeof(double) * N * k, cudaMemcpyDeviceToDevice, s));
     theta = th;
@@ -1345,7 +1455,9 @@ void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout,
   if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "Davidson needs tables and diagonal");
   SBDGB_REQUIRE(o.nroots >= 1 && o.nroots <= kMaxBlock, SBDGB_E_INPUT, "nroots must be in [1, 8]");
   SBDGB_REQUIRE((size_t)o.nroots <= p.N, SBDGB_E_INPUT, "more roots than determinants");
-  if (o.precision == SBDGB_MIXED)
+  if (o.precision == SBDGB_MIXED && o.refine_every == 0)
+    davidson_two_phase(p, o, E, Xout, rep);
+  else if (o.precision == SBDGB_MIXED)
     davidson_mixed(p, o, E, Xout, rep);
   else
     davidson_fp64(p, o, E, Xout, rep);

@@ -400,7 +400,7 @@ class TPBProblem:
         return out
 
     def davidson(self, nroots: int = 1, max_nb: int = 20, eps: float = 1e-8, max_it: int = 100,
-                 init: int = 0, precision: int = FP64, refine_every: int = 4, max_time: float = 0.0,
+                 init: int = 0, precision: int = FP64, refine_every: int = 0, max_time: float = 0.0,
                  want_vectors: bool = True, X0: np.ndarray | None = None, verbose: bool = False) -> DavidsonResult:
         o = DavidsonOpts()
         self.lib.sbdgb_davidson_default_opts(C.byref(o))

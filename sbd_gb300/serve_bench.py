@@ -81,9 +81,9 @@ def run_serial(reqs, cfg: int):
     return lat, E
 
 
-def run_serving(reqs, cfg: int, precision: int, rate: float, workers: int, seed: int):
+def run_serving(reqs, cfg: int, precision: int, rate: float, workers: int, seed: int, refine_every: int = 0):
     from .serving import Server
-    o = solver_opts(cfg)
+    o = dict(solver_opts(cfg), refine_every=refine_every)
     n = len(reqs)
     rng = np.random.default_rng(seed)
     arrivals = np.zeros(n) if math.isinf(rate) else np.cumsum(rng.exponential(1.0 / rate, n))
@@ -173,6 +173,8 @@ def main(argv=None) -> int:
     ap.add_argument("--batch", type=int, default=0,
                     help="also time the batched solver with this many problems per call (0: skip)")
     ap.add_argument("--batch-precisions", default="fp64,mixed")
+    ap.add_argument("--refine-every", type=int, default=0,
+                    help="mixed form of the request loop: FP64 refinement every k steps, 0 = two-phase")
     a = ap.parse_args(argv)
     n = a.requests or (512 if a.config == 4 else 4096)
     rates = [float(x) for x in (a.rates or ("20,200,inf" if a.config == 4 else "inf")).split(",")]
@@ -195,7 +197,7 @@ def main(argv=None) -> int:
     for prec in precs:
         for rate in rates:
             m = n if math.isinf(rate) else max(16, min(n, int(rate * a.max_arrival_seconds)))
-            res, wall, st = run_serving(reqs[:m], a.config, prec, rate, a.workers, a.seed)
+            res, wall, st = run_serving(reqs[:m], a.config, prec, rate, a.workers, a.seed, a.refine_every)
             if prec == 0 and math.isinf(rate) and m == n:
                 # FP64 energies of the requests the plain path did not time
                 ref_E = [ref_E[i] if ref_E[i] is not None else res[i]["energies"] for i in range(n)]

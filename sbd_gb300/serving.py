@@ -50,7 +50,7 @@ class Server:
         return self.lib.sbdgb_server_last_error(self.h).decode()
 
     def submit(self, norb: int, astr, bstr, h1, eri, ecore: float = 0.0, nroots: int = 1, eps: float = 1e-8,
-               max_nb: int = 20, max_it: int = 100, init: int = 1, precision: int = FP64, refine_every: int = 4,
+               max_nb: int = 20, max_it: int = 100, init: int = 1, precision: int = FP64, refine_every: int = 0,
                want_vectors: bool = False) -> int:
         """Queues one solve and returns its ticket (the inputs are copied)."""
         a = np.ascontiguousarray(astr, dtype=np.uint64)

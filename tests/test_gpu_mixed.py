@@ -26,12 +26,15 @@ def test_mixed_sigma_close_to_fp64(engine):
     assert max_rel(s32.cpu().double().numpy(), ref) < 5e-6
 
 
+@pytest.mark.parametrize("refine_every", [4, 0])
 @pytest.mark.parametrize("name,k", [("cfg0_shape_L16", 1), ("spin_L12", 3), ("wide_L36", 2)])
-def test_mixed_davidson_matches_fp64(engine, name, k):
+def test_mixed_davidson_matches_fp64(engine, name, k, refine_every):
+    """refine_every 4: FP64 anchors and an FP32 subspace; 0: the two-phase form
+    (FP32 Davidson, then FP64 from its lowest Ritz vectors)."""
     c = load(name)
     p = TPBProblem(engine, c.norb, c.astr, c.bstr, c.h1, c.eri, c.ecore)
     r64 = p.davidson(nroots=k, max_nb=16, eps=1e-9, init=1)
-    rmx = p.davidson(nroots=k, max_nb=16, eps=1e-9, init=1, precision=MIXED, refine_every=4)
+    rmx = p.davidson(nroots=k, max_nb=16, eps=1e-9, init=1, precision=MIXED, refine_every=refine_every)
     assert r64.report["converged"] and rmx.report["converged"]
     assert np.max(np.abs(rmx.energies - r64.energies)) < 1e-9
     assert np.allclose(rmx.energies, c.lowest[:k], atol=1e-8, rtol=0)
@@ -49,3 +52,17 @@ def test_mixed_davidson_config0_shape(engine):
     rmx = p.davidson(nroots=1, max_nb=20, eps=1e-8, init=1, precision=MIXED, want_vectors=False)
     assert r64.report["converged"] and rmx.report["converged"]
     assert abs(rmx.energies[0] - r64.energies[0]) < 1e-6
+
+
+@pytest.mark.parametrize("refine_every", [4, 0])
+def test_mixed_davidson_two_roots_norb16(engine, refine_every):
+    """Both mixed forms at a size with restarts (N = 40,000, 2 roots), against FP64."""
+    prob = make_problem(16, 5, 5, 200, seed=3)
+    p = TPBProblem.from_problem(engine, prob)
+    r64 = p.davidson(nroots=2, max_nb=12, eps=1e-8, init=1, want_vectors=False)
+    rmx = p.davidson(nroots=2, max_nb=12, eps=1e-8, init=1, precision=MIXED, refine_every=refine_every,
+                     want_vectors=False)
+    assert r64.report["converged"] and rmx.report["converged"]
+    assert np.max(np.abs(rmx.energies - r64.energies)) < 1e-8
+    if refine_every == 0:
+        assert rmx.report["sigma_fp64"] < r64.report["sigma_fp64"]

@@ -48,12 +48,16 @@ def test_fp64_results_same_alone_and_in_mix(alone):
             assert ov >= 1 - 1e-8
 
 
-def test_mixed_results_in_mix_match_fp64_alone(alone):
+@pytest.mark.parametrize("refine_every", [4, 0])
+def test_mixed_results_in_mix_match_fp64_alone(alone, refine_every):
+    """Both mixed forms in the request loop; every request fits its footprint
+    (a request whose workspaces outgrow its reservation fails with E_NOMEM)."""
     from sbd_gb300.engine import MIXED
     from sbd_gb300.serving import Server
     mix = _mix()
     with Server(0, workers=3) as srv:
-        tickets = [srv.submit_problem(p, nroots=k, eps=1e-8, max_nb=20, init=1, precision=MIXED) for p, k in mix]
+        tickets = [srv.submit_problem(p, nroots=k, eps=1e-8, max_nb=20, init=1, precision=MIXED,
+                                      refine_every=refine_every) for p, k in mix]
         res = [srv.wait(t, timeout=300) for t in tickets]
     for r, a in zip(res, alone):
         assert r["status"] == 0, r["message"]

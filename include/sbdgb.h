@@ -291,6 +291,7 @@ typedef struct {
   uint64_t submitted, completed, failed, launches;
   size_t budget_bytes, reserved_bytes, peak_reserved_bytes;
   int workers, running, peak_running, queued;
+  uint64_t batched;  /* requests solved in batched groups of two or more */
 } sbdgb_serve_stats;
 
 typedef struct sbdgb_server sbdgb_server;
@@ -302,7 +303,10 @@ typedef struct sbdgb_server sbdgb_server;
  * fits goes first, but none passes a request already passed 2*workers times.
  * A request reserves an upper bound of its device memory at submission and
  * shrinks it to its real size once its tables are built; it cannot use more
- * than it reserved.  Results are those of sbdgb_davidson on the lone problem. */
+ * than it reserved.  Requests of at most 300,000 determinants that start
+ * together with equal options (init 1, subspace <= 32, FP64 or the two-phase
+ * mixed form) are solved as one sbdgb_batch_davidson batch of up to 64.
+ * Results are those of sbdgb_davidson on the lone problem (to rounding). */
 int sbdgb_server_create(int device, int workers, size_t hbm_budget_bytes, sbdgb_server **out);
 /* Queues a request and returns its ticket.  SBDGB_E_NOMEM if its reservation
  * alone exceeds the budget. */

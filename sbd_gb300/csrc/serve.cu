@@ -21,6 +21,15 @@
 // sigma tile shapes come from the problem size, not from timing runs, since
 // timings taken while other solves run are not meaningful.
 //
+// Small requests are batched: a worker that takes a request of at most
+// kBatchMaxN determinants also takes the other queued small requests with the
+// same solver options (up to kBatchMax, within the HBM left) and solves them
+// together with sbdgb_batch_davidson, all in lock step, one graph launch per
+// Davidson iteration.  That is the same algorithm as sbdgb_davidson (the
+// mixed form is the two-phase one), so a request's energies agree with a lone
+// solve to rounding (~1e-13), and its result does not otherwise depend on what
+// else runs.
+//
 // Each solve is the same computation as sbdgb_davidson on a lone problem: the
 // result of a request does not depend on what else runs.
 #include <algorithm>
@@ -51,6 +60,8 @@ uint64_t entry_bound(size_t n, int norb, int nocc) {
 }
 
 constexpr size_t kSlack = size_t(1) << 20;  // allocation rounding and small staging buffers
+constexpr uint64_t kBatchMaxN = 300000;      // requests up to this many determinants are batched
+constexpr int kBatchMax = 64;                // requests per batched solve
 
 struct Request {
   uint64_t ticket = 0;
@@ -83,7 +94,7 @@ struct sbdgb_server {
   std::condition_variable cv_work, cv_done;
   std::deque<Request *> queue;
   std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
-  uint64_t next = 1, submitted = 0, completed = 0, failed = 0, launches = 0;
+  uint64_t next = 1, submitted = 0, completed = 0, failed = 0, launches = 0, batched = 0;
   bool stop = false;
   std::vector<sbdgb_ctx *> ctxs;
   std::vector<std::thread> threads;
@@ -104,6 +115,105 @@ Request *admit(sbdgb_server *S) {
     if (r->bypassed >= S->max_bypass) return nullptr;  // nothing may pass an aged request
   }
   return nullptr;
+}
+
+// Whether a request can join a batched solve (the batched solver's options:
+// start on the lowest diagonal, subspace <= 32, no time limit, and for the
+// mixed precision the two-phase form).
+bool batchable(const Request *r) {
+  const sbdgb_davidson_opts &o = r->o;
+  return (uint64_t)r->a.size() * r->b.size() <= kBatchMaxN && o.init == 1 && o.max_nb <= 32 && o.max_time <= 0.0 &&
+         (o.precision == SBDGB_FP64 || (o.precision == SBDGB_MIXED && o.refine_every == 0));
+}
+
+bool same_opts(const Request *x, const Request *y) {
+  const sbdgb_davidson_opts &a = x->o, &b = y->o;
+  return a.nroots == b.nroots && a.max_nb == b.max_nb && a.max_it == b.max_it && a.eps == b.eps &&
+         a.precision == b.precision && a.refine_every == b.refine_every && a.init == b.init;
+}
+
+// The queued requests that can join r's batched solve (called with the lock
+// held; r is admitted already).  Stops at an aged request that does not join.
+void gather(sbdgb_server *S, Request *r, std::vector<Request *> &group) {
+  group.assign(1, r);
+  if (!batchable(r)) return;
+  size_t reserved = S->reserved + r->reserve;
+  for (size_t i = 0; i < S->queue.size() && (int)group.size() < kBatchMax;) {
+    Request *q = S->queue[i];
+    if (batchable(q) && same_opts(q, r) && reserved + q->reserve <= S->budget) {
+      reserved += q->reserve;
+      group.push_back(q);
+      S->queue.erase(S->queue.begin() + (long)i);
+      continue;
+    }
+    if (q->bypassed >= S->max_bypass) break;
+    ++i;
+  }
+}
+
+void finish_result(Request *r, int status, const std::string &msg, const double *E, const sbdgb_report &rep,
+                   int wid) {
+  sbdgb_result &res = r->res;
+  res.status = status;
+  if (status != SBDGB_OK) set_message(res, msg);
+  res.nroots = r->o.nroots;
+  for (int j = 0; j < r->o.nroots && j < 8; ++j) {
+    res.energies[j] = E ? E[j] : 0.0;
+    res.resid[j] = rep.resid[j];
+  }
+  res.iterations = rep.iterations;
+  res.sigma_calls = rep.sigma_calls;
+  res.converged = rep.converged;
+  res.worker = wid;
+  res.reserved_bytes = r->reserve;
+  res.ndet = (uint64_t)r->a.size() * r->b.size();
+}
+
+// Several small requests in one batched solve on the worker's context.
+void run_batch(sbdgb_server *S, std::vector<Request *> &group, sbdgb_ctx *ctx, int wid) {
+  sbdgb::Ctx &c = ctx->c;
+  const uint64_t launches0 = c.launches;
+  size_t budget = 0;
+  for (Request *r : group) budget += r->reserve;
+  c.budget = budget;
+  std::vector<sbdgb_problem *> ps;
+  std::vector<Request *> live;
+  for (Request *r : group) {
+    sbdgb_problem *p = nullptr;
+    int rc = sbdgb_problem_create(ctx, r->norb, r->a.data(), r->a.size(), r->b.data(), r->b.size(), r->h1.data(),
+                                  r->eri.data(), r->ecore, &p);
+    if (rc == SBDGB_OK) rc = sbdgb_build_tables(p);
+    if (rc == SBDGB_OK) rc = sbdgb_diag_terms(p, nullptr);
+    if (rc != SBDGB_OK) {
+      finish_result(r, rc, c.last_error, nullptr, sbdgb_report{}, wid);
+      if (p) sbdgb_problem_destroy(p);
+      continue;
+    }
+    ps.push_back(p);
+    live.push_back(r);
+  }
+  if (!live.empty()) {
+    const int k = live[0]->o.nroots, n = (int)live.size();
+    std::vector<double> E((size_t)n * k);
+    std::vector<sbdgb_report> reps(n);
+    std::vector<double *> X(n);
+    bool any_x = false;
+    for (int i = 0; i < n; ++i) {
+      X[i] = live[i]->X;
+      any_x = any_x || X[i];
+    }
+    const int rc = sbdgb_batch_davidson(ctx, ps.data(), n, &live[0]->o, E.data(), reps.data(),
+                                        any_x ? X.data() : nullptr);
+    for (int i = 0; i < n; ++i)
+      finish_result(live[i], rc, c.last_error, E.data() + (size_t)i * k, rc == SBDGB_OK ? reps[i] : sbdgb_report{},
+                    wid);
+  }
+  for (sbdgb_problem *p : ps) sbdgb_problem_destroy(p);
+  cudaStreamSynchronize(c.stream);  // the pool frees are done before the reservations go
+  cudaGetLastError();
+  c.in_use = 0;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->launches += c.launches - launches0;
 }
 
 void run_request(sbdgb_server *S, Request *r, sbdgb_ctx *ctx, int wid) {
@@ -164,30 +274,42 @@ void run_request(sbdgb_server *S, Request *r, sbdgb_ctx *ctx, int wid) {
 void worker_loop(sbdgb_server *S, int wid) {
   sbdgb_ctx *ctx = S->ctxs[(size_t)wid];
   cudaSetDevice(S->device);
+  std::vector<Request *> group;
   for (;;) {
     Request *r = nullptr;
     {
       std::unique_lock<std::mutex> lk(S->mu);
       S->cv_work.wait(lk, [&] { return S->stop || (r = admit(S)) != nullptr; });
       if (!r) return;  // stopping, nothing admitted
-      S->reserved += r->reserve;
+      gather(S, r, group);
+      const auto now = Clock::now();
+      for (Request *q : group) {
+        S->reserved += q->reserve;
+        q->t_start = now;
+      }
       S->peak_reserved = std::max(S->peak_reserved, S->reserved);
-      S->running++;
+      S->running += (int)group.size();
+      if (group.size() > 1) S->batched += group.size();
       S->peak_running = std::max(S->peak_running, S->running);
-      r->t_start = Clock::now();
     }
-    run_request(S, r, ctx, wid);
+    if (group.size() == 1)
+      run_request(S, r, ctx, wid);
+    else
+      run_batch(S, group, ctx, wid);
     {
       std::lock_guard<std::mutex> lk(S->mu);
-      r->t_end = Clock::now();
-      r->res.queue_seconds = secs(r->t_submit, r->t_start);
-      r->res.run_seconds = secs(r->t_start, r->t_end);
-      r->res.total_seconds = secs(r->t_submit, r->t_end);
-      S->reserved -= r->reserve;
-      S->running--;
-      S->completed++;
-      if (r->res.status != SBDGB_OK) S->failed++;
-      r->done = true;
+      const auto now = Clock::now();
+      for (Request *q : group) {
+        q->t_end = now;
+        q->res.queue_seconds = secs(q->t_submit, q->t_start);
+        q->res.run_seconds = secs(q->t_start, q->t_end);
+        q->res.total_seconds = secs(q->t_submit, q->t_end);
+        S->reserved -= q->reserve;
+        S->running--;
+        S->completed++;
+        if (q->res.status != SBDGB_OK) S->failed++;
+        q->done = true;
+      }
     }
     S->cv_done.notify_all();
     S->cv_work.notify_all();
@@ -334,6 +456,7 @@ int sbdgb_server_stats(sbdgb_server *S, sbdgb_serve_stats *st) {
   st->running = S->running;
   st->peak_running = S->peak_running;
   st->queued = (int)S->queue.size();
+  st->batched = S->batched;
   return SBDGB_OK;
 }
 

@@ -69,7 +69,7 @@ class ServeStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("failed", C.c_uint64),
                 ("launches", C.c_uint64), ("budget_bytes", C.c_size_t), ("reserved_bytes", C.c_size_t),
                 ("peak_reserved_bytes", C.c_size_t), ("workers", C.c_int), ("running", C.c_int),
-                ("peak_running", C.c_int), ("queued", C.c_int)]
+                ("peak_running", C.c_int), ("queued", C.c_int), ("batched", C.c_uint64)]
 
 
 _lib = None

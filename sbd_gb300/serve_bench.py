@@ -154,7 +154,7 @@ def summarize(results, wall, st, ref_E, precision, rate):
             "failed": len(failed), "first_error": failed[0]["message"] if failed else None,
             "not_converged": sum(1 for r in results if not r["converged"]),
             "peak_running": st["peak_running"], "peak_reserved_GB": st["peak_reserved_bytes"] / 1e9,
-            "launches": st["launches"]}
+            "launches": st["launches"], "batched_requests": st["batched"]}
 
 
 def main(argv=None) -> int:

@@ -104,3 +104,22 @@ def test_wait_timeout_failed_request_and_shutdown():
     for _ in range(3):
         srv.submit_problem(first, nroots=1, eps=1e-8)
     srv.close()
+
+
+def test_small_requests_are_batched(alone):
+    """With one worker busy, the small requests queued behind it start together
+    as one batched solve; each result equals the lone solve."""
+    from sbd_gb300.generators import make_problem
+    from sbd_gb300.serving import Server
+    blocker = make_problem(16, 6, 6, 900, 900, seed=11)  # 810,000 determinants: solved alone
+    mix = _mix()
+    with Server(0, workers=1) as srv:
+        t0 = srv.submit_problem(blocker, nroots=1, eps=1e-8)
+        ts = [srv.submit_problem(p, nroots=1, eps=1e-9, max_nb=20, init=1) for p, _ in mix]
+        assert srv.wait(t0, timeout=300)["status"] == 0
+        res = [srv.wait(t, timeout=300) for t in ts]
+        st = srv.stats()
+    assert st["batched"] >= 2
+    for (p, k), r, a in zip(mix, res, alone):
+        assert r["status"] == 0, r["message"]
+        assert abs(r["energies"][0] - a.energies[0]) <= 1e-10

@@ -240,7 +240,7 @@ int sbdgb_lanczos(sbdgb_problem *p, const sbdgb_davidson_opts *o, double *E, dou
  * iteration each.  No counterpart in the reference.  Options as for
  * sbdgb_davidson with nroots 1..8 and init 1; the subspace is capped at 32.
  * precision MIXED runs the iteration on FP32 vectors and an FP32 sigma until
- * every residual is below 2e-6 |E|, then in FP64 from the lowest Ritz vectors
+ * every residual is below 5e-7 |E|, then in FP64 from the lowest Ritz vectors
  * of that phase to the full tolerance (rep->sigma_fp64 counts the FP64
  * products).  E: count*nroots energies; reps (may be NULL): count reports; X
  * (may be NULL, entries may be NULL): count host buffers of nroots*N for the

@@ -59,7 +59,7 @@ constexpr int kSub = 512;  // elements per block of the kernels without partial 
 constexpr int kSubPer = kCH / kSub;
 constexpr int kT = 256;    // threads per element block
 constexpr int kStepLaunches = 12;
-constexpr double kMixedRel = 2e-6;  // FP32 phase: residual below this times |theta|
+constexpr double kMixedRel = 5e-7;  // FP32 phase: residual below this times |theta|
 constexpr size_t kKpSmem = 48 * 1024;  // largest (P|Q) table staged in shared memory by sigma
 
 struct Chunk {

@@ -1045,7 +1045,7 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
 }
 
 // Two-phase mixed form (precision MIXED with refine_every 0): the Davidson
-// iteration first in FP32 until every residual is below 2e-6 |theta| (at most
+// iteration first in FP32 until every residual is below 5e-7 |theta| (at most
 // 4 max_nb iterations), then in FP64 from the lowest 2k Ritz vectors of that
 // phase (at most 8) to the full tolerance.  FP64 runs at 1/64 of the FP32
 // rate on this GPU; the FP32 phase takes most of the iterations and the FP64
@@ -1060,7 +1060,7 @@ void davidson_two_phase(Problem &p, const sbdgb_davidson_opts &o, double *E, dou
   double *seeds = (double *)workspace(p, WS_C64, sizeof(double) * N * std::max(nseed, k));
   int written = 0;
   CorePhase p32;
-  p32.eps_rel = 2e-6;
+  p32.eps_rel = 5e-7;
   p32.step_cap = 4 * max_nb;
   p32.seed_out = seeds;
   p32.nseed_out = nseed;

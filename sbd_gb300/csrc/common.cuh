@@ -5,7 +5,9 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <array>
 #include <cstdio>
+#include <map>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -167,6 +169,14 @@ struct Ctx {
   cudaMemPool_t pool = nullptr;
   bool autotune = true;
   double *pinned = nullptr;  // page-locked read-back buffer (kPinnedDoubles), made on first use
+  // Autotuned sigma shapes by problem shape (precision, norb, na, nb, alpha and
+  // beta table entries): a problem of a shape seen before on this context takes
+  // the shapes the autotuner chose then instead of timing the candidates again.
+  struct Tuned {
+    int a, b;
+    float ms[3][8];
+  };
+  std::map<std::array<uint64_t, 6>, Tuned> tuned;
 };
 
 constexpr size_t kPinnedDoubles = 8192;

@@ -266,6 +266,14 @@ template <typename T>
 void autotune(Problem &p, Args<T> a, cudaStream_t s) {
   const int prec = std::is_same<T, double>::value ? 0 : 1;
   if (p.tune_a[prec] >= 0 && p.tune_b[prec] >= 0) return;
+  const std::array<uint64_t, 6> key{(uint64_t)prec, (uint64_t)p.norb, p.na, p.nb, p.A.ns + p.A.nd, p.B.ns + p.B.nd};
+  const auto hit = p.ctx->tuned.find(key);
+  if (hit != p.ctx->tuned.end()) {
+    p.tune_a[prec] = hit->second.a;
+    p.tune_b[prec] = hit->second.b;
+    std::copy(&hit->second.ms[0][0], &hit->second.ms[0][0] + 3 * 8, &p.tune_ms[prec][0][0]);
+    return;
+  }
   a.S = (T *)workspace(p, WS_TUNE, sizeof(T) * p.N);
   a.accumulate = 0;
   cudaEvent_t e0, e1;
@@ -327,6 +335,9 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
     p.tune_a[prec] = best_fs;
     p.tune_b[prec] = kFusedShape;
   }
+  Ctx::Tuned t{p.tune_a[prec], p.tune_b[prec], {}};
+  std::copy(&p.tune_ms[prec][0][0], &p.tune_ms[prec][0][0] + 3 * 8, &t.ms[0][0]);
+  p.ctx->tuned[key] = t;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   release_workspace(p, WS_TUNE);

@@ -1,6 +1,7 @@
 """Times sigma and Davidson on one of the synthetic benchmark configurations.
 
     python -m sbd_gb300.probe --config 1 --reps 5 [--davidson 1] [--mixed 1]
+    python -m sbd_gb300.probe --config 4 --request 94 --davidson 1   (one config-4 request)
 
 Prints one JSON line: problem sizes and nonzero counts, table/diagonal build
 times, the FP64 and mixed sigma times (CUDA events on the launch stream, after
@@ -24,7 +25,8 @@ def main(argv=None) -> int:
     from .engine import MIXED, Engine, TPBProblem
 
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 3])
+    ap.add_argument("--config", type=int, default=1, choices=[0, 1, 3, 4])
+    ap.add_argument("--request", type=int, default=94, help="config 4: the request of the seeded mix")
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--davidson", type=int, default=0)
     ap.add_argument("--mixed", type=int, default=1)
@@ -32,7 +34,12 @@ def main(argv=None) -> int:
     a = ap.parse_args(argv)
     build.build()
     t = time.time()
-    prob = {0: G.config0, 1: G.config1, 3: G.config3}[a.config]()
+    eps, max_nb = 1e-8, 24
+    if a.config == 4:
+        prob, a.nroots = G.config4_request(a.request)
+        eps, max_nb = 1e-7, 20
+    else:
+        prob = {0: G.config0, 1: G.config1, 3: G.config3}[a.config]()
     tgen = time.time() - t
     eng = Engine(0)
     t = time.time()
@@ -86,8 +93,11 @@ def main(argv=None) -> int:
             out[f"sigma_mixed_block{nv}_ms_per_vector"] = ms_b / nv
     if a.davidson:
         for prec, name in ((0, "fp64"), (MIXED, "mixed")):
-            r = p.davidson(nroots=a.nroots, max_nb=24, eps=1e-8, init=1, precision=prec, want_vectors=False)
-            out[f"dav_{name}"] = {"E": r.energies.tolist(), **r.report}
+            torch.cuda.synchronize()
+            t = time.time()
+            r = p.davidson(nroots=a.nroots, max_nb=max_nb, eps=eps, init=1, precision=prec, want_vectors=False)
+            torch.cuda.synchronize()
+            out[f"dav_{name}"] = {"E": r.energies.tolist(), "wall_s": time.time() - t, **r.report}
     print(json.dumps(out))
     p.close()
     eng.close()

@@ -95,45 +95,23 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
 #pragma unroll
     for (int c = 0; c < CPT; ++c) part[c] = T(0);
     const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
-    if constexpr (std::is_same<T, double>::value) {
-      // FP64: the beta singles of each column outside (their table entries
-      // are read once per thread), the alpha singles of the row inside (the
-      // same entries for every thread: broadcast loads), so a term costs two
-      // scattered loads (the (P|Q) value and C) instead of five
+    // the beta singles of each column outside (their table entries are read
+    // once per thread), the alpha singles of the row inside (the same entries
+    // for every thread: broadcast loads): a term costs two scattered loads
+    // (the (P|Q) value and C) instead of five, and one more popcount
 #pragma unroll
-      for (int c = 0; c < CPT; ++c) {
-        for (uint32_t q = q0[c]; q < q1[c]; ++q) {
-          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-          const Wd mb = word<Wd>(a.B.mask_s, q);
-          const uint32_t kb = (cb >> 16) & 0x7fffu, sb = cb >> 31;
-          for (uint32_t p = p0; p < p1; ++p) {
-            const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
-            const uint32_t ph =
-                (parity(beta[c] & word<Wd>(a.A.mask_s, p)) ^ parity(word<Wd>(a.astr, ja) & mb) ^ (ca >> 31) ^ sb) &
-                1u;
-            madd<T>(acc[c], part[c], flip(__ldg(a.Kp + ((ca >> 16) & 0x7fffu) * a.npair + kb), ph),
-                    __ldg(a.C + (size_t)ja * a.nb + jb));
-          }
-        }
-      }
-    } else {
-      // FP32: the alpha singles outside, so the alpha part of the phase is
-      // taken once per pair (these kernels are bound by integer work)
-      for (uint32_t p = p0; p < p1; ++p) {
-        const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
-        const Wd ma = word<Wd>(a.A.mask_s, p);
-        const Wd alpha_ket = word<Wd>(a.astr, ja);
-        const T *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
-        const T *crow = a.C + (size_t)ja * a.nb;
-#pragma unroll
-        for (int c = 0; c < CPT; ++c) {
-          const uint32_t pa = parity(beta[c] & ma) ^ (ca >> 31);
-          for (uint32_t q = q0[c]; q < q1[c]; ++q) {
-            const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-            const Wd mb = word<Wd>(a.B.mask_s, q);
-            const uint32_t ph = (pa ^ parity(alpha_ket & mb) ^ (cb >> 31)) & 1u;
-            madd<T>(acc[c], part[c], flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph), __ldg(crow + jb));
-          }
+    for (int c = 0; c < CPT; ++c) {
+      for (uint32_t q = q0[c]; q < q1[c]; ++q) {
+        const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+        const Wd mb = word<Wd>(a.B.mask_s, q);
+        const uint32_t kb = (cb >> 16) & 0x7fffu, sb = cb >> 31;
+        for (uint32_t p = p0; p < p1; ++p) {
+          const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
+          const uint32_t ph =
+              (parity(beta[c] & word<Wd>(a.A.mask_s, p)) ^ parity(word<Wd>(a.astr, ja) & mb) ^ (ca >> 31) ^ sb) &
+              1u;
+          madd<T>(acc[c], part[c], flip(__ldg(a.Kp + ((ca >> 16) & 0x7fffu) * a.npair + kb), ph),
+                  __ldg(a.C + (size_t)ja * a.nb + jb));
         }
       }
     }
@@ -528,21 +506,45 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
 #pragma unroll
       for (int c = 0; c < CPT; ++c) part[n][c] = 0.f;
     const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
-    for (uint32_t p = p0; p < p1; ++p) {
-      const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
-      const Wd ma = word<Wd>(a.A.mask_s, p);
-      const Wd alpha_ket = word<Wd>(a.astr, ja);
-      const float *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
-      const uint32_t rowoff = ja * a.nb;
+    if constexpr (sizeof(Wd) == 8) {
+      // 64-bit words: beta singles outside, alpha singles inside (as in
+      // k_sigma_alpha); with 32-bit words the extra popcount per term costs
+      // more than the loads it saves once NV vectors share them
 #pragma unroll
       for (int c = 0; c < CPT; ++c) {
-        const uint32_t pa = parity(beta[c] & ma) ^ (ca >> 31);
         for (uint32_t q = q0[c]; q < q1[c]; ++q) {
           const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-          const uint32_t ph = (pa ^ parity(alpha_ket & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31)) & 1u;
-          const float kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
+          const Wd mb = word<Wd>(a.B.mask_s, q);
+          const uint32_t kb = (cb >> 16) & 0x7fffu, sb = cb >> 31;
+          for (uint32_t p = p0; p < p1; ++p) {
+            const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
+            const uint32_t ph =
+                (parity(beta[c] & word<Wd>(a.A.mask_s, p)) ^ parity(word<Wd>(a.astr, ja) & mb) ^ (ca >> 31) ^ sb) &
+                1u;
+            const float kv = flip(__ldg(a.Kp + ((ca >> 16) & 0x7fffu) * a.npair + kb), ph);
+            const uint32_t off = ja * a.nb + jb;
 #pragma unroll
-          for (int n = 0; n < NV; ++n) part[n][c] = fmaf(kv, __ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
+            for (int n = 0; n < NV; ++n) part[n][c] = fmaf(kv, __ldg(m.Cv[n] + off), part[n][c]);
+          }
+        }
+      }
+    } else {
+      for (uint32_t p = p0; p < p1; ++p) {
+        const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
+        const Wd ma = word<Wd>(a.A.mask_s, p);
+        const Wd alpha_ket = word<Wd>(a.astr, ja);
+        const float *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
+        const uint32_t rowoff = ja * a.nb;
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+          const uint32_t pa = parity(beta[c] & ma) ^ (ca >> 31);
+          for (uint32_t q = q0[c]; q < q1[c]; ++q) {
+            const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+            const uint32_t ph = (pa ^ parity(alpha_ket & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31)) & 1u;
+            const float kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
+#pragma unroll
+            for (int n = 0; n < NV; ++n) part[n][c] = fmaf(kv, __ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
+          }
         }
       }
     }

@@ -133,7 +133,10 @@ def test_sigma_every_tile_shape(gcase, shapes):
 @pytest.mark.parametrize("shapes", [(0, 0), (1, 2), (3, 3), (0, 4), (3, 4)])
 @pytest.mark.parametrize("nvec", [2, 3, 4, 5])
 def test_mixed_block_sigma_equals_single(gcase, shapes, nvec):
-    """The multi-vector FP32 product gives each vector's single-vector product bit for bit."""
+    """The multi-vector FP32 product gives each vector's single-vector product: bit
+    for bit when both sum the alpha-beta terms in the same order (norb > 32), to
+    FP32 rounding otherwise (with 32-bit words the single-vector kernel takes the
+    beta singles outside, the multi-vector one inside)."""
     import torch
     c, p = gcase
     p.diag_terms()
@@ -147,4 +150,7 @@ def test_mixed_block_sigma_equals_single(gcase, shapes, nvec):
         y = torch.empty(N, dtype=torch.float32, device="cuda")
         p.sigma_mixed_device(X[j].data_ptr(), y.data_ptr(), stream=0)
         torch.cuda.synchronize()
-        assert torch.equal(Y[j], y), (j, shapes)
+        if c.norb > 32:
+            assert torch.equal(Y[j], y), (j, shapes)
+        else:
+            assert max_rel(Y[j].double().cpu().numpy(), y.double().cpu().numpy()) <= 2e-6, (j, shapes)

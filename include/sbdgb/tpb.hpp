@@ -538,6 +538,7 @@ inline SBD generate_sbd_data(int argc, char *argv[]) {
     else if (a == "--bit_length") d.bit_length = std::atoi(v);
     else if (a == "--nroots") d.nroots = std::atoi(v);
     else if (a == "--precision") d.precision = std::atoi(v);
+    else if (a == "--refine_every") d.refine_every = std::atoi(v);
     else if (a == "--device") d.device = std::atoi(v);
   }
   return d;

@@ -139,8 +139,11 @@ def make_problem():
 
 def cpu_sample(prob, rows: int, nsigma: float, threads: int) -> dict:
     """Times the oracle port's sigma on `rows` alpha rows and scales to a solve."""
+    import oracle.oracle as orc
     from oracle.oracle import Oracle
     os.environ["OMP_NUM_THREADS"] = str(threads)
+    # a launcher (torchrun) may have started the OpenMP runtime with one thread
+    orc.lib().orc_set_threads(threads)
     o = Oracle.from_problem(prob)
     r0, r1 = 0, rows
     C = np.random.default_rng(5).uniform(-1.0, 1.0, prob.ndet)

@@ -48,6 +48,8 @@ def lib():
         L.orc_ints_create.restype = C.c_void_p
         L.orc_ints_create.argtypes = [C.c_int, C.c_double, _f64p, _f64p]
         L.orc_ints_destroy.argtypes = [C.c_void_p]
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_set_threads.restype = None
         L.orc_excitations.restype = C.c_int
         L.orc_excitations.argtypes = [_u64p, C.c_size_t, C.c_int, C.c_int, C.c_int, C.c_int,
                                       _szp, _szp, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]

@@ -75,6 +75,10 @@ orc_ints *orc_ints_create(int L, double I0, const double *h1, const double *eri_
   return t;
 }
 
+void orc_set_threads(int n) {
+  if (n > 0) omp_set_num_threads(n);
+}
+
 void orc_ints_destroy(orc_ints *t) {
   if (!t) return;
   free(t->I1);

@@ -39,6 +39,11 @@ typedef struct orc_ints orc_ints;
 orc_ints *orc_ints_create(int L, double I0, const double *h1, const double *eri_packed);
 void orc_ints_destroy(orc_ints *ints);
 
+/* Threads of the following parallel loops (omp_set_num_threads); n <= 0 keeps
+ * the current setting.  A launcher may export OMP_NUM_THREADS=1 before the
+ * OpenMP runtime starts; the timed CPU baseline sets its own count here. */
+void orc_set_threads(int n);
+
 /* Excitation lists of one spin (helper.h:185-342, GenerateExcitation with
  * bra = ket = the whole list, i.e. MPI size 1).  spin = 0 (alpha) stores
  * spin-orbital indices 2p, spin = 1 (beta) stores 2p+1.

@@ -965,7 +965,13 @@ void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph
         Q.insert(Q.end(), v.begin(), v.end());
         ++m;
       }
-      sv.combine<F>(V, HV, nv, m, Q, th, X, HX, nullptr);
+      // V Q and HV Q (m <= 3k columns) in blocks of at most 16 columns
+      for (int b0 = 0; b0 < m; b0 += 16) {
+        const int mb = std::min(16, m - b0);
+        const std::vector<double> Qb(Q.begin() + (size_t)nv * b0, Q.begin() + (size_t)nv * (b0 + mb));
+        sv.combine<F>(V, HV, nv, mb, Qb, std::vector<double>(mb, 0.0), X + (size_t)b0 * N, HX + (size_t)b0 * N,
+                      nullptr);
+      }
       SBDGB_CUDA(cudaMemcpyAsync(V, X, sizeof(F) * N * m, cudaMemcpyDeviceToDevice, s));
       SBDGB_CUDA(cudaMemcpyAsync(HV, HX, sizeof(F) * N * m, cudaMemcpyDeviceToDevice, s));
       std::vector<double> A((size_t)nv * nv), AQ((size_t)nv * m, 0.0), Hn((size_t)m * m, 0.0), cn((size_t)m * kk, 0.0);

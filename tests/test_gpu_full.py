@@ -158,3 +158,17 @@ def test_more_roots_than_determinants_is_an_error(engine):
         p.davidson(nroots=3)
     assert e.value.status == 1
     p.close()
+
+
+def test_eight_roots_restart_basis_over_sixteen_columns(engine):
+    """Eight roots with a small subspace: once some roots converge the restart
+    keeps 2k Ritz vectors plus previous directions (up to 24 columns)."""
+    prob = make_problem(12, 4, 4, 150, 140, seed=23)
+    p = TPBProblem.from_problem(engine, prob)
+    try:
+        w = Oracle.from_problem(prob).lowest(8)
+        r = p.davidson(nroots=8, max_nb=26, eps=1e-9, init=1, want_vectors=False)
+        assert r.report["converged"] and r.report["restarts"] > 0
+        assert np.allclose(r.energies, w, atol=1e-8)
+    finally:
+        p.close()

@@ -66,3 +66,30 @@ def test_mixed_davidson_two_roots_norb16(engine, refine_every):
     assert np.max(np.abs(rmx.energies - r64.energies)) < 1e-8
     if refine_every == 0:
         assert rmx.report["sigma_fp64"] < r64.report["sigma_fp64"]
+
+
+def test_two_phase_caller_start_vectors_and_many_roots(engine):
+    """The two-phase form with init 2 (caller vectors seed the FP32 phase) and
+    with eight roots, against the FP64 solver."""
+    prob = make_problem(12, 4, 4, 120, 110, seed=17)
+    p = TPBProblem.from_problem(engine, prob)
+    r64 = p.davidson(nroots=8, max_nb=24, eps=1e-8, init=1, want_vectors=True)
+    assert r64.report["converged"]
+    r8 = p.davidson(nroots=8, max_nb=24, eps=1e-8, init=1, precision=MIXED, refine_every=0, want_vectors=False)
+    assert r8.report["converged"]
+    assert np.max(np.abs(r8.energies - r64.energies)) < 1e-8
+    # start from slightly perturbed FP64 vectors: converges to the same pair
+    X0 = r64.vectors[:2] + 1e-3 * np.random.default_rng(0).standard_normal((2, prob.ndet))
+    r2 = p.davidson(nroots=2, max_nb=16, eps=1e-8, init=2, precision=MIXED, refine_every=0, X0=X0)
+    assert r2.report["converged"]
+    assert np.max(np.abs(r2.energies - r64.energies[:2])) < 1e-8
+
+
+@pytest.mark.parametrize("na,nb,k", [(1, 5, 3), (2, 2, 3)])
+def test_two_phase_more_than_half_the_space_in_roots(engine, na, nb, k):
+    from oracle.oracle import Oracle
+    prob = make_problem(8, 3, 3, na, nb, seed=70 + na + nb)
+    p = TPBProblem.from_problem(engine, prob)
+    w = np.linalg.eigvalsh(Oracle.from_problem(prob).hamiltonian().toarray())
+    r = p.davidson(nroots=k, max_nb=24, eps=1e-9, init=1, precision=MIXED, refine_every=0, want_vectors=False)
+    assert np.allclose(r.energies, w[:k], atol=1e-8)

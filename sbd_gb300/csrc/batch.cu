@@ -21,11 +21,12 @@
 //     blocks per chunk, so that the last few problems still fill the GPU;
 //   - dot products leave one partial per chunk (no atomics) that a
 //     per-problem warp sums in chunk order, so results are deterministic;
-//   - the projected eigenproblem (n <= 32) is cyclic Jacobi by one warp per
-//     problem, which also does the small coefficient-space work;
+//   - the projected eigenproblem (n <= 32) is a parallel-order Jacobi by one
+//     warp per problem, which also does the small coefficient-space work;
 //   - sigma is the fused per-element form (diagonal, alpha pairs of the row,
 //     alpha x beta singles, beta pairs of the column) for up to 8 vectors at
-//     once, sharing the index, value and phase work between the vectors.
+//     once, sharing the index, value and phase work between the vectors; the
+//     (P|Q) table sits in shared memory when it fits.
 //
 // Mixed form (precision MIXED): FP64 arithmetic runs at 1/64 of the FP32 rate
 // on this GPU and the FP64 sigma above keeps the FP64 pipe ~97% busy, so the
@@ -38,9 +39,9 @@
 // removes FP64 iterations (about 60% of the FP64 sigma products on the
 // norb-12 batch).
 #include <algorithm>
-#include <type_traits>
 #include <chrono>
 #include <cmath>
+#include <type_traits>
 
 #include "common.cuh"
 #include "sigma_dev.cuh"

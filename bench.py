@@ -15,7 +15,9 @@ diagonal resident, starting from the lowest diagonal entries).
           per-product device time is recorded with CUDA events on its launch
           stream during the timed region; algorithmic bytes per product are
           24*N + 8*nnz_off (read C and hii, write sigma, one 8-byte C read per
-          off-diagonal element)
+          off-diagonal element).  roofline.fp64 gives the same product against
+          the measured FP64 FMA rate (one FMA per nonzero), which is what
+          bounds these kernels on this GPU
   cpu_baseline : the CPU oracle port of the reference's TRADMODE sigma (OpenMP,
           all host cores) timed on a bounded sample of alpha rows and scaled to
           the solve's sigma count
@@ -252,6 +254,11 @@ def run_gpu(args):
     sigma_ms_per = sigma_ms / max(ncalls, 1)
     achieved = bytes_sigma / (sigma_ms_per * 1e-3) / 1e9
     peak, peak_kind = peaks()
+    # the sigma kernels are bound by the FP64 FMA pipe: one FMA per off-diagonal
+    # element and per diagonal element, against the measured FP64 FMA rate
+    from sbd_gb300.engine import measure_fp64_rates
+    rates = measure_fp64_rates(local)
+    fp64_achieved = 2.0 * (nnz_off + N) / (sigma_ms_per * 1e-3) / 1e12
     tiles = p.tuning(0)
 
     # mixed-precision form on the same problem (reported beside the FP64 headline)
@@ -366,7 +373,12 @@ def run_gpu(args):
                          "frac": achieved / peak, "traffic": traffic,
                          "kernel": ("sigma operator (fused k_sigma_alpha)" if tiles.get("beta_shape") == "fused"
                                     else "sigma operator (k_transpose + k_sigma_alpha + k_sigma_beta)"),
-                         "algorithmic_bytes": bytes_sigma, "peak_kind": f"{peak_kind} hbm_gbs"},
+                         "algorithmic_bytes": bytes_sigma, "peak_kind": f"{peak_kind} hbm_gbs",
+                         "fp64": {"unit": "TFLOP/s", "achieved": fp64_achieved, "peak": rates["dfma_tflops"],
+                                  "frac": fp64_achieved / rates["dfma_tflops"],
+                                  "peak_kind": "measured FP64 FMA pipe (sbdgb_measure_fp64_rates)",
+                                  "fp64_tensor_peak": rates["dmma_tflops"],
+                                  "flops": "2 x (nnz_off + N) per sigma"}},
             "mixed_precision": mixed,
             "serving": serving,
             "batched": batched,

@@ -158,6 +158,13 @@ int sbdgb_problem_set_tuning(sbdgb_problem *p, int precision, int shape_a, int s
  * shape otherwise, and records no timing events. */
 int sbdgb_sigma_noalloc(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accumulate, void *stream);
 
+/* Measured FP64 rates of `device` in TFLOP/s (no reference counterpart): the
+ * FP64 FMA pipe and the FP64 tensor path (mma.sync m8n8k4 f64), each from a
+ * register-only loop over 8 blocks of 256 threads per SM timed with CUDA
+ * events.  The sigma kernels and the solver's vector algebra are bound by the
+ * FP64 FMA rate; the bench reports them against it. */
+int sbdgb_measure_fp64_rates(int device, double *dfma_tflops, double *dmma_tflops);
+
 /* Occupation density of a vector (OccupationDensity, chemistry/tpb/
  * occupation.h:11-95, as sbd::tpb::diag reports it with do_rdm == 0,
  * sbdiag.h:666-699): density[2p] = sum over determinants of |W|^2 with alpha

@@ -139,31 +139,88 @@ def make_problem():
     return config1()
 
 
-def cpu_sample(prob, rows: int, nsigma: float, threads: int) -> dict:
-    """Times the oracle port's sigma on `rows` alpha rows and scales to a solve."""
-    import oracle.oracle as orc
-    from oracle.oracle import Oracle
-    os.environ["OMP_NUM_THREADS"] = str(threads)
-    # a launcher (torchrun) may have started the OpenMP runtime with one thread
-    orc.lib().orc_set_threads(threads)
-    o = Oracle.from_problem(prob)
-    r0, r1 = 0, rows
-    C = np.random.default_rng(5).uniform(-1.0, 1.0, prob.ndet)
-    hii = o.hii(rows=(r0, r1))
-    t = time.perf_counter()
-    o.mult(C, rows=(r0, r1), hii=hii)
-    dt = time.perf_counter() - t
-    t_sigma = dt * prob.astr.size / rows
-    solve = t_sigma * nsigma
-    return {"value": 1.0 / solve, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": (f"oracle port (restated reference TRADMODE mult, OpenMP {threads} threads) on alpha rows "
-                       f"[{r0},{r1}) of {prob.astr.size}: {dt:.2f} s -> {t_sigma:.1f} s per sigma x "
-                       f"{nsigma:.0f} sigma products per solve (the GPU solve's count); vector algebra not counted"),
-            "sigma_seconds_est": t_sigma}
+# sigma products per config-1 solve: the GPU FP64 solve's count on this
+# problem (2 roots, subspace 24, tol 1e-8; bench line "sigma_products_per_solve").
+# The reference arm runs without a GPU and takes it from here.
+NSIGMA_CONFIG1 = 139
+
+
+class ReferenceCPU:
+    """The reference's CPU path for the config-1 solve, timed on the host cores.
+
+    The oracle port restates the reference's TRADMODE mult (chemistry/tpb/
+    mult.h:440-558) and the vector algebra of its Davidson step (davidson.h:
+    778-923), OpenMP on `threads` threads.  One solve is modelled as nsigma
+    sigma products, each followed by one Davidson step's vector algebra at the
+    mean subspace position (the work per step grows linearly with it).  A
+    slice is a contiguous range of alpha rows: the sigma rows of that range
+    plus the step algebra on its share of the elements.  Slices [i*na/K,
+    (i+1)*na/K) for i < K cover one full sigma product and one full step, so
+    K timed slices measure that exactly; the diagonal (once per solve) and the
+    3x3-24x24 eigensolves are not counted.
+    """
+
+    def __init__(self, prob, threads: int, nsigma: float, max_nb: int = MAX_NB):
+        import oracle.oracle as orc
+        from oracle.oracle import Oracle
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+        orc.lib().orc_set_threads(threads)  # a launcher may have started OpenMP with one thread
+        self.lib = orc.lib()
+        self.threads, self.nsigma, self.max_nb = threads, float(nsigma), max_nb
+        self.na, self.nb = prob.astr.size, prob.bstr.size
+        self.o = Oracle.from_problem(prob)
+        rng = np.random.default_rng(5)
+        self.C = rng.uniform(-1.0, 1.0, prob.ndet)
+        self.S = np.zeros(prob.ndet)
+        self.hii = self.o.hii()
+        self.ib = max_nb // 2  # mean subspace position of a step, (max_nb - 1) / 2 rounded up
+        self._alg = None
+
+    def slice_rows(self, i: int, k: int) -> tuple[int, int]:
+        return self.na * i // k, self.na * (i + 1) // k
+
+    def run_slice(self, r0: int, r1: int) -> dict:
+        n = (r1 - r0) * self.nb
+        if self._alg is None or self._alg[0].size < (self.ib + 2) * n:
+            rng = np.random.default_rng(6)
+            self._alg = (rng.uniform(-1, 1, (self.ib + 2) * n), rng.uniform(-1, 1, (self.ib + 1) * n),
+                         np.zeros(n), np.zeros(n))
+        Ca, HCa, W, R = self._alg
+        t0 = time.perf_counter()
+        self.o.mult(self.C, out=self.S, rows=(r0, r1), hii=self.hii)
+        t1 = time.perf_counter()
+        self.lib.orc_algebra_step(Ca[:(self.ib + 2) * n], HCa[:(self.ib + 1) * n], W[:n], R[:n],
+                                  self.hii[r0 * self.nb:r1 * self.nb], n, self.ib)
+        t2 = time.perf_counter()
+        return {"sigma_s": t1 - t0, "algebra_s": t2 - t1, "total_s": t2 - t0}
+
+    def describe(self, k: int, sigma_s: float, algebra_s: float) -> str:
+        return (f"oracle port (restated reference TRADMODE mult + Davidson step algebra, OpenMP {self.threads} "
+                f"threads), config 1 in {k} slices of alpha rows covering one full sigma product: "
+                f"{sigma_s:.1f} s sigma + {algebra_s:.2f} s step algebra (subspace position {self.ib} of "
+                f"{self.max_nb}) per step, x {self.nsigma:.0f} steps per solve (the GPU FP64 solve's sigma "
+                f"count on this problem); diagonal and small eigensolves not counted")
+
+
+def cpu_baseline(prob, nsigma: float, threads: int, k: int = 20) -> dict:
+    """The CPU baseline beside the GPU number: one full sigma + step algebra
+    of the reference's CPU path (ReferenceCPU), scaled to a solve."""
+    ref = ReferenceCPU(prob, threads, nsigma)
+    sig = alg = 0.0
+    for i in range(k):
+        t = ref.run_slice(*ref.slice_rows(i, k))
+        sig += t["sigma_s"]
+        alg += t["algebra_s"]
+    return {"value": 1.0 / (nsigma * (sig + alg)), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": ref.describe(k, sig, alg), "sigma_seconds": sig, "algebra_seconds": alg}
 
 
 def run_reference(args):
-    """--impl reference: the reference's CPU algorithm (oracle port) on the host cores."""
+    """--impl reference: the reference's CPU algorithm (oracle port) on the host
+    cores.  Each step is one slice of the config-1 solve (ReferenceCPU): the K
+    timed steps together are one full sigma product and one Davidson step's
+    vector algebra, i.e. 1/nsigma of a solve, so ms_per_step is the measured
+    time of a step and value = 1 / (nsigma x the timed region)."""
     dist, rank, ws = dist_init()
     if rank != 0:
         return 0
@@ -171,26 +228,124 @@ def run_reference(args):
     orc.build()
     threads = os.cpu_count() or 1
     prob = make_problem()
-    nsigma = float(os.environ.get("SBDGB_REF_NSIGMA", "40"))
-    rows = int(os.environ.get("SBDGB_REF_ROWS", "6"))
-    cpu_sample(prob, 1, nsigma, threads)  # warm the tables and caches
-    vals = []
+    ref = ReferenceCPU(prob, threads, NSIGMA_CONFIG1)
+    K = max(1, args.steps)
+    for i in range(args.warmup):
+        ref.run_slice(*ref.slice_rows(i % K, K))
+    sig = alg = 0.0
     t0 = time.perf_counter()
-    for step in range(args.warmup + args.steps):
-        s = cpu_sample(prob, rows, nsigma, threads)
-        if step >= args.warmup:
-            vals.append(s["value"])
+    for i in range(K):
+        t = ref.run_slice(*ref.slice_rows(i, K))
+        sig += t["sigma_s"]
+        alg += t["algebra_s"]
     wall = time.perf_counter() - t0
-    value = float(np.median(vals))
+    value = 1.0 / (NSIGMA_CONFIG1 * wall)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / value,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * wall / K,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "inputs": "host memory"},
+            "data": "synthetic", "config": config_block(prob, ws),
+            "step": (f"one of {K} slices of alpha rows of the config-1 solve's sigma product plus its share of a "
+                     f"Davidson step's vector algebra; the timed region is 1/{NSIGMA_CONFIG1} of a solve "
+                     "(value extrapolates it to solves/s)"),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": s["sample"]},
+                             "sample": ref.describe(K, sig, alg)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": wall}
     print(json.dumps(line))
+    return 0
+
+
+def config_block(prob, ws: int = 1) -> dict:
+    """The line's config: the same keys and values in both arms."""
+    return {"workload": WORKLOAD, "parallelism": f"replicas x{ws}",
+            "l2": "inputs larger than L2 (288 MB per vector, 13.8 GB subspace)", "ndet": int(prob.ndet)}
+
+
+def run_sigma_probe(a) -> int:
+    """--sigma-probe CONFIG: times sigma (and optionally one Davidson solve per
+    precision) on one synthetic configuration and prints one JSON line:
+    problem sizes and nonzero counts, table/diagonal build times, the FP64 and
+    mixed sigma times (CUDA events on the launch stream, after two untimed
+    products) with their model bandwidth (24N + 8 nnz bytes FP64, 16N + 4 nnz
+    mixed), the mixed product of 2-4 vectors at once (time per vector) and the
+    autotuner's tile choice.  Config 4 takes one request of the seeded mix
+    (--request).  This is the command the ncu summaries under profiles/ run."""
+    import torch
+
+    from sbd_gb300 import build
+    from sbd_gb300 import generators as G
+    from sbd_gb300.engine import MIXED, Engine, TPBProblem
+
+    a.config = a.sigma_probe
+    build.build()
+    t = time.time()
+    eps, max_nb = 1e-8, 24
+    if a.config == 4:
+        prob, a.nroots = G.config4_request(a.request)
+        eps, max_nb = 1e-7, 20
+    else:
+        prob = {0: G.config0, 1: G.config1, 3: G.config3}[a.config]()
+    tgen = time.time() - t
+    eng = Engine(0)
+    t = time.time()
+    p = TPBProblem.from_problem(eng, prob)
+    p.build_tables()
+    torch.cuda.synchronize()
+    ttab = time.time() - t
+    t = time.time()
+    p.diag_terms()
+    tdiag = time.time() - t
+    (sa, da), (sb, db) = p.table_counts(0), p.table_counts(1)
+    N = prob.ndet
+    na, nb = prob.astr.size, prob.bstr.size
+    nnz = nb * (sa + da) + na * (sb + db) + sa * sb
+    out = {"config": a.config, "N": N, "na": na, "nb": nb, "singles_a": sa, "doubles_a": da, "singles_b": sb,
+           "doubles_b": db, "nnz_off": nnz, "nnz_per_row": nnz / N, "t_gen": tgen, "t_tables": ttab, "t_diag": tdiag}
+    st = torch.cuda.current_stream()
+    C = torch.rand(N, dtype=torch.float64, device="cuda") * 2 - 1
+    S = torch.empty_like(C)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(a.reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / a.reps
+
+    ms = timed(lambda: p.sigma_device(C.data_ptr(), S.data_ptr(), stream=st.cuda_stream))
+    out["sigma_fp64_ms"] = ms
+    out["sigma_fp64_GBs_model"] = (24 * N + 8 * nnz) / (ms * 1e-3) / 1e9
+    out["sigma_fp64_Gnnz_s"] = nnz / (ms * 1e-3) / 1e9
+    out["tuning_fp64"] = p.tuning(0)
+    if a.mixed:
+        C32 = C.float()
+        S32 = torch.empty_like(C32)
+        msm = timed(lambda: p.sigma_mixed_device(C32.data_ptr(), S32.data_ptr(), stream=st.cuda_stream))
+        out["sigma_mixed_ms"] = msm
+        out["sigma_mixed_GBs_model"] = (16 * N + 4 * nnz) / (msm * 1e-3) / 1e9
+        out["sigma_mixed_relerr"] = float((S32.double() - S).abs().max() / S.abs().max())
+        out["tuning_mixed"] = p.tuning(MIXED)
+        # several FP32 vectors per product: time per vector
+        for nv in (2, 3, 4):
+            X = torch.rand(nv, N, dtype=torch.float32, device="cuda") * 2 - 1
+            Y = torch.empty_like(X)
+            ms_b = timed(lambda: p.sigma_mixed_block_device(X.data_ptr(), Y.data_ptr(), nv, stream=st.cuda_stream))
+            out[f"sigma_mixed_block{nv}_ms_per_vector"] = ms_b / nv
+    if a.davidson:
+        for prec, name in ((0, "fp64"), (MIXED, "mixed")):
+            torch.cuda.synchronize()
+            t = time.time()
+            r = p.davidson(nroots=a.nroots, max_nb=max_nb, eps=eps, init=1, precision=prec, want_vectors=False)
+            torch.cuda.synchronize()
+            out[f"dav_{name}"] = {"E": r.energies.tolist(), "wall_s": time.time() - t, **r.report}
+    print(json.dumps(out))
+    p.close()
+    eng.close()
     return 0
 
 
@@ -282,7 +437,7 @@ def run_gpu(args):
     h2d = prob.astr.nbytes + prob.bstr.nbytes + prob.ints.h1.nbytes + prob.ints.eri.nbytes
     d2h = NROOTS * N * 8 + NROOTS * 8
     p.close()
-    for _ in range(max(1, args.e2e_steps)):
+    for _ in range(max(1, args.e2e_steps if args.e2e_steps is not None else args.steps)):
         torch.cuda.synchronize()
         t = time.perf_counter()
         q = TPBProblem.from_problem(eng, prob)
@@ -350,8 +505,7 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
-            cpu = cpu_sample(prob, args.cpu_rows, float(np.mean(nsig)), os.cpu_count() or 1)
-            cpu.pop("sigma_seconds_est", None)
+            cpu = cpu_baseline(prob, float(np.mean(nsig)), os.cpu_count() or 1)
         except Exception as e:  # the baseline is reported, not required
             cpu = {"error": str(e)}
 
@@ -361,9 +515,8 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * t_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "parallelism": f"replicas x{ws}",
-                       "l2": "inputs larger than L2 (288 MB per vector, 13.8 GB subspace)",
-                       "nnz_offdiag": int(nnz_off), "nnz_per_row": nnz_off / N},
+            "config": config_block(prob, ws),
+            "problem": {"nnz_offdiag": int(nnz_off), "nnz_per_row": nnz_off / N},
             "energies": [float(x) for x in energies],
             "latency_s": {"p50": float(np.percentile(lat_sorted, 50)), "p99": float(np.percentile(lat_sorted, 99))},
             "sigma_products_per_solve": float(np.mean(nsig)),
@@ -401,8 +554,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--cpu-rows", type=int, default=48)
+    ap.add_argument("--e2e-steps", type=int, default=None, help="end-to-end solves (default: --steps)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--mixed-steps", type=int, default=2)
@@ -412,7 +564,16 @@ def main():
                     help="config-2 problems for the batched block (0: skip)")
     ap.add_argument("--batch-serial", type=int, default=32,
                     help="of which solved one at a time on the plain FP64 path")
+    ap.add_argument("--sigma-probe", type=int, default=None, choices=[0, 1, 3, 4],
+                    help="time sigma on one configuration instead of the solve benchmark")
+    ap.add_argument("--request", type=int, default=94, help="--sigma-probe 4: the request of the seeded mix")
+    ap.add_argument("--reps", type=int, default=5, help="--sigma-probe: timed products")
+    ap.add_argument("--davidson", type=int, default=0, help="--sigma-probe: also one solve per precision")
+    ap.add_argument("--mixed", type=int, default=1, help="--sigma-probe: also the mixed sigma")
+    ap.add_argument("--nroots", type=int, default=2, help="--sigma-probe: roots of the solve")
     args = ap.parse_args()
+    if args.sigma_probe is not None:
+        return run_sigma_probe(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -31,11 +31,17 @@ def build() -> str:
     return LIB_PATH
 
 
-def build_reference(reference_root: str = "/root/reference") -> str | None:
-    """Compiles the reference harness into oracle/_ref when the reference tree exists."""
-    if not os.path.isdir(os.path.join(reference_root, "include", "sbd")):
+def build_reference(reference_root: str | None = None) -> str | None:
+    """Compiles the reference harness into oracle/_ref when the reference tree
+    exists.  The tree is `reference_root`, else $SBD_REFERENCE_ROOT, else the
+    default that oracle/Makefile names; without a tree nothing is built."""
+    root = reference_root or os.environ.get("SBD_REFERENCE_ROOT")
+    cmd = ["make", "-s", "-C", HERE, "ref"] + ([f"REFERENCE_ROOT={root}"] if root else [])
+    probe = subprocess.run(["make", "-s", "-C", HERE, "reference-root"] + cmd[5:], capture_output=True, text=True)
+    tree = probe.stdout.strip()
+    if probe.returncode != 0 or not os.path.isdir(os.path.join(tree, "include", "sbd")):
         return None
-    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REFERENCE_ROOT={reference_root}"], check=True)
+    subprocess.run(cmd, check=True)
     return REF_BIN
 
 
@@ -70,6 +76,8 @@ def lib():
                                       + [_f64p, _f64p, _f64p])
         L.orc_inner.restype = C.c_double
         L.orc_inner.argtypes = [_f64p, _f64p, C.c_size_t]
+        L.orc_algebra_step.restype = None
+        L.orc_algebra_step.argtypes = [_f64p, _f64p, _f64p, _f64p, _f64p, C.c_size_t, C.c_int]
         L.orc_symeig.argtypes = [C.c_int, _f64p, C.c_int, _f64p]
         _lib = L
     return _lib

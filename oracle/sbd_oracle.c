@@ -485,6 +485,51 @@ void orc_symeig(int n, double *A, int lda, double *w) {
 
 /* ---- Davidson: chemistry/tpb/davidson.h:707-970 ------------------------ */
 
+/* The vector algebra of one step of the reference's Davidson
+ * (chemistry/tpb/davidson.h:778-923) at subspace position ib, on n elements,
+ * without the sigma product: the ib+1 projections <C_j|HC_ib> (:802-805),
+ * the Ritz vector and residual over the ib+1 basis vectors (:818-843), their
+ * normalisations, the preconditioner (:899-908) and the modified Gram-Schmidt
+ * of the new direction (:909-923).  The Ritz coefficients are fixed (the
+ * operation count does not depend on them), so this times the reference's
+ * per-step vector work on a slice of a vector.  C holds ib+2 vectors of n
+ * (C[ib+1] receives the new direction), HC ib+1, W and R one each. */
+void orc_algebra_step(double *C, const double *HC, double *W, double *R, const double *hii, size_t n, int ib) {
+  const double eps_reg = 1.0e-12;
+  double *U = (double *)malloc(sizeof(double) * (size_t)(ib + 1));
+  volatile double sink = 0.0;
+  for (int jb = 0; jb <= ib; ++jb) sink += orc_inner(C + (size_t)jb * n, HC + (size_t)ib * n, n);
+  for (int kb = 0; kb <= ib; ++kb) U[kb] = 1.0 / sqrt((double)(ib + 1));
+  const double E0 = -1.0;
+#pragma omp parallel for
+  for (size_t s = 0; s < n; ++s) {
+    double w = C[s] * U[0], r = HC[s] * (-U[0]);
+    for (int kb = 1; kb <= ib; ++kb) {
+      w += C[(size_t)kb * n + s] * U[kb];
+      r += HC[(size_t)kb * n + s] * (-U[kb]);
+    }
+    W[s] = w;
+    R[s] = r + E0 * w;
+  }
+  sink += orc_normalize(W, n);
+  sink += orc_normalize(R, n);
+  double *cn = C + (size_t)(ib + 1) * n;
+#pragma omp parallel for
+  for (size_t s = 0; s < n; ++s) {
+    double den = E0 - hii[s];
+    cn[s] = (fabs(den) > eps_reg) ? R[s] / den : R[s] / (den - eps_reg);
+  }
+  for (int kb = 0; kb < ib + 1; ++kb) {
+    double olap = -orc_inner(C + (size_t)kb * n, cn, n);
+    const double *ck = C + (size_t)kb * n;
+#pragma omp parallel for
+    for (size_t s = 0; s < n; ++s) cn[s] += ck[s] * olap;
+  }
+  sink += orc_normalize(cn, n);
+  free(U);
+  (void)sink;
+}
+
 int orc_davidson(const orc_ints *t, const uint64_t *astr, size_t na, const uint64_t *bstr, size_t nb, int words,
                  int bit_length, const size_t *aoff_s, const uint64_t *aket_s, const int32_t *acran_s,
                  const size_t *aoff_d, const uint64_t *aket_d, const int32_t *acran_d, const size_t *boff_s,

@@ -112,6 +112,9 @@ void orc_correlation(const uint64_t *astr, size_t na, const uint64_t *bstr, size
 
 /* Kahan-compensated inner product (framework/dm_vector.h:23-51). */
 double orc_inner(const double *x, const double *y, size_t n);
+/* The vector algebra of one Davidson step at subspace position ib on n
+ * elements (timing only; C: ib+2 vectors, HC: ib+1). */
+void orc_algebra_step(double *C, const double *HC, double *W, double *R, const double *hii, size_t n, int ib);
 
 /* Symmetric eigensolver for the small projected matrix: cyclic Jacobi with
  * eigenvalues sorted ascending (stands in for hp_numeric.h:503-520 dsyev).

@@ -12,7 +12,9 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def names() -> list[str]:
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz")))
+    """The synthetic reference-harness cases (molecules.npz holds the molecular sets)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(GOLDEN, "*.npz"))
+                  if os.path.basename(p) != "molecules.npz")
 
 
 class Case:
@@ -49,3 +51,26 @@ def load(name: str) -> Case:
 def max_rel(x: np.ndarray, ref: np.ndarray) -> float:
     den = max(float(np.abs(ref).max()), 1e-300)
     return float(np.abs(np.asarray(x) - np.asarray(ref)).max()) / den
+
+
+class Molecule:
+    """One molecule of tests/golden/molecules.npz (written by make_molecules.py
+    from the reference's data/ directory): integrals, and per string list the
+    strings (alpha = beta) and the energy the reference publishes for it."""
+
+    def __init__(self, d, name: str):
+        self.name = name
+        self.norb = int(d[f"{name}/norb"])
+        self.nelec = int(d[f"{name}/nelec"])
+        self.ecore = float(d[f"{name}/ecore"])
+        self.h1 = d[f"{name}/h1"]
+        self.eri = d[f"{name}/eri"]
+        self.labels = [str(x) for x in d[f"{name}/labels"]]
+        self.strings = {lb: d[f"{name}/{lb}/strings"].astype(np.uint64) for lb in self.labels}
+        self.energy = {lb: float(d[f"{name}/{lb}/energy"]) for lb in self.labels}
+        self.source = {lb: str(d[f"{name}/{lb}/source"]) for lb in self.labels}
+
+
+def molecule(name: str) -> Molecule:
+    with np.load(os.path.join(GOLDEN, "molecules.npz")) as d:
+        return Molecule(d, name)

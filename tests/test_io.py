@@ -8,7 +8,6 @@ import pytest
 from sbd_gb300 import fcidump, strings
 from sbd_gb300.generators import config0, draw_strings, make_problem
 
-REF = "/root/reference"
 
 
 def test_string_round_trip():
@@ -76,12 +75,30 @@ def test_generators_shapes_and_determinism():
     assert s.size == 495 and np.unique(s).size == 495
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "data", "h2o")), reason="reference data not present")
-def test_oracle_reproduces_published_h2o_energy():
-    """H2O cc-pVDZ, 275 alpha strings: -76.23594663 Ha (data/h2o/README.md:6)."""
+@pytest.mark.parametrize("mol,label", [("h2o", "1em3"), ("n2", "1em3")])
+def test_oracle_reproduces_published_energies(mol, label):
+    """The oracle's Davidson on the reference's own molecular inputs (H2O
+    cc-pVDZ, 275 alpha strings: -76.23594663 Ha, data/h2o/README.md:6; N2
+    6-31G, 239 strings: -109.04162110 Ha, data/n2/README.md:6), read from the
+    committed fixture tests/golden/molecules.npz."""
+    from golden_io import molecule
     from oracle.oracle import Oracle
-    ints = fcidump.read_integrals(os.path.join(REF, "data/h2o/fcidump.txt"))
-    a = strings.load_strings(os.path.join(REF, "data/h2o/h2o-1em3-alpha.txt"), ints.norb)
-    o = Oracle(ints.norb, ints.h1, ints.eri, ints.ecore, a, a)
+    m = molecule(mol)
+    a = m.strings[label]
+    o = Oracle(m.norb, m.h1, m.eri, m.ecore, a, a)
     E, W, ns, r = o.davidson(max_it=20, max_nb=10, eps=1e-8)
-    assert abs(o.energy(W) - (-76.23594663)) < 5e-9
+    assert abs(o.energy(W) - m.energy[label]) < 1e-8
+
+
+def test_molecule_fixture_matches_reference_files():
+    """molecules.npz holds what the reference's data files say (checked where
+    the reference tree is present; SBD_REFERENCE_ROOT names it)."""
+    ref = os.environ.get("SBD_REFERENCE_ROOT", "")
+    if not os.path.isdir(os.path.join(ref, "data", "h2o")):
+        pytest.skip("reference data not present (set SBD_REFERENCE_ROOT)")
+    from golden_io import molecule
+    m = molecule("h2o")
+    ints = fcidump.read_integrals(os.path.join(ref, "data/h2o/fcidump.txt"))
+    assert np.array_equal(ints.eri, m.eri) and np.array_equal(ints.h1, m.h1)
+    a = strings.load_strings(os.path.join(ref, "data/h2o/h2o-1em4-alpha.txt"), ints.norb)
+    assert np.array_equal(a, m.strings["1em4"])

@@ -283,6 +283,9 @@ def run_sigma_probe(a) -> int:
     if a.config == 4:
         prob, a.nroots = G.config4_request(a.request)
         eps, max_nb = 1e-7, 20
+    elif a.strings:  # the configuration's generator with fewer strings per spin (a smaller case to profile)
+        norb, nel, seed = {0: (16, 5, 0), 1: (36, 12, 1), 3: (58, 16, 3)}[a.config]
+        prob = G.make_problem(norb, nel, nel, a.strings, a.strings, seed=seed)
     else:
         prob = {0: G.config0, 1: G.config1, 3: G.config3}[a.config]()
     tgen = time.time() - t
@@ -571,6 +574,8 @@ def main():
     ap.add_argument("--davidson", type=int, default=0, help="--sigma-probe: also one solve per precision")
     ap.add_argument("--mixed", type=int, default=1, help="--sigma-probe: also the mixed sigma")
     ap.add_argument("--nroots", type=int, default=2, help="--sigma-probe: roots of the solve")
+    ap.add_argument("--strings", type=int, default=0,
+                    help="--sigma-probe 0/1/3: strings per spin instead of the configuration's (a smaller case)")
     args = ap.parse_args()
     if args.sigma_probe is not None:
         return run_sigma_probe(args)

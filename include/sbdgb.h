@@ -46,7 +46,7 @@ enum sbdgb_status {
 
 enum sbdgb_precision {
   SBDGB_FP64 = 0,  /* plain: FP64 storage and arithmetic */
-  SBDGB_MIXED = 1  /* FP32 vectors and products, FP64 accumulation and refinement */
+  SBDGB_MIXED = 1  /* FP32 vectors and products, float-float accumulation, FP64 refinement */
 };
 
 typedef struct sbdgb_ctx sbdgb_ctx;
@@ -122,8 +122,10 @@ int sbdgb_diag_terms(sbdgb_problem *p, double *hii_out);
  * accumulate == 0 writes Wb = H*Wk.  stream: a cudaStream_t, or NULL for the
  * context's stream (pass cudaStreamLegacy for the legacy default stream). */
 int sbdgb_sigma(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accumulate, void *stream);
-/* Mixed-precision sigma: FP32 vectors, FP32 products, FP64 accumulation of
- * each element's sum, FP32 result. */
+/* Mixed-precision sigma: FP32 vectors, FP32 products and pair-list sums, a
+ * float-float accumulator per element (an FP32 sum and the rounding errors of
+ * the additions into it, about 48 bits; FP32 instructions only) and the FP64
+ * diagonal as FP32 hi + lo parts; FP32 result. */
 int sbdgb_sigma_mixed(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, void *stream);
 /* sbdgb_sigma_mixed for nvec vectors stored one after another (nvec*N floats
  * in and out).  Up to four vectors share each element's phase and address,
@@ -134,14 +136,21 @@ int sbdgb_sigma_mixed_block(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev
  * for each of the n_shapes candidates of kernel A (alpha sweep) and B (beta
  * sweep).  Shapes: 0 = 8x128, 1 = 8x256, 2 = 8x512, 3 = 16x256 rows x columns;
  * shape_b = 4 means the beta sweep is fused into kernel A (one kernel, no
- * transposed copy; chosen when that is faster, typically for short beta lists).
+ * transposed copy; chosen when that is faster, typically for short beta lists);
+ * shape_b = 5 means the single streaming kernel for sparse rows (16-byte
+ * accesses along beta, every task type in one pass), with shape_a 0 or 1 for
+ * row tiles of 8 or 16 rows (chosen for problems with a few nonzeros per row).
  * The first product of each precision tunes (and synchronises), so make it
  * before any stream capture. */
 int sbdgb_problem_tuning(const sbdgb_problem *p, int precision, int *shape_a, int *shape_b, float *ms_a,
                          float *ms_b, int n_shapes);
+/* The autotuner's times (ms, 0 where not measured) of the fused kernel in
+ * shapes 0..3 (ms_fused[4]) and of the sparse-row kernel with 8 and 16 rows
+ * per tile (ms_sparse[2]); either pointer may be NULL. */
+int sbdgb_problem_tuning_times(const sbdgb_problem *p, int precision, float *ms_fused, float *ms_sparse);
 /* Sets the sigma tile shapes of one precision instead of the autotuner's
- * choice (shape_a 0..3, shape_b 0..4 as above); results do not depend on it
- * beyond the order of floating-point sums. */
+ * choice (shape_a 0..3 with shape_b 0..4, or shape_a 0..1 with shape_b 5, as
+ * above); results do not depend on it beyond the order of floating-point sums. */
 int sbdgb_problem_set_tuning(sbdgb_problem *p, int precision, int shape_a, int shape_b);
 
 /* sigma that makes no device allocation.  No counterpart in the reference:

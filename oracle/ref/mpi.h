@@ -173,7 +173,8 @@ inline int MPI_Allgatherv(const void *s, int sn, MPI_Datatype st, void *r, const
   sbdgb_mpi_shim::copy_if_distinct(s, rr, (size_t)sn * sbdgb_mpi_shim::type_size(st)); return 0;
 }
 inline int MPI_Scatter(const void *s, int sn, MPI_Datatype st, void *r, int, MPI_Datatype, int, MPI_Comm) {
-  if (s) sbdgb_mpi_shim::copy_if_distinct(s, r, (size_t)sn * sbdgb_mpi_shim::type_size(st)); return 0;
+  if (s) sbdgb_mpi_shim::copy_if_distinct(s, r, (size_t)sn * sbdgb_mpi_shim::type_size(st));
+  return 0;
 }
 inline int MPI_Alltoall(const void *s, int sn, MPI_Datatype st, void *r, int, MPI_Datatype, MPI_Comm) {
   sbdgb_mpi_shim::copy_if_distinct(s, r, (size_t)sn * sbdgb_mpi_shim::type_size(st)); return 0;

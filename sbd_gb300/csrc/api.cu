@@ -122,12 +122,14 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
     b += 16 * N * k;
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;
     b += 4 * N + 4 * N * std::min<size_t>(4, k);
+    b += 8 * N;  // the diagonal as FP32 hi and lo parts
   } else {
     const size_t mmax = (size_t)std::max(std::min(o.max_nb, 64) - (int)k, 2 * (int)k);
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;  // FP32 tables
     b += 4 * N;                                                                          // FP32 transpose
     b += 4 * N * std::min<size_t>(4, k);  // transposed copies of the vectors of one multi-vector product
     b += 32 * N * k + 4 * N * (k + mmax) + 4 * N * mmax + 12 * N * k + 4 * (8 * 3 * 64 + 64);
+    b += 8 * N;  // the diagonal as FP32 hi and lo parts
   }
   return b;
 }
@@ -423,9 +425,19 @@ int sbdgb_problem_tuning(const sbdgb_problem *pr, int precision, int *shape_a, i
   return SBDGB_OK;
 }
 
+int sbdgb_problem_tuning_times(const sbdgb_problem *pr, int precision, float *ms_fused, float *ms_sparse) {
+  if (!pr || (precision != 0 && precision != 1)) return SBDGB_E_INPUT;
+  const sbdgb::Problem &p = pr->p;
+  for (int i = 0; i < 4; ++i)
+    if (ms_fused) ms_fused[i] = p.tune_ms[precision][2][i];
+  for (int i = 0; i < 2; ++i)
+    if (ms_sparse) ms_sparse[i] = p.tune_ms[precision][2][4 + i];
+  return SBDGB_OK;
+}
+
 int sbdgb_problem_set_tuning(sbdgb_problem *pr, int precision, int shape_a, int shape_b) {
   if (!pr || (precision != 0 && precision != 1)) return SBDGB_E_INPUT;
-  if (shape_a < 0 || shape_a > 3 || shape_b < 0 || shape_b > 4) return SBDGB_E_INPUT;
+  if (shape_a < 0 || shape_a > 3 || shape_b < 0 || shape_b > 5 || (shape_b == 5 && shape_a > 1)) return SBDGB_E_INPUT;
   pr->p.tune_a[precision] = shape_a;
   pr->p.tune_b[precision] = shape_b;
   return SBDGB_OK;

@@ -134,6 +134,7 @@ struct Problem {
   double *CT = nullptr;   // transpose scratch
   float *CTf = nullptr;   // mixed transpose scratch
   float *Kpf = nullptr, *Jbf = nullptr, *Jaf = nullptr;
+  float *hii_hi = nullptr, *hii_lo = nullptr;  // mixed form: hii = hi + lo in FP32 parts
   float *val_sf[2] = {nullptr, nullptr}, *val_df[2] = {nullptr, nullptr};
   void *ws[WS_COUNT] = {};
   size_t ws_bytes[WS_COUNT] = {};

@@ -81,12 +81,19 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
     const uint32_t ia = ia0 + r;
-    double acc[CPT];
-    // diagonal term (mult.h:169-174), FP64 diagonal in both forms
+    AccT<T> acc[CPT];
+    // diagonal term (mult.h:169-174): FP64, or hi/lo FP32 parts of the FP64
+    // diagonal in the mixed form
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       const size_t k = (size_t)ia * a.nb + col[c];
-      acc[c] = ok[c] ? (__ldg(a.hii + k) - a.shift) * (double)__ldg(a.C + k) : 0.0;
+      acc_zero(acc[c]);
+      if (ok[c]) {
+        if constexpr (std::is_same<T, double>::value)
+          acc[c] = (__ldg(a.hii + k) - a.shift) * __ldg(a.C + k);
+        else
+          acc[c] = ff_diag(__ldg(a.hii_hi + k), __ldg(a.hii_lo + k), a.shift_hi, a.shift_lo, __ldg(a.C + k));
+      }
     }
     // alpha singles and doubles (task type 2, mult.h:450-488)
     same_spin_row<CPT, T, Wd>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, a.C, a.nb, ia, col, ok, beta, acc);
@@ -110,8 +117,8 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
           const uint32_t ph =
               (parity(beta[c] & word<Wd>(a.A.mask_s, p)) ^ parity(word<Wd>(a.astr, ja) & mb) ^ (ca >> 31) ^ sb) &
               1u;
-          madd<T>(acc[c], part[c], flip(__ldg(a.Kp + ((ca >> 16) & 0x7fffu) * a.npair + kb), ph),
-                  __ldg(a.C + (size_t)ja * a.nb + jb));
+          madd(acc[c], part[c], flip(__ldg(a.Kp + ((ca >> 16) & 0x7fffu) * a.npair + kb), ph),
+               __ldg(a.C + (size_t)ja * a.nb + jb));
         }
       }
     }
@@ -125,21 +132,25 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
           const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
           const uint32_t ph = parity(arow & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31);
           const T j = __ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia);
-          madd<T>(acc[c], part[c], flip(__ldg(a.val_sb + q) + j, ph), __ldg(crow_a + jb));
+          madd(acc[c], part[c], flip(__ldg(a.val_sb + q) + j, ph), __ldg(crow_a + jb));
         }
         for (uint32_t q = d0[c]; q < d1[c]; ++q) {
           const uint32_t jb = __ldg(a.B.ket_d + q);
-          madd<T>(acc[c], part[c], flip(__ldg(a.val_db + q), parity(arow & word<Wd>(a.B.mask_d, q))),
-                  __ldg(crow_a + jb));
+          madd(acc[c], part[c], flip(__ldg(a.val_db + q), parity(arow & word<Wd>(a.B.mask_d, q))),
+               __ldg(crow_a + jb));
         }
       }
     }
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
-      if constexpr (!std::is_same<T, double>::value) acc[c] += (double)part[c];
+      acc_add_part(acc[c], part[c]);
       if (ok[c]) {
         const size_t k = (size_t)ia * a.nb + col[c];
-        a.S[k] = (T)(a.accumulate ? (double)a.S[k] + acc[c] : acc[c]);
+        if (a.accumulate) acc_add_part(acc[c], a.S[k]);
+        if constexpr (std::is_same<T, double>::value)
+          a.S[k] = a.accumulate ? a.S[k] + acc[c] : acc[c];
+        else
+          a.S[k] = ff_value(acc[c]);
       }
     }
   }
@@ -151,7 +162,7 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
 template <int TA, int CPT, typename T, typename Wd>
 __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
   constexpr int TB = kThreads * CPT;
-  __shared__ double tile[TA][TB];
+  __shared__ AccT<T> tile[TA][TB];
   const uint32_t t = __ldg(a.tile_order + blockIdx.x);
   const uint32_t ib0 = __ldg(a.tile_start + t);
   const uint32_t rend = __ldg(a.tile_start + t + 1) - ib0;  // <= TA
@@ -167,9 +178,9 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
   }
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
-    double acc[CPT];
+    AccT<T> acc[CPT];
 #pragma unroll
-    for (int c = 0; c < CPT; ++c) acc[c] = 0.0;
+    for (int c = 0; c < CPT; ++c) acc_zero(acc[c]);
     same_spin_row<CPT, T, Wd>(a.B, a.val_sb, a.val_db, a.Ja, a.na, a.CT, a.na, ib0 + r, col, ok, alpha, acc);
 #pragma unroll
     for (int c = 0; c < CPT; ++c) tile[r][threadIdx.x + kThreads * c] = acc[c];
@@ -179,8 +190,221 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
   for (int c = 0; c < CPT; ++c)
     if (ok[c]) {
       T *srow = a.S + (size_t)col[c] * a.nb + ib0;
-      for (uint32_t r = 0; r < rend; ++r) srow[r] = (T)((double)srow[r] + tile[r][threadIdx.x + kThreads * c]);
+      for (uint32_t r = 0; r < rend; ++r) {
+        AccT<T> t = tile[r][threadIdx.x + kThreads * c];
+        if constexpr (std::is_same<T, double>::value) {
+          srow[r] = srow[r] + t;
+        } else {
+          ff_add(t, srow[r]);
+          srow[r] = ff_value(t);
+        }
+      }
     }
+}
+
+// ---- sparse rows: every task type in one streaming pass ---------------------------
+//
+// For problems with few nonzeros per row (norb 58, 12000 x 12000 strings:
+// 0.48 per row) sigma is a stream over hii, C and sigma.  k_sigma_sparse does
+// every task type in one pass, with no transposed copy:
+//  * a CTA owns one work-balanced tile of at most TA alpha rows and 128*VW
+//    beta columns; a thread owns VW consecutive columns, so hii, C and sigma
+//    move in 16-byte accesses (VW = 2 doubles, or 4 floats) when the row
+//    length allows it (VW = 1 otherwise);
+//  * the diagonal terms of all rows of the tile are loaded first (TA
+//    independent vector loads per thread in flight);
+//  * beta pairs (task type 1, mult.h:489-525) belong to a column: for each
+//    pair of a thread's columns the tile's rows are gathered together;
+//  * alpha pairs (type 2, mult.h:450-488) and alpha x beta pairs (type 0,
+//    :527-557) belong to a row and are read once per CTA (broadcast loads).
+// Rows are unrolled (TA accumulators per column live in registers).  FP32
+// (mixed form): FP32 products and partial sums, float-float accumulation per
+// element, no FP64 instruction.
+template <int VW, typename T>
+__device__ __forceinline__ void load_v(const T *__restrict__ p, T (&x)[VW]) {
+  if constexpr (VW == 1) {
+    x[0] = __ldg(p);
+  } else if constexpr (sizeof(T) * VW == 16) {
+    const uint4 u = __ldg(reinterpret_cast<const uint4 *>(p));
+    memcpy(x, &u, 16);
+  } else {
+    const uint2 u = __ldg(reinterpret_cast<const uint2 *>(p));
+    memcpy(x, &u, 8);
+  }
+}
+template <int VW, typename T>
+__device__ __forceinline__ void store_v(T *__restrict__ p, const T (&x)[VW]) {
+  if constexpr (VW == 1) {
+    *p = x[0];
+  } else if constexpr (sizeof(T) * VW == 16) {
+    uint4 u;
+    memcpy(&u, x, 16);
+    *reinterpret_cast<uint4 *>(p) = u;
+  } else {
+    uint2 u;
+    memcpy(&u, x, 8);
+    *reinterpret_cast<uint2 *>(p) = u;
+  }
+}
+
+template <int RG, int VW, typename T, typename Wd>
+__device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint32_t nr, uint32_t c0,
+                                            const Wd (&beta)[VW], const uint32_t (&q0)[VW],
+                                            const uint32_t (&q1)[VW]) {
+  constexpr bool kF64 = std::is_same<T, double>::value;
+  Wd arow[RG];
+#pragma unroll
+  for (int r = 0; r < RG; ++r) arow[r] = (uint32_t)r < nr ? word<Wd>(a.astr, ia0 + r) : Wd(0);
+  AccT<T> acc[RG][VW];
+  T part[RG][VW];
+  // diagonal terms of every row of the group (mult.h:169-174)
+#pragma unroll
+  for (int r = 0; r < RG; ++r) {
+#pragma unroll
+    for (int v = 0; v < VW; ++v) {
+      acc_zero(acc[r][v]);
+      part[r][v] = T(0);
+    }
+    if ((uint32_t)r < nr) {
+      const size_t k = (size_t)(ia0 + r) * a.nb + c0;
+      T x[VW];
+      load_v<VW>(a.C + k, x);
+      if constexpr (kF64) {
+        double h[VW];
+        load_v<VW>(a.hii + k, h);
+#pragma unroll
+        for (int v = 0; v < VW; ++v) acc[r][v] = (h[v] - a.shift) * x[v];
+      } else {
+        float hh[VW], hl[VW];
+        load_v<VW>(a.hii_hi + k, hh);
+        load_v<VW>(a.hii_lo + k, hl);
+#pragma unroll
+        for (int v = 0; v < VW; ++v) acc[r][v] = ff_diag(hh[v], hl[v], a.shift_hi, a.shift_lo, x[v]);
+      }
+    }
+  }
+  // beta singles and doubles of this thread's columns (task type 1)
+#pragma unroll
+  for (int v = 0; v < VW; ++v) {
+    const uint32_t d0 = __ldg(a.B.off_d + c0 + v), d1 = __ldg(a.B.off_d + c0 + v + 1);
+    for (uint32_t q = d0; q < d1; ++q) {
+      const uint32_t jb = __ldg(a.B.ket_d + q);
+      const T val = __ldg(a.val_db + q);
+      const Wd m = word<Wd>(a.B.mask_d, q);
+      T x[RG];
+#pragma unroll
+      for (int r = 0; r < RG; ++r) x[r] = (uint32_t)r < nr ? __ldg(a.C + (size_t)(ia0 + r) * a.nb + jb) : T(0);
+#pragma unroll
+      for (int r = 0; r < RG; ++r) madd(acc[r][v], part[r][v], flip(val, parity(arow[r] & m)), x[r]);
+    }
+    for (uint32_t q = q0[v]; q < q1[v]; ++q) {
+      const uint32_t jb = __ldg(a.B.ket_s + q), code = __ldg(a.B.code_s + q);
+      const T val = __ldg(a.val_sb + q);
+      const Wd m = word<Wd>(a.B.mask_s, q);
+      const T *jrow = a.Ja + (size_t)((code >> 16) & 0x7fffu) * a.na + ia0;
+      T x[RG], j[RG];
+#pragma unroll
+      for (int r = 0; r < RG; ++r) {
+        x[r] = (uint32_t)r < nr ? __ldg(a.C + (size_t)(ia0 + r) * a.nb + jb) : T(0);
+        j[r] = (uint32_t)r < nr ? __ldg(jrow + r) : T(0);
+      }
+#pragma unroll
+      for (int r = 0; r < RG; ++r)
+        madd(acc[r][v], part[r][v], flip(val + j[r], parity(arow[r] & m) ^ (code >> 31)), x[r]);
+    }
+  }
+  // alpha pairs of each row (task type 2) and alpha x beta pairs (type 0)
+#pragma unroll
+  for (int r = 0; r < RG; ++r) {
+    if ((uint32_t)r >= nr) break;
+    const uint32_t ia = ia0 + r;
+    const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
+    for (uint32_t p = p0; p < p1; ++p) {
+      const uint32_t ja = __ldg(a.A.ket_s + p), code = __ldg(a.A.code_s + p);
+      const T val = __ldg(a.val_sa + p);
+      const Wd m = word<Wd>(a.A.mask_s, p);
+      const uint32_t P = (code >> 16) & 0x7fffu;
+      T x[VW], j[VW];
+      load_v<VW>(a.C + (size_t)ja * a.nb + c0, x);
+      load_v<VW>(a.Jb + (size_t)P * a.nb + c0, j);
+#pragma unroll
+      for (int v = 0; v < VW; ++v)
+        madd(acc[r][v], part[r][v], flip(val + j[v], parity(beta[v] & m) ^ (code >> 31)), x[v]);
+      // alpha x beta: this alpha single with every beta single of the column
+      const Wd aket = word<Wd>(a.astr, ja);
+      const T *krow = a.Kp + (size_t)P * a.npair;
+#pragma unroll
+      for (int v = 0; v < VW; ++v)
+        for (uint32_t q = q0[v]; q < q1[v]; ++q) {
+          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+          const uint32_t ph =
+              (parity(beta[v] & m) ^ parity(aket & word<Wd>(a.B.mask_s, q)) ^ (code >> 31) ^ (cb >> 31)) & 1u;
+          madd(acc[r][v], part[r][v], flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph),
+               __ldg(a.C + (size_t)ja * a.nb + jb));
+        }
+    }
+    const uint32_t e0 = __ldg(a.A.off_d + ia), e1 = __ldg(a.A.off_d + ia + 1);
+    for (uint32_t p = e0; p < e1; ++p) {
+      const uint32_t ja = __ldg(a.A.ket_d + p);
+      const T val = __ldg(a.val_da + p);
+      const Wd m = word<Wd>(a.A.mask_d, p);
+      T x[VW];
+      load_v<VW>(a.C + (size_t)ja * a.nb + c0, x);
+#pragma unroll
+      for (int v = 0; v < VW; ++v) madd(acc[r][v], part[r][v], flip(val, parity(beta[v] & m)), x[v]);
+    }
+  }
+  // write back
+#pragma unroll
+  for (int r = 0; r < RG; ++r) {
+    if ((uint32_t)r >= nr) break;
+    const size_t k = (size_t)(ia0 + r) * a.nb + c0;
+    T out[VW];
+    if (a.accumulate) {
+      T old[VW];
+      load_v<VW>(a.S + k, old);
+#pragma unroll
+      for (int v = 0; v < VW; ++v) {
+        acc_add_part(acc[r][v], part[r][v]);
+        if constexpr (kF64) {
+          out[v] = old[v] + acc[r][v];
+        } else {
+          ff_add(acc[r][v], old[v]);
+          out[v] = ff_value(acc[r][v]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < VW; ++v) {
+        acc_add_part(acc[r][v], part[r][v]);
+        out[v] = (T)acc_value(acc[r][v]);
+      }
+    }
+    store_v<VW>(a.S + k, out);
+  }
+}
+
+// One CTA: a row tile of at most TA rows, swept RG rows at a time (RG
+// accumulators per column in registers: 8 in FP64, 4 in the float-float form).
+template <int TA, int VW, typename T, typename Wd>
+__global__ void __launch_bounds__(kThreads) k_sigma_sparse(Args<T> a) {
+  constexpr int RG = std::is_same<T, double>::value ? 8 : 4;
+  const uint32_t tile = __ldg(a.tile_order + blockIdx.x);
+  const uint32_t ia0 = __ldg(a.tile_start + tile);
+  const uint32_t rend = __ldg(a.tile_start + tile + 1) - ia0;  // 1..TA
+  const uint32_t c0 = blockIdx.y * (kThreads * VW) + threadIdx.x * VW;
+  if (c0 >= a.nb) return;  // nb is a multiple of VW: a vector is wholly in or out
+  Wd beta[VW];
+  uint32_t q0[VW], q1[VW];
+#pragma unroll
+  for (int v = 0; v < VW; ++v) {
+    beta[v] = word<Wd>(a.bstr, c0 + v);
+    q0[v] = __ldg(a.B.off_s + c0 + v);
+    q1[v] = __ldg(a.B.off_s + c0 + v + 1);
+  }
+#pragma unroll 1
+  for (uint32_t g = 0; g < rend; g += RG)
+    sparse_rows<RG, VW, T, Wd>(a, ia0 + g, min((uint32_t)RG, rend - g), c0, beta, q0, q1);
 }
 
 // out[c][r] = in[r][c] for an R x Cn row-major matrix.
@@ -204,10 +428,24 @@ __global__ void k_to_float(const double *__restrict__ x, float *__restrict__ y, 
     y[e] = (float)x[e];
 }
 
+// hi = fp32(x), lo = fp32(x - hi): the FP64 diagonal as two FP32 parts
+// (hi + lo carries 48 bits of it) for the mixed-form kernels.
+__global__ void k_split(const double *__restrict__ x, float *__restrict__ hi, float *__restrict__ lo, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const double v = x[e];
+    const float h = (float)v;
+    hi[e] = h;
+    lo[e] = (float)(v - (double)h);
+  }
+}
+
 // ---- tile shapes and the autotuner ---------------------------------------------
 
 constexpr int kNumShapes = 4;
-constexpr int kFusedShape = 4;  // tune_b value meaning "beta sweep fused into kernel A"
+constexpr int kFusedShape = 4;   // tune_b value meaning "beta sweep fused into kernel A"
+constexpr int kSparseShape = 5;  // tune_b value meaning "k_sigma_sparse"; tune_a 0/1 = 8/16 rows per tile
+constexpr int kNumSparse = 2;
+inline bool needs_transpose(int shape_b) { return shape_b != kFusedShape && shape_b != kSparseShape; }
 constexpr int kShapeTA[kNumShapes] = {8, 8, 8, 16};
 constexpr int kShapeCPT[kNumShapes] = {1, 2, 4, 2};
 
@@ -245,6 +483,37 @@ void launch_a(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
     default: launch_a_shape<T, 16, 2, F>(p, a, s); break;
   }
 }
+inline bool aligned16(const void *x) { return ((uintptr_t)x & 15u) == 0; }
+
+// The single streaming kernel for sparse rows: TA = 8 (variant 0) or 16 rows
+// per tile; 16-byte vectors when the row length and the pointers allow.
+template <typename T, int TA, typename Wd>
+void launch_sparse_ta(const Problem &p, Args<T> a, cudaStream_t s) {
+  constexpr int v = TA == 8 ? 0 : 1;
+  constexpr int VW = 16 / (int)sizeof(T);
+  a.tile_start = p.tile_start[0][v];
+  a.tile_order = p.tile_order[0][v];
+  const bool vec = p.nb % VW == 0 && aligned16(a.C) && aligned16(a.S) && aligned16(a.Jb) &&
+                   (std::is_same<T, double>::value ? aligned16(a.hii) : aligned16(a.hii_hi) && aligned16(a.hii_lo));
+  if (vec) {
+    dim3 g(p.n_tiles[0][v], (p.nb + kThreads * VW - 1) / (kThreads * VW));
+    k_sigma_sparse<TA, VW, T, Wd><<<g, kThreads, 0, s>>>(a);
+  } else {
+    dim3 g(p.n_tiles[0][v], (p.nb + kThreads - 1) / kThreads);
+    k_sigma_sparse<TA, 1, T, Wd><<<g, kThreads, 0, s>>>(a);
+  }
+}
+template <typename T>
+void launch_sparse(const Problem &p, const Args<T> &a, int variant, cudaStream_t s) {
+  if (p.norb <= 32) {
+    if (variant == 0) launch_sparse_ta<T, 8, uint32_t>(p, a, s);
+    else launch_sparse_ta<T, 16, uint32_t>(p, a, s);
+  } else {
+    if (variant == 0) launch_sparse_ta<T, 8, unsigned long long>(p, a, s);
+    else launch_sparse_ta<T, 16, unsigned long long>(p, a, s);
+  }
+}
+
 // The fused single-kernel product (no transposed copy), in shape `shape`.
 template <typename T>
 void launch_fused(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
@@ -334,7 +603,30 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
       best_fs = sh;
     }
   }
-  if (best_f < two_kernels) {
+  // the single streaming kernel for sparse rows
+  float best_s = 1e30f;
+  int best_ss = 0;
+  for (int sh = 0; sh < kNumSparse; ++sh) {
+    for (int rep = 0; rep < 2; ++rep) {
+      SBDGB_CUDA(cudaEventRecord(e0, s));
+      launch_sparse<T>(p, a, sh, s);
+      SBDGB_CUDA(cudaEventRecord(e1, s));
+      count_launch(p.ctx);
+    }
+    SBDGB_CUDA(cudaGetLastError());
+    SBDGB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    SBDGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    p.tune_ms[prec][2][kNumShapes + sh] = ms;
+    if (ms < best_s) {
+      best_s = ms;
+      best_ss = sh;
+    }
+  }
+  if (best_s < two_kernels && best_s <= best_f) {
+    p.tune_a[prec] = best_ss;
+    p.tune_b[prec] = kSparseShape;
+  } else if (best_f < two_kernels) {
     p.tune_a[prec] = best_fs;
     p.tune_b[prec] = kFusedShape;
   }
@@ -352,11 +644,23 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
 // pairs per string on average), where its per-thread lists diverge little.
 inline int size_shape(uint32_t columns) { return columns <= 1024 ? 0 : 1; }
 
+// Nonzeros per row of H off the diagonal (same-spin pairs of both spins and
+// the alpha x beta products, from the table sizes).
+inline double nnz_per_row(const Problem &p) {
+  const double sa = p.na ? (double)p.A.ns / p.na : 0.0, sb = p.nb ? (double)p.B.ns / p.nb : 0.0;
+  return (p.na ? (double)(p.A.ns + p.A.nd) / p.na : 0.0) + (p.nb ? (double)(p.B.ns + p.B.nd) / p.nb : 0.0) + sa * sb;
+}
+
 template <typename T>
 bool needs_tuning(Problem &p) {
   const int prec = std::is_same<T, double>::value ? 0 : 1;
   if (p.tune_a[prec] >= 0 && p.tune_b[prec] >= 0) return false;
   if (p.ctx->autotune) return true;
+  if (nnz_per_row(p) <= 8.0) {
+    p.tune_a[prec] = 0;
+    p.tune_b[prec] = kSparseShape;
+    return false;
+  }
   p.tune_a[prec] = size_shape(p.nb);
   p.tune_b[prec] = (p.B.ns + p.B.nd) <= 8ull * p.nb ? kFusedShape : size_shape(p.na);
   return false;
@@ -366,6 +670,12 @@ template <typename T>
 void launch(Problem &p, const Args<T> &a, cudaStream_t s) {
   const int prec = std::is_same<T, double>::value ? 0 : 1;
   if (p.tune_a[prec] < 0 || p.tune_b[prec] < 0) autotune<T>(p, a, s);
+  if (p.tune_b[prec] == kSparseShape) {
+    launch_sparse<T>(p, a, p.tune_a[prec], s);
+    count_launch(p.ctx, 1);
+    SBDGB_CUDA(cudaGetLastError());
+    return;
+  }
   if (p.tune_b[prec] == kFusedShape) {
     launch_fused<T>(p, a, p.tune_a[prec], s);
     count_launch(p.ctx, 1);
@@ -400,7 +710,7 @@ __device__ __forceinline__ void same_spin_row_mv(const SpinTables &Tb, const flo
                                                  const float *__restrict__ vd, const float *__restrict__ Jo,
                                                  uint32_t ldj, const float *const (&In)[kMaxNV], uint32_t ldin,
                                                  uint32_t row, const uint32_t (&col)[CPT], const bool (&ok)[CPT],
-                                                 const Wd (&opp)[CPT], double (&acc)[NV][CPT]) {
+                                                 const Wd (&opp)[CPT], FF (&acc)[NV][CPT]) {
   float part[NV][CPT];
 #pragma unroll
   for (int n = 0; n < NV; ++n)
@@ -464,7 +774,7 @@ __device__ __forceinline__ void same_spin_row_mv(const SpinTables &Tb, const flo
 #pragma unroll
   for (int n = 0; n < NV; ++n)
 #pragma unroll
-    for (int c = 0; c < CPT; ++c) acc[n][c] += (double)part[n][c];
+    for (int c = 0; c < CPT; ++c) ff_add(acc[n][c], part[n][c]);
 }
 
 template <int TA, int CPT, int NV, typename Wd, bool kFused>
@@ -491,13 +801,14 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
     const uint32_t ia = ia0 + r;
-    double acc[NV][CPT];
+    FF acc[NV][CPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       const uint32_t k = ia * a.nb + col[c];
-      const double h = ok[c] ? __ldg(a.hii + k) - a.shift : 0.0;
+      const float hh = ok[c] ? __ldg(a.hii_hi + k) : 0.f, hl = ok[c] ? __ldg(a.hii_lo + k) : 0.f;
 #pragma unroll
-      for (int n = 0; n < NV; ++n) acc[n][c] = ok[c] ? h * (double)__ldg(m.Cv[n] + k) : 0.0;
+      for (int n = 0; n < NV; ++n)
+        acc[n][c] = ok[c] ? ff_diag(hh, hl, a.shift_hi, a.shift_lo, __ldg(m.Cv[n] + k)) : FF{0.f, 0.f};
     }
     same_spin_row_mv<CPT, NV, Wd>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, m.Cv, a.nb, ia, col, ok, beta, acc);
     float part[NV][CPT];
@@ -573,7 +884,10 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
       if (ok[c]) {
         const uint32_t k = ia * a.nb + col[c];
 #pragma unroll
-        for (int n = 0; n < NV; ++n) m.Sv[n][k] = (float)(acc[n][c] + (double)part[n][c]);
+        for (int n = 0; n < NV; ++n) {
+          ff_add(acc[n][c], part[n][c]);
+          m.Sv[n][k] = ff_value(acc[n][c]);
+        }
       }
   }
 }
@@ -582,7 +896,7 @@ template <int TA, int CPT, int NV, typename Wd>
 __global__ void __launch_bounds__(kThreads) k_sigma_beta_mv(ArgsMV m) {
   const Args<float> &a = m.a;
   constexpr int TB = kThreads * CPT;
-  extern __shared__ double tile_mv[];  // [NV][TA][TB]
+  extern __shared__ FF tile_mv[];  // [NV][TA][TB]
   const uint32_t t = __ldg(a.tile_order + blockIdx.x);
   const uint32_t ib0 = __ldg(a.tile_start + t);
   const uint32_t rend = __ldg(a.tile_start + t + 1) - ib0;
@@ -598,11 +912,11 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta_mv(ArgsMV m) {
   }
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
-    double acc[NV][CPT];
+    FF acc[NV][CPT];
 #pragma unroll
     for (int n = 0; n < NV; ++n)
 #pragma unroll
-      for (int c = 0; c < CPT; ++c) acc[n][c] = 0.0;
+      for (int c = 0; c < CPT; ++c) acc[n][c] = FF{0.f, 0.f};
     same_spin_row_mv<CPT, NV, Wd>(a.B, a.val_sb, a.val_db, a.Ja, a.na, m.CTv, a.na, ib0 + r, col, ok, alpha, acc);
 #pragma unroll
     for (int n = 0; n < NV; ++n)
@@ -615,8 +929,11 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta_mv(ArgsMV m) {
 #pragma unroll
       for (int n = 0; n < NV; ++n) {
         float *srow = m.Sv[n] + (size_t)col[c] * a.nb + ib0;
-        for (uint32_t r = 0; r < rend; ++r)
-          srow[r] = (float)((double)srow[r] + tile_mv[((size_t)n * TA + r) * TB + threadIdx.x + kThreads * c]);
+        for (uint32_t r = 0; r < rend; ++r) {
+          FF t = tile_mv[((size_t)n * TA + r) * TB + threadIdx.x + kThreads * c];
+          ff_add(t, srow[r]);
+          srow[r] = ff_value(t);
+        }
       }
 }
 
@@ -641,7 +958,7 @@ void launch_b_mv_shape(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
   m.a.tile_start = p.tile_start[1][v];
   m.a.tile_order = p.tile_order[1][v];
   dim3 g(p.n_tiles[1][v], (p.na + TB - 1) / TB);
-  const size_t smem = sizeof(double) * NV * TA * TB;
+  const size_t smem = sizeof(FF) * NV * TA * TB;
   if (p.norb <= 32) {
     auto k = k_sigma_beta_mv<TA, CPT, NV, uint32_t>;
     SBDGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -681,6 +998,15 @@ int shape_b_mv(int tuned) {
 
 template <int NV>
 void launch_mv(const Problem &p, const ArgsMV &m, cudaStream_t s) {
+  if (p.tune_b[1] == kSparseShape) {  // a stream per vector: nothing to share between vectors
+    for (int n = 0; n < NV; ++n) {
+      Args<float> a = m.a;
+      a.C = m.Cv[n];
+      a.S = m.Sv[n];
+      launch_sparse<float>(p, a, p.tune_a[1], s);
+    }
+    return;
+  }
   if (p.tune_b[1] == kFusedShape) {
     launch_a_mv<NV, true>(p, m, p.tune_a[1], s);
   } else {
@@ -724,6 +1050,9 @@ Args<T> base_args(Problem &p, const T *C, T *S, int accumulate) {
   a.na = p.na;
   a.nb = p.nb;
   a.hii = p.hii;
+  a.hii_hi = p.hii_hi;
+  a.hii_lo = p.hii_lo;
+  a.shift_hi = a.shift_lo = 0.f;
   a.C = C;
   a.S = S;
   a.accumulate = accumulate;
@@ -732,6 +1061,13 @@ Args<T> base_args(Problem &p, const T *C, T *S, int accumulate) {
   a.B = p.B;
   a.npair = p.npair;
   return a;
+}
+
+// The shift of a mixed-form product as FP32 hi + lo (FP64 kept for the FP64 kernels).
+void set_shift(Args<float> &a, double shift) {
+  a.shift = shift;
+  a.shift_hi = (float)shift;
+  a.shift_lo = (float)(shift - (double)a.shift_hi);
 }
 
 // Rows [start[t], start[t+1]) of at most cap rows each, closed once their
@@ -820,14 +1156,18 @@ void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, 
   a.Ja = p.Ja;
   a.Kp = p.Kp;
   const int sa = p.tune_a[0] >= 0 ? p.tune_a[0] : 1, sb = p.tune_b[0] >= 0 ? p.tune_b[0] : 1;
-  if (sb == kFusedShape) {
+  if (sb == kSparseShape) {
+    launch_sparse<double>(p, a, sa, s);
+    count_launch(p.ctx, 1);
+  } else if (sb == kFusedShape) {
     launch_fused<double>(p, a, sa, s);
+    count_launch(p.ctx, 1);
   } else {
     transpose<double>(p, C, CT, p.na, p.nb, s);
     launch_a<double>(p, a, sa, s);
     launch_b<double>(p, a, sb, s);
+    count_launch(p.ctx, 2);
   }
-  count_launch(p.ctx, 2);
   SBDGB_CUDA(cudaGetLastError());
 }
 
@@ -850,7 +1190,7 @@ void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStre
   }
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   begin_timing(p, s, ev0, ev1);
-  if (p.tune_b[0] != kFusedShape) transpose<double>(p, C, p.CT, p.na, p.nb, s);
+  if (needs_transpose(p.tune_b[0])) transpose<double>(p, C, p.CT, p.na, p.nb, s);
   launch<double>(p, a, s);
   end_timing(p, s, ev0, ev1);
 }
@@ -866,6 +1206,13 @@ void prepare_mixed(Problem &p, cudaStream_t s) {
   to_float(p, p.Kp, p.Kpf, npp, s);
   to_float(p, p.Jb, p.Jbf, (size_t)p.npair * p.nb, s);
   to_float(p, p.Ja, p.Jaf, (size_t)p.npair * p.na, s);
+  p.hii_hi = (float *)dev_alloc(p, sizeof(float) * (p.N ? p.N : 1));
+  p.hii_lo = (float *)dev_alloc(p, sizeof(float) * (p.N ? p.N : 1));
+  if (p.N) {
+    const unsigned blocks = (unsigned)std::min<size_t>((p.N + 255) / 256, 4096);
+    k_split<<<blocks, 256, 0, s>>>(p.hii, p.hii_hi, p.hii_lo, p.N);
+    count_launch(p.ctx);
+  }
   for (int sp = 0; sp < 2; ++sp) {
     SpinTables &T = sp == 0 ? p.A : p.B;
     p.val_sf[sp] = (float *)dev_alloc(p, sizeof(float) * (T.ns ? T.ns : 1));
@@ -883,7 +1230,7 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double sh
   if (!p.CTf) p.CTf = (float *)dev_alloc(p, sizeof(float) * p.N);
   if (p.N == 0) return;
   Args<float> a = base_args<float>(p, C, S, 0);
-  a.shift = shift;
+  set_shift(a, shift);
   a.CT = p.CTf;
   a.val_sa = p.val_sf[0];
   a.val_da = p.val_df[0];
@@ -898,7 +1245,7 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double sh
   }
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   begin_timing(p, s, ev0, ev1);
-  if (p.tune_b[1] != kFusedShape) transpose<float>(p, C, p.CTf, p.na, p.nb, s);
+  if (needs_transpose(p.tune_b[1])) transpose<float>(p, C, p.CTf, p.na, p.nb, s);
   launch<float>(p, a, s);
   end_timing(p, s, ev0, ev1);
 }
@@ -917,7 +1264,7 @@ void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStrea
   if (needs_tuning<float>(p)) sigma_mixed(p, C, S, s, shift);  // tunes the FP32 shapes on the first vector
   ArgsMV m{};
   m.a = base_args<float>(p, C, S, 0);
-  m.a.shift = shift;
+  set_shift(m.a, shift);
   m.a.val_sa = p.val_sf[0];
   m.a.val_da = p.val_df[0];
   m.a.val_sb = p.val_sf[1];
@@ -925,7 +1272,7 @@ void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStrea
   m.a.Jb = p.Jbf;
   m.a.Ja = p.Jaf;
   m.a.Kp = p.Kpf;
-  const bool fused = p.tune_b[1] == kFusedShape;
+  const bool fused = !needs_transpose(p.tune_b[1]);
   float *CT = fused ? nullptr : (float *)workspace(p, WS_CTMV, sizeof(float) * p.N * (size_t)nvec);
   for (int n = 0; n < nvec; ++n) {
     m.Cv[n] = C + (size_t)n * p.N;
@@ -941,7 +1288,7 @@ void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStrea
     default: launch_mv<4>(p, m, s); break;
   }
   end_timing(p, s, ev0, ev1);
-  count_launch(p.ctx, fused ? 1 : 2);
+  count_launch(p.ctx, p.tune_b[1] == kSparseShape ? nvec : fused ? 1 : 2);
   SBDGB_CUDA(cudaGetLastError());
 }
 

@@ -17,11 +17,55 @@ __device__ __forceinline__ float flip(float x, uint32_t ph) {
   return __int_as_float(__float_as_int(x) ^ (int)(ph << 31));
 }
 
+// Float-float accumulator of the mixed form: an FP32 sum hi and the rounding
+// errors of the additions into it in lo (Knuth's TwoSum), so hi + lo keeps
+// FP32 partial sums to about 48 bits, as an FP64 accumulator would, with FP32
+// instructions only.  The FP64 pipe of this GPU issues at 1/64 of the FP32
+// rate; FP64 adds and conversions per element bounded the FP32 kernels.
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ void ff_add(FF &a, float x) {
+  const float s = a.hi + x;
+  const float bb = s - a.hi;
+  a.lo += (a.hi - (s - bb)) + (x - bb);
+  a.hi = s;
+}
+__device__ __forceinline__ void ff_add(FF &a, const FF &b) {
+  ff_add(a, b.hi);
+  a.lo += b.lo;
+}
+__device__ __forceinline__ float ff_value(const FF &a) { return a.hi + a.lo; }
+// (h_hi + h_lo - s_hi - s_lo) * x as a float-float: the two differences are
+// exact or nearly so when the shift is close to the diagonal (the case the
+// shift is for), their sum is split by TwoSum, and fmaf recovers the rounding
+// error of the leading product.
+__device__ __forceinline__ FF ff_diag(float h_hi, float h_lo, float s_hi, float s_lo, float x) {
+  const float a = h_hi - s_hi, b = h_lo - s_lo;
+  const float dh = a + b;
+  const float bb = dh - a;
+  const float dl = (a - (dh - bb)) + (b - bb);
+  const float p = dh * x;
+  return FF{p, fmaf(dl, x, fmaf(dh, x, -p))};
+}
+
+// Per-element accumulator: FP64 in the FP64 form, float-float in the mixed form.
+template <typename T>
+using AccT = typename std::conditional<std::is_same<T, double>::value, double, FF>::type;
+__device__ __forceinline__ void acc_zero(double &a) { a = 0.0; }
+__device__ __forceinline__ void acc_zero(FF &a) { a = FF{0.f, 0.f}; }
+__device__ __forceinline__ void acc_add_part(double &, double) {}
+__device__ __forceinline__ void acc_add_part(FF &a, float part) { ff_add(a, part); }
+__device__ __forceinline__ double acc_value(double a) { return a; }
+__device__ __forceinline__ float acc_value(const FF &a) { return ff_value(a); }
+
 template <typename T>
 struct Args {
   const uint64_t *astr, *bstr;
   uint32_t na, nb;
   const double *hii;
+  const float *hii_hi, *hii_lo;  // mixed form: hii = hi + lo, both FP32 (no FP64 in the FP32 kernels)
+  float shift_hi, shift_lo;      // mixed form: the shift split the same way
   const T *C;   // N, row-major [ia][ib]
   const T *CT;  // N, transposed [ib][ia]
   T *S;
@@ -48,13 +92,11 @@ __device__ __forceinline__ Wd word(const uint64_t *a, size_t i) {
 __device__ __forceinline__ uint32_t parity(uint32_t x) { return __popc(x) & 1u; }
 __device__ __forceinline__ uint32_t parity(unsigned long long x) { return __popcll(x) & 1u; }
 
-template <typename T>
-__device__ __forceinline__ void madd(double &acc, T &part, T v, T x) {
-  if constexpr (std::is_same<T, double>::value)
-    acc = fma(v, x, acc);
-  else
-    part = fmaf(v, x, part);
-}
+// One term v*x: into the FP64 accumulator directly, or into the FP32 partial
+// sum of the current pair list (merged into the float-float accumulator once
+// per list).
+__device__ __forceinline__ void madd(double &acc, double &, double v, double x) { acc = fma(v, x, acc); }
+__device__ __forceinline__ void madd(FF &, float &part, float v, float x) { part = fmaf(v, x, part); }
 
 // Same-spin excitations of one row applied to this thread's CPT columns.
 // In: ket-major input rows (ld = ldin); Jo: opposite-spin Coulomb table
@@ -66,7 +108,7 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
                                               const T *__restrict__ vd, const T *__restrict__ Jo, uint32_t ldj,
                                               const T *__restrict__ In, uint32_t ldin, uint32_t row,
                                               const uint32_t (&col)[CPT], const bool (&ok)[CPT],
-                                              const Wd (&opp)[CPT], double (&acc)[CPT]) {
+                                              const Wd (&opp)[CPT], AccT<T> (&acc)[CPT]) {
   T part[CPT];
 #pragma unroll
   for (int c = 0; c < CPT; ++c) part[c] = T(0);
@@ -96,7 +138,7 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
           const uint32_t ph = parity(opp[c] & m[u]) ^ (code[u] >> 31);
-          madd<T>(acc[c], part[c], flip(v[u] + j[u], ph), x[u]);
+          madd(acc[c], part[c], flip(v[u] + j[u], ph), x[u]);
         }
       }
   }
@@ -109,7 +151,7 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
       if (ok[c]) {
         const uint32_t ph = parity(opp[c] & m) ^ (code >> 31);
         const T j = __ldg(Jo + (((code >> 16) & 0x7fffu) * ldj + col[c]));
-        madd<T>(acc[c], part[c], flip(v + j, ph), __ldg(In + (ket * ldin + col[c])));
+        madd(acc[c], part[c], flip(v + j, ph), __ldg(In + (ket * ldin + col[c])));
       }
   }
   // doubles, four at a time
@@ -132,7 +174,7 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
 #pragma unroll
         for (int u = 0; u < 4; ++u) x[u] = __ldg(In + (ket[u] * ldin + col[c]));
 #pragma unroll
-        for (int u = 0; u < 4; ++u) madd<T>(acc[c], part[c], flip(v[u], parity(opp[c] & m[u])), x[u]);
+        for (int u = 0; u < 4; ++u) madd(acc[c], part[c], flip(v[u], parity(opp[c] & m[u])), x[u]);
       }
   }
   for (; p < d1; ++p) {
@@ -141,12 +183,10 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
     const Wd m = word<Wd>(Tb.mask_d, p);
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
-      if (ok[c]) madd<T>(acc[c], part[c], flip(v, parity(opp[c] & m)), __ldg(In + (ket * ldin + col[c])));
+      if (ok[c]) madd(acc[c], part[c], flip(v, parity(opp[c] & m)), __ldg(In + (ket * ldin + col[c])));
   }
-  if constexpr (!std::is_same<T, double>::value) {
 #pragma unroll
-    for (int c = 0; c < CPT; ++c) acc[c] += (double)part[c];
-  }
+  for (int c = 0; c < CPT; ++c) acc_add_part(acc[c], part[c]);
 }
 
 

@@ -179,3 +179,36 @@ def test_measured_fp64_rates():
     from sbd_gb300.engine import measure_fp64_rates
     r = measure_fp64_rates(0)
     assert 0.05 < r["dfma_tflops"] < 200.0 and 0.05 < r["dmma_tflops"] < 200.0
+
+
+@pytest.mark.parametrize("nb", [280, 283])
+@pytest.mark.parametrize("variant", [0, 1])
+def test_sparse_kernel_against_oracle(engine, nb, variant):
+    """The sparse-row streaming kernel (16-byte accesses when the beta count is a
+    multiple of the vector width, 280; one element per thread otherwise, 283),
+    in both row-tile sizes: overwrite and accumulate forms against the oracle,
+    and the mixed form against it at the FP32 bound."""
+    torch = pytest.importorskip("torch")
+    prob = make_problem(16, 5, 5, 300, nb, seed=41)
+    p = TPBProblem.from_problem(engine, prob)
+    p.build_tables()
+    p.diag_terms()
+    p.set_tuning(0, variant, 5)
+    p.set_tuning(1, variant, 5)
+    o = Oracle.from_problem(prob)
+    rng = np.random.default_rng(variant + nb)
+    C = rng.uniform(-1, 1, prob.ndet)
+    ref = o.mult(C)
+    assert max_rel(p.mult(C), ref) <= 1e-12
+    base = rng.uniform(-1, 1, prob.ndet)
+    c = torch.tensor(C, device="cuda")
+    s = torch.tensor(base, device="cuda")
+    p.sigma_device(c.data_ptr(), s.data_ptr(), accumulate=True, stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert max_rel(s.cpu().numpy(), base + ref) <= 1e-12
+    c32 = c.float()
+    s32 = torch.empty_like(c32)
+    p.sigma_mixed_device(c32.data_ptr(), s32.data_ptr(), stream=torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert max_rel(s32.double().cpu().numpy(), ref) <= 5e-6
+    p.close()

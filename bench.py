@@ -134,6 +134,20 @@ def max_over_ranks(dist, x: float) -> float:
     return float(t.item())
 
 
+def measure_fp64_rates(device: int) -> dict:
+    """FP64 FMA-pipe and FP64 tensor-path rates of the device in TFLOP/s, from
+    the benchmark's own probe library (sbd_gb300/bench_csrc/rates.cu)."""
+    import ctypes as C
+    from sbd_gb300 import build
+    L = C.CDLL(build.RATES_LIB)
+    L.sbdgb_measure_fp64_rates.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    a, b = C.c_double(), C.c_double()
+    rc = L.sbdgb_measure_fp64_rates(device, C.byref(a), C.byref(b))
+    if rc != 0:
+        raise RuntimeError(f"FP64 rate probe failed ({rc})")
+    return {"dfma_tflops": a.value, "dmma_tflops": b.value}
+
+
 def make_problem():
     from sbd_gb300.generators import config1
     return config1()
@@ -333,6 +347,15 @@ def run_sigma_probe(a) -> int:
         out["sigma_mixed_GBs_model"] = (16 * N + 4 * nnz) / (msm * 1e-3) / 1e9
         out["sigma_mixed_relerr"] = float((S32.double() - S).abs().max() / S.abs().max())
         out["tuning_mixed"] = p.tuning(MIXED)
+        # double-float product (the second phase of the mixed solver)
+        Cd = torch.stack([C.float(), (C - C.float().double()).float()], dim=1).reshape(-1).contiguous()
+        Sd = torch.empty_like(Cd)
+        msd = timed(lambda: p.sigma_df_device(Cd.data_ptr(), Sd.data_ptr(), stream=st.cuda_stream))
+        out["sigma_df_ms"] = msd
+        sd = Sd.double().reshape(-1, 2).sum(dim=1)
+        out["sigma_df_relerr"] = float((sd - S).abs().max() / S.abs().max())
+        out["tuning_df"] = p.tuning(2)
+        del Cd, Sd, sd
         # several FP32 vectors per product: time per vector
         for nv in (2, 3, 4):
             X = torch.rand(nv, N, dtype=torch.float32, device="cuda") * 2 - 1
@@ -414,7 +437,6 @@ def run_gpu(args):
     peak, peak_kind = peaks()
     # the sigma kernels are bound by the FP64 FMA pipe: one FMA per off-diagonal
     # element and per diagonal element, against the measured FP64 FMA rate
-    from sbd_gb300.engine import measure_fp64_rates
     rates = measure_fp64_rates(local)
     fp64_achieved = 2.0 * (nnz_off + N) / (sigma_ms_per * 1e-3) / 1e12
     tiles = p.tuning(0)
@@ -532,7 +554,7 @@ def run_gpu(args):
                          "algorithmic_bytes": bytes_sigma, "peak_kind": f"{peak_kind} hbm_gbs",
                          "fp64": {"unit": "TFLOP/s", "achieved": fp64_achieved, "peak": rates["dfma_tflops"],
                                   "frac": fp64_achieved / rates["dfma_tflops"],
-                                  "peak_kind": "measured FP64 FMA pipe (sbdgb_measure_fp64_rates)",
+                                  "peak_kind": "measured FP64 FMA pipe (bench_csrc/rates.cu)",
                                   "fp64_tensor_peak": rates["dmma_tflops"],
                                   "flops": "2 x (nnz_off + N) per sigma"}},
             "mixed_precision": mixed,

@@ -46,7 +46,8 @@ enum sbdgb_status {
 
 enum sbdgb_precision {
   SBDGB_FP64 = 0,  /* plain: FP64 storage and arithmetic */
-  SBDGB_MIXED = 1  /* FP32 vectors and products, float-float accumulation, FP64 refinement */
+  SBDGB_MIXED = 1  /* FP32 phase, double-float phase, FP64 check of the result (refine_every 0),
+                      or FP32 subspace with FP64 refinement (refine_every > 0) */
 };
 
 typedef struct sbdgb_ctx sbdgb_ctx;
@@ -127,12 +128,19 @@ int sbdgb_sigma(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accu
  * the additions into it, about 48 bits; FP32 instructions only) and the FP64
  * diagonal as FP32 hi + lo parts; FP32 result. */
 int sbdgb_sigma_mixed(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, void *stream);
+/* Double-float sigma: each element of Wk_dev and Wb_dev is a pair of FP32
+ * numbers (hi, lo) whose sum is the value (2N floats, hi first; 48 significand
+ * bits), and every product and sum is a double-float operation on the FP32
+ * pipe.  This is the sigma of the second phase of the mixed solver: about
+ * 2^-47 relative rounding per operation, several times the FP64 FMA rate of
+ * this GPU.  accumulate as for sbdgb_sigma. */
+int sbdgb_sigma_df(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, int accumulate, void *stream);
 /* sbdgb_sigma_mixed for nvec vectors stored one after another (nvec*N floats
  * in and out).  Up to four vectors share each element's phase and address,
  * which is most of the FP32 kernels' work; results equal nvec single calls. */
 int sbdgb_sigma_mixed_block(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev, int nvec, void *stream);
 /* The sigma tile shapes the autotuner picked on this problem's first product
- * (precision 0 = FP64, 1 = mixed; -1 = not tuned yet) and the time it measured
+ * (precision 0 = FP64, 1 = mixed FP32, 2 = double-float; -1 = not tuned yet) and the time it measured
  * for each of the n_shapes candidates of kernel A (alpha sweep) and B (beta
  * sweep).  Shapes: 0 = 8x128, 1 = 8x256, 2 = 8x512, 3 = 16x256 rows x columns;
  * shape_b = 4 means the beta sweep is fused into kernel A (one kernel, no
@@ -166,13 +174,6 @@ int sbdgb_problem_set_tuning(sbdgb_problem *p, int precision, int shape_a, int s
  * It uses the autotuned tile shapes when the problem has them, the default
  * shape otherwise, and records no timing events. */
 int sbdgb_sigma_noalloc(sbdgb_problem *p, const double *Wk_dev, double *Wb_dev, int accumulate, void *stream);
-
-/* Measured FP64 rates of `device` in TFLOP/s (no reference counterpart): the
- * FP64 FMA pipe and the FP64 tensor path (mma.sync m8n8k4 f64), each from a
- * register-only loop over 8 blocks of 256 threads per SM timed with CUDA
- * events.  The sigma kernels and the solver's vector algebra are bound by the
- * FP64 FMA rate; the bench reports them against it. */
-int sbdgb_measure_fp64_rates(int device, double *dfma_tflops, double *dmma_tflops);
 
 /* Occupation density of a vector (OccupationDensity, chemistry/tpb/
  * occupation.h:11-95, as sbd::tpb::diag reports it with do_rdm == 0,
@@ -218,7 +219,9 @@ typedef struct {
                         1: unit vectors on the lowest diagonal entries,
                         2: caller-supplied vectors in X */
   int precision;     /* sbdgb_precision */
-  int refine_every;  /* MIXED: 0 (default) = FP32 Davidson, then FP64 from its lowest Ritz vectors;
+  int refine_every;  /* MIXED: 0 (default) = FP32 Davidson, then double-float Davidson from its
+                        lowest Ritz vectors to the tolerance, then FP64 sigma, Rayleigh-Ritz and
+                        residual of the result (continuing in FP64 only if they miss it);
                         k > 0 = FP64 anchors, FP32 subspace, FP64 sigma and residual every k steps */
   int verbose;       /* print one line per iteration like the reference */
 } sbdgb_davidson_opts;
@@ -226,7 +229,7 @@ typedef struct {
 typedef struct {
   int iterations;    /* Davidson steps taken */
   int sigma_calls;   /* sigma products (FP64 + mixed) */
-  int sigma_fp64;    /* of which FP64 */
+  int sigma_fp64;    /* of which FP64 (the others FP32 or double-float) */
   int restarts;
   int converged;     /* 1 if every root reached eps */
   double seconds;    /* wall time of the solve */

@@ -4,9 +4,11 @@
 // run.  The sigma kernels and the Davidson vector algebra are bound by the
 // first on this GPU; the second tells whether moving the tall-skinny
 // projections to the FP64 tensor path would pay.
+//
+// A benchmark utility, not part of the engine: built into its own library
+// (libsbdgb_rates.so) that only bench.py loads, to state the FP64 roof the
+// sigma kernels are measured against.  Returns 0 on success, 3 on a CUDA error.
 #include <cuda_runtime.h>
-
-#include "sbdgb.h"
 
 namespace {
 
@@ -42,36 +44,36 @@ __global__ void __launch_bounds__(kRateThreads) k_rate_dmma(double *out) {
 }  // namespace
 
 extern "C" int sbdgb_measure_fp64_rates(int device, double *dfma_tflops, double *dmma_tflops) {
-  if (!dfma_tflops || !dmma_tflops) return SBDGB_E_INPUT;
+  if (!dfma_tflops || !dmma_tflops) return 1;
   int sms = 0;
   if (cudaSetDevice(device) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
     cudaGetLastError();
-    return SBDGB_E_CUDA;
+    return 3;
   }
   const int blocks = sms * 8;
   double *out = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaStream_t s = nullptr;
-  int rc = SBDGB_OK;
+  int rc = 0;
   if (cudaMalloc(&out, sizeof(double) * blocks) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
       cudaEventCreate(&e1) != cudaSuccess || cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
-    rc = SBDGB_E_CUDA;
+    rc = 3;
   float ms_fma = 0.f, ms_mma = 0.f;
-  for (int rep = 0; rep < 2 && rc == SBDGB_OK; ++rep) {  // the first run is untimed
+  for (int rep = 0; rep < 2 && rc == 0; ++rep) {  // the first run is untimed
     cudaEventRecord(e0, s);
     k_rate_dfma<<<blocks, kRateThreads, 0, s>>>(out);
     cudaEventRecord(e1, s);
-    if (cudaEventSynchronize(e1) != cudaSuccess) rc = SBDGB_E_CUDA;
+    if (cudaEventSynchronize(e1) != cudaSuccess) rc = 3;
     cudaEventElapsedTime(&ms_fma, e0, e1);
     cudaEventRecord(e0, s);
     k_rate_dmma<<<blocks, kRateThreads, 0, s>>>(out);
     cudaEventRecord(e1, s);
-    if (cudaEventSynchronize(e1) != cudaSuccess) rc = SBDGB_E_CUDA;
+    if (cudaEventSynchronize(e1) != cudaSuccess) rc = 3;
     cudaEventElapsedTime(&ms_mma, e0, e1);
   }
-  if (rc == SBDGB_OK && cudaGetLastError() != cudaSuccess) rc = SBDGB_E_CUDA;
-  if (rc == SBDGB_OK) {
+  if (rc == 0 && cudaGetLastError() != cudaSuccess) rc = 3;
+  if (rc == 0) {
     // FMAs: 8 per thread per iteration; one m8n8k4 per warp is 256 FMAs, 4 per iteration
     const double fma = (double)blocks * kRateThreads * kRateIters * 8;
     const double mma = (double)blocks * (kRateThreads / 32) * kRateIters * 4 * 256;

@@ -57,9 +57,26 @@ def build(verbose: bool = False, extra: list[str] | None = None) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    _build_rates(extra)
     if verbose:
         print(LIB)
     return LIB
+
+
+RATES_SRC = os.path.join(HERE, "bench_csrc", "rates.cu")
+RATES_LIB = os.path.join(OUT, "libsbdgb_rates.so")
+
+
+def _build_rates(extra: list[str]) -> str:
+    """The FP64 rate probe of the benchmark (bench_csrc/rates.cu), a library of
+    its own: it is a measurement utility, not part of the engine's ABI."""
+    if os.path.exists(RATES_LIB) and os.path.getmtime(RATES_LIB) >= os.path.getmtime(RATES_SRC):
+        return RATES_LIB
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *extra, "-shared", RATES_SRC, "-o", RATES_LIB, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed on {RATES_SRC}:\n{r.stdout}\n{r.stderr}")
+    return RATES_LIB
 
 
 if __name__ == "__main__":

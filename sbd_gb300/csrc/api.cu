@@ -114,22 +114,25 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
   if (!mixed) {
     b += 16 * N * max_nb + 64 * N * k;  // basis and sigma; 3k restart vectors and their sigma; T; U
   } else if (o.refine_every == 0) {
-    // two-phase form: the FP64 solver's buffers (its start block holds up to
-    // 2k seed vectors), the same shapes in FP32, 2k FP64 seed vectors, FP32
-    // tables, the FP32 transpose and multi-vector scratch
-    b += 16 * N * max_nb + 72 * N * k;
+    // three-phase form: the FP32 solver's buffers and the double-float
+    // solver's (its start block holds up to 2k seeds), 2k FP64 seed vectors,
+    // the final FP64 check's buffers (subspace at most 4k), FP32 and
+    // double-float tables, the FP32 transpose and multi-vector scratch
     b += 8 * N * max_nb + 32 * N * k;
+    b += 16 * N * max_nb + 72 * N * k;
     b += 16 * N * k;
+    b += 16 * N * std::min<size_t>(max_nb, 4 * k) + 64 * N * k;
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;
+    b += 8 * npair * npair + 8 * npair * (na + nb) + 8 * (entries_a + entries_b) + 32;
     b += 4 * N + 4 * N * std::min<size_t>(4, k);
-    b += 8 * N;  // the diagonal as FP32 hi and lo parts
+    b += 8 * N;  // the diagonal as double-float
   } else {
     const size_t mmax = (size_t)std::max(std::min(o.max_nb, 64) - (int)k, 2 * (int)k);
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;  // FP32 tables
     b += 4 * N;                                                                          // FP32 transpose
     b += 4 * N * std::min<size_t>(4, k);  // transposed copies of the vectors of one multi-vector product
     b += 32 * N * k + 4 * N * (k + mmax) + 4 * N * mmax + 12 * N * k + 4 * (8 * 3 * 64 + 64);
-    b += 8 * N;  // the diagonal as FP32 hi and lo parts
+    b += 8 * N;  // the diagonal as double-float (hi and lo FP32 parts)
   }
   return b;
 }
@@ -401,6 +404,19 @@ int sbdgb_sigma_mixed(sbdgb_problem *pr, const float *Wk_dev, float *Wb_dev, voi
   });
 }
 
+int sbdgb_sigma_df(sbdgb_problem *pr, const float *Wk_dev, float *Wb_dev, int accumulate, void *stream) {
+  if (!pr || !Wk_dev || !Wb_dev) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    sbdgb::Problem &p = pr->p;
+    SBDGB_REQUIRE(p.tables && p.diag, SBDGB_E_STATE, "build tables and diagonal first");
+    SBDGB_REQUIRE(((uintptr_t)Wk_dev | (uintptr_t)Wb_dev) % 8 == 0, SBDGB_E_INPUT,
+                  "double-float vectors must be 8-byte aligned");
+    cudaStream_t s = stream ? (cudaStream_t)stream : p.ctx->stream;
+    sbdgb::sigma_df(p, reinterpret_cast<const sbdgb::dfloat *>(Wk_dev), reinterpret_cast<sbdgb::dfloat *>(Wb_dev),
+                    accumulate, s, 0.0, false);
+  });
+}
+
 int sbdgb_sigma_mixed_block(sbdgb_problem *pr, const float *Wk_dev, float *Wb_dev, int nvec, void *stream) {
   if (!pr || !Wk_dev || !Wb_dev || nvec < 1) return SBDGB_E_INPUT;
   return guarded(pr->p.ctx, [&] {
@@ -414,7 +430,7 @@ int sbdgb_sigma_mixed_block(sbdgb_problem *pr, const float *Wk_dev, float *Wb_de
 
 int sbdgb_problem_tuning(const sbdgb_problem *pr, int precision, int *shape_a, int *shape_b, float *ms_a,
                          float *ms_b, int n_shapes) {
-  if (!pr || (precision != 0 && precision != 1)) return SBDGB_E_INPUT;
+  if (!pr || precision < 0 || precision > 5) return SBDGB_E_INPUT;
   const sbdgb::Problem &p = pr->p;
   if (shape_a) *shape_a = p.tune_a[precision];
   if (shape_b) *shape_b = p.tune_b[precision];
@@ -426,7 +442,7 @@ int sbdgb_problem_tuning(const sbdgb_problem *pr, int precision, int *shape_a, i
 }
 
 int sbdgb_problem_tuning_times(const sbdgb_problem *pr, int precision, float *ms_fused, float *ms_sparse) {
-  if (!pr || (precision != 0 && precision != 1)) return SBDGB_E_INPUT;
+  if (!pr || precision < 0 || precision > 5) return SBDGB_E_INPUT;
   const sbdgb::Problem &p = pr->p;
   for (int i = 0; i < 4; ++i)
     if (ms_fused) ms_fused[i] = p.tune_ms[precision][2][i];
@@ -436,7 +452,7 @@ int sbdgb_problem_tuning_times(const sbdgb_problem *pr, int precision, float *ms
 }
 
 int sbdgb_problem_set_tuning(sbdgb_problem *pr, int precision, int shape_a, int shape_b) {
-  if (!pr || (precision != 0 && precision != 1)) return SBDGB_E_INPUT;
+  if (!pr || precision < 0 || precision > 5) return SBDGB_E_INPUT;
   if (shape_a < 0 || shape_a > 3 || shape_b < 0 || shape_b > 5 || (shape_b == 5 && shape_a > 1)) return SBDGB_E_INPUT;
   pr->p.tune_a[precision] = shape_a;
   pr->p.tune_b[precision] = shape_b;

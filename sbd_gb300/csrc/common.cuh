@@ -13,6 +13,7 @@
 #include <string>
 #include <vector>
 
+#include "df.cuh"
 #include "sbdgb.h"
 
 namespace sbdgb {
@@ -112,6 +113,7 @@ enum WsSlot {
   WS_DIAG0, WS_DIAG1, WS_DIAG2,
   WS_VF, WS_HVF, WS_CF, WS_SF, WS_RES64, WS_C64, WS_TUNE,
   WS_U, WS_UF, WS_RED2, WS_NORM_A, WS_NORM_B, WS_OCC, WS_RDM1, WS_RDM2, WS_RDMAB, WS_CTMV,
+  WS_VD, WS_HVD, WS_XD, WS_HXD, WS_TD, WS_UD,
   WS_COUNT
 };
 
@@ -134,7 +136,11 @@ struct Problem {
   double *CT = nullptr;   // transpose scratch
   float *CTf = nullptr;   // mixed transpose scratch
   float *Kpf = nullptr, *Jbf = nullptr, *Jaf = nullptr;
-  float *hii_hi = nullptr, *hii_lo = nullptr;  // mixed form: hii = hi + lo in FP32 parts
+  dfloat *hii_df = nullptr;  // hii as double-float (FP32 and double-float kernels)
+  // double-float copies of the tables and integral tables (double-float phase of the mixed form)
+  dfloat *Kpd = nullptr, *Jbd = nullptr, *Jad = nullptr;
+  dfloat *val_sd[2] = {nullptr, nullptr}, *val_dd[2] = {nullptr, nullptr};
+  bool df_ready = false;
   float *val_sf[2] = {nullptr, nullptr}, *val_df[2] = {nullptr, nullptr};
   void *ws[WS_COUNT] = {};
   size_t ws_bytes[WS_COUNT] = {};
@@ -144,8 +150,10 @@ struct Problem {
   // tiles in order[] (heaviest first).
   uint32_t *tile_start[2][2] = {}, *tile_order[2][2] = {};
   uint32_t n_tiles[2][2] = {};
-  int tune_a[2] = {-1, -1}, tune_b[2] = {-1, -1};  // autotuned sigma tile shapes (FP64, mixed)
-  float tune_ms[2][3][8] = {};                       // timings the autotuner saw (A, B, fused)
+  // autotuned sigma tile shapes: FP64, FP32, double-float, in the interleaved
+  // (0..2) and block (3..5) orderings
+  int tune_a[6] = {-1, -1, -1, -1, -1, -1}, tune_b[6] = {-1, -1, -1, -1, -1, -1};
+  float tune_ms[6][3][8] = {};  // timings the autotuner saw (A, B, fused + sparse)
   size_t bytes = 0;
   std::vector<void *> allocs;
   // host copies of strings
@@ -180,7 +188,7 @@ struct Ctx {
   std::map<std::array<uint64_t, 6>, Tuned> tuned;
 };
 
-constexpr size_t kPinnedDoubles = 8192;
+constexpr size_t kPinnedDoubles = 16384;
 double *pinned_buffer(Ctx *c);
 
 // sigma timing hooks (api.cu)
@@ -209,14 +217,27 @@ void export_tables(const Problem &p, int spin, uint64_t *off_s, uint64_t *ket_s,
 void build_diag(Problem &p, cudaStream_t s);
 // sigma.cu
 void build_row_tiles(Problem &p, cudaStream_t s);
-void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s);
+// block: the block-ordering product (H_block = eta H eta, no opposite-spin
+// parities) that the solvers use on eta-signed vectors; false: the
+// reference's interleaved convention.
+void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s, bool block = false);
 void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, double *CT, cudaStream_t s);
 // (H - shift) C in the mixed form: the diagonal term is formed in FP64 before
 // the result is rounded, so a shift near the spectrum keeps FP32 outputs small.
-void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double shift = 0.0);
+void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double shift = 0.0, bool block = false);
 // The same for nvec <= 4 vectors at once (inputs and outputs at stride N).
-void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStream_t s, double shift = 0.0);
+void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStream_t s, double shift = 0.0,
+                       bool block = false);
 void prepare_mixed(Problem &p, cudaStream_t s);
+// Double-float form: (H - shift) C, or accumulated into S (the second phase of the mixed solver).
+void sigma_df(Problem &p, const dfloat *C, dfloat *S, int accumulate, cudaStream_t s, double shift = 0.0,
+              bool block = false);
+// x_j *= eta for nvec vectors of N (T = double, float or dfloat): converts
+// between the interleaved convention and the block one (an involution).
+template <typename T>
+void apply_eta(Problem &p, T *x, int nvec, cudaStream_t s);
+void prepare_df(Problem &p, cudaStream_t s);
+void split_hii(Problem &p, cudaStream_t s);
 // davidson.cu
 void davidson(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X, sbdgb_report *rep);
 void lanczos(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X, sbdgb_report *rep);

@@ -70,7 +70,8 @@ template <typename TV, typename TW, int NV, int NW>
 __global__ void __launch_bounds__(kRed) k_dots(Ptrs<TV, kMaxV> V, Ptrs<TW, kMaxW> W, size_t N,
                                                double *__restrict__ partial) {
   constexpr bool kF32 = std::is_same<TV, float>::value && std::is_same<TW, float>::value;
-  using Acc = typename std::conditional<kF32, float, double>::type;
+  constexpr bool kDF = std::is_same<TV, dfloat>::value || std::is_same<TW, dfloat>::value;
+  using Acc = typename std::conditional<kF32, float, typename std::conditional<kDF, dfloat, double>::type>::type;
   Acc acc[NV][NW], cmp[NV][NW];
 #pragma unroll
   for (int i = 0; i < NV; ++i)
@@ -82,10 +83,10 @@ __global__ void __launch_bounds__(kRed) k_dots(Ptrs<TV, kMaxV> V, Ptrs<TW, kMaxW
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     Acc w[NW];
 #pragma unroll
-    for (int j = 0; j < NW; ++j) w[j] = (Acc)__ldg(W.p[j] + e);
+    for (int j = 0; j < NW; ++j) w[j] = (Acc)ldg(W.p[j] + e);
 #pragma unroll
     for (int i = 0; i < NV; ++i) {
-      const Acc v = (Acc)__ldg(V.p[i] + e);
+      const Acc v = (Acc)ldg(V.p[i] + e);
 #pragma unroll
       for (int j = 0; j < NW; ++j) {
         if constexpr (kF32) {
@@ -134,6 +135,7 @@ struct CombineArgs {
   int nv;
   int k;
   const double *hii;
+  const dfloat *hii_df;  // hii as double-float (read instead of hii by the FP32 and double-float forms)
   F *X;             // k x N or null
   F *HX;            // k x N or null
   F *T;             // k x N or null: preconditioned residual
@@ -141,6 +143,8 @@ struct CombineArgs {
   double *partial;  // blocks x k residual norm^2 partials (x 3k with U: norm^2, x.T, x.U)
   Vals<kMaxCoef> coef;  // nv x k column-major (coef[j + nv*r])
   Vals<16> theta;       // k
+  const double *coef_dev;   // or these on the device (the Rayleigh-Ritz result), when not null
+  const double *theta_dev;
 };
 
 // X_r = V c_r, HX_r = HV c_r, R_r = HX_r - theta_r X_r, T_r = R_r / (theta_r - d)
@@ -156,8 +160,8 @@ template <int K, typename F>
 __global__ void __launch_bounds__(kRed) k_combine(CombineArgs<F> a) {
   __shared__ F cs[kMaxCoef];
   __shared__ F th[16];
-  for (int t = threadIdx.x; t < a.nv * K; t += kRed) cs[t] = (F)a.coef.v[t];
-  if (threadIdx.x < K) th[threadIdx.x] = (F)a.theta.v[threadIdx.x];
+  for (int t = threadIdx.x; t < a.nv * K; t += kRed) cs[t] = (F)(a.coef_dev ? a.coef_dev[t] : a.coef.v[t]);
+  if (threadIdx.x < K) th[threadIdx.x] = (F)(a.theta_dev ? a.theta_dev[threadIdx.x] : a.theta.v[threadIdx.x]);
   __syncthreads();
   F rn[K], xt[K], xu[K];
 #pragma unroll
@@ -170,15 +174,22 @@ __global__ void __launch_bounds__(kRed) k_combine(CombineArgs<F> a) {
       h[r] = F(0);
     }
     for (int j = 0; j < a.nv; ++j) {
-      const F v = __ldg(a.V + (size_t)j * a.N + e);
-      const F hv = __ldg(a.HV + (size_t)j * a.N + e);
+      const F v = ldg(a.V + (size_t)j * a.N + e);
+      const F hv = ldg(a.HV + (size_t)j * a.N + e);
 #pragma unroll
       for (int r = 0; r < K; ++r) {
         x[r] = fma(v, cs[j + a.nv * r], x[r]);
         h[r] = fma(hv, cs[j + a.nv * r], h[r]);
       }
     }
-    const F d = a.hii ? (F)__ldg(a.hii + e) : F(0);
+    F d = F(0);
+    if constexpr (std::is_same<F, double>::value) {
+      if (a.hii) d = ldg(a.hii + e);
+    } else if constexpr (std::is_same<F, float>::value) {
+      if (a.hii_df) d = ldg(a.hii_df + e).hi;
+    } else {
+      if (a.hii_df) d = ldg(a.hii_df + e);
+    }
 #pragma unroll
     for (int r = 0; r < K; ++r) {
       const F res = h[r] - th[r] * x[r];
@@ -240,7 +251,7 @@ __global__ void __launch_bounds__(kRed) k_project_out(const T *__restrict__ V, i
 #pragma unroll
     for (int r = 0; r < K; ++r) t[r] = Tv[(size_t)r * N + e];
     for (int j = 0; j < nv; ++j) {
-      const T v = __ldg(V + (size_t)j * N + e);
+      const T v = ldg(V + (size_t)j * N + e);
 #pragma unroll
       for (int r = 0; r < K; ++r) t[r] = fma(-v, gs[j + nv * r], t[r]);
     }
@@ -258,7 +269,7 @@ __global__ void __launch_bounds__(kRed) k_lincomb(const T *__restrict__ X, int n
   __syncthreads();
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     T x[kMaxBlock];
-    for (int j = 0; j < nx; ++j) x[j] = __ldg(X + (size_t)j * N + e);
+    for (int j = 0; j < nx; ++j) x[j] = ldg(X + (size_t)j * N + e);
     for (int q = 0; q < ny; ++q) {
       T y = T(0);
       for (int j = 0; j < nx; ++j) y = fma(x[j], ms[j + nx * q], y);
@@ -384,7 +395,7 @@ __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
 #pragma unroll
     for (int q = 0; q < K; ++q) r[q] = x[q] = 0.f;
     for (int j = 0; j < a.k; ++j) {
-      const float xf = __ldg(a.Xf + (size_t)j * a.N + e), rf = __ldg(a.Rf + (size_t)j * a.N + e);
+      const float xf = ldg(a.Xf + (size_t)j * a.N + e), rf = ldg(a.Rf + (size_t)j * a.N + e);
 #pragma unroll
       for (int q = 0; q < K; ++q) {
         r[q] = fmaf(fmaf(c[q][64 + j], xf, rf), c[q][j], r[q]);
@@ -392,14 +403,14 @@ __global__ void __launch_bounds__(kRed) k_mixed_residual(MixedResArgs a) {
       }
     }
     for (int l = 0; l < a.m; ++l) {
-      const float w = __ldg(a.W + (size_t)l * a.N + e), hw = __ldg(a.HW + (size_t)l * a.N + e);
+      const float w = ldg(a.W + (size_t)l * a.N + e), hw = ldg(a.HW + (size_t)l * a.N + e);
 #pragma unroll
       for (int q = 0; q < K; ++q) {
         r[q] = fmaf(fmaf(-th[q], w, hw), c[q][128 + l], r[q]);
         x[q] = fmaf(w, c[q][128 + l], x[q]);
       }
     }
-    const double d = __ldg(a.hii + e);
+    const double d = ldg(a.hii + e);
 #pragma unroll
     for (int q = 0; q < K; ++q) {
       kahan_add(s[q], comp[q], r[q] * r[q]);
@@ -447,9 +458,9 @@ __global__ void __launch_bounds__(kRed) k_mixed_assemble(const double *__restric
   __syncthreads();
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     double v = 0.0;
-    for (int j = 0; j < k; ++j) v = fma(__ldg(X + (size_t)j * N + e), sx[j], v);
+    for (int j = 0; j < k; ++j) v = fma(ldg(X + (size_t)j * N + e), sx[j], v);
     float w = 0.f;
-    for (int l = 0; l < m; ++l) w = fmaf(__ldg(W + (size_t)l * N + e), sw[l], w);
+    for (int l = 0; l < m; ++l) w = fmaf(ldg(W + (size_t)l * N + e), sw[l], w);
     y[e] = v + (double)w;
   }
 }
@@ -463,7 +474,7 @@ __global__ void __launch_bounds__(kRed) k_lz_update(double *__restrict__ HC, con
                                                      double *__restrict__ partial) {
   double s = 0.0;
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
-    const double h = fma(-a, __ldg(Cb + e), HC[e]);
+    const double h = fma(-a, ldg(Cb + e), HC[e]);
     HC[e] = h;
     next[e] = h;
     s = fma(h, h, s);
@@ -485,7 +496,7 @@ __global__ void __launch_bounds__(kRed) k_lz_scale(double *__restrict__ next, do
   const double ib = 1.0 / b;
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     next[e] *= ib;
-    HC[e] = -b * __ldg(Cb + e);
+    HC[e] = -b * ldg(Cb + e);
   }
 }
 
@@ -497,8 +508,126 @@ __global__ void __launch_bounds__(kRed) k_lz_ritz(const double *__restrict__ C, 
   __syncthreads();
   for (size_t e = blockIdx.x * (size_t)kRed + threadIdx.x; e < N; e += (size_t)gridDim.x * kRed) {
     double w = 0.0;
-    for (int j = 0; j < n; ++j) w = fma(us[j], __ldg(C + (size_t)j * N + e), w);
+    for (int j = 0; j < n; ++j) w = fma(us[j], ldg(C + (size_t)j * N + e), w);
     W[e] = w;
+  }
+}
+
+// ---- Rayleigh-Ritz on the device ------------------------------------------------
+
+// M[(i0 + i) + ld (j0 + j)] = sum over blocks of partial[b][i * mw + j] (and the
+// transposed entry when sym): a dots pass written into the projected matrix.
+__global__ void k_sum_partials_mat(const double *__restrict__ partial, int nblocks, int mv, int mw,
+                                   double *__restrict__ M, int ld, int i0, int j0, int sym) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= mv * mw) return;
+  double x = 0.0;
+  for (int b = 0; b < nblocks; ++b) x += partial[(size_t)b * mv * mw + t];
+  const int i = i0 + t / mw, j = j0 + t % mw;
+  M[i + (size_t)ld * j] = x;
+  if (sym) M[j + (size_t)ld * i] = x;
+}
+
+constexpr int kRR = 64;  // largest projected matrix (max_nb <= 64)
+
+__device__ __forceinline__ double block_sum64(double v, double *tmp) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) tmp[threadIdx.x >> 5] = v;
+  __syncthreads();
+  const double r = tmp[0] + tmp[1];
+  __syncthreads();
+  return r;
+}
+
+// Eigenvalues (ascending) and eigenvectors of the symmetric part of the n x n
+// leading block of Hs (ld), n <= 64, by one block of 64 threads: out[0..n) the
+// eigenvalues, out[n + i + n j] the eigenvector matrix (column j).  The
+// reference solves this with LAPACK dsyev on the host (framework/hp_numeric.h:
+// 503-520); here it is a parallel-order Jacobi: each sweep is n' - 1 rounds
+// (n' = n rounded up to even) of the round-robin pairing, the n'/2 rotations of
+// a round act on disjoint index pairs, so their parameters are computed by
+// n'/2 threads at once and applied together (thread l updates row / column l).
+// FP64 divisions and square roots, 1/64 rate on this GPU, are taken once per
+// round instead of once per pair.
+__global__ void __launch_bounds__(kRR) k_rr(const double *__restrict__ Hs, int ld, int n, double *__restrict__ out) {
+  extern __shared__ double sm[];
+  double *Aw = sm, *Wv = sm + (size_t)n * n;
+  __shared__ double rc[kRR / 2], rs[kRR / 2], tmp[2];
+  __shared__ int rp[kRR / 2], rq[kRR / 2];
+  const int l = threadIdx.x;
+  for (int t = l; t < n * n; t += kRR) {
+    const int i = t % n, j = t / n;
+    Aw[t] = 0.5 * (Hs[i + (size_t)ld * j] + Hs[j + (size_t)ld * i]);
+    Wv[t] = (i == j) ? 1.0 : 0.0;
+  }
+  __syncthreads();
+  const int n2 = (n + 1) & ~1, np = n2 / 2;
+  auto idx = [&](int pos, int r) { return pos == 0 ? 0 : 1 + (pos - 1 + r) % (n2 - 1); };
+  for (int sweep = 0; sweep < 60 && n > 1; ++sweep) {
+    double off = 0.0, dg = 0.0;
+    if (l < n)
+      for (int j = 0; j < n; ++j) {
+        const double x = Aw[l + n * j];
+        if (l == j) dg += x * x; else off += x * x;
+      }
+    off = block_sum64(off, tmp);
+    dg = block_sum64(dg, tmp);
+    if (off <= 1e-30 * (dg + 1e-300)) break;
+    for (int r = 0; r < n2 - 1; ++r) {
+      if (l < np) {
+        const int a = idx(l, r), b = idx(n2 - 1 - l, r);
+        const int pp = min(a, b), q = max(a, b);
+        double c = 1.0, sn = 0.0;
+        if (q < n) {  // q == n is the padding index of odd n
+          const double apq = Aw[pp + n * q];
+          if (fabs(apq) >= 1e-300) {
+            const double th = (Aw[q + n * q] - Aw[pp + n * pp]) / (2.0 * apq);
+            const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            sn = t * c;
+          }
+        }
+        rp[l] = pp;
+        rq[l] = q;
+        rc[l] = c;
+        rs[l] = sn;
+      }
+      __syncthreads();
+      if (l < n)  // columns p, q of every pair: row l
+        for (int i = 0; i < np; ++i) {
+          const int pp = rp[i], q = rq[i];
+          if (q >= n || rs[i] == 0.0) continue;
+          const double c = rc[i], sn = rs[i];
+          const double akp = Aw[l + n * pp], akq = Aw[l + n * q];
+          Aw[l + n * pp] = c * akp - sn * akq;
+          Aw[l + n * q] = sn * akp + c * akq;
+        }
+      __syncthreads();
+      if (l < n)  // rows p, q of every pair: column l; and the eigenvectors: row l
+        for (int i = 0; i < np; ++i) {
+          const int pp = rp[i], q = rq[i];
+          if (q >= n || rs[i] == 0.0) continue;
+          const double c = rc[i], sn = rs[i];
+          const double apk = Aw[pp + n * l], aqk = Aw[q + n * l];
+          Aw[pp + n * l] = c * apk - sn * aqk;
+          Aw[q + n * l] = sn * apk + c * aqk;
+          const double vkp = Wv[l + n * pp], vkq = Wv[l + n * q];
+          Wv[l + n * pp] = c * vkp - sn * vkq;
+          Wv[l + n * q] = sn * vkp + c * vkq;
+        }
+      __syncthreads();
+    }
+  }
+  // ascending order: rank of each eigenvalue (ties by index), then scatter
+  if (l < n) {
+    const double e = Aw[l + n * l];
+    int rank = 0;
+    for (int j = 0; j < n; ++j) {
+      const double f = Aw[j + n * j];
+      rank += (f < e) || (f == e && j < l);
+    }
+    out[rank] = e;
+    for (int i = 0; i < n; ++i) out[n + i + (size_t)n * rank] = Wv[i + n * l];
   }
 }
 
@@ -511,6 +640,8 @@ struct Solver {
   int blocks;
   double *partial = nullptr;  // blocks * kMaxV*kMaxW per batched dots pass
   double *red = nullptr;      // reduced results (device)
+  double *hs = nullptr;       // projected matrix on the device (kRR x kRR, ld kRR)
+  double *rr = nullptr;       // Rayleigh-Ritz result on the device: n eigenvalues, n x n eigenvectors
   double *host = nullptr;     // pinned read-back buffer of the context
 
   Solver(Problem &pp, cudaStream_t ss) : p(pp), s(ss), N(pp.N) {
@@ -520,8 +651,63 @@ struct Solver {
     blocks = (int)std::max<size_t>(1, std::min<size_t>(want, (size_t)sms * 4));
     partial = (double *)workspace(p, WS_PARTIAL,
                                   sizeof(double) * ((size_t)blocks * kMaxV * kMaxW * kMaxChunks + 64));
-    red = (double *)workspace(p, WS_RED, sizeof(double) * 4096);
+    red = (double *)workspace(p, WS_RED, sizeof(double) * (4096 + kRR * kRR + kRR + kRR * kRR));
+    hs = red + 4096;
+    rr = hs + kRR * kRR;
     host = pinned_buffer(p.ctx);
+  }
+
+  // The projected matrix columns [j0, j0 + nw) = V^T W written on the device
+  // (rows 0..nv, and the transposed entries): no read-back.
+  template <typename TV, typename TW>
+  void dots_into_hs(const TV *V0, int nv, const TW *W0, int nw, int j0) {
+    int batch = 0;
+    for (int jb = 0; jb < nw; jb += kMaxW) {
+      const int mw = std::min(kMaxW, nw - jb);
+      Ptrs<TW, kMaxW> wp{};
+      for (int j = 0; j < kMaxW; ++j) wp.p[j] = W0 + (size_t)(jb + std::min(j, mw - 1)) * N;
+      for (int i0 = 0; i0 < nv; i0 += kMaxV) {
+        const int mv = std::min(kMaxV, nv - i0);
+        Ptrs<TV, kMaxV> vp{};
+        for (int i = 0; i < kMaxV; ++i) vp.p[i] = V0 + (size_t)(i0 + std::min(i, mv - 1)) * N;
+        double *part = partial + (size_t)(batch % kMaxChunks) * blocks * kMaxV * kMaxW;
+        launch_dots<TV, TW>(vp, wp, mv, mw, part);
+        k_sum_partials_mat<<<(mv * mw + 63) / 64, 64, 0, s>>>(part, blocks, mv, mw, hs, kRR, i0, j0 + jb, 1);
+        count_launch(p.ctx);
+        ++batch;
+      }
+    }
+    SBDGB_CUDA(cudaGetLastError());
+  }
+
+  // Rayleigh-Ritz of the leading n x n block of the device projected matrix,
+  // on the device (k_rr); the result stays in rr until read back.
+  void rayleigh_ritz(int n) {
+    SBDGB_REQUIRE(n >= 1 && n <= kRR, SBDGB_E_UNSUPPORTED, "projected matrix larger than 64");
+    const size_t smem = sizeof(double) * 2 * (size_t)n * n;
+    SBDGB_CUDA(cudaFuncSetAttribute(k_rr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_rr<<<1, kRR, smem, s>>>(hs, kRR, n, rr);
+    count_launch(p.ctx);
+    SBDGB_CUDA(cudaGetLastError());
+  }
+
+  // The device projected matrix's leading n x n block (column-major, ld ld) to the host.
+  void read_hs(int n, std::vector<double> &H, int ld) {
+    SBDGB_CUDA(cudaMemcpy2DAsync(host, sizeof(double) * n, hs, sizeof(double) * kRR, sizeof(double) * n, n,
+                                 cudaMemcpyDeviceToHost, s));
+    SBDGB_CUDA(cudaStreamSynchronize(s));
+    std::fill(H.begin(), H.end(), 0.0);
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) H[i + (size_t)ld * j] = host[i + (size_t)n * j];
+  }
+  // Replaces the device projected matrix by the n x n matrix H (column-major, ld ld).
+  void write_hs(int n, const std::vector<double> &H, int ld) {
+    double *stage = host + kPinnedDoubles / 2;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) stage[i + (size_t)n * j] = H[i + (size_t)ld * j];
+    SBDGB_CUDA(cudaMemcpy2DAsync(hs, sizeof(double) * kRR, stage, sizeof(double) * n, sizeof(double) * n, n,
+                                 cudaMemcpyHostToDevice, s));
+    SBDGB_CUDA(cudaStreamSynchronize(s));  // the staging area is reused
   }
 
   // Copies n reduced values from red to the pinned buffer and waits for them.
@@ -604,14 +790,24 @@ struct Solver {
 
   // Ritz vectors (optional), their sigma (optional) and the preconditioned
   // residuals (optional) of the combination c; returns the residual norms.
+  //
+  // With dev_rr, the coefficients and theta are the device Rayleigh-Ritz result
+  // (rr: eigenvalues, then the eigenvector matrix) and come back to the host,
+  // with the residual norms, in *rr_host (n eigenvalues, n x n eigenvectors).
   template <typename F>
   std::vector<double> combine(const F *V, const F *HV, int nv, int k, const std::vector<double> &c,
-                              const std::vector<double> &theta, F *X, F *HX, F *T, F *U = nullptr) {
+                              const std::vector<double> &theta, F *X, F *HX, F *T, F *U = nullptr,
+                              std::vector<double> *rr_host = nullptr) {
     SBDGB_REQUIRE((size_t)nv * k <= (size_t)kMaxCoef && k <= 16, SBDGB_E_UNSUPPORTED, "subspace too large");
     if (!T) U = nullptr;
-    CombineArgs<F> a{V, HV, N, nv, k, p.hii, X, HX, T, U, partial, {}, {}};
-    std::copy(c.begin(), c.begin() + (size_t)nv * k, a.coef.v);
-    for (int r = 0; r < k; ++r) a.theta.v[r] = r < (int)theta.size() ? theta[r] : 0.0;
+    CombineArgs<F> a{V, HV, N, nv, k, p.hii, p.hii_df, X, HX, T, U, partial, {}, {}, nullptr, nullptr};
+    if (rr_host) {
+      a.coef_dev = rr + nv;
+      a.theta_dev = rr;
+    } else {
+      std::copy(c.begin(), c.begin() + (size_t)nv * k, a.coef.v);
+      for (int r = 0; r < k; ++r) a.theta.v[r] = r < (int)theta.size() ? theta[r] : 0.0;
+    }
     switch (k) {
 #define SBDGB_K(KK) \
   case KK: k_combine<KK, F><<<blocks, kRed, 0, s>>>(a); break;
@@ -624,7 +820,10 @@ struct Solver {
     k_sum_partials<<<1, 64, 0, s>>>(partial, blocks, width, red);
     count_launch(p.ctx, 2);
     SBDGB_CUDA(cudaGetLastError());
+    const int nrr = rr_host ? nv + nv * nv : 0;
+    if (nrr) SBDGB_CUDA(cudaMemcpyAsync(host + width, rr, sizeof(double) * nrr, cudaMemcpyDeviceToHost, s));
     const double *h = read_back(width);
+    if (rr_host) rr_host->assign(h + width, h + width + nrr);
     std::vector<double> v(h, h + width);
     std::vector<double> rn(v.begin(), v.begin() + k);
     for (auto &x : rn) x = std::sqrt(std::max(0.0, x));
@@ -781,6 +980,7 @@ struct Solver {
     if (o.init == 2) {
       SBDGB_REQUIRE(Xin != nullptr, SBDGB_E_INPUT, "init 2 needs starting vectors in X");
       SBDGB_CUDA(cudaMemcpyAsync(T, Xin, sizeof(double) * N * k, cudaMemcpyHostToDevice, s));
+      apply_eta<double>(p, T, k, s);  // the solvers work in the block ordering
       return;
     }
     std::vector<size_t> pos;
@@ -831,46 +1031,55 @@ struct CorePhase {
   double *seed_out = nullptr;     // the lowest min(nseed_out, available) Ritz vectors
   int nseed_out = 0;
   int *nseed_written = nullptr;
+  int max_nb_cap = 0;             // > 0: subspace at most this large (the final FP64 check)
 };
 
-// The Davidson iteration in storage precision F: FP64 (the plain solver), or
-// FP32 (the first phase of the two-phase mixed form: FP32 vectors, the FP32
-// sigma of the mixed kernels, FP32 vector algebra with FP64 block sums; the
-// projected matrix and Rayleigh-Ritz stay FP64).
+// The Davidson iteration in storage precision F: FP64 (the plain solver),
+// FP32 (the first phase of the mixed form: FP32 vectors, the FP32 sigma of the
+// mixed kernels, FP32 vector algebra with FP64 block sums) or double-float (its
+// second phase: double-float vectors, sigma and vector algebra on the FP32
+// pipe).  The projected matrix and Rayleigh-Ritz stay FP64 in every form.
 template <typename F>
 void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph, double *E, double *Xout,
                    sbdgb_report &r) {
   using clock = std::chrono::steady_clock;
   constexpr bool kF64 = std::is_same<F, double>::value;
+  constexpr bool kDF = std::is_same<F, dfloat>::value;
+  auto slot = [](int f64, int f32, int df) { return kF64 ? f64 : kDF ? df : f32; };
   const auto t0 = clock::now();
   const int k = o.nroots;
   const size_t N = p.N;
   SBDGB_REQUIRE(k <= kMaxBlock, SBDGB_E_UNSUPPORTED, "at most 8 roots");
   int max_nb = std::max(o.max_nb, 2 * k);
+  if (ph.max_nb_cap > 0) max_nb = std::min(max_nb, std::max(ph.max_nb_cap, 2 * k));
   max_nb = (int)std::min<size_t>((size_t)max_nb, N);
   SBDGB_REQUIRE(max_nb <= 64, SBDGB_E_INPUT, "max_nb must be <= 64");
   cudaStream_t s = p.ctx->stream;
   Solver sv(p, s);
   const int nstart = ph.seed ? ph.nseed : k;
-  F *V = (F *)workspace(p, kF64 ? WS_V : WS_VF, sizeof(F) * N * max_nb);
-  F *HV = (F *)workspace(p, kF64 ? WS_HV : WS_HVF, sizeof(F) * N * max_nb);
-  F *X = (F *)workspace(p, kF64 ? WS_X : WS_CF, sizeof(F) * N * 3 * k);  // restart basis (<= 3k)
-  F *HX = (F *)workspace(p, kF64 ? WS_HX : WS_SF, sizeof(F) * N * 3 * k);
-  F *T = (F *)workspace(p, kF64 ? WS_T : WS_RES64, sizeof(F) * N * std::max(k, nstart));
-  F *U = (F *)workspace(p, kF64 ? WS_U : WS_UF, sizeof(F) * N * k);
-  const double drop = kF64 ? 1e-8 : 1e-5;  // relative norm below which a new direction is dropped
+  F *V = (F *)workspace(p, slot(WS_V, WS_VF, WS_VD), sizeof(F) * N * max_nb);
+  F *HV = (F *)workspace(p, slot(WS_HV, WS_HVF, WS_HVD), sizeof(F) * N * max_nb);
+  F *X = (F *)workspace(p, slot(WS_X, WS_CF, WS_XD), sizeof(F) * N * 3 * k);  // restart basis (<= 3k)
+  F *HX = (F *)workspace(p, slot(WS_HX, WS_SF, WS_HXD), sizeof(F) * N * 3 * k);
+  F *T = (F *)workspace(p, slot(WS_T, WS_RES64, WS_TD), sizeof(F) * N * std::max(k, nstart));
+  F *U = (F *)workspace(p, slot(WS_U, WS_UF, WS_UD), sizeof(F) * N * k);
+  // relative norm below which a new direction is dropped
+  const double drop = kF64 ? 1e-8 : kDF ? 1e-7 : 1e-5;
 
   int nv = 0;
-  if (ph.seed) {
-    SBDGB_REQUIRE(kF64, SBDGB_E_STATE, "seed vectors start the FP64 core only");
+  if (ph.seed && kF64) {
     nv = sv.orthonormalize_block<double>(ph.seed, ph.nseed, (const double *)V, 0, (double *)V, drop);
+  } else if (ph.seed) {
+    k_convert<double, F><<<sv.blocks, kRed, 0, s>>>(ph.seed, T, N * (size_t)ph.nseed);
+    count_launch(p.ctx);
+    nv = sv.orthonormalize_block<F>(T, ph.nseed, V, 0, V, drop);
   } else if (kF64) {
     sv.start_vectors(o, k, (double *)T, Xout);
     nv = sv.orthonormalize_block<double>((double *)T, k, (const double *)V, 0, (double *)V, drop);
   } else {
     double *T64 = (double *)workspace(p, WS_C64, sizeof(double) * N * k);
     sv.start_vectors(o, k, T64, Xout);
-    k_convert<double, float><<<sv.blocks, kRed, 0, s>>>(T64, (float *)T, N * k);
+    k_convert<double, F><<<sv.blocks, kRed, 0, s>>>(T64, T, N * k);
     count_launch(p.ctx);
     nv = sv.orthonormalize_block<F>(T, k, V, 0, V, drop);
   }
@@ -880,22 +1089,18 @@ void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph
   auto extend = [&](int from, int to) {
     if constexpr (kF64) {
       for (int j = from; j < to; ++j) {
-        sigma_fp64(p, V + (size_t)j * N, HV + (size_t)j * N, 0, s);
+        sigma_fp64(p, V + (size_t)j * N, HV + (size_t)j * N, 0, s, true);
         r.sigma_fp64++;
       }
+    } else if constexpr (kDF) {
+      for (int j = from; j < to; ++j) sigma_df(p, V + (size_t)j * N, HV + (size_t)j * N, 0, s, 0.0, true);
     } else {
       for (int j = from; j < to; j += 4)
-        sigma_mixed_multi(p, V + (size_t)j * N, HV + (size_t)j * N, std::min(4, to - j), s, 0.0);
+        sigma_mixed_multi(p, V + (size_t)j * N, HV + (size_t)j * N, std::min(4, to - j), s, 0.0, true);
     }
     r.sigma_calls += to - from;
-    std::vector<double> G;
-    sv.dots_c<F, F>(V, to, HV + (size_t)from * N, to - from, G);
-    for (int jj = 0; jj < to - from; ++jj)
-      for (int i = 0; i < to; ++i) {
-        const double g = G[(size_t)i + (size_t)to * jj];
-        Hs[(size_t)i + (size_t)max_nb * (from + jj)] = g;
-        Hs[(size_t)(from + jj) + (size_t)max_nb * i] = g;
-      }
+    // the new columns of the projected matrix, written on the device
+    sv.dots_into_hs<F, F>(V, to, HV + (size_t)from * N, to - from, from);
   };
   extend(0, nv);
 
@@ -908,23 +1113,23 @@ void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph
   if (ph.step_cap > 0) max_steps = std::min(max_steps, ph.step_cap);
   auto tol = [&](int q) { return std::max(o.eps, ph.eps_rel * std::fabs(th[q])); };
   while (true) {
-    // Rayleigh-Ritz on the projected matrix
-    std::vector<double> A((size_t)nv * nv);
-    for (int j = 0; j < nv; ++j)
-      for (int i = 0; i < nv; ++i)
-        A[i + (size_t)nv * j] = 0.5 * (Hs[i + (size_t)max_nb * j] + Hs[j + (size_t)max_nb * i]);
-    jacobi_eig(nv, A, theta, Y);
+    // Rayleigh-Ritz on the device projected matrix (FP64, on the GPU), then
+    // the residual norms and preconditioned corrections from its result
+    // (Ritz vectors not materialised); the eigenpairs come back with the norms
+    sv.rayleigh_ritz(nv);
     rotated = false;
     kk = std::min(k, nv);
+    std::vector<double> rrh;
+    resid = sv.combine<F>(V, HV, nv, kk, c, th, nullptr, nullptr, T, U, &rrh);
+    theta.assign(rrh.begin(), rrh.begin() + nv);
+    Y.assign(rrh.begin() + nv, rrh.end());
     c.assign((size_t)nv * kk, 0.0);
     for (int q = 0; q < kk; ++q)
       for (int i = 0; i < nv; ++i) c[i + (size_t)nv * q] = Y[i + (size_t)nv * q];
     th.assign(theta.begin(), theta.begin() + kk);
-    // residual norms and preconditioned corrections; Ritz vectors not materialised
-    resid = sv.combine<F>(V, HV, nv, kk, c, th, nullptr, nullptr, T, U);
     iter++;
     r.iterations++;
-    if (o.verbose) print_iter(kF64 ? "" : " (FP32 phase)", iter, resid, th, kk);
+    if (o.verbose) print_iter(kF64 ? "" : kDF ? " (double-float phase)" : " (FP32 phase)", iter, resid, th, kk);
     converged = kk == k;
     for (int q = 0; q < kk; ++q) converged = converged && (resid[q] < tol(q));
     const double elapsed = std::chrono::duration<double>(clock::now() - t0).count();
@@ -974,6 +1179,7 @@ void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph
       }
       SBDGB_CUDA(cudaMemcpyAsync(V, X, sizeof(F) * N * m, cudaMemcpyDeviceToDevice, s));
       SBDGB_CUDA(cudaMemcpyAsync(HV, HX, sizeof(F) * N * m, cudaMemcpyDeviceToDevice, s));
+      sv.read_hs(nv, Hs, max_nb);  // the projected matrix, for its basis change
       std::vector<double> A((size_t)nv * nv), AQ((size_t)nv * m, 0.0), Hn((size_t)m * m, 0.0), cn((size_t)m * kk, 0.0);
       for (int j = 0; j < nv; ++j)
         for (int i = 0; i < nv; ++i)
@@ -990,6 +1196,7 @@ void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph
       std::fill(Hs.begin(), Hs.end(), 0.0);
       for (int b = 0; b < m; ++b)
         for (int a2 = 0; a2 < m; ++a2) Hs[a2 + (size_t)max_nb * b] = Hn[a2 + (size_t)m * b];
+      sv.write_hs(m, Hs, max_nb);
       c = cn;
       nv = m;
       rotated = true;
@@ -1020,6 +1227,7 @@ void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph
   for (int q = 0; q < k; ++q) E[q] = q < (int)theta.size() ? theta[q] : NAN;
   if (Xout && kF64) {
     sv.combine<F>(V, HV, nv, kk, c, th, X, nullptr, nullptr);
+    apply_eta<F>(p, X, kk, s);  // back to the interleaved convention
     SBDGB_CUDA(cudaMemcpyAsync(Xout, X, sizeof(double) * N * kk, cudaMemcpyDeviceToHost, s));
   }
   if (ph.seed_out) {
@@ -1050,17 +1258,24 @@ void davidson_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *
   if (rep) *rep = r;
 }
 
-// Two-phase mixed form (precision MIXED with refine_every 0): the Davidson
-// iteration first in FP32 until every residual is below 5e-7 |theta| (at most
-// 4 max_nb iterations), then in FP64 from the lowest 2k Ritz vectors of that
-// phase (at most 8) to the full tolerance.  FP64 runs at 1/64 of the FP32
-// rate on this GPU; the FP32 phase takes most of the iterations and the FP64
-// phase ends at the FP64 solver's answer.
+// Mixed form (precision MIXED with refine_every 0), in three phases:
+//  1. FP32: the Davidson iteration on FP32 vectors with the FP32 sigma until
+//     every residual is below 5e-7 |theta| (at most 4 max_nb iterations);
+//  2. double-float: the same iteration on double-float vectors (48-bit
+//     values, sigma and vector algebra on the FP32 pipe) from the lowest 2k
+//     Ritz vectors of phase 1 (at most 8) to the full tolerance;
+//  3. FP64: the lowest k Ritz vectors of phase 2 as the start of the FP64
+//     iteration, whose first step recomputes their FP64 sigma, Rayleigh-Ritz
+//     and residuals and stops there when those meet the tolerance (it goes on
+//     in FP64, in a subspace of at most 4k, when they do not).
+// FP64 runs at 1/64 of the FP32 rate on this GPU: phases 1 and 2 take the
+// iterations, and the energies, vectors and residuals reported are FP64.
 void davidson_two_phase(Problem &p, const sbdgb_davidson_opts &o, double *E, double *Xout, sbdgb_report *rep) {
   const int k = o.nroots;
   const size_t N = p.N;
   cudaStream_t s = p.ctx->stream;
   prepare_mixed(p, s);
+  prepare_df(p, s);
   const int max_nb = (int)std::min<size_t>((size_t)std::max(o.max_nb, 2 * k), N);
   const int nseed = std::max(k, std::min(std::min(2 * k, kMaxBlock), max_nb));
   double *seeds = (double *)workspace(p, WS_C64, sizeof(double) * N * std::max(nseed, k));
@@ -1074,15 +1289,28 @@ void davidson_two_phase(Problem &p, const sbdgb_davidson_opts &o, double *E, dou
   sbdgb_report r32{};
   std::vector<double> E32(k);
   davidson_core<float>(p, o, p32, E32.data(), Xout, r32);  // Xout: start vectors of init 2 (not written)
+  CorePhase pdf;
+  pdf.seed = seeds;
+  pdf.nseed = written;
+  pdf.eps_rel = 2e-14;  // the double-float rounding floor: FP64 finishes below it
+  pdf.seed_out = seeds;
+  pdf.nseed_out = k;
+  pdf.nseed_written = &written;
+  sbdgb_report rdf{};
+  std::vector<double> Edf(k);
+  davidson_core<dfloat>(p, o, pdf, Edf.data(), nullptr, rdf);
+  release_workspace(p, WS_VD);
+  release_workspace(p, WS_HVD);
   CorePhase p64;
   p64.seed = seeds;
   p64.nseed = written;
+  p64.max_nb_cap = 4 * k;
   sbdgb_report r{};
   davidson_core<double>(p, o, p64, E, Xout, r);
-  r.iterations += r32.iterations;
-  r.sigma_calls += r32.sigma_calls;
-  r.restarts += r32.restarts;
-  r.seconds += r32.seconds;
+  r.iterations += r32.iterations + rdf.iterations;
+  r.sigma_calls += r32.sigma_calls + rdf.sigma_calls;
+  r.restarts += r32.restarts + rdf.restarts;
+  r.seconds += r32.seconds + rdf.seconds;
   if (rep) *rep = r;
 }
 
@@ -1122,7 +1350,7 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
   // FP64 sigma of the anchors, Rayleigh-Ritz among them, FP64 residual norms
   auto refine_rr = [&]() {
     for (int j = 0; j < k; ++j) {
-      sigma_fp64(p, X + (size_t)j * N, S + (size_t)j * N, 0, s);
+      sigma_fp64(p, X + (size_t)j * N, S + (size_t)j * N, 0, s, true);
       r.sigma_calls++;
       r.sigma_fp64++;
     }
@@ -1211,7 +1439,7 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       const int added = sv.orthonormalize_block<float>(Tf, seed, XW, k, W, 1e-3);
       for (int j = 0; j < added; j += 4) {
         const int nv = std::min(4, added - j);
-        sigma_mixed_multi(p, W + (size_t)j * N, HW + (size_t)j * N, nv, s, shift);
+        sigma_mixed_multi(p, W + (size_t)j * N, HW + (size_t)j * N, nv, s, shift, true);
         r.sigma_calls += nv;
       }
       if (added > 0) {
@@ -1279,7 +1507,7 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
       }
       for (int j = m; j < m + added; j += 4) {
         const int nv = std::min(4, m + added - j);
-        sigma_mixed_multi(p, W + (size_t)j * N, HW + (size_t)j * N, nv, s, shift);
+        sigma_mixed_multi(p, W + (size_t)j * N, HW + (size_t)j * N, nv, s, shift, true);
         r.sigma_calls += nv;
       }
       // projected quantities of the new columns
@@ -1346,7 +1574,10 @@ void davidson_mixed(Problem &p, const sbdgb_davidson_opts &o, double *E, double 
   r.iterations = std::max(r.iterations, iter);
   for (int q = 0; q < k && q < 16; ++q) r.resid[q] = resid[q];
   for (int q = 0; q < k; ++q) E[q] = theta[q];
-  if (Xout) SBDGB_CUDA(cudaMemcpyAsync(Xout, X, sizeof(double) * N * k, cudaMemcpyDeviceToHost, s));
+  if (Xout) {
+    apply_eta<double>(p, X, k, s);  // back to the interleaved convention
+    SBDGB_CUDA(cudaMemcpyAsync(Xout, X, sizeof(double) * N * k, cudaMemcpyDeviceToHost, s));
+  }
   SBDGB_CUDA(cudaStreamSynchronize(s));
   r.seconds = std::chrono::duration<double>(clock::now() - t0).count();
   if (rep) *rep = r;
@@ -1395,7 +1626,7 @@ void lanczos_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X
     for (int ib = 0; ib < nb; ++ib) {
       ++n;
       double *Cb = Cv + (size_t)ib * N;
-      sigma_fp64(p, Cb, HC, 1, s);
+      sigma_fp64(p, Cb, HC, 1, s, true);
       r.sigma_calls++;
       r.sigma_fp64++;
       r.iterations++;
@@ -1442,7 +1673,10 @@ void lanczos_fp64(Problem &p, const sbdgb_davidson_opts &o, double *E, double *X
   r.converged = stop ? 1 : 0;
   r.resid[0] = change;
   E[0] = E0;
-  if (Xout) SBDGB_CUDA(cudaMemcpyAsync(Xout, W, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+  if (Xout) {
+    apply_eta<double>(p, W, 1, s);  // back to the interleaved convention
+    SBDGB_CUDA(cudaMemcpyAsync(Xout, W, sizeof(double) * N, cudaMemcpyDeviceToHost, s));
+  }
   SBDGB_CUDA(cudaStreamSynchronize(s));
   r.seconds = std::chrono::duration<double>(clock::now() - t0).count();
   if (rep) *rep = r;

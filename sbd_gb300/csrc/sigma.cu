@@ -52,12 +52,12 @@ constexpr int kThreads = 128;
 // added here too, reading row ia of C directly (per-thread pair lists, no
 // transposed copy); for sparse beta lists this replaces the transpose and the
 // beta sweep.
-template <int TA, int CPT, typename T, typename Wd, bool kFused>
+template <int TA, int CPT, typename T, typename Wd, bool kFused, bool kB>
 __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
   constexpr int TB = kThreads * CPT;
-  const uint32_t tile = __ldg(a.tile_order + blockIdx.x);
-  const uint32_t ia0 = __ldg(a.tile_start + tile);
-  const uint32_t rend = __ldg(a.tile_start + tile + 1) - ia0;  // <= TA
+  const uint32_t tile = ldg(a.tile_order + blockIdx.x);
+  const uint32_t ia0 = ldg(a.tile_start + tile);
+  const uint32_t rend = ldg(a.tile_start + tile + 1) - ia0;  // <= TA
   const uint32_t ib0 = blockIdx.y * TB;
   uint32_t col[CPT], q0[CPT], q1[CPT];
   bool ok[CPT];
@@ -67,15 +67,15 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
     col[c] = ib0 + threadIdx.x + kThreads * c;
     ok[c] = col[c] < a.nb;
     beta[c] = ok[c] ? word<Wd>(a.bstr, col[c]) : Wd(0);
-    q0[c] = ok[c] ? __ldg(a.B.off_s + col[c]) : 0u;
-    q1[c] = ok[c] ? __ldg(a.B.off_s + col[c] + 1) : 0u;
+    q0[c] = ok[c] ? ldg(a.B.off_s + col[c]) : 0u;
+    q1[c] = ok[c] ? ldg(a.B.off_s + col[c] + 1) : 0u;
   }
   uint32_t d0[kFused ? CPT : 1], d1[kFused ? CPT : 1];
   if constexpr (kFused) {
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
-      d0[c] = ok[c] ? __ldg(a.B.off_d + col[c]) : 0u;
-      d1[c] = ok[c] ? __ldg(a.B.off_d + col[c] + 1) : 0u;
+      d0[c] = ok[c] ? ldg(a.B.off_d + col[c]) : 0u;
+      d1[c] = ok[c] ? ldg(a.B.off_d + col[c] + 1) : 0u;
     }
   }
 #pragma unroll 1
@@ -89,19 +89,23 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
       const size_t k = (size_t)ia * a.nb + col[c];
       acc_zero(acc[c]);
       if (ok[c]) {
-        if constexpr (std::is_same<T, double>::value)
-          acc[c] = (__ldg(a.hii + k) - a.shift) * __ldg(a.C + k);
-        else
-          acc[c] = ff_diag(__ldg(a.hii_hi + k), __ldg(a.hii_lo + k), a.shift_hi, a.shift_lo, __ldg(a.C + k));
+        if constexpr (std::is_same<T, double>::value) {
+          acc[c] = ldg(a.hii + k) * ldg(a.C + k);  // the FP64 form has no shift: one FP64 op
+        } else if constexpr (std::is_same<T, float>::value) {
+          const dfloat h = ldg(a.hii_df + k);
+          acc[c] = ff_diag(h.hi, h.lo, a.shift_df.hi, a.shift_df.lo, ldg(a.C + k));
+        } else {
+          acc[c] = (ldg(a.hii_df + k) - a.shift_df) * ldg(a.C + k);
+        }
       }
     }
     // alpha singles and doubles (task type 2, mult.h:450-488)
-    same_spin_row<CPT, T, Wd>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, a.C, a.nb, ia, col, ok, beta, acc);
+    same_spin_row<CPT, T, Wd, kB>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, a.C, a.nb, ia, col, ok, beta, acc);
     // alpha single x beta single (task type 0, mult.h:527-557)
     T part[CPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) part[c] = T(0);
-    const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
+    const uint32_t p0 = ldg(a.A.off_s + ia), p1 = ldg(a.A.off_s + ia + 1);
     // the beta singles of each column outside (their table entries are read
     // once per thread), the alpha singles of the row inside (the same entries
     // for every thread: broadcast loads): a term costs two scattered loads
@@ -109,16 +113,16 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       for (uint32_t q = q0[c]; q < q1[c]; ++q) {
-        const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-        const Wd mb = word<Wd>(a.B.mask_s, q);
+        const uint32_t jb = ldg(a.B.ket_s + q), cb = ldg(a.B.code_s + q);
+        const Wd mb = mask_of<kB, Wd>(a.B.mask_s, q);
         const uint32_t kb = (cb >> 16) & 0x7fffu, sb = cb >> 31;
         for (uint32_t p = p0; p < p1; ++p) {
-          const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
+          const uint32_t ja = ldg(a.A.ket_s + p), ca = ldg(a.A.code_s + p);
           const uint32_t ph =
-              (parity(beta[c] & word<Wd>(a.A.mask_s, p)) ^ parity(word<Wd>(a.astr, ja) & mb) ^ (ca >> 31) ^ sb) &
+              (par<kB>(beta[c] & mask_of<kB, Wd>(a.A.mask_s, p)) ^ par<kB>(word<Wd>(a.astr, ja) & mb) ^ (ca >> 31) ^ sb) &
               1u;
-          madd(acc[c], part[c], flip(__ldg(a.Kp + ((ca >> 16) & 0x7fffu) * a.npair + kb), ph),
-               __ldg(a.C + (size_t)ja * a.nb + jb));
+          madd(acc[c], part[c], flip(ldg(a.Kp + ((ca >> 16) & 0x7fffu) * a.npair + kb), ph),
+               ldg(a.C + (size_t)ja * a.nb + jb));
         }
       }
     }
@@ -129,15 +133,15 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
 #pragma unroll
       for (int c = 0; c < CPT; ++c) {
         for (uint32_t q = q0[c]; q < q1[c]; ++q) {
-          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-          const uint32_t ph = parity(arow & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31);
-          const T j = __ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia);
-          madd(acc[c], part[c], flip(__ldg(a.val_sb + q) + j, ph), __ldg(crow_a + jb));
+          const uint32_t jb = ldg(a.B.ket_s + q), cb = ldg(a.B.code_s + q);
+          const uint32_t ph = par<kB>(arow & mask_of<kB, Wd>(a.B.mask_s, q)) ^ (cb >> 31);
+          const T j = ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia);
+          madd(acc[c], part[c], flip(ldg(a.val_sb + q) + j, ph), ldg(crow_a + jb));
         }
         for (uint32_t q = d0[c]; q < d1[c]; ++q) {
-          const uint32_t jb = __ldg(a.B.ket_d + q);
-          madd(acc[c], part[c], flip(__ldg(a.val_db + q), parity(arow & word<Wd>(a.B.mask_d, q))),
-               __ldg(crow_a + jb));
+          const uint32_t jb = ldg(a.B.ket_d + q);
+          madd(acc[c], part[c], flip(ldg(a.val_db + q), par<kB>(arow & mask_of<kB, Wd>(a.B.mask_d, q))),
+               ldg(crow_a + jb));
         }
       }
     }
@@ -146,11 +150,12 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
       acc_add_part(acc[c], part[c]);
       if (ok[c]) {
         const size_t k = (size_t)ia * a.nb + col[c];
-        if (a.accumulate) acc_add_part(acc[c], a.S[k]);
-        if constexpr (std::is_same<T, double>::value)
-          a.S[k] = a.accumulate ? a.S[k] + acc[c] : acc[c];
-        else
+        if constexpr (std::is_same<T, float>::value) {
+          if (a.accumulate) ff_add(acc[c], a.S[k]);
           a.S[k] = ff_value(acc[c]);
+        } else {
+          a.S[k] = a.accumulate ? a.S[k] + acc[c] : acc[c];
+        }
       }
     }
   }
@@ -159,13 +164,13 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
 // beta singles and doubles (task type 1, mult.h:489-525) on the transposed
 // vector.  Row results are staged in shared memory; each thread then adds the
 // TA consecutive beta entries of its alpha rows into sigma.
-template <int TA, int CPT, typename T, typename Wd>
+template <int TA, int CPT, typename T, typename Wd, bool kB>
 __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
   constexpr int TB = kThreads * CPT;
   __shared__ AccT<T> tile[TA][TB];
-  const uint32_t t = __ldg(a.tile_order + blockIdx.x);
-  const uint32_t ib0 = __ldg(a.tile_start + t);
-  const uint32_t rend = __ldg(a.tile_start + t + 1) - ib0;  // <= TA
+  const uint32_t t = ldg(a.tile_order + blockIdx.x);
+  const uint32_t ib0 = ldg(a.tile_start + t);
+  const uint32_t rend = ldg(a.tile_start + t + 1) - ib0;  // <= TA
   const uint32_t ia0 = blockIdx.y * TB;
   uint32_t col[CPT];
   bool ok[CPT];
@@ -181,7 +186,7 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
     AccT<T> acc[CPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) acc_zero(acc[c]);
-    same_spin_row<CPT, T, Wd>(a.B, a.val_sb, a.val_db, a.Ja, a.na, a.CT, a.na, ib0 + r, col, ok, alpha, acc);
+    same_spin_row<CPT, T, Wd, kB>(a.B, a.val_sb, a.val_db, a.Ja, a.na, a.CT, a.na, ib0 + r, col, ok, alpha, acc);
 #pragma unroll
     for (int c = 0; c < CPT; ++c) tile[r][threadIdx.x + kThreads * c] = acc[c];
   }
@@ -192,11 +197,11 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
       T *srow = a.S + (size_t)col[c] * a.nb + ib0;
       for (uint32_t r = 0; r < rend; ++r) {
         AccT<T> t = tile[r][threadIdx.x + kThreads * c];
-        if constexpr (std::is_same<T, double>::value) {
-          srow[r] = srow[r] + t;
-        } else {
+        if constexpr (std::is_same<T, float>::value) {
           ff_add(t, srow[r]);
           srow[r] = ff_value(t);
+        } else {
+          srow[r] = srow[r] + t;
         }
       }
     }
@@ -222,18 +227,25 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
 // element, no FP64 instruction.
 template <int VW, typename T>
 __device__ __forceinline__ void load_v(const T *__restrict__ p, T (&x)[VW]) {
+  static_assert(VW == 1 || sizeof(T) * VW == 8 || sizeof(T) * VW == 16 || sizeof(T) * VW == 32,
+                "vector loads of 8, 16 or 32 bytes");
   if constexpr (VW == 1) {
-    x[0] = __ldg(p);
+    x[0] = ldg(p);
+  } else if constexpr (sizeof(T) * VW == 32) {  // the double-float diagonal of four FP32 columns
+    const uint4 u0 = ldg(reinterpret_cast<const uint4 *>(p)), u1 = ldg(reinterpret_cast<const uint4 *>(p) + 1);
+    memcpy(x, &u0, 16);
+    memcpy(reinterpret_cast<char *>(x) + 16, &u1, 16);
   } else if constexpr (sizeof(T) * VW == 16) {
-    const uint4 u = __ldg(reinterpret_cast<const uint4 *>(p));
+    const uint4 u = ldg(reinterpret_cast<const uint4 *>(p));
     memcpy(x, &u, 16);
   } else {
-    const uint2 u = __ldg(reinterpret_cast<const uint2 *>(p));
+    const uint2 u = ldg(reinterpret_cast<const uint2 *>(p));
     memcpy(x, &u, 8);
   }
 }
 template <int VW, typename T>
 __device__ __forceinline__ void store_v(T *__restrict__ p, const T (&x)[VW]) {
+  static_assert(VW == 1 || sizeof(T) * VW == 8 || sizeof(T) * VW == 16, "vector stores of 8 or 16 bytes");
   if constexpr (VW == 1) {
     *p = x[0];
   } else if constexpr (sizeof(T) * VW == 16) {
@@ -247,7 +259,7 @@ __device__ __forceinline__ void store_v(T *__restrict__ p, const T (&x)[VW]) {
   }
 }
 
-template <int RG, int VW, typename T, typename Wd>
+template <int RG, int VW, typename T, typename Wd, bool kB>
 __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint32_t nr, uint32_t c0,
                                             const Wd (&beta)[VW], const uint32_t (&q0)[VW],
                                             const uint32_t (&q1)[VW]) {
@@ -273,44 +285,48 @@ __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint
         double h[VW];
         load_v<VW>(a.hii + k, h);
 #pragma unroll
-        for (int v = 0; v < VW; ++v) acc[r][v] = (h[v] - a.shift) * x[v];
+        for (int v = 0; v < VW; ++v) acc[r][v] = h[v] * x[v];  // the FP64 form has no shift
       } else {
-        float hh[VW], hl[VW];
-        load_v<VW>(a.hii_hi + k, hh);
-        load_v<VW>(a.hii_lo + k, hl);
+        dfloat h[VW];
+        load_v<VW>(a.hii_df + k, h);
 #pragma unroll
-        for (int v = 0; v < VW; ++v) acc[r][v] = ff_diag(hh[v], hl[v], a.shift_hi, a.shift_lo, x[v]);
+        for (int v = 0; v < VW; ++v) {
+          if constexpr (std::is_same<T, float>::value)
+            acc[r][v] = ff_diag(h[v].hi, h[v].lo, a.shift_df.hi, a.shift_df.lo, x[v]);
+          else
+            acc[r][v] = (h[v] - a.shift_df) * x[v];
+        }
       }
     }
   }
   // beta singles and doubles of this thread's columns (task type 1)
 #pragma unroll
   for (int v = 0; v < VW; ++v) {
-    const uint32_t d0 = __ldg(a.B.off_d + c0 + v), d1 = __ldg(a.B.off_d + c0 + v + 1);
+    const uint32_t d0 = ldg(a.B.off_d + c0 + v), d1 = ldg(a.B.off_d + c0 + v + 1);
     for (uint32_t q = d0; q < d1; ++q) {
-      const uint32_t jb = __ldg(a.B.ket_d + q);
-      const T val = __ldg(a.val_db + q);
-      const Wd m = word<Wd>(a.B.mask_d, q);
+      const uint32_t jb = ldg(a.B.ket_d + q);
+      const T val = ldg(a.val_db + q);
+      const Wd m = mask_of<kB, Wd>(a.B.mask_d, q);
       T x[RG];
 #pragma unroll
-      for (int r = 0; r < RG; ++r) x[r] = (uint32_t)r < nr ? __ldg(a.C + (size_t)(ia0 + r) * a.nb + jb) : T(0);
+      for (int r = 0; r < RG; ++r) x[r] = (uint32_t)r < nr ? ldg(a.C + (size_t)(ia0 + r) * a.nb + jb) : T(0);
 #pragma unroll
-      for (int r = 0; r < RG; ++r) madd(acc[r][v], part[r][v], flip(val, parity(arow[r] & m)), x[r]);
+      for (int r = 0; r < RG; ++r) madd(acc[r][v], part[r][v], flip(val, par<kB>(arow[r] & m)), x[r]);
     }
     for (uint32_t q = q0[v]; q < q1[v]; ++q) {
-      const uint32_t jb = __ldg(a.B.ket_s + q), code = __ldg(a.B.code_s + q);
-      const T val = __ldg(a.val_sb + q);
-      const Wd m = word<Wd>(a.B.mask_s, q);
+      const uint32_t jb = ldg(a.B.ket_s + q), code = ldg(a.B.code_s + q);
+      const T val = ldg(a.val_sb + q);
+      const Wd m = mask_of<kB, Wd>(a.B.mask_s, q);
       const T *jrow = a.Ja + (size_t)((code >> 16) & 0x7fffu) * a.na + ia0;
       T x[RG], j[RG];
 #pragma unroll
       for (int r = 0; r < RG; ++r) {
-        x[r] = (uint32_t)r < nr ? __ldg(a.C + (size_t)(ia0 + r) * a.nb + jb) : T(0);
-        j[r] = (uint32_t)r < nr ? __ldg(jrow + r) : T(0);
+        x[r] = (uint32_t)r < nr ? ldg(a.C + (size_t)(ia0 + r) * a.nb + jb) : T(0);
+        j[r] = (uint32_t)r < nr ? ldg(jrow + r) : T(0);
       }
 #pragma unroll
       for (int r = 0; r < RG; ++r)
-        madd(acc[r][v], part[r][v], flip(val + j[r], parity(arow[r] & m) ^ (code >> 31)), x[r]);
+        madd(acc[r][v], part[r][v], flip(val + j[r], par<kB>(arow[r] & m) ^ (code >> 31)), x[r]);
     }
   }
   // alpha pairs of each row (task type 2) and alpha x beta pairs (type 0)
@@ -318,40 +334,40 @@ __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint
   for (int r = 0; r < RG; ++r) {
     if ((uint32_t)r >= nr) break;
     const uint32_t ia = ia0 + r;
-    const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
+    const uint32_t p0 = ldg(a.A.off_s + ia), p1 = ldg(a.A.off_s + ia + 1);
     for (uint32_t p = p0; p < p1; ++p) {
-      const uint32_t ja = __ldg(a.A.ket_s + p), code = __ldg(a.A.code_s + p);
-      const T val = __ldg(a.val_sa + p);
-      const Wd m = word<Wd>(a.A.mask_s, p);
+      const uint32_t ja = ldg(a.A.ket_s + p), code = ldg(a.A.code_s + p);
+      const T val = ldg(a.val_sa + p);
+      const Wd m = mask_of<kB, Wd>(a.A.mask_s, p);
       const uint32_t P = (code >> 16) & 0x7fffu;
       T x[VW], j[VW];
       load_v<VW>(a.C + (size_t)ja * a.nb + c0, x);
       load_v<VW>(a.Jb + (size_t)P * a.nb + c0, j);
 #pragma unroll
       for (int v = 0; v < VW; ++v)
-        madd(acc[r][v], part[r][v], flip(val + j[v], parity(beta[v] & m) ^ (code >> 31)), x[v]);
+        madd(acc[r][v], part[r][v], flip(val + j[v], par<kB>(beta[v] & m) ^ (code >> 31)), x[v]);
       // alpha x beta: this alpha single with every beta single of the column
       const Wd aket = word<Wd>(a.astr, ja);
       const T *krow = a.Kp + (size_t)P * a.npair;
 #pragma unroll
       for (int v = 0; v < VW; ++v)
         for (uint32_t q = q0[v]; q < q1[v]; ++q) {
-          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
+          const uint32_t jb = ldg(a.B.ket_s + q), cb = ldg(a.B.code_s + q);
           const uint32_t ph =
-              (parity(beta[v] & m) ^ parity(aket & word<Wd>(a.B.mask_s, q)) ^ (code >> 31) ^ (cb >> 31)) & 1u;
-          madd(acc[r][v], part[r][v], flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph),
-               __ldg(a.C + (size_t)ja * a.nb + jb));
+              (par<kB>(beta[v] & m) ^ par<kB>(aket & mask_of<kB, Wd>(a.B.mask_s, q)) ^ (code >> 31) ^ (cb >> 31)) & 1u;
+          madd(acc[r][v], part[r][v], flip(ldg(krow + ((cb >> 16) & 0x7fffu)), ph),
+               ldg(a.C + (size_t)ja * a.nb + jb));
         }
     }
-    const uint32_t e0 = __ldg(a.A.off_d + ia), e1 = __ldg(a.A.off_d + ia + 1);
+    const uint32_t e0 = ldg(a.A.off_d + ia), e1 = ldg(a.A.off_d + ia + 1);
     for (uint32_t p = e0; p < e1; ++p) {
-      const uint32_t ja = __ldg(a.A.ket_d + p);
-      const T val = __ldg(a.val_da + p);
-      const Wd m = word<Wd>(a.A.mask_d, p);
+      const uint32_t ja = ldg(a.A.ket_d + p);
+      const T val = ldg(a.val_da + p);
+      const Wd m = mask_of<kB, Wd>(a.A.mask_d, p);
       T x[VW];
       load_v<VW>(a.C + (size_t)ja * a.nb + c0, x);
 #pragma unroll
-      for (int v = 0; v < VW; ++v) madd(acc[r][v], part[r][v], flip(val, parity(beta[v] & m)), x[v]);
+      for (int v = 0; v < VW; ++v) madd(acc[r][v], part[r][v], flip(val, par<kB>(beta[v] & m)), x[v]);
     }
   }
   // write back
@@ -366,11 +382,11 @@ __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint
 #pragma unroll
       for (int v = 0; v < VW; ++v) {
         acc_add_part(acc[r][v], part[r][v]);
-        if constexpr (kF64) {
-          out[v] = old[v] + acc[r][v];
-        } else {
+        if constexpr (std::is_same<T, float>::value) {
           ff_add(acc[r][v], old[v]);
           out[v] = ff_value(acc[r][v]);
+        } else {
+          out[v] = old[v] + acc[r][v];
         }
       }
     } else {
@@ -384,14 +400,15 @@ __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint
   }
 }
 
-// One CTA: a row tile of at most TA rows, swept RG rows at a time (RG
-// accumulators per column in registers: 8 in FP64, 4 in the float-float form).
-template <int TA, int VW, typename T, typename Wd>
+// One CTA: a row tile of at most TA rows, swept RG = 4 rows at a time (RG
+// accumulators per column in registers; few registers keep enough warps
+// resident to cover the latency of the gathers).
+template <int TA, int VW, typename T, typename Wd, bool kB>
 __global__ void __launch_bounds__(kThreads) k_sigma_sparse(Args<T> a) {
-  constexpr int RG = std::is_same<T, double>::value ? 8 : 4;
-  const uint32_t tile = __ldg(a.tile_order + blockIdx.x);
-  const uint32_t ia0 = __ldg(a.tile_start + tile);
-  const uint32_t rend = __ldg(a.tile_start + tile + 1) - ia0;  // 1..TA
+  constexpr int RG = 4;
+  const uint32_t tile = ldg(a.tile_order + blockIdx.x);
+  const uint32_t ia0 = ldg(a.tile_start + tile);
+  const uint32_t rend = ldg(a.tile_start + tile + 1) - ia0;  // 1..TA
   const uint32_t c0 = blockIdx.y * (kThreads * VW) + threadIdx.x * VW;
   if (c0 >= a.nb) return;  // nb is a multiple of VW: a vector is wholly in or out
   Wd beta[VW];
@@ -399,12 +416,12 @@ __global__ void __launch_bounds__(kThreads) k_sigma_sparse(Args<T> a) {
 #pragma unroll
   for (int v = 0; v < VW; ++v) {
     beta[v] = word<Wd>(a.bstr, c0 + v);
-    q0[v] = __ldg(a.B.off_s + c0 + v);
-    q1[v] = __ldg(a.B.off_s + c0 + v + 1);
+    q0[v] = ldg(a.B.off_s + c0 + v);
+    q1[v] = ldg(a.B.off_s + c0 + v + 1);
   }
 #pragma unroll 1
   for (uint32_t g = 0; g < rend; g += RG)
-    sparse_rows<RG, VW, T, Wd>(a, ia0 + g, min((uint32_t)RG, rend - g), c0, beta, q0, q1);
+    sparse_rows<RG, VW, T, Wd, kB>(a, ia0 + g, min((uint32_t)RG, rend - g), c0, beta, q0, q1);
 }
 
 // out[c][r] = in[r][c] for an R x Cn row-major matrix.
@@ -428,14 +445,22 @@ __global__ void k_to_float(const double *__restrict__ x, float *__restrict__ y, 
     y[e] = (float)x[e];
 }
 
-// hi = fp32(x), lo = fp32(x - hi): the FP64 diagonal as two FP32 parts
-// (hi + lo carries 48 bits of it) for the mixed-form kernels.
-__global__ void k_split(const double *__restrict__ x, float *__restrict__ hi, float *__restrict__ lo, size_t n) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
-    const double v = x[e];
-    const float h = (float)v;
-    hi[e] = h;
-    lo[e] = (float)(v - (double)h);
+// y = double-float(x): hi = fp32(x), lo = fp32(x - hi) (hi + lo carries 48
+// bits of x), for the diagonal and tables of the FP32 and double-float kernels.
+__global__ void k_split(const double *__restrict__ x, dfloat *__restrict__ y, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x)
+    y[e] = dfloat(x[e]);
+}
+
+// x_v *= eta(ia, ib) for nvec vectors at stride N (the sign between the
+// interleaved and the block determinant of element ia * nb + ib).
+template <typename T>
+__global__ void k_eta(T *__restrict__ x, const uint64_t *__restrict__ astr, const uint64_t *__restrict__ bstr,
+                      uint32_t nb, uint32_t N, int nvec) {
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < N; e += gridDim.x * blockDim.x) {
+    const uint32_t ia = e / nb, ib = e - ia * nb;
+    if (eta_parity(ldg(astr + ia), ldg(bstr + ib)))
+      for (int v = 0; v < nvec; ++v) x[(size_t)v * N + e] = -x[(size_t)v * N + e];
   }
 }
 
@@ -449,84 +474,93 @@ inline bool needs_transpose(int shape_b) { return shape_b != kFusedShape && shap
 constexpr int kShapeTA[kNumShapes] = {8, 8, 8, 16};
 constexpr int kShapeCPT[kNumShapes] = {1, 2, 4, 2};
 
-template <typename T, int TA, int CPT, bool F>
+// Launchers: kB selects the block-ordering kernels (no opposite-spin
+// parities; no string words are read for phases, so one word width serves).
+template <typename T, int TA, int CPT, bool F, bool kB>
 void launch_a_shape(const Problem &p, Args<T> a, cudaStream_t s) {
   constexpr int TB = kThreads * CPT;
   constexpr int v = TA == 8 ? 0 : 1;
   a.tile_start = p.tile_start[0][v];
   a.tile_order = p.tile_order[0][v];
   dim3 g(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
-  if (p.norb <= 32)
-    k_sigma_alpha<TA, CPT, T, uint32_t, F><<<g, kThreads, 0, s>>>(a);
+  if (kB || p.norb <= 32)
+    k_sigma_alpha<TA, CPT, T, uint32_t, F, kB><<<g, kThreads, 0, s>>>(a);
   else
-    k_sigma_alpha<TA, CPT, T, unsigned long long, F><<<g, kThreads, 0, s>>>(a);
+    k_sigma_alpha<TA, CPT, T, unsigned long long, F, kB><<<g, kThreads, 0, s>>>(a);
 }
-template <typename T, int TA, int CPT>
+template <typename T, int TA, int CPT, bool kB>
 void launch_b_shape(const Problem &p, Args<T> a, cudaStream_t s) {
   constexpr int TB = kThreads * CPT;
   constexpr int v = TA == 8 ? 0 : 1;
   a.tile_start = p.tile_start[1][v];
   a.tile_order = p.tile_order[1][v];
   dim3 g(p.n_tiles[1][v], (p.na + TB - 1) / TB);
-  if (p.norb <= 32)
-    k_sigma_beta<TA, CPT, T, uint32_t><<<g, kThreads, 0, s>>>(a);
+  if (kB || p.norb <= 32)
+    k_sigma_beta<TA, CPT, T, uint32_t, kB><<<g, kThreads, 0, s>>>(a);
   else
-    k_sigma_beta<TA, CPT, T, unsigned long long><<<g, kThreads, 0, s>>>(a);
+    k_sigma_beta<TA, CPT, T, unsigned long long, kB><<<g, kThreads, 0, s>>>(a);
 }
 
-template <typename T, bool F = false>
+template <typename T, bool kB, bool F = false>
 void launch_a(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
   switch (shape) {
-    case 0: launch_a_shape<T, 8, 1, F>(p, a, s); break;
-    case 1: launch_a_shape<T, 8, 2, F>(p, a, s); break;
-    case 2: launch_a_shape<T, 8, 4, F>(p, a, s); break;
-    default: launch_a_shape<T, 16, 2, F>(p, a, s); break;
+    case 0: launch_a_shape<T, 8, 1, F, kB>(p, a, s); break;
+    case 1: launch_a_shape<T, 8, 2, F, kB>(p, a, s); break;
+    case 2: launch_a_shape<T, 8, 4, F, kB>(p, a, s); break;
+    default: launch_a_shape<T, 16, 2, F, kB>(p, a, s); break;
   }
 }
 inline bool aligned16(const void *x) { return ((uintptr_t)x & 15u) == 0; }
 
 // The single streaming kernel for sparse rows: TA = 8 (variant 0) or 16 rows
 // per tile; 16-byte vectors when the row length and the pointers allow.
-template <typename T, int TA, typename Wd>
+template <typename T, int TA, typename Wd, bool kB>
 void launch_sparse_ta(const Problem &p, Args<T> a, cudaStream_t s) {
   constexpr int v = TA == 8 ? 0 : 1;
   constexpr int VW = 16 / (int)sizeof(T);
   a.tile_start = p.tile_start[0][v];
   a.tile_order = p.tile_order[0][v];
   const bool vec = p.nb % VW == 0 && aligned16(a.C) && aligned16(a.S) && aligned16(a.Jb) &&
-                   (std::is_same<T, double>::value ? aligned16(a.hii) : aligned16(a.hii_hi) && aligned16(a.hii_lo));
+                   (std::is_same<T, double>::value ? aligned16(a.hii) : aligned16(a.hii_df));
   if (vec) {
     dim3 g(p.n_tiles[0][v], (p.nb + kThreads * VW - 1) / (kThreads * VW));
-    k_sigma_sparse<TA, VW, T, Wd><<<g, kThreads, 0, s>>>(a);
+    k_sigma_sparse<TA, VW, T, Wd, kB><<<g, kThreads, 0, s>>>(a);
   } else {
     dim3 g(p.n_tiles[0][v], (p.nb + kThreads - 1) / kThreads);
-    k_sigma_sparse<TA, 1, T, Wd><<<g, kThreads, 0, s>>>(a);
+    k_sigma_sparse<TA, 1, T, Wd, kB><<<g, kThreads, 0, s>>>(a);
   }
 }
-template <typename T>
+template <typename T, bool kB>
 void launch_sparse(const Problem &p, const Args<T> &a, int variant, cudaStream_t s) {
-  if (p.norb <= 32) {
-    if (variant == 0) launch_sparse_ta<T, 8, uint32_t>(p, a, s);
-    else launch_sparse_ta<T, 16, uint32_t>(p, a, s);
+  if (kB || p.norb <= 32) {
+    if (variant == 0) launch_sparse_ta<T, 8, uint32_t, kB>(p, a, s);
+    else launch_sparse_ta<T, 16, uint32_t, kB>(p, a, s);
   } else {
-    if (variant == 0) launch_sparse_ta<T, 8, unsigned long long>(p, a, s);
-    else launch_sparse_ta<T, 16, unsigned long long>(p, a, s);
+    if (variant == 0) launch_sparse_ta<T, 8, unsigned long long, kB>(p, a, s);
+    else launch_sparse_ta<T, 16, unsigned long long, kB>(p, a, s);
   }
 }
 
 // The fused single-kernel product (no transposed copy), in shape `shape`.
-template <typename T>
+template <typename T, bool kB>
 void launch_fused(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
-  launch_a<T, true>(p, a, shape, s);
+  launch_a<T, kB, true>(p, a, shape, s);
 }
-template <typename T>
+template <typename T, bool kB>
 void launch_b(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
   switch (shape) {
-    case 0: launch_b_shape<T, 8, 1>(p, a, s); break;
-    case 1: launch_b_shape<T, 8, 2>(p, a, s); break;
-    case 2: launch_b_shape<T, 8, 4>(p, a, s); break;
-    default: launch_b_shape<T, 16, 2>(p, a, s); break;
+    case 0: launch_b_shape<T, 8, 1, kB>(p, a, s); break;
+    case 1: launch_b_shape<T, 8, 2, kB>(p, a, s); break;
+    case 2: launch_b_shape<T, 8, 4, kB>(p, a, s); break;
+    default: launch_b_shape<T, 16, 2, kB>(p, a, s); break;
   }
+}
+
+// Tuning slot of a kernel family: precision (0 FP64, 1 FP32, 2 double-float)
+// in the interleaved (0..2) or block (3..5) ordering.
+template <typename T, bool kB>
+constexpr int slot_of() {
+  return prec_of<T>() + (kB ? 3 : 0);
 }
 
 template <typename T>
@@ -534,9 +568,9 @@ void transpose(Problem &p, const T *in, T *out, uint32_t R, uint32_t Cn, cudaStr
 
 // Times every tile shape of both kernels once (after one untimed run) on the
 // problem's own vectors, writing into scratch, and keeps the fastest.
-template <typename T>
+template <typename T, bool kB>
 void autotune(Problem &p, Args<T> a, cudaStream_t s) {
-  const int prec = std::is_same<T, double>::value ? 0 : 1;
+  const int prec = slot_of<T, kB>();
   if (p.tune_a[prec] >= 0 && p.tune_b[prec] >= 0) return;
   const std::array<uint64_t, 6> key{(uint64_t)prec, (uint64_t)p.norb, p.na, p.nb, p.A.ns + p.A.nd, p.B.ns + p.B.nd};
   const auto hit = p.ctx->tuned.find(key);
@@ -558,9 +592,9 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
       for (int rep = 0; rep < 2; ++rep) {
         SBDGB_CUDA(cudaEventRecord(e0, s));
         if (kern == 0)
-          launch_a<T>(p, a, sh, s);
+          launch_a<T, kB>(p, a, sh, s);
         else
-          launch_b<T>(p, a, sh, s);
+          launch_b<T, kB>(p, a, sh, s);
         SBDGB_CUDA(cudaEventRecord(e1, s));
         count_launch(p.ctx);
       }
@@ -589,7 +623,7 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
   for (int sh = 0; sh < kNumShapes; ++sh) {
     for (int rep = 0; rep < 2; ++rep) {
       SBDGB_CUDA(cudaEventRecord(e0, s));
-      launch_fused<T>(p, a, sh, s);
+      launch_fused<T, kB>(p, a, sh, s);
       SBDGB_CUDA(cudaEventRecord(e1, s));
       count_launch(p.ctx);
     }
@@ -609,7 +643,7 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
   for (int sh = 0; sh < kNumSparse; ++sh) {
     for (int rep = 0; rep < 2; ++rep) {
       SBDGB_CUDA(cudaEventRecord(e0, s));
-      launch_sparse<T>(p, a, sh, s);
+      launch_sparse<T, kB>(p, a, sh, s);
       SBDGB_CUDA(cudaEventRecord(e1, s));
       count_launch(p.ctx);
     }
@@ -651,9 +685,9 @@ inline double nnz_per_row(const Problem &p) {
   return (p.na ? (double)(p.A.ns + p.A.nd) / p.na : 0.0) + (p.nb ? (double)(p.B.ns + p.B.nd) / p.nb : 0.0) + sa * sb;
 }
 
-template <typename T>
+template <typename T, bool kB>
 bool needs_tuning(Problem &p) {
-  const int prec = std::is_same<T, double>::value ? 0 : 1;
+  const int prec = slot_of<T, kB>();
   if (p.tune_a[prec] >= 0 && p.tune_b[prec] >= 0) return false;
   if (p.ctx->autotune) return true;
   if (nnz_per_row(p) <= 8.0) {
@@ -666,24 +700,24 @@ bool needs_tuning(Problem &p) {
   return false;
 }
 
-template <typename T>
+template <typename T, bool kB>
 void launch(Problem &p, const Args<T> &a, cudaStream_t s) {
-  const int prec = std::is_same<T, double>::value ? 0 : 1;
-  if (p.tune_a[prec] < 0 || p.tune_b[prec] < 0) autotune<T>(p, a, s);
+  const int prec = slot_of<T, kB>();
+  if (p.tune_a[prec] < 0 || p.tune_b[prec] < 0) autotune<T, kB>(p, a, s);
   if (p.tune_b[prec] == kSparseShape) {
-    launch_sparse<T>(p, a, p.tune_a[prec], s);
+    launch_sparse<T, kB>(p, a, p.tune_a[prec], s);
     count_launch(p.ctx, 1);
     SBDGB_CUDA(cudaGetLastError());
     return;
   }
   if (p.tune_b[prec] == kFusedShape) {
-    launch_fused<T>(p, a, p.tune_a[prec], s);
+    launch_fused<T, kB>(p, a, p.tune_a[prec], s);
     count_launch(p.ctx, 1);
     SBDGB_CUDA(cudaGetLastError());
     return;
   }
-  launch_a<T>(p, a, p.tune_a[prec], s);
-  launch_b<T>(p, a, p.tune_b[prec], s);
+  launch_a<T, kB>(p, a, p.tune_a[prec], s);
+  launch_b<T, kB>(p, a, p.tune_b[prec], s);
   count_launch(p.ctx, 2);
   SBDGB_CUDA(cudaGetLastError());
 }
@@ -705,7 +739,7 @@ struct ArgsMV {
   float *Sv[kMaxNV];
 };
 
-template <int CPT, int NV, typename Wd>
+template <int CPT, int NV, typename Wd, bool kB>
 __device__ __forceinline__ void same_spin_row_mv(const SpinTables &Tb, const float *__restrict__ vs,
                                                  const float *__restrict__ vd, const float *__restrict__ Jo,
                                                  uint32_t ldj, const float *const (&In)[kMaxNV], uint32_t ldin,
@@ -716,22 +750,22 @@ __device__ __forceinline__ void same_spin_row_mv(const SpinTables &Tb, const flo
   for (int n = 0; n < NV; ++n)
 #pragma unroll
     for (int c = 0; c < CPT; ++c) part[n][c] = 0.f;
-  const uint32_t p0 = __ldg(Tb.off_s + row), p1 = __ldg(Tb.off_s + row + 1);
+  const uint32_t p0 = ldg(Tb.off_s + row), p1 = ldg(Tb.off_s + row + 1);
   for (uint32_t p = p0; p < p1; ++p) {
-    const uint32_t ket = __ldg(Tb.ket_s + p), code = __ldg(Tb.code_s + p);
-    const float v = __ldg(vs + p);
-    const Wd m = word<Wd>(Tb.mask_s, p);
+    const uint32_t ket = ldg(Tb.ket_s + p), code = ldg(Tb.code_s + p);
+    const float v = ldg(vs + p);
+    const Wd m = mask_of<kB, Wd>(Tb.mask_s, p);
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
       if (ok[c]) {
         const uint32_t off = ket * ldin + col[c];
-        const float sv = flip(v + __ldg(Jo + (((code >> 16) & 0x7fffu) * ldj + col[c])),
-                              parity(opp[c] & m) ^ (code >> 31));
+        const float sv = flip(v + ldg(Jo + (((code >> 16) & 0x7fffu) * ldj + col[c])),
+                              par<kB>(opp[c] & m) ^ (code >> 31));
 #pragma unroll
-        for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, __ldg(In[n] + off), part[n][c]);
+        for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, ldg(In[n] + off), part[n][c]);
       }
   }
-  const uint32_t d0 = __ldg(Tb.off_d + row), d1 = __ldg(Tb.off_d + row + 1);
+  const uint32_t d0 = ldg(Tb.off_d + row), d1 = ldg(Tb.off_d + row + 1);
   uint32_t p = d0;
   for (; p + 2 <= d1; p += 2) {
     uint32_t ket[2];
@@ -739,9 +773,9 @@ __device__ __forceinline__ void same_spin_row_mv(const SpinTables &Tb, const flo
     Wd m[2];
 #pragma unroll
     for (int u = 0; u < 2; ++u) {
-      ket[u] = __ldg(Tb.ket_d + p + u);
-      v[u] = __ldg(vd + p + u);
-      m[u] = word<Wd>(Tb.mask_d, p + u);
+      ket[u] = ldg(Tb.ket_d + p + u);
+      v[u] = ldg(vd + p + u);
+      m[u] = mask_of<kB, Wd>(Tb.mask_d, p + u);
     }
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
@@ -750,25 +784,25 @@ __device__ __forceinline__ void same_spin_row_mv(const SpinTables &Tb, const flo
 #pragma unroll
         for (int u = 0; u < 2; ++u)
 #pragma unroll
-          for (int n = 0; n < NV; ++n) x[u][n] = __ldg(In[n] + (ket[u] * ldin + col[c]));
+          for (int n = 0; n < NV; ++n) x[u][n] = ldg(In[n] + (ket[u] * ldin + col[c]));
 #pragma unroll
         for (int u = 0; u < 2; ++u) {
-          const float sv = flip(v[u], parity(opp[c] & m[u]));
+          const float sv = flip(v[u], par<kB>(opp[c] & m[u]));
 #pragma unroll
           for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, x[u][n], part[n][c]);
         }
       }
   }
   if (p < d1) {
-    const uint32_t ket = __ldg(Tb.ket_d + p);
-    const float v = __ldg(vd + p);
-    const Wd m = word<Wd>(Tb.mask_d, p);
+    const uint32_t ket = ldg(Tb.ket_d + p);
+    const float v = ldg(vd + p);
+    const Wd m = mask_of<kB, Wd>(Tb.mask_d, p);
 #pragma unroll
     for (int c = 0; c < CPT; ++c)
       if (ok[c]) {
-        const float sv = flip(v, parity(opp[c] & m));
+        const float sv = flip(v, par<kB>(opp[c] & m));
 #pragma unroll
-        for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, __ldg(In[n] + (ket * ldin + col[c])), part[n][c]);
+        for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, ldg(In[n] + (ket * ldin + col[c])), part[n][c]);
       }
   }
 #pragma unroll
@@ -777,13 +811,13 @@ __device__ __forceinline__ void same_spin_row_mv(const SpinTables &Tb, const flo
     for (int c = 0; c < CPT; ++c) ff_add(acc[n][c], part[n][c]);
 }
 
-template <int TA, int CPT, int NV, typename Wd, bool kFused>
+template <int TA, int CPT, int NV, typename Wd, bool kFused, bool kB>
 __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
   const Args<float> &a = m.a;
   constexpr int TB = kThreads * CPT;
-  const uint32_t tile = __ldg(a.tile_order + blockIdx.x);
-  const uint32_t ia0 = __ldg(a.tile_start + tile);
-  const uint32_t rend = __ldg(a.tile_start + tile + 1) - ia0;
+  const uint32_t tile = ldg(a.tile_order + blockIdx.x);
+  const uint32_t ia0 = ldg(a.tile_start + tile);
+  const uint32_t rend = ldg(a.tile_start + tile + 1) - ia0;
   const uint32_t ib0 = blockIdx.y * TB;
   uint32_t col[CPT], q0[CPT], q1[CPT], d0[CPT], d1[CPT];
   bool ok[CPT];
@@ -793,10 +827,10 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
     col[c] = ib0 + threadIdx.x + kThreads * c;
     ok[c] = col[c] < a.nb;
     beta[c] = ok[c] ? word<Wd>(a.bstr, col[c]) : Wd(0);
-    q0[c] = ok[c] ? __ldg(a.B.off_s + col[c]) : 0u;
-    q1[c] = ok[c] ? __ldg(a.B.off_s + col[c] + 1) : 0u;
-    d0[c] = (kFused && ok[c]) ? __ldg(a.B.off_d + col[c]) : 0u;
-    d1[c] = (kFused && ok[c]) ? __ldg(a.B.off_d + col[c] + 1) : 0u;
+    q0[c] = ok[c] ? ldg(a.B.off_s + col[c]) : 0u;
+    q1[c] = ok[c] ? ldg(a.B.off_s + col[c] + 1) : 0u;
+    d0[c] = (kFused && ok[c]) ? ldg(a.B.off_d + col[c]) : 0u;
+    d1[c] = (kFused && ok[c]) ? ldg(a.B.off_d + col[c] + 1) : 0u;
   }
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
@@ -805,18 +839,19 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       const uint32_t k = ia * a.nb + col[c];
-      const float hh = ok[c] ? __ldg(a.hii_hi + k) : 0.f, hl = ok[c] ? __ldg(a.hii_lo + k) : 0.f;
+      const dfloat h = ok[c] ? ldg(a.hii_df + k) : dfloat(0.f, 0.f);
+      const float hh = h.hi, hl = h.lo;
 #pragma unroll
       for (int n = 0; n < NV; ++n)
-        acc[n][c] = ok[c] ? ff_diag(hh, hl, a.shift_hi, a.shift_lo, __ldg(m.Cv[n] + k)) : FF{0.f, 0.f};
+        acc[n][c] = ok[c] ? ff_diag(hh, hl, a.shift_df.hi, a.shift_df.lo, ldg(m.Cv[n] + k)) : FF{0.f, 0.f};
     }
-    same_spin_row_mv<CPT, NV, Wd>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, m.Cv, a.nb, ia, col, ok, beta, acc);
+    same_spin_row_mv<CPT, NV, Wd, kB>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, m.Cv, a.nb, ia, col, ok, beta, acc);
     float part[NV][CPT];
 #pragma unroll
     for (int n = 0; n < NV; ++n)
 #pragma unroll
       for (int c = 0; c < CPT; ++c) part[n][c] = 0.f;
-    const uint32_t p0 = __ldg(a.A.off_s + ia), p1 = __ldg(a.A.off_s + ia + 1);
+    const uint32_t p0 = ldg(a.A.off_s + ia), p1 = ldg(a.A.off_s + ia + 1);
     if constexpr (sizeof(Wd) == 8) {
       // 64-bit words: beta singles outside, alpha singles inside (as in
       // k_sigma_alpha); with 32-bit words the extra popcount per term costs
@@ -824,37 +859,37 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
 #pragma unroll
       for (int c = 0; c < CPT; ++c) {
         for (uint32_t q = q0[c]; q < q1[c]; ++q) {
-          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-          const Wd mb = word<Wd>(a.B.mask_s, q);
+          const uint32_t jb = ldg(a.B.ket_s + q), cb = ldg(a.B.code_s + q);
+          const Wd mb = mask_of<kB, Wd>(a.B.mask_s, q);
           const uint32_t kb = (cb >> 16) & 0x7fffu, sb = cb >> 31;
           for (uint32_t p = p0; p < p1; ++p) {
-            const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
+            const uint32_t ja = ldg(a.A.ket_s + p), ca = ldg(a.A.code_s + p);
             const uint32_t ph =
-                (parity(beta[c] & word<Wd>(a.A.mask_s, p)) ^ parity(word<Wd>(a.astr, ja) & mb) ^ (ca >> 31) ^ sb) &
+                (par<kB>(beta[c] & mask_of<kB, Wd>(a.A.mask_s, p)) ^ par<kB>(word<Wd>(a.astr, ja) & mb) ^ (ca >> 31) ^ sb) &
                 1u;
-            const float kv = flip(__ldg(a.Kp + ((ca >> 16) & 0x7fffu) * a.npair + kb), ph);
+            const float kv = flip(ldg(a.Kp + ((ca >> 16) & 0x7fffu) * a.npair + kb), ph);
             const uint32_t off = ja * a.nb + jb;
 #pragma unroll
-            for (int n = 0; n < NV; ++n) part[n][c] = fmaf(kv, __ldg(m.Cv[n] + off), part[n][c]);
+            for (int n = 0; n < NV; ++n) part[n][c] = fmaf(kv, ldg(m.Cv[n] + off), part[n][c]);
           }
         }
       }
     } else {
       for (uint32_t p = p0; p < p1; ++p) {
-        const uint32_t ja = __ldg(a.A.ket_s + p), ca = __ldg(a.A.code_s + p);
-        const Wd ma = word<Wd>(a.A.mask_s, p);
+        const uint32_t ja = ldg(a.A.ket_s + p), ca = ldg(a.A.code_s + p);
+        const Wd ma = mask_of<kB, Wd>(a.A.mask_s, p);
         const Wd alpha_ket = word<Wd>(a.astr, ja);
         const float *krow = a.Kp + (size_t)((ca >> 16) & 0x7fffu) * a.npair;
         const uint32_t rowoff = ja * a.nb;
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
-          const uint32_t pa = parity(beta[c] & ma) ^ (ca >> 31);
+          const uint32_t pa = par<kB>(beta[c] & ma) ^ (ca >> 31);
           for (uint32_t q = q0[c]; q < q1[c]; ++q) {
-            const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-            const uint32_t ph = (pa ^ parity(alpha_ket & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31)) & 1u;
-            const float kv = flip(__ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
+            const uint32_t jb = ldg(a.B.ket_s + q), cb = ldg(a.B.code_s + q);
+            const uint32_t ph = (pa ^ par<kB>(alpha_ket & mask_of<kB, Wd>(a.B.mask_s, q)) ^ (cb >> 31)) & 1u;
+            const float kv = flip(ldg(krow + ((cb >> 16) & 0x7fffu)), ph);
 #pragma unroll
-            for (int n = 0; n < NV; ++n) part[n][c] = fmaf(kv, __ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
+            for (int n = 0; n < NV; ++n) part[n][c] = fmaf(kv, ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
           }
         }
       }
@@ -865,17 +900,17 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
 #pragma unroll
       for (int c = 0; c < CPT; ++c) {
         for (uint32_t q = q0[c]; q < q1[c]; ++q) {
-          const uint32_t jb = __ldg(a.B.ket_s + q), cb = __ldg(a.B.code_s + q);
-          const uint32_t ph = parity(arow & word<Wd>(a.B.mask_s, q)) ^ (cb >> 31);
-          const float sv = flip(__ldg(a.val_sb + q) + __ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia), ph);
+          const uint32_t jb = ldg(a.B.ket_s + q), cb = ldg(a.B.code_s + q);
+          const uint32_t ph = par<kB>(arow & mask_of<kB, Wd>(a.B.mask_s, q)) ^ (cb >> 31);
+          const float sv = flip(ldg(a.val_sb + q) + ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia), ph);
 #pragma unroll
-          for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, __ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
+          for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
         }
         for (uint32_t q = d0[c]; q < d1[c]; ++q) {
-          const uint32_t jb = __ldg(a.B.ket_d + q);
-          const float sv = flip(__ldg(a.val_db + q), parity(arow & word<Wd>(a.B.mask_d, q)));
+          const uint32_t jb = ldg(a.B.ket_d + q);
+          const float sv = flip(ldg(a.val_db + q), par<kB>(arow & mask_of<kB, Wd>(a.B.mask_d, q)));
 #pragma unroll
-          for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, __ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
+          for (int n = 0; n < NV; ++n) part[n][c] = fmaf(sv, ldg(m.Cv[n] + (rowoff + jb)), part[n][c]);
         }
       }
     }
@@ -892,14 +927,14 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
   }
 }
 
-template <int TA, int CPT, int NV, typename Wd>
+template <int TA, int CPT, int NV, typename Wd, bool kB>
 __global__ void __launch_bounds__(kThreads) k_sigma_beta_mv(ArgsMV m) {
   const Args<float> &a = m.a;
   constexpr int TB = kThreads * CPT;
   extern __shared__ FF tile_mv[];  // [NV][TA][TB]
-  const uint32_t t = __ldg(a.tile_order + blockIdx.x);
-  const uint32_t ib0 = __ldg(a.tile_start + t);
-  const uint32_t rend = __ldg(a.tile_start + t + 1) - ib0;
+  const uint32_t t = ldg(a.tile_order + blockIdx.x);
+  const uint32_t ib0 = ldg(a.tile_start + t);
+  const uint32_t rend = ldg(a.tile_start + t + 1) - ib0;
   const uint32_t ia0 = blockIdx.y * TB;
   uint32_t col[CPT];
   bool ok[CPT];
@@ -917,7 +952,7 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta_mv(ArgsMV m) {
     for (int n = 0; n < NV; ++n)
 #pragma unroll
       for (int c = 0; c < CPT; ++c) acc[n][c] = FF{0.f, 0.f};
-    same_spin_row_mv<CPT, NV, Wd>(a.B, a.val_sb, a.val_db, a.Ja, a.na, m.CTv, a.na, ib0 + r, col, ok, alpha, acc);
+    same_spin_row_mv<CPT, NV, Wd, kB>(a.B, a.val_sb, a.val_db, a.Ja, a.na, m.CTv, a.na, ib0 + r, col, ok, alpha, acc);
 #pragma unroll
     for (int n = 0; n < NV; ++n)
 #pragma unroll
@@ -937,7 +972,7 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta_mv(ArgsMV m) {
       }
 }
 
-template <int TA, int CPT, int NV, bool F>
+template <int TA, int CPT, int NV, bool F, bool kB>
 void launch_a_mv_shape(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
   ArgsMV m = mv;
   constexpr int TB = kThreads * CPT;
@@ -945,12 +980,12 @@ void launch_a_mv_shape(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
   m.a.tile_start = p.tile_start[0][v];
   m.a.tile_order = p.tile_order[0][v];
   dim3 g(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
-  if (p.norb <= 32)
-    k_sigma_alpha_mv<TA, CPT, NV, uint32_t, F><<<g, kThreads, 0, s>>>(m);
+  if (kB || p.norb <= 32)
+    k_sigma_alpha_mv<TA, CPT, NV, uint32_t, F, kB><<<g, kThreads, 0, s>>>(m);
   else
-    k_sigma_alpha_mv<TA, CPT, NV, unsigned long long, F><<<g, kThreads, 0, s>>>(m);
+    k_sigma_alpha_mv<TA, CPT, NV, unsigned long long, F, kB><<<g, kThreads, 0, s>>>(m);
 }
-template <int TA, int CPT, int NV>
+template <int TA, int CPT, int NV, bool kB>
 void launch_b_mv_shape(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
   ArgsMV m = mv;
   constexpr int TB = kThreads * CPT;
@@ -959,32 +994,32 @@ void launch_b_mv_shape(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
   m.a.tile_order = p.tile_order[1][v];
   dim3 g(p.n_tiles[1][v], (p.na + TB - 1) / TB);
   const size_t smem = sizeof(FF) * NV * TA * TB;
-  if (p.norb <= 32) {
-    auto k = k_sigma_beta_mv<TA, CPT, NV, uint32_t>;
+  if (kB || p.norb <= 32) {
+    auto k = k_sigma_beta_mv<TA, CPT, NV, uint32_t, kB>;
     SBDGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k<<<g, kThreads, smem, s>>>(m);
   } else {
-    auto k = k_sigma_beta_mv<TA, CPT, NV, unsigned long long>;
+    auto k = k_sigma_beta_mv<TA, CPT, NV, unsigned long long, kB>;
     SBDGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k<<<g, kThreads, smem, s>>>(m);
   }
 }
-template <int NV, bool F>
+template <int NV, bool F, bool kB>
 void launch_a_mv(const Problem &p, const ArgsMV &m, int shape, cudaStream_t s) {
   switch (shape) {
-    case 0: launch_a_mv_shape<8, 1, NV, F>(p, m, s); break;
-    case 1: launch_a_mv_shape<8, 2, NV, F>(p, m, s); break;
-    case 2: launch_a_mv_shape<8, 4, NV, F>(p, m, s); break;
-    default: launch_a_mv_shape<16, 2, NV, F>(p, m, s); break;
+    case 0: launch_a_mv_shape<8, 1, NV, F, kB>(p, m, s); break;
+    case 1: launch_a_mv_shape<8, 2, NV, F, kB>(p, m, s); break;
+    case 2: launch_a_mv_shape<8, 4, NV, F, kB>(p, m, s); break;
+    default: launch_a_mv_shape<16, 2, NV, F, kB>(p, m, s); break;
   }
 }
-template <int NV>
+template <int NV, bool kB>
 void launch_b_mv(const Problem &p, const ArgsMV &m, int shape, cudaStream_t s) {
   switch (shape) {
-    case 0: launch_b_mv_shape<8, 1, NV>(p, m, s); break;
-    case 1: launch_b_mv_shape<8, 2, NV>(p, m, s); break;
-    case 2: launch_b_mv_shape<8, 4, NV>(p, m, s); break;
-    default: launch_b_mv_shape<16, 2, NV>(p, m, s); break;
+    case 0: launch_b_mv_shape<8, 1, NV, kB>(p, m, s); break;
+    case 1: launch_b_mv_shape<8, 2, NV, kB>(p, m, s); break;
+    case 2: launch_b_mv_shape<8, 4, NV, kB>(p, m, s); break;
+    default: launch_b_mv_shape<16, 2, NV, kB>(p, m, s); break;
   }
 }
 // Kernel B stages NV x TA x TB doubles; shapes whose staging would exceed
@@ -996,22 +1031,23 @@ int shape_b_mv(int tuned) {
   return fits(1) ? 1 : 0;
 }
 
-template <int NV>
+template <int NV, bool kB>
 void launch_mv(const Problem &p, const ArgsMV &m, cudaStream_t s) {
-  if (p.tune_b[1] == kSparseShape) {  // a stream per vector: nothing to share between vectors
+  constexpr int ts = slot_of<float, kB>();
+  if (p.tune_b[ts] == kSparseShape) {  // a stream per vector: nothing to share between vectors
     for (int n = 0; n < NV; ++n) {
       Args<float> a = m.a;
       a.C = m.Cv[n];
       a.S = m.Sv[n];
-      launch_sparse<float>(p, a, p.tune_a[1], s);
+      launch_sparse<float, kB>(p, a, p.tune_a[ts], s);
     }
     return;
   }
-  if (p.tune_b[1] == kFusedShape) {
-    launch_a_mv<NV, true>(p, m, p.tune_a[1], s);
+  if (p.tune_b[ts] == kFusedShape) {
+    launch_a_mv<NV, true, kB>(p, m, p.tune_a[ts], s);
   } else {
-    launch_a_mv<NV, false>(p, m, p.tune_a[1], s);
-    launch_b_mv<NV>(p, m, shape_b_mv<NV>(p.tune_b[1]), s);
+    launch_a_mv<NV, false, kB>(p, m, p.tune_a[ts], s);
+    launch_b_mv<NV, kB>(p, m, shape_b_mv<NV>(p.tune_b[ts]), s);
   }
 }
 
@@ -1026,6 +1062,13 @@ void to_float(Problem &p, const double *x, float *y, size_t n, cudaStream_t s) {
   if (n == 0) return;
   unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
   k_to_float<<<blocks, 256, 0, s>>>(x, y, n);
+  count_launch(p.ctx);
+}
+
+void to_df(Problem &p, const double *x, dfloat *y, size_t n, cudaStream_t s) {
+  if (n == 0) return;
+  unsigned blocks = (unsigned)std::min<size_t>((n + 255) / 256, 4096);
+  k_split<<<blocks, 256, 0, s>>>(x, y, n);
   count_launch(p.ctx);
 }
 
@@ -1050,9 +1093,8 @@ Args<T> base_args(Problem &p, const T *C, T *S, int accumulate) {
   a.na = p.na;
   a.nb = p.nb;
   a.hii = p.hii;
-  a.hii_hi = p.hii_hi;
-  a.hii_lo = p.hii_lo;
-  a.shift_hi = a.shift_lo = 0.f;
+  a.hii_df = p.hii_df;
+  a.shift_df = dfloat(0.f, 0.f);
   a.C = C;
   a.S = S;
   a.accumulate = accumulate;
@@ -1066,8 +1108,7 @@ Args<T> base_args(Problem &p, const T *C, T *S, int accumulate) {
 // The shift of a mixed-form product as FP32 hi + lo (FP64 kept for the FP64 kernels).
 void set_shift(Args<float> &a, double shift) {
   a.shift = shift;
-  a.shift_hi = (float)shift;
-  a.shift_lo = (float)(shift - (double)a.shift_hi);
+  a.shift_df = dfloat(shift);
 }
 
 // Rows [start[t], start[t+1]) of at most cap rows each, closed once their
@@ -1098,6 +1139,26 @@ void make_tiles(const std::vector<double> &work, int cap, std::vector<uint32_t> 
 }
 
 }  // namespace
+
+template <typename T>
+void apply_eta(Problem &p, T *x, int nvec, cudaStream_t s) {
+  if (p.N == 0 || nvec <= 0) return;
+  const unsigned blocks = (unsigned)std::min<uint64_t>((p.N + 255) / 256, 8192);
+  k_eta<T><<<blocks, 256, 0, s>>>(x, p.astr, p.bstr, p.nb, (uint32_t)p.N, nvec);
+  count_launch(p.ctx);
+  SBDGB_CUDA(cudaGetLastError());
+}
+template void apply_eta<double>(Problem &, double *, int, cudaStream_t);
+template void apply_eta<float>(Problem &, float *, int, cudaStream_t);
+template void apply_eta<dfloat>(Problem &, dfloat *, int, cudaStream_t);
+
+// hii as double-float, made once per problem (the FP32 kernels read its hi and
+// lo parts, the double-float kernels the pair).
+void split_hii(Problem &p, cudaStream_t s) {
+  if (p.hii_df) return;
+  p.hii_df = (dfloat *)dev_alloc(p, sizeof(dfloat) * (p.N ? p.N : 1));
+  to_df(p, p.hii, p.hii_df, p.N, s);
+}
 
 // Row tiles of both sigma kernels (alpha rows for kernel A, beta rows for
 // kernel B) for the row caps 8 and 16.  A row's work is its same-spin pair
@@ -1157,21 +1218,39 @@ void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, 
   a.Kp = p.Kp;
   const int sa = p.tune_a[0] >= 0 ? p.tune_a[0] : 1, sb = p.tune_b[0] >= 0 ? p.tune_b[0] : 1;
   if (sb == kSparseShape) {
-    launch_sparse<double>(p, a, sa, s);
+    launch_sparse<double, false>(p, a, sa, s);
     count_launch(p.ctx, 1);
   } else if (sb == kFusedShape) {
-    launch_fused<double>(p, a, sa, s);
+    launch_fused<double, false>(p, a, sa, s);
     count_launch(p.ctx, 1);
   } else {
     transpose<double>(p, C, CT, p.na, p.nb, s);
-    launch_a<double>(p, a, sa, s);
-    launch_b<double>(p, a, sb, s);
+    launch_a<double, false>(p, a, sa, s);
+    launch_b<double, false>(p, a, sb, s);
     count_launch(p.ctx, 2);
   }
   SBDGB_CUDA(cudaGetLastError());
 }
 
-void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s) {
+namespace {
+// One product with the problem's tuned shapes (tuning first if needed), timed
+// when the context records sigma timing; CT is the transpose scratch.
+template <typename T, bool kB>
+void run_sigma(Problem &p, const Args<T> &a, T *CT, cudaStream_t s) {
+  constexpr int ts = slot_of<T, kB>();
+  if (needs_tuning<T, kB>(p)) {
+    transpose<T>(p, a.C, CT, p.na, p.nb, s);
+    autotune<T, kB>(p, a, s);
+  }
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  begin_timing(p, s, ev0, ev1);
+  if (needs_transpose(p.tune_b[ts])) transpose<T>(p, a.C, CT, p.na, p.nb, s);
+  launch<T, kB>(p, a, s);
+  end_timing(p, s, ev0, ev1);
+}
+}  // namespace
+
+void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStream_t s, bool block) {
   if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "sigma needs tables and diagonal");
   if (!p.CT) p.CT = (double *)dev_alloc(p, sizeof(double) * p.N);
   if (p.N == 0) return;
@@ -1184,15 +1263,58 @@ void sigma_fp64(Problem &p, const double *C, double *S, int accumulate, cudaStre
   a.Jb = p.Jb;
   a.Ja = p.Ja;
   a.Kp = p.Kp;
-  if (needs_tuning<double>(p)) {
-    transpose<double>(p, C, p.CT, p.na, p.nb, s);
-    autotune<double>(p, a, s);
+  if (block)
+    run_sigma<double, true>(p, a, p.CT, s);
+  else
+    run_sigma<double, false>(p, a, p.CT, s);
+}
+
+// Double-float copies of the table values and integral tables, for the
+// double-float phase of the mixed form.
+void prepare_df(Problem &p, cudaStream_t s) {
+  if (p.df_ready) return;
+  if (!p.tables || !p.diag) throw Error(SBDGB_E_STATE, "double-float sigma needs tables and diagonal");
+  split_hii(p, s);
+  const size_t npp = (size_t)p.npair * p.npair;
+  p.Kpd = (dfloat *)dev_alloc(p, sizeof(dfloat) * npp);
+  p.Jbd = (dfloat *)dev_alloc(p, sizeof(dfloat) * (size_t)p.npair * p.nb);
+  p.Jad = (dfloat *)dev_alloc(p, sizeof(dfloat) * (size_t)p.npair * p.na);
+  to_df(p, p.Kp, p.Kpd, npp, s);
+  to_df(p, p.Jb, p.Jbd, (size_t)p.npair * p.nb, s);
+  to_df(p, p.Ja, p.Jad, (size_t)p.npair * p.na, s);
+  for (int sp = 0; sp < 2; ++sp) {
+    SpinTables &T = sp == 0 ? p.A : p.B;
+    p.val_sd[sp] = (dfloat *)dev_alloc(p, sizeof(dfloat) * (T.ns ? T.ns : 1));
+    p.val_dd[sp] = (dfloat *)dev_alloc(p, sizeof(dfloat) * (T.nd ? T.nd : 1));
+    to_df(p, T.val_s, p.val_sd[sp], T.ns, s);
+    to_df(p, T.val_d, p.val_dd[sp], T.nd, s);
   }
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  begin_timing(p, s, ev0, ev1);
-  if (needs_transpose(p.tune_b[0])) transpose<double>(p, C, p.CT, p.na, p.nb, s);
-  launch<double>(p, a, s);
-  end_timing(p, s, ev0, ev1);
+  SBDGB_CUDA(cudaGetLastError());
+  SBDGB_CUDA(cudaStreamSynchronize(s));
+  p.df_ready = true;
+}
+
+// (H - shift) C in double-float (or accumulated into S): the same kernels as
+// the FP64 form with double-float values, products and sums.
+void sigma_df(Problem &p, const dfloat *C, dfloat *S, int accumulate, cudaStream_t s, double shift, bool block) {
+  prepare_df(p, s);
+  if (!p.CT) p.CT = (double *)dev_alloc(p, sizeof(double) * p.N);  // the FP64 transpose scratch, same size
+  if (p.N == 0) return;
+  Args<dfloat> a = base_args<dfloat>(p, C, S, accumulate);
+  a.shift_df = dfloat(shift);
+  dfloat *CT = reinterpret_cast<dfloat *>(p.CT);
+  a.CT = CT;
+  a.val_sa = p.val_sd[0];
+  a.val_da = p.val_dd[0];
+  a.val_sb = p.val_sd[1];
+  a.val_db = p.val_dd[1];
+  a.Jb = p.Jbd;
+  a.Ja = p.Jad;
+  a.Kp = p.Kpd;
+  if (block)
+    run_sigma<dfloat, true>(p, a, CT, s);
+  else
+    run_sigma<dfloat, false>(p, a, CT, s);
 }
 
 // FP32 copies of the table values and integral tables used by the mixed form.
@@ -1206,13 +1328,7 @@ void prepare_mixed(Problem &p, cudaStream_t s) {
   to_float(p, p.Kp, p.Kpf, npp, s);
   to_float(p, p.Jb, p.Jbf, (size_t)p.npair * p.nb, s);
   to_float(p, p.Ja, p.Jaf, (size_t)p.npair * p.na, s);
-  p.hii_hi = (float *)dev_alloc(p, sizeof(float) * (p.N ? p.N : 1));
-  p.hii_lo = (float *)dev_alloc(p, sizeof(float) * (p.N ? p.N : 1));
-  if (p.N) {
-    const unsigned blocks = (unsigned)std::min<size_t>((p.N + 255) / 256, 4096);
-    k_split<<<blocks, 256, 0, s>>>(p.hii, p.hii_hi, p.hii_lo, p.N);
-    count_launch(p.ctx);
-  }
+  split_hii(p, s);
   for (int sp = 0; sp < 2; ++sp) {
     SpinTables &T = sp == 0 ? p.A : p.B;
     p.val_sf[sp] = (float *)dev_alloc(p, sizeof(float) * (T.ns ? T.ns : 1));
@@ -1225,10 +1341,8 @@ void prepare_mixed(Problem &p, cudaStream_t s) {
   p.mixed_ready = true;
 }
 
-void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double shift) {
-  prepare_mixed(p, s);
-  if (!p.CTf) p.CTf = (float *)dev_alloc(p, sizeof(float) * p.N);
-  if (p.N == 0) return;
+namespace {
+Args<float> mixed_args(Problem &p, const float *C, float *S, double shift) {
   Args<float> a = base_args<float>(p, C, S, 0);
   set_shift(a, shift);
   a.CT = p.CTf;
@@ -1239,40 +1353,29 @@ void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double sh
   a.Jb = p.Jbf;
   a.Ja = p.Jaf;
   a.Kp = p.Kpf;
-  if (needs_tuning<float>(p)) {
-    transpose<float>(p, C, p.CTf, p.na, p.nb, s);
-    autotune<float>(p, a, s);
-  }
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  begin_timing(p, s, ev0, ev1);
-  if (needs_transpose(p.tune_b[1])) transpose<float>(p, C, p.CTf, p.na, p.nb, s);
-  launch<float>(p, a, s);
-  end_timing(p, s, ev0, ev1);
+  return a;
+}
+}  // namespace
+
+void sigma_mixed(Problem &p, const float *C, float *S, cudaStream_t s, double shift, bool block) {
+  prepare_mixed(p, s);
+  if (!p.CTf) p.CTf = (float *)dev_alloc(p, sizeof(float) * p.N);
+  if (p.N == 0) return;
+  const Args<float> a = mixed_args(p, C, S, shift);
+  if (block)
+    run_sigma<float, true>(p, a, p.CTf, s);
+  else
+    run_sigma<float, false>(p, a, p.CTf, s);
 }
 
-// (H - shift) C_j for nvec FP32 vectors at once (nvec <= 4; vectors and
-// results at stride N), through the multi-vector kernels.
-void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStream_t s, double shift) {
-  if (nvec <= 0) return;
-  if (nvec == 1) {
-    sigma_mixed(p, C, S, s, shift);
-    return;
-  }
-  SBDGB_REQUIRE(nvec <= kMaxNV, SBDGB_E_UNSUPPORTED, "at most 4 vectors per multi-vector sigma");
-  prepare_mixed(p, s);
-  if (p.N == 0) return;
-  if (needs_tuning<float>(p)) sigma_mixed(p, C, S, s, shift);  // tunes the FP32 shapes on the first vector
+namespace {
+template <bool kB>
+void sigma_mixed_multi_impl(Problem &p, const float *C, float *S, int nvec, cudaStream_t s, double shift) {
+  constexpr int ts = slot_of<float, kB>();
+  if (needs_tuning<float, kB>(p)) sigma_mixed(p, C, S, s, shift, kB);  // tunes the FP32 shapes on the first vector
   ArgsMV m{};
-  m.a = base_args<float>(p, C, S, 0);
-  set_shift(m.a, shift);
-  m.a.val_sa = p.val_sf[0];
-  m.a.val_da = p.val_df[0];
-  m.a.val_sb = p.val_sf[1];
-  m.a.val_db = p.val_df[1];
-  m.a.Jb = p.Jbf;
-  m.a.Ja = p.Jaf;
-  m.a.Kp = p.Kpf;
-  const bool fused = !needs_transpose(p.tune_b[1]);
+  m.a = mixed_args(p, C, S, shift);
+  const bool fused = !needs_transpose(p.tune_b[ts]);
   float *CT = fused ? nullptr : (float *)workspace(p, WS_CTMV, sizeof(float) * p.N * (size_t)nvec);
   for (int n = 0; n < nvec; ++n) {
     m.Cv[n] = C + (size_t)n * p.N;
@@ -1283,13 +1386,32 @@ void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStrea
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   begin_timing(p, s, ev0, ev1);
   switch (nvec) {
-    case 2: launch_mv<2>(p, m, s); break;
-    case 3: launch_mv<3>(p, m, s); break;
-    default: launch_mv<4>(p, m, s); break;
+    case 2: launch_mv<2, kB>(p, m, s); break;
+    case 3: launch_mv<3, kB>(p, m, s); break;
+    default: launch_mv<4, kB>(p, m, s); break;
   }
   end_timing(p, s, ev0, ev1);
-  count_launch(p.ctx, p.tune_b[1] == kSparseShape ? nvec : fused ? 1 : 2);
+  count_launch(p.ctx, p.tune_b[ts] == kSparseShape ? nvec : fused ? 1 : 2);
   SBDGB_CUDA(cudaGetLastError());
+}
+}  // namespace
+
+// (H - shift) C_j for nvec FP32 vectors at once (nvec <= 4; vectors and
+// results at stride N), through the multi-vector kernels.
+void sigma_mixed_multi(Problem &p, const float *C, float *S, int nvec, cudaStream_t s, double shift, bool block) {
+  if (nvec <= 0) return;
+  if (nvec == 1) {
+    sigma_mixed(p, C, S, s, shift, block);
+    return;
+  }
+  SBDGB_REQUIRE(nvec <= kMaxNV, SBDGB_E_UNSUPPORTED, "at most 4 vectors per multi-vector sigma");
+  prepare_mixed(p, s);
+  if (!p.CTf) p.CTf = (float *)dev_alloc(p, sizeof(float) * p.N);
+  if (p.N == 0) return;
+  if (block)
+    sigma_mixed_multi_impl<true>(p, C, S, nvec, s, shift);
+  else
+    sigma_mixed_multi_impl<false>(p, C, S, nvec, s, shift);
 }
 
 }  // namespace sbdgb

@@ -24,7 +24,7 @@ SYMBOLS = [
     "sbdgb_abi_version", "sbdgb_ctx_create", "sbdgb_ctx_destroy", "sbdgb_last_error", "sbdgb_ctx_bytes_in_use",
     "sbdgb_ctx_launch_count", "sbdgb_ctx_set_stream", "sbdgb_ctx_enable_timing", "sbdgb_ctx_sigma_timing", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
     "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
-    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_mixed_block", "sbdgb_sigma_noalloc", "sbdgb_measure_fp64_rates", "sbdgb_occupation_density", "sbdgb_string_weights", "sbdgb_string_cut_counts", "sbdgb_rdm", "sbdgb_problem_tuning", "sbdgb_problem_tuning_times", "sbdgb_problem_set_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
+    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_df", "sbdgb_sigma_mixed_block", "sbdgb_sigma_noalloc", "sbdgb_occupation_density", "sbdgb_string_weights", "sbdgb_string_cut_counts", "sbdgb_rdm", "sbdgb_problem_tuning", "sbdgb_problem_tuning_times", "sbdgb_problem_set_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
     "sbdgb_davidson", "sbdgb_lanczos", "sbdgb_batch_davidson", "sbdgb_server_create", "sbdgb_server_submit", "sbdgb_server_poll", "sbdgb_server_wait",
     "sbdgb_server_stats", "sbdgb_server_last_error", "sbdgb_server_destroy",
 ]
@@ -114,8 +114,8 @@ def load(path: str = LIB_PATH):
     L.sbdgb_sigma.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_sigma_mixed.argtypes = [vp, vp, vp, vp]
     L.sbdgb_sigma_mixed_block.argtypes = [vp, vp, vp, C.c_int, vp]
+    L.sbdgb_sigma_df.argtypes = [vp, vp, vp, C.c_int, vp]
     L.sbdgb_sigma_noalloc.argtypes = [vp, vp, vp, C.c_int, vp]
-    L.sbdgb_measure_fp64_rates.argtypes = [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.sbdgb_occupation_density.argtypes = [vp, vp, _f64p, vp]
     L.sbdgb_string_weights.argtypes = [vp, vp, _f64p, _f64p, vp]
     L.sbdgb_rdm.argtypes = [vp, vp, _f64p, vp, vp]
@@ -214,15 +214,6 @@ def batch_davidson(engine: Engine, problems: list, nroots: int = 1, max_nb: int 
     engine.check(engine.lib.sbdgb_batch_davidson(engine.h, hs, n, C.byref(o), E, reps, xp))
     return [DavidsonResult(E[i * nroots:(i + 1) * nroots].copy(), xs[i] if xs else None, reps[i].as_dict(nroots))
             for i in range(n)]
-
-
-def measure_fp64_rates(device: int = 0) -> dict:
-    """Measured FP64 FMA-pipe and FP64 tensor-path rates of the device (TFLOP/s)."""
-    a, b = C.c_double(0.0), C.c_double(0.0)
-    rc = load().sbdgb_measure_fp64_rates(device, C.byref(a), C.byref(b))
-    if rc != SBDGB_OK:
-        raise SbdgbError(rc, "measure_fp64_rates")
-    return {"dfma_tflops": a.value, "dmma_tflops": b.value}
 
 
 def footprint(norb: int, na: int, nb: int, max_nb: int, nroots: int, precision: int = FP64) -> int:
@@ -351,6 +342,10 @@ class TPBProblem:
 
     def sigma_mixed_device(self, c_ptr: int, s_ptr: int, stream: int | None = None):
         self.engine.check(self.lib.sbdgb_sigma_mixed(self.h, c_ptr, s_ptr, self._stream_arg(stream)))
+
+    def sigma_df_device(self, c_ptr: int, s_ptr: int, accumulate: bool = False, stream: int | None = None):
+        """Double-float sigma on device vectors of N (hi, lo) FP32 pairs."""
+        self.engine.check(self.lib.sbdgb_sigma_df(self.h, c_ptr, s_ptr, int(accumulate), self._stream_arg(stream)))
 
     def sigma_mixed_block_device(self, c_ptr: int, s_ptr: int, nvec: int, stream: int | None = None):
         self.engine.check(self.lib.sbdgb_sigma_mixed_block(self.h, c_ptr, s_ptr, nvec, self._stream_arg(stream)))

@@ -175,8 +175,9 @@ def test_eight_roots_restart_basis_over_sixteen_columns(engine):
 
 
 def test_measured_fp64_rates():
-    """The rate probe runs and gives plausible FP64 rates (TFLOP/s)."""
-    from sbd_gb300.engine import measure_fp64_rates
+    """The bench's FP64 rate probe (its own library, not the engine's) runs and
+    gives plausible FP64 rates (TFLOP/s)."""
+    from bench import measure_fp64_rates
     r = measure_fp64_rates(0)
     assert 0.05 < r["dfma_tflops"] < 200.0 and 0.05 < r["dmma_tflops"] < 200.0
 

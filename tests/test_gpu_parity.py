@@ -154,3 +154,33 @@ def test_mixed_block_sigma_equals_single(gcase, shapes, nvec):
             assert torch.equal(Y[j], y), (j, shapes)
         else:
             assert max_rel(Y[j].double().cpu().numpy(), y.double().cpu().numpy()) <= 2e-6, (j, shapes)
+
+
+def _df(x):
+    """A float64 array as interleaved double-float pairs (hi, lo)."""
+    hi = x.astype(np.float32)
+    lo = (x - hi.astype(np.float64)).astype(np.float32)
+    return np.stack([hi, lo], axis=-1).ravel()
+
+
+@pytest.mark.parametrize("shapes", [None, (1, 1), (3, 4), (0, 5)])
+def test_double_float_sigma_matches_reference(gcase, shapes):
+    """The double-float sigma (48-bit values, FP32-pipe arithmetic) against the
+    reference sigma at 1e-12, in the autotuned shape and forced ones, in the
+    overwrite and accumulate forms."""
+    import torch
+    c, p = gcase
+    p.diag_terms()
+    if shapes is not None:
+        p.set_tuning(2, *shapes)
+    X = torch.tensor(_df(c.C), device="cuda")
+    Y = torch.zeros_like(X)
+    st = torch.cuda.current_stream().cuda_stream
+    p.sigma_df_device(X.data_ptr(), Y.data_ptr(), stream=st)
+    y = Y.double().cpu().numpy().reshape(-1, 2).sum(axis=1)
+    assert max_rel(y, c.sigma) <= 1e-12
+    base = np.random.default_rng(4).uniform(-1, 1, c.C.size)
+    Y = torch.tensor(_df(base), device="cuda")
+    p.sigma_df_device(X.data_ptr(), Y.data_ptr(), accumulate=True, stream=st)
+    y = Y.double().cpu().numpy().reshape(-1, 2).sum(axis=1)
+    assert max_rel(y, base + c.sigma) <= 1e-12

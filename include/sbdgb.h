@@ -160,6 +160,20 @@ int sbdgb_problem_tuning_times(const sbdgb_problem *p, int precision, float *ms_
  * choice (shape_a 0..3 with shape_b 0..4, or shape_a 0..1 with shape_b 5, as
  * above); results do not depend on it beyond the order of floating-point sums. */
 int sbdgb_problem_set_tuning(sbdgb_problem *p, int precision, int shape_a, int shape_b);
+/* Whether the alpha x beta single pairs of sigma (task type 0) run in a kernel
+ * of their own (split = 1: the tuned shapes skip them and a kernel that stages
+ * the rows of C and (P|Q) of each alpha row's singles in shared memory adds
+ * them; 0: inside the alpha sweep; -1: not decided yet), and the autotuner's
+ * time of one product without and with the split (ms[2], 0 where not
+ * measured; ms may be NULL).  The autotuner decides by timing; untimed
+ * contexts split when there are at least 4 such pairs per determinant and
+ * the staging fits in shared memory.  precision as above, + 3 for the
+ * solvers' block ordering (vectors multiplied by the sign between the
+ * interleaved and the block determinant).  No counterpart in the reference. */
+int sbdgb_problem_split(const sbdgb_problem *p, int precision, int *split, float *ms);
+/* Sets that choice (0 or 1) for one precision; 1 is refused with
+ * SBDGB_E_UNSUPPORTED when the staging does not fit in shared memory. */
+int sbdgb_problem_set_split(sbdgb_problem *p, int precision, int split);
 
 /* sigma that makes no device allocation.  No counterpart in the reference:
  * it is for callers that cannot call cudaMalloc once they run (a host

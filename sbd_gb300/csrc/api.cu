@@ -459,6 +459,30 @@ int sbdgb_problem_set_tuning(sbdgb_problem *pr, int precision, int shape_a, int 
   return SBDGB_OK;
 }
 
+int sbdgb_problem_split(const sbdgb_problem *pr, int precision, int *split, float *ms) {
+  if (!pr || precision < 0 || precision > 5) return SBDGB_E_INPUT;
+  if (split) *split = pr->p.split_ab[precision];
+  if (ms) {
+    ms[0] = pr->p.tune_ab_ms[precision][0];
+    ms[1] = pr->p.tune_ab_ms[precision][1];
+  }
+  return SBDGB_OK;
+}
+
+int sbdgb_problem_set_split(sbdgb_problem *pr, int precision, int split) {
+  if (!pr || precision < 0 || precision > 5 || split < 0 || split > 1) return SBDGB_E_INPUT;
+  return guarded(pr->p.ctx, [&] {
+    sbdgb::Problem &p = pr->p;
+    SBDGB_REQUIRE(p.tables, SBDGB_E_STATE, "build tables first");
+    const int prec = precision % 3;
+    const bool fits = prec == 0   ? sbdgb::ab_fits<double>(p)
+                      : prec == 1 ? sbdgb::ab_fits<float>(p)
+                                  : sbdgb::ab_fits<sbdgb::dfloat>(p);
+    SBDGB_REQUIRE(split == 0 || fits, SBDGB_E_UNSUPPORTED, "alpha x beta staging does not fit in shared memory");
+    p.split_ab[precision] = split;
+  });
+}
+
 int sbdgb_mult_host(sbdgb_problem *pr, const double *hii, const double *Wk, double *Wb) {
   if (!pr || !Wk || !Wb) return SBDGB_E_INPUT;
   return guarded(pr->p.ctx, [&] {

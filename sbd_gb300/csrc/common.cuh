@@ -154,6 +154,14 @@ struct Problem {
   // (0..2) and block (3..5) orderings
   int tune_a[6] = {-1, -1, -1, -1, -1, -1}, tune_b[6] = {-1, -1, -1, -1, -1, -1};
   float tune_ms[6][3][8] = {};  // timings the autotuner saw (A, B, fused + sparse)
+  // 1: the alpha x beta single pairs run in their own kernel (sigma_ab.cu)
+  // after the tuned shapes, which then skip them; -1 = not decided yet
+  int split_ab[6] = {-1, -1, -1, -1, -1, -1};
+  float tune_ab_ms[6][2] = {};  // the autotuner's time of the tuned shapes without and with the split
+  // alpha rows with at least one single (most singles first) and beta columns
+  // by decreasing single count: the work order of the alpha x beta kernel
+  uint32_t *ab_rows = nullptr, *ab_cols = nullptr;
+  uint32_t n_ab_rows = 0;
   size_t bytes = 0;
   std::vector<void *> allocs;
   // host copies of strings
@@ -182,8 +190,9 @@ struct Ctx {
   // beta table entries): a problem of a shape seen before on this context takes
   // the shapes the autotuner chose then instead of timing the candidates again.
   struct Tuned {
-    int a, b;
+    int a, b, split_ab;
     float ms[3][8];
+    float ab_ms[2];
   };
   std::map<std::array<uint64_t, 6>, Tuned> tuned;
 };
@@ -217,6 +226,10 @@ void export_tables(const Problem &p, int spin, uint64_t *off_s, uint64_t *ket_s,
 void build_diag(Problem &p, cudaStream_t s);
 // sigma.cu
 void build_row_tiles(Problem &p, cudaStream_t s);
+// sigma_ab.cu: whether the alpha x beta kernel's shared-memory staging (C
+// rows and (P|Q) rows of its element type T) fits this problem.
+template <typename T>
+bool ab_fits(const Problem &p);
 // block: the block-ordering product (H_block = eta H eta, no opposite-spin
 // parities) that the solvers use on eta-signed vectors; false: the
 // reference's interleaved convention.

@@ -112,6 +112,7 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
     // (the (P|Q) value and C) instead of five, and one more popcount
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
+      if (a.skip_ab) break;  // left to k_sigma_ab
       for (uint32_t q = q0[c]; q < q1[c]; ++q) {
         const uint32_t jb = ldg(a.B.ket_s + q), cb = ldg(a.B.code_s + q);
         const Wd mb = mask_of<kB, Wd>(a.B.mask_s, q);
@@ -347,6 +348,7 @@ __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint
       for (int v = 0; v < VW; ++v)
         madd(acc[r][v], part[r][v], flip(val + j[v], par<kB>(beta[v] & m) ^ (code >> 31)), x[v]);
       // alpha x beta: this alpha single with every beta single of the column
+      if (a.skip_ab) continue;  // left to k_sigma_ab
       const Wd aket = word<Wd>(a.astr, ja);
       const T *krow = a.Kp + (size_t)P * a.npair;
 #pragma unroll
@@ -556,6 +558,28 @@ void launch_b(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
   }
 }
 
+// One product in shapes (sa, sb) on a transposed copy already made when the
+// shapes need one; with split > 0 those kernels skip the alpha x beta single
+// pairs and k_sigma_ab adds them afterwards.
+template <typename T, bool kB>
+void launch_shapes(Problem &p, const Args<T> &a, int sa, int sb, int split, cudaStream_t s) {
+  Args<T> b = a;
+  b.skip_ab = split > 0 ? 1 : 0;
+  if (sb == kSparseShape) {
+    launch_sparse<T, kB>(p, b, sa, s);
+    count_launch(p.ctx, 1);
+  } else if (sb == kFusedShape) {
+    launch_fused<T, kB>(p, b, sa, s);
+    count_launch(p.ctx, 1);
+  } else {
+    launch_a<T, kB>(p, b, sa, s);
+    launch_b<T, kB>(p, b, sb, s);
+    count_launch(p.ctx, 2);
+  }
+  SBDGB_CUDA(cudaGetLastError());
+  if (split > 0) launch_ab<T>(p, a, kB, s);
+}
+
 // Tuning slot of a kernel family: precision (0 FP64, 1 FP32, 2 double-float)
 // in the interleaved (0..2) or block (3..5) ordering.
 template <typename T, bool kB>
@@ -577,7 +601,9 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
   if (hit != p.ctx->tuned.end()) {
     p.tune_a[prec] = hit->second.a;
     p.tune_b[prec] = hit->second.b;
+    p.split_ab[prec] = hit->second.split_ab;
     std::copy(&hit->second.ms[0][0], &hit->second.ms[0][0] + 3 * 8, &p.tune_ms[prec][0][0]);
+    std::copy(hit->second.ab_ms, hit->second.ab_ms + 2, p.tune_ab_ms[prec]);
     return;
   }
   a.S = (T *)workspace(p, WS_TUNE, sizeof(T) * p.N);
@@ -664,8 +690,27 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
     p.tune_a[prec] = best_fs;
     p.tune_b[prec] = kFusedShape;
   }
-  Ctx::Tuned t{p.tune_a[prec], p.tune_b[prec], {}};
+  // the alpha x beta single pairs in their own kernel, against inside the
+  // chosen shapes (each timed over two products, transposed copy included)
+  p.split_ab[prec] = 0;
+  if (ab_fits<T>(p)) {
+    for (int sp = 0; sp < 2; ++sp) {
+      SBDGB_CUDA(cudaEventRecord(e0, s));
+      for (int rep = 0; rep < 2; ++rep) {
+        if (needs_transpose(p.tune_b[prec])) transpose<T>(p, a.C, const_cast<T *>(a.CT), p.na, p.nb, s);
+        launch_shapes<T, kB>(p, a, p.tune_a[prec], p.tune_b[prec], sp, s);
+      }
+      SBDGB_CUDA(cudaEventRecord(e1, s));
+      SBDGB_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      SBDGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      p.tune_ab_ms[prec][sp] = 0.5f * ms;
+    }
+    p.split_ab[prec] = p.tune_ab_ms[prec][1] < p.tune_ab_ms[prec][0] ? 1 : 0;
+  }
+  Ctx::Tuned t{p.tune_a[prec], p.tune_b[prec], p.split_ab[prec], {}, {}};
   std::copy(&p.tune_ms[prec][0][0], &p.tune_ms[prec][0][0] + 3 * 8, &t.ms[0][0]);
+  std::copy(p.tune_ab_ms[prec], p.tune_ab_ms[prec] + 2, t.ab_ms);
   p.ctx->tuned[key] = t;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -685,11 +730,18 @@ inline double nnz_per_row(const Problem &p) {
   return (p.na ? (double)(p.A.ns + p.A.nd) / p.na : 0.0) + (p.nb ? (double)(p.B.ns + p.B.nd) / p.nb : 0.0) + sa * sb;
 }
 
+// Alpha x beta single pairs per determinant above which the untimed choice
+// gives them their own kernel (k_sigma_ab stages rows per alpha single; with
+// a few singles per string on both sides that staging is cheap per term).
+constexpr double kAbSplitPerElement = 4.0;
+
 template <typename T, bool kB>
 bool needs_tuning(Problem &p) {
   const int prec = slot_of<T, kB>();
   if (p.tune_a[prec] >= 0 && p.tune_b[prec] >= 0) return false;
   if (p.ctx->autotune) return true;
+  p.split_ab[prec] =
+      (ab_fits<T>(p) && (double)p.A.ns * (double)p.B.ns >= kAbSplitPerElement * (double)p.N) ? 1 : 0;
   if (nnz_per_row(p) <= 8.0) {
     p.tune_a[prec] = 0;
     p.tune_b[prec] = kSparseShape;
@@ -704,22 +756,7 @@ template <typename T, bool kB>
 void launch(Problem &p, const Args<T> &a, cudaStream_t s) {
   const int prec = slot_of<T, kB>();
   if (p.tune_a[prec] < 0 || p.tune_b[prec] < 0) autotune<T, kB>(p, a, s);
-  if (p.tune_b[prec] == kSparseShape) {
-    launch_sparse<T, kB>(p, a, p.tune_a[prec], s);
-    count_launch(p.ctx, 1);
-    SBDGB_CUDA(cudaGetLastError());
-    return;
-  }
-  if (p.tune_b[prec] == kFusedShape) {
-    launch_fused<T, kB>(p, a, p.tune_a[prec], s);
-    count_launch(p.ctx, 1);
-    SBDGB_CUDA(cudaGetLastError());
-    return;
-  }
-  launch_a<T, kB>(p, a, p.tune_a[prec], s);
-  launch_b<T, kB>(p, a, p.tune_b[prec], s);
-  count_launch(p.ctx, 2);
-  SBDGB_CUDA(cudaGetLastError());
+  launch_shapes<T, kB>(p, a, p.tune_a[prec], p.tune_b[prec], p.split_ab[prec], s);
 }
 
 // ---- multi-vector FP32 products (mixed form) --------------------------------------
@@ -851,7 +888,7 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
     for (int n = 0; n < NV; ++n)
 #pragma unroll
       for (int c = 0; c < CPT; ++c) part[n][c] = 0.f;
-    const uint32_t p0 = ldg(a.A.off_s + ia), p1 = ldg(a.A.off_s + ia + 1);
+    const uint32_t p0 = ldg(a.A.off_s + ia), p1 = a.skip_ab ? p0 : ldg(a.A.off_s + ia + 1);  // skip: k_sigma_ab
     if constexpr (sizeof(Wd) == 8) {
       // 64-bit words: beta singles outside, alpha singles inside (as in
       // k_sigma_alpha); with 32-bit words the extra popcount per term costs
@@ -1032,8 +1069,11 @@ int shape_b_mv(int tuned) {
 }
 
 template <int NV, bool kB>
-void launch_mv(const Problem &p, const ArgsMV &m, cudaStream_t s) {
+void launch_mv(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
   constexpr int ts = slot_of<float, kB>();
+  const bool split = p.split_ab[ts] > 0;
+  ArgsMV m = mv;
+  m.a.skip_ab = split ? 1 : 0;
   if (p.tune_b[ts] == kSparseShape) {  // a stream per vector: nothing to share between vectors
     for (int n = 0; n < NV; ++n) {
       Args<float> a = m.a;
@@ -1041,14 +1081,19 @@ void launch_mv(const Problem &p, const ArgsMV &m, cudaStream_t s) {
       a.S = m.Sv[n];
       launch_sparse<float, kB>(p, a, p.tune_a[ts], s);
     }
-    return;
-  }
-  if (p.tune_b[ts] == kFusedShape) {
+  } else if (p.tune_b[ts] == kFusedShape) {
     launch_a_mv<NV, true, kB>(p, m, p.tune_a[ts], s);
   } else {
     launch_a_mv<NV, false, kB>(p, m, p.tune_a[ts], s);
     launch_b_mv<NV, kB>(p, m, shape_b_mv<NV>(p.tune_b[ts]), s);
   }
+  if (split)  // the alpha x beta pairs of each vector in k_sigma_ab
+    for (int n = 0; n < NV; ++n) {
+      Args<float> a = mv.a;
+      a.C = mv.Cv[n];
+      a.S = mv.Sv[n];
+      launch_ab<float>(p, a, kB, s);
+    }
 }
 
 template <typename T>
@@ -1194,6 +1239,23 @@ void build_row_tiles(Problem &p, cudaStream_t s) {
                                  cudaMemcpyHostToDevice, s));
     }
   }
+  // work order of the alpha x beta kernel: alpha rows with singles, most
+  // first; beta columns by decreasing single count
+  std::vector<uint32_t> rows, cols(p.nb);
+  for (uint32_t r = 0; r < p.na; ++r)
+    if (os[0][r + 1] > os[0][r]) rows.push_back(r);
+  std::stable_sort(rows.begin(), rows.end(),
+                   [&](uint32_t x, uint32_t y) { return os[0][x + 1] - os[0][x] > os[0][y + 1] - os[0][y]; });
+  for (uint32_t c = 0; c < p.nb; ++c) cols[c] = c;
+  std::stable_sort(cols.begin(), cols.end(),
+                   [&](uint32_t x, uint32_t y) { return os[1][x + 1] - os[1][x] > os[1][y + 1] - os[1][y]; });
+  p.n_ab_rows = (uint32_t)rows.size();
+  p.ab_rows = (uint32_t *)dev_alloc(p, sizeof(uint32_t) * std::max<size_t>(rows.size(), 1));
+  p.ab_cols = (uint32_t *)dev_alloc(p, sizeof(uint32_t) * std::max<size_t>(cols.size(), 1));
+  if (!rows.empty())
+    SBDGB_CUDA(cudaMemcpyAsync(p.ab_rows, rows.data(), sizeof(uint32_t) * rows.size(), cudaMemcpyHostToDevice, s));
+  if (!cols.empty())
+    SBDGB_CUDA(cudaMemcpyAsync(p.ab_cols, cols.data(), sizeof(uint32_t) * cols.size(), cudaMemcpyHostToDevice, s));
   SBDGB_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
 }
 
@@ -1217,19 +1279,8 @@ void sigma_fp64_scratch(Problem &p, const double *C, double *S, int accumulate, 
   a.Ja = p.Ja;
   a.Kp = p.Kp;
   const int sa = p.tune_a[0] >= 0 ? p.tune_a[0] : 1, sb = p.tune_b[0] >= 0 ? p.tune_b[0] : 1;
-  if (sb == kSparseShape) {
-    launch_sparse<double, false>(p, a, sa, s);
-    count_launch(p.ctx, 1);
-  } else if (sb == kFusedShape) {
-    launch_fused<double, false>(p, a, sa, s);
-    count_launch(p.ctx, 1);
-  } else {
-    transpose<double>(p, C, CT, p.na, p.nb, s);
-    launch_a<double, false>(p, a, sa, s);
-    launch_b<double, false>(p, a, sb, s);
-    count_launch(p.ctx, 2);
-  }
-  SBDGB_CUDA(cudaGetLastError());
+  if (needs_transpose(sb)) transpose<double>(p, C, CT, p.na, p.nb, s);
+  launch_shapes<double, false>(p, a, sa, sb, p.tune_a[0] >= 0 ? p.split_ab[0] : 0, s);
 }
 
 namespace {
@@ -1391,7 +1442,7 @@ void sigma_mixed_multi_impl(Problem &p, const float *C, float *S, int nvec, cuda
     default: launch_mv<4, kB>(p, m, s); break;
   }
   end_timing(p, s, ev0, ev1);
-  count_launch(p.ctx, p.tune_b[ts] == kSparseShape ? nvec : fused ? 1 : 2);
+  count_launch(p.ctx, p.tune_b[ts] == kSparseShape ? nvec : fused ? 1 : 2);  // (k_sigma_ab counts its own)
   SBDGB_CUDA(cudaGetLastError());
 }
 }  // namespace

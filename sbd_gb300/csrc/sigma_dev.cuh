@@ -91,6 +91,7 @@ struct Args {
   int npair;
   const uint32_t *tile_start, *tile_order;  // row tiles of the kernel's row spin
   double shift;  // sigma = (H - shift) C in the FP32 and double-float forms; the FP64 form has none
+  int skip_ab = 0;  // 1: leave the alpha x beta single pairs to k_sigma_ab (sigma_ab.cu)
 };
 
 // Strings and phase masks as 32-bit words when norb <= 32 (half the integer
@@ -241,4 +242,10 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
 
 
 }  // namespace sdev
+
+// sigma_ab.cu: the alpha x beta single pairs in a kernel of their own, added
+// into a.S (block: the block ordering's phases).
+template <typename T>
+void launch_ab(const Problem &p, const sdev::Args<T> &a, bool block, cudaStream_t s);
+
 }  // namespace sbdgb

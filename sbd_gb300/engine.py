@@ -24,7 +24,7 @@ SYMBOLS = [
     "sbdgb_abi_version", "sbdgb_ctx_create", "sbdgb_ctx_destroy", "sbdgb_last_error", "sbdgb_ctx_bytes_in_use",
     "sbdgb_ctx_launch_count", "sbdgb_ctx_set_stream", "sbdgb_ctx_enable_timing", "sbdgb_ctx_sigma_timing", "sbdgb_check_comm_sizes", "sbdgb_problem_create", "sbdgb_problem_destroy",
     "sbdgb_problem_footprint", "sbdgb_build_tables", "sbdgb_table_counts", "sbdgb_export_tables",
-    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_df", "sbdgb_sigma_mixed_block", "sbdgb_sigma_noalloc", "sbdgb_occupation_density", "sbdgb_string_weights", "sbdgb_string_cut_counts", "sbdgb_rdm", "sbdgb_problem_tuning", "sbdgb_problem_tuning_times", "sbdgb_problem_set_tuning", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
+    "sbdgb_diag_terms", "sbdgb_sigma", "sbdgb_sigma_mixed", "sbdgb_sigma_df", "sbdgb_sigma_mixed_block", "sbdgb_sigma_noalloc", "sbdgb_occupation_density", "sbdgb_string_weights", "sbdgb_string_cut_counts", "sbdgb_rdm", "sbdgb_problem_tuning", "sbdgb_problem_tuning_times", "sbdgb_problem_set_tuning", "sbdgb_problem_split", "sbdgb_problem_set_split", "sbdgb_mult_host", "sbdgb_davidson_default_opts",
     "sbdgb_davidson", "sbdgb_lanczos", "sbdgb_batch_davidson", "sbdgb_server_create", "sbdgb_server_submit", "sbdgb_server_poll", "sbdgb_server_wait",
     "sbdgb_server_stats", "sbdgb_server_last_error", "sbdgb_server_destroy",
 ]
@@ -124,6 +124,8 @@ def load(path: str = LIB_PATH):
     L.sbdgb_problem_tuning.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
     L.sbdgb_problem_tuning_times.argtypes = [vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.sbdgb_problem_split.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
+    L.sbdgb_problem_set_split.argtypes = [vp, C.c_int, C.c_int]
     L.sbdgb_problem_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_int]
     L.sbdgb_davidson_default_opts.argtypes = [C.POINTER(DavidsonOpts)]
     L.sbdgb_davidson_default_opts.restype = None
@@ -319,12 +321,26 @@ class TPBProblem:
             alpha = ["8 rows", "16 rows"][a.value]
         return {"alpha_shape": alpha, "beta_shape": shapes[b.value] if b.value >= 0 else None,
                 "alpha_ms": [round(x, 4) for x in ma], "beta_ms": [round(x, 4) for x in mb],
-                "fused_ms": [round(x, 4) for x in mf], "sparse_ms": [round(x, 4) for x in ms]}
+                "fused_ms": [round(x, 4) for x in mf], "sparse_ms": [round(x, 4) for x in ms],
+                "alpha_beta": self.split(precision)}
 
     def set_tuning(self, precision: int, shape_a: int, shape_b: int):
         """Forces the sigma tile shapes (shape_b 4 = the fused single kernel, 5 = the
         sparse-row kernel with shape_a 0/1 = 8/16 rows per tile)."""
         self.engine.check(self.lib.sbdgb_problem_set_tuning(self.h, precision, shape_a, shape_b))
+
+    def split(self, precision: int = FP64) -> dict:
+        """Whether sigma's alpha x beta single pairs run in their own kernel (1),
+        inside the tuned shapes (0) or are undecided (-1), with the autotuner's
+        time (ms) of one product without and with that kernel."""
+        sp = C.c_int(-1)
+        ms = (C.c_float * 2)()
+        self.engine.check(self.lib.sbdgb_problem_split(self.h, precision, C.byref(sp), ms))
+        return {"split": sp.value, "ms_inline": ms[0], "ms_split": ms[1]}
+
+    def set_split(self, precision: int, split: int):
+        """Forces the alpha x beta pairs into their own kernel (1) or into the tuned shapes (0)."""
+        self.engine.check(self.lib.sbdgb_problem_set_split(self.h, precision, split))
 
     def sigma(self, C_in: np.ndarray) -> np.ndarray:
         return self.mult(C_in)

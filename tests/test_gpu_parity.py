@@ -184,3 +184,58 @@ def test_double_float_sigma_matches_reference(gcase, shapes):
     p.sigma_df_device(X.data_ptr(), Y.data_ptr(), accumulate=True, stream=st)
     y = Y.double().cpu().numpy().reshape(-1, 2).sum(axis=1)
     assert max_rel(y, base + c.sigma) <= 1e-12
+
+
+@pytest.mark.parametrize("shapes", [(1, 1), (3, 4), (1, 5)])
+def test_sigma_alpha_beta_kernel(gcase, shapes):
+    """The alpha x beta single pairs in their own kernel (k_sigma_ab: the C rows
+    and (P|Q) rows of each alpha row's singles staged in shared memory) next to
+    each kind of the other kernels (two sweeps, fused, sparse-row), in FP64
+    (1e-12), double-float (1e-12) and FP32 (1e-5), overwrite and accumulate."""
+    import torch
+    c, p = gcase
+    p.diag_terms()
+    st = torch.cuda.current_stream().cuda_stream
+    for prec in (0, 1, 2):
+        p.set_tuning(prec, *shapes)
+        p.set_split(prec, 1)
+    try:
+        for prec in (0, 1, 2):
+            assert p.split(prec)["split"] == 1
+        assert max_rel(p.mult(c.C), c.sigma) <= 1e-12
+        base = np.linspace(-1.0, 1.0, c.C.size)
+        assert max_rel(p.mult(c.C, base.copy()) - base, c.sigma) <= 1e-12
+        C32 = torch.tensor(c.C, dtype=torch.float32, device="cuda")
+        S32 = torch.empty_like(C32)
+        p.sigma_mixed_device(C32.data_ptr(), S32.data_ptr(), stream=st)
+        torch.cuda.synchronize()
+        assert max_rel(S32.double().cpu().numpy(), c.sigma) <= 1e-5
+        X = torch.tensor(_df(c.C), device="cuda")
+        Y = torch.zeros_like(X)
+        p.sigma_df_device(X.data_ptr(), Y.data_ptr(), stream=st)
+        torch.cuda.synchronize()
+        assert max_rel(Y.double().cpu().numpy().reshape(-1, 2).sum(axis=1), c.sigma) <= 1e-12
+    finally:
+        for prec in (0, 1, 2):
+            p.set_split(prec, 0)
+
+
+def test_solvers_with_alpha_beta_kernel(gcase):
+    """The solvers' products in the block ordering with the alpha x beta kernel
+    (forced on for FP64, FP32 and double-float) reach the reference energy: the
+    plain FP64 Davidson and the mixed form."""
+    from sbd_gb300.engine import MIXED
+    c, p = gcase
+    p.diag_terms()
+    for prec in (3, 4, 5):
+        p.set_tuning(prec, 1, 1)
+        p.set_split(prec, 1)
+    try:
+        r = p.davidson(nroots=1, max_nb=12, eps=1e-10, max_it=200, init=0)
+        assert r.report["converged"] and abs(r.energies[0] - c.energy) < 1e-8
+        rm = p.davidson(nroots=1, max_nb=12, eps=1e-10, max_it=200, init=0, precision=MIXED)
+        assert rm.report["converged"] and abs(rm.energies[0] - c.energy) < 1e-8
+        assert p.split(3)["split"] == 1
+    finally:
+        for prec in (3, 4, 5):
+            p.set_split(prec, 0)

@@ -275,6 +275,24 @@ def config_block(prob, ws: int = 1) -> dict:
             "l2": "inputs larger than L2 (288 MB per vector, 13.8 GB subspace)", "ndet": int(prob.ndet)}
 
 
+def capture_stdout(fn):
+    """fn()'s result and what it wrote to file descriptor 1 (the engine's
+    per-iteration lines), kept out of the probe's JSON output."""
+    import tempfile
+    sys.stdout.flush()
+    with tempfile.TemporaryFile(mode="w+") as tmp:
+        saved = os.dup(1)
+        os.dup2(tmp.fileno(), 1)
+        try:
+            r = fn()
+        finally:
+            sys.stdout.flush()
+            os.dup2(saved, 1)
+            os.close(saved)
+        tmp.seek(0)
+        return r, tmp.read()
+
+
 def run_sigma_probe(a) -> int:
     """--sigma-probe CONFIG: times sigma (and optionally one Davidson solve per
     precision) on one synthetic configuration and prints one JSON line:
@@ -365,10 +383,21 @@ def run_sigma_probe(a) -> int:
     if a.davidson:
         for prec, name in ((0, "fp64"), (MIXED, "mixed")):
             torch.cuda.synchronize()
+            eng.enable_timing(True)
+            eng.sigma_timing()
             t = time.time()
-            r = p.davidson(nroots=a.nroots, max_nb=max_nb, eps=eps, init=1, precision=prec, want_vectors=False)
+            r, log = capture_stdout(lambda: p.davidson(nroots=a.nroots, max_nb=max_nb, eps=eps, init=1,
+                                                       precision=prec, want_vectors=False, verbose=True))
             torch.cuda.synchronize()
-            out[f"dav_{name}"] = {"E": r.energies.tolist(), "wall_s": time.time() - t, **r.report}
+            wall = time.time() - t
+            ncalls, sig_ms = eng.sigma_timing()
+            eng.enable_timing(False)
+            lines = [x for x in log.splitlines() if "iteration" in x]
+            phases = {"fp32": sum("(FP32 phase)" in x for x in lines),
+                      "double_float": sum("(double-float phase)" in x for x in lines)}
+            phases["fp64"] = len(lines) - phases["fp32"] - phases["double_float"]
+            out[f"dav_{name}"] = {"E": r.energies.tolist(), "wall_s": wall, "sigma_ms_total": sig_ms,
+                                  "sigma_products_timed": ncalls, "iterations_by_phase": phases, **r.report}
     print(json.dumps(out))
     p.close()
     eng.close()

@@ -106,6 +106,10 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
   b += 16 * (na + nb + 4);  // sigma row tiles (two row caps, start + order per spin)
   // diagonal and its workspaces
   b += 8 * N + 8 * (na + nb + 2) + 8 * (na * L + 1);
+  // work order of the alpha x beta kernel: rows, columns, slice starts, and
+  // 12 bytes per beta single in slices of 32 (padding at most 31 x the
+  // longest list, itself at most L^2 / 4 singles)
+  b += 4 * (na + nb) + 4 * (nb / 32 + 2) + 12 * (entries_b + 32 * (L * L / 4 + 1));
   // FP64 sigma transpose scratch (also used by the mixed refinement)
   b += 8 * N;
   // solver reductions (partial sums of at most 4 blocks per SM of 64 values, staging)
@@ -125,14 +129,14 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;
     b += 8 * npair * npair + 8 * npair * (na + nb) + 8 * (entries_a + entries_b) + 32;
     b += 4 * N + 4 * N * std::min<size_t>(4, k);
-    b += 8 * N;  // the diagonal as double-float
+    b += 8 * N + 4 * N;  // the diagonal as double-float and as FP32
   } else {
     const size_t mmax = (size_t)std::max(std::min(o.max_nb, 64) - (int)k, 2 * (int)k);
     b += 4 * npair * npair + 4 * npair * (na + nb) + 4 * (entries_a + entries_b) + 16;  // FP32 tables
     b += 4 * N;                                                                          // FP32 transpose
     b += 4 * N * std::min<size_t>(4, k);  // transposed copies of the vectors of one multi-vector product
     b += 32 * N * k + 4 * N * (k + mmax) + 4 * N * mmax + 12 * N * k + 4 * (8 * 3 * 64 + 64);
-    b += 8 * N;  // the diagonal as double-float (hi and lo FP32 parts)
+    b += 8 * N + 4 * N;  // the diagonal as double-float (hi and lo FP32 parts) and as FP32
   }
   return b;
 }

@@ -137,6 +137,7 @@ struct Problem {
   float *CTf = nullptr;   // mixed transpose scratch
   float *Kpf = nullptr, *Jbf = nullptr, *Jaf = nullptr;
   dfloat *hii_df = nullptr;  // hii as double-float (FP32 and double-float kernels)
+  float *hii_f = nullptr;    // hii in FP32 (the FP32 kernels' unshifted products)
   // double-float copies of the tables and integral tables (double-float phase of the mixed form)
   dfloat *Kpd = nullptr, *Jbd = nullptr, *Jad = nullptr;
   dfloat *val_sd[2] = {nullptr, nullptr}, *val_dd[2] = {nullptr, nullptr};
@@ -158,10 +159,12 @@ struct Problem {
   // after the tuned shapes, which then skip them; -1 = not decided yet
   int split_ab[6] = {-1, -1, -1, -1, -1, -1};
   float tune_ab_ms[6][2] = {};  // the autotuner's time of the tuned shapes without and with the split
-  // alpha rows with at least one single (most singles first) and beta columns
-  // by decreasing single count: the work order of the alpha x beta kernel
-  uint32_t *ab_rows = nullptr, *ab_cols = nullptr;
-  uint32_t n_ab_rows = 0;
+  // work order of the alpha x beta kernel (sigma_ab.cu): alpha rows with at
+  // least one single (most singles first); beta columns by decreasing single
+  // count in slices of 32, each slice's beta singles interleaved by lane
+  uint32_t *ab_rows = nullptr, *ab_cols = nullptr, *ab_slice = nullptr, *ab_ent = nullptr;
+  uint64_t *ab_mask = nullptr;
+  uint32_t n_ab_rows = 0, n_ab_slices = 0;
   size_t bytes = 0;
   std::vector<void *> allocs;
   // host copies of strings
@@ -227,9 +230,12 @@ void build_diag(Problem &p, cudaStream_t s);
 // sigma.cu
 void build_row_tiles(Problem &p, cudaStream_t s);
 // sigma_ab.cu: whether the alpha x beta kernel's shared-memory staging (C
-// rows and (P|Q) rows of its element type T) fits this problem.
+// rows and (P|Q) rows of its element type T) fits this problem; its work
+// order from the host copies of the single-excitation offsets of both spins.
 template <typename T>
 bool ab_fits(const Problem &p);
+void build_ab_order(Problem &p, const std::vector<uint32_t> &off_a, const std::vector<uint32_t> &off_b,
+                    cudaStream_t s);
 // block: the block-ordering product (H_block = eta H eta, no opposite-spin
 // parities) that the solvers use on eta-signed vectors; false: the
 // reference's interleaved convention.

@@ -92,8 +92,12 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
         if constexpr (std::is_same<T, double>::value) {
           acc[c] = ldg(a.hii + k) * ldg(a.C + k);  // the FP64 form has no shift: one FP64 op
         } else if constexpr (std::is_same<T, float>::value) {
-          const dfloat h = ldg(a.hii_df + k);
-          acc[c] = ff_diag(h.hi, h.lo, a.shift_df.hi, a.shift_df.lo, ldg(a.C + k));
+          if (a.hii_f) {
+            acc[c] = ff_prod(ldg(a.hii_f + k), ldg(a.C + k));
+          } else {
+            const dfloat h = ldg(a.hii_df + k);
+            acc[c] = ff_diag(h.hi, h.lo, a.shift_df.hi, a.shift_df.lo, ldg(a.C + k));
+          }
         } else {
           acc[c] = (ldg(a.hii_df + k) - a.shift_df) * ldg(a.C + k);
         }
@@ -263,7 +267,8 @@ __device__ __forceinline__ void store_v(T *__restrict__ p, const T (&x)[VW]) {
 template <int RG, int VW, typename T, typename Wd, bool kB>
 __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint32_t nr, uint32_t c0,
                                             const Wd (&beta)[VW], const uint32_t (&q0)[VW],
-                                            const uint32_t (&q1)[VW]) {
+                                            const uint32_t (&q1)[VW], const uint32_t (&d0)[VW],
+                                            const uint32_t (&d1)[VW]) {
   constexpr bool kF64 = std::is_same<T, double>::value;
   Wd arow[RG];
 #pragma unroll
@@ -287,6 +292,11 @@ __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint
         load_v<VW>(a.hii + k, h);
 #pragma unroll
         for (int v = 0; v < VW; ++v) acc[r][v] = h[v] * x[v];  // the FP64 form has no shift
+      } else if (std::is_same<T, float>::value && a.hii_f) {
+        float h[VW];
+        load_v<VW>(reinterpret_cast<const float *>(a.hii_f) + k, h);
+#pragma unroll
+        for (int v = 0; v < VW; ++v) acc_diag_f(acc[r][v], h[v], x[v]);
       } else {
         dfloat h[VW];
         load_v<VW>(a.hii_df + k, h);
@@ -303,8 +313,7 @@ __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint
   // beta singles and doubles of this thread's columns (task type 1)
 #pragma unroll
   for (int v = 0; v < VW; ++v) {
-    const uint32_t d0 = ldg(a.B.off_d + c0 + v), d1 = ldg(a.B.off_d + c0 + v + 1);
-    for (uint32_t q = d0; q < d1; ++q) {
+    for (uint32_t q = d0[v]; q < d1[v]; ++q) {
       const uint32_t jb = ldg(a.B.ket_d + q);
       const T val = ldg(a.val_db + q);
       const Wd m = mask_of<kB, Wd>(a.B.mask_d, q);
@@ -408,22 +417,29 @@ __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint
 template <int TA, int VW, typename T, typename Wd, bool kB>
 __global__ void __launch_bounds__(kThreads) k_sigma_sparse(Args<T> a) {
   constexpr int RG = 4;
-  const uint32_t tile = ldg(a.tile_order + blockIdx.x);
+  // one-dimensional grid, column chunks fastest: the CTAs of one row tile run
+  // together, so the rows of C that a tile's beta pairs gather across the
+  // whole row are in L2 while its other chunks stream them
+  const uint32_t nchunk = (a.nb + kThreads * VW - 1) / (kThreads * VW);
+  const uint32_t tix = blockIdx.x / nchunk, chunk = blockIdx.x - tix * nchunk;
+  const uint32_t tile = ldg(a.tile_order + tix);
   const uint32_t ia0 = ldg(a.tile_start + tile);
   const uint32_t rend = ldg(a.tile_start + tile + 1) - ia0;  // 1..TA
-  const uint32_t c0 = blockIdx.y * (kThreads * VW) + threadIdx.x * VW;
+  const uint32_t c0 = chunk * (kThreads * VW) + threadIdx.x * VW;
   if (c0 >= a.nb) return;  // nb is a multiple of VW: a vector is wholly in or out
   Wd beta[VW];
-  uint32_t q0[VW], q1[VW];
+  uint32_t q0[VW], q1[VW], d0[VW], d1[VW];
 #pragma unroll
   for (int v = 0; v < VW; ++v) {
     beta[v] = word<Wd>(a.bstr, c0 + v);
     q0[v] = ldg(a.B.off_s + c0 + v);
     q1[v] = ldg(a.B.off_s + c0 + v + 1);
+    d0[v] = ldg(a.B.off_d + c0 + v);
+    d1[v] = ldg(a.B.off_d + c0 + v + 1);
   }
 #pragma unroll 1
   for (uint32_t g = 0; g < rend; g += RG)
-    sparse_rows<RG, VW, T, Wd, kB>(a, ia0 + g, min((uint32_t)RG, rend - g), c0, beta, q0, q1);
+    sparse_rows<RG, VW, T, Wd, kB>(a, ia0 + g, min((uint32_t)RG, rend - g), c0, beta, q0, q1, d0, d1);
 }
 
 // out[c][r] = in[r][c] for an R x Cn row-major matrix.
@@ -523,12 +539,13 @@ void launch_sparse_ta(const Problem &p, Args<T> a, cudaStream_t s) {
   a.tile_start = p.tile_start[0][v];
   a.tile_order = p.tile_order[0][v];
   const bool vec = p.nb % VW == 0 && aligned16(a.C) && aligned16(a.S) && aligned16(a.Jb) &&
-                   (std::is_same<T, double>::value ? aligned16(a.hii) : aligned16(a.hii_df));
+                   (std::is_same<T, double>::value ? aligned16(a.hii) : aligned16(a.hii_df)) &&
+                   (a.hii_f == nullptr || aligned16(a.hii_f));
   if (vec) {
-    dim3 g(p.n_tiles[0][v], (p.nb + kThreads * VW - 1) / (kThreads * VW));
+    const unsigned g = p.n_tiles[0][v] * ((p.nb + kThreads * VW - 1) / (kThreads * VW));
     k_sigma_sparse<TA, VW, T, Wd, kB><<<g, kThreads, 0, s>>>(a);
   } else {
-    dim3 g(p.n_tiles[0][v], (p.nb + kThreads - 1) / kThreads);
+    const unsigned g = p.n_tiles[0][v] * ((p.nb + kThreads - 1) / kThreads);
     k_sigma_sparse<TA, 1, T, Wd, kB><<<g, kThreads, 0, s>>>(a);
   }
 }
@@ -876,11 +893,17 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       const uint32_t k = ia * a.nb + col[c];
-      const dfloat h = ok[c] ? ldg(a.hii_df + k) : dfloat(0.f, 0.f);
-      const float hh = h.hi, hl = h.lo;
+      if (a.hii_f) {
+        const float h = ok[c] ? ldg(a.hii_f + k) : 0.f;
 #pragma unroll
-      for (int n = 0; n < NV; ++n)
-        acc[n][c] = ok[c] ? ff_diag(hh, hl, a.shift_df.hi, a.shift_df.lo, ldg(m.Cv[n] + k)) : FF{0.f, 0.f};
+        for (int n = 0; n < NV; ++n) acc[n][c] = ok[c] ? ff_prod(h, ldg(m.Cv[n] + k)) : FF{0.f, 0.f};
+      } else {
+        const dfloat h = ok[c] ? ldg(a.hii_df + k) : dfloat(0.f, 0.f);
+        const float hh = h.hi, hl = h.lo;
+#pragma unroll
+        for (int n = 0; n < NV; ++n)
+          acc[n][c] = ok[c] ? ff_diag(hh, hl, a.shift_df.hi, a.shift_df.lo, ldg(m.Cv[n] + k)) : FF{0.f, 0.f};
+      }
     }
     same_spin_row_mv<CPT, NV, Wd, kB>(a.A, a.val_sa, a.val_da, a.Jb, a.nb, m.Cv, a.nb, ia, col, ok, beta, acc);
     float part[NV][CPT];
@@ -1139,6 +1162,7 @@ Args<T> base_args(Problem &p, const T *C, T *S, int accumulate) {
   a.nb = p.nb;
   a.hii = p.hii;
   a.hii_df = p.hii_df;
+  a.hii_f = nullptr;
   a.shift_df = dfloat(0.f, 0.f);
   a.C = C;
   a.S = S;
@@ -1239,23 +1263,7 @@ void build_row_tiles(Problem &p, cudaStream_t s) {
                                  cudaMemcpyHostToDevice, s));
     }
   }
-  // work order of the alpha x beta kernel: alpha rows with singles, most
-  // first; beta columns by decreasing single count
-  std::vector<uint32_t> rows, cols(p.nb);
-  for (uint32_t r = 0; r < p.na; ++r)
-    if (os[0][r + 1] > os[0][r]) rows.push_back(r);
-  std::stable_sort(rows.begin(), rows.end(),
-                   [&](uint32_t x, uint32_t y) { return os[0][x + 1] - os[0][x] > os[0][y + 1] - os[0][y]; });
-  for (uint32_t c = 0; c < p.nb; ++c) cols[c] = c;
-  std::stable_sort(cols.begin(), cols.end(),
-                   [&](uint32_t x, uint32_t y) { return os[1][x + 1] - os[1][x] > os[1][y + 1] - os[1][y]; });
-  p.n_ab_rows = (uint32_t)rows.size();
-  p.ab_rows = (uint32_t *)dev_alloc(p, sizeof(uint32_t) * std::max<size_t>(rows.size(), 1));
-  p.ab_cols = (uint32_t *)dev_alloc(p, sizeof(uint32_t) * std::max<size_t>(cols.size(), 1));
-  if (!rows.empty())
-    SBDGB_CUDA(cudaMemcpyAsync(p.ab_rows, rows.data(), sizeof(uint32_t) * rows.size(), cudaMemcpyHostToDevice, s));
-  if (!cols.empty())
-    SBDGB_CUDA(cudaMemcpyAsync(p.ab_cols, cols.data(), sizeof(uint32_t) * cols.size(), cudaMemcpyHostToDevice, s));
+  build_ab_order(p, os[0], os[1], s);
   SBDGB_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
 }
 
@@ -1380,6 +1388,8 @@ void prepare_mixed(Problem &p, cudaStream_t s) {
   to_float(p, p.Jb, p.Jbf, (size_t)p.npair * p.nb, s);
   to_float(p, p.Ja, p.Jaf, (size_t)p.npair * p.na, s);
   split_hii(p, s);
+  p.hii_f = (float *)dev_alloc(p, sizeof(float) * (p.N ? p.N : 1));
+  to_float(p, p.hii, p.hii_f, p.N, s);
   for (int sp = 0; sp < 2; ++sp) {
     SpinTables &T = sp == 0 ? p.A : p.B;
     p.val_sf[sp] = (float *)dev_alloc(p, sizeof(float) * (T.ns ? T.ns : 1));
@@ -1396,6 +1406,7 @@ namespace {
 Args<float> mixed_args(Problem &p, const float *C, float *S, double shift) {
   Args<float> a = base_args<float>(p, C, S, 0);
   set_shift(a, shift);
+  a.hii_f = shift == 0.0 ? p.hii_f : nullptr;
   a.CT = p.CTf;
   a.val_sa = p.val_sf[0];
   a.val_da = p.val_df[0];

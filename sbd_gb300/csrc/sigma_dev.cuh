@@ -51,6 +51,16 @@ __device__ __forceinline__ FF ff_diag(float h_hi, float h_lo, float s_hi, float 
   return FF{p, fmaf(dl, x, fmaf(dh, x, -p))};
 }
 
+// x * h as a float-float (the product's rounding error by one FMA): the
+// diagonal term of an unshifted FP32 product.
+__device__ __forceinline__ FF ff_prod(float h, float x) {
+  const float p = h * x;
+  return FF{p, fmaf(h, x, -p)};
+}
+__device__ __forceinline__ void acc_diag_f(FF &acc, float h, float x) { acc = ff_prod(h, x); }
+template <typename A, typename X>
+__device__ __forceinline__ void acc_diag_f(A &, float, X) {}  // only FP32 kernels read the FP32 diagonal
+
 // Per-element accumulator: FP64 in the FP64 form, float-float in the FP32
 // kernels of the mixed form, double-float (the vectors' own format) in its
 // double-float phase.
@@ -79,6 +89,9 @@ struct Args {
   const double *hii;
   const dfloat *hii_df;  // FP32 and double-float kernels: hii as hi + lo (no FP64 instruction in them)
   dfloat shift_df;       // the shift split the same way
+  // FP32 kernels with no shift: hii rounded to FP32 (4 bytes a determinant
+  // instead of 8; its rounding, 2^-24 relative, is that of the FP32 result)
+  const float *hii_f;
   const T *C;   // N, row-major [ia][ib]
   const T *CT;  // N, transposed [ib][ia]
   T *S;

@@ -148,6 +148,23 @@ def measure_fp64_rates(device: int) -> dict:
     return {"dfma_tflops": a.value, "dmma_tflops": b.value}
 
 
+def measure_fp64_overlap(device: int) -> dict:
+    """Times (ms) of an FP64 FMA loop, an FP64 MMA loop and one loop with the
+    work of both (bench_csrc/rates.cu): near the longer of the two when the FMA
+    pipe and the FP64 tensor path run concurrently, near their sum when they
+    share the FP64 units."""
+    import ctypes as C
+    from sbd_gb300 import build
+    L = C.CDLL(build.RATES_LIB)
+    fp = C.POINTER(C.c_float)
+    L.sbdgb_measure_fp64_overlap.argtypes = [C.c_int, fp, fp, fp]
+    a, b, c = C.c_float(), C.c_float(), C.c_float()
+    rc = L.sbdgb_measure_fp64_overlap(device, C.byref(a), C.byref(b), C.byref(c))
+    if rc != 0:
+        raise RuntimeError(f"FP64 overlap probe failed ({rc})")
+    return {"fma_ms": a.value, "mma_ms": b.value, "both_ms": c.value}
+
+
 def make_problem():
     from sbd_gb300.generators import config1
     return config1()
@@ -404,6 +421,74 @@ def run_sigma_probe(a) -> int:
     return 0
 
 
+def config3_block(eng, peak: float, peak_kind: str, reps: int = 10) -> dict:
+    """sigma on config 3 (norb 58, 16+16 electrons, 12000 x 12000 strings,
+    N = 1.44e8, 1.15 GB per FP64 vector: larger than L2 every product) in FP64
+    and in the mixed form's FP32 product, CUDA events on the launch stream
+    after two untimed products, against the HBM roofline: algorithmic bytes
+    24 N + 8 nnz_off (FP64: read C and hii, write sigma, one C read per
+    nonzero) and 12 N + 4 nnz_off (FP32: the unshifted product reads hii in
+    FP32); then one Davidson solve per precision (1 root, tol 1e-7)."""
+    import torch
+
+    from sbd_gb300.engine import MIXED, TPBProblem
+    from sbd_gb300.generators import config3
+    prob = config3()
+    p = TPBProblem.from_problem(eng, prob)
+    p.build_tables()
+    p.diag_terms()
+    (sa, da), (sb, db) = p.table_counts(0), p.table_counts(1)
+    N, na, nb = prob.ndet, prob.astr.size, prob.bstr.size
+    nnz = nb * (sa + da) + na * (sb + db) + sa * sb
+    st = torch.cuda.Stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    C = torch.rand(N, dtype=torch.float64, device="cuda") * 2 - 1
+    S = torch.empty_like(C)
+    ms64 = timed(lambda: p.sigma_device(C.data_ptr(), S.data_ptr(), stream=st.cuda_stream))
+    C32 = C.float()
+    S32 = torch.empty_like(C32)
+    ms32 = timed(lambda: p.sigma_mixed_device(C32.data_ptr(), S32.data_ptr(), stream=st.cuda_stream))
+    rel32 = float((S32.double() - S).abs().max() / S.abs().max())
+    del C, S, C32, S32
+    b64, b32 = 24.0 * N + 8.0 * nnz, 12.0 * N + 4.0 * nnz
+    out = {"workload": "config3: norb 58, 16+16 electrons, 12000x12000 strings (N=144,000,000)",
+           "nnz_per_row": nnz / N,
+           "fp64": {"ms": ms64, "tiles": p.tuning(0),
+                    "roofline": {"bound": "hbm", "achieved": b64 / (ms64 * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                                 "frac": b64 / (ms64 * 1e-3) / 1e9 / peak, "algorithmic_bytes": b64,
+                                 "peak_kind": f"{peak_kind} hbm_gbs"}},
+           "mixed_fp32": {"ms": ms32, "tiles": p.tuning(MIXED), "max_rel_err_vs_fp64": rel32,
+                          "roofline": {"bound": "hbm", "achieved": b32 / (ms32 * 1e-3) / 1e9, "peak": peak,
+                                       "unit": "GB/s", "frac": b32 / (ms32 * 1e-3) / 1e9 / peak,
+                                       "algorithmic_bytes": b32, "peak_kind": f"{peak_kind} hbm_gbs"}},
+           "mixed_vs_fp64_sigma": ms64 / ms32}
+    E = {}
+    for prec, name in ((0, "fp64"), (MIXED, "mixed")):
+        for _ in range(2):  # the second solve is timed (the first tunes the solver's sigma shapes)
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            r = p.davidson(nroots=1, max_nb=20, eps=1e-7, init=1, precision=prec, want_vectors=False)
+            torch.cuda.synchronize()
+        E[name] = r.energies
+        out[f"solve_{name}"] = {"seconds": time.perf_counter() - t, "iterations": r.report["iterations"],
+                                "sigma_products": r.report["sigma_calls"], "converged": r.report["converged"]}
+    out["solve_max_abs_dE"] = float(np.max(np.abs(E["mixed"] - E["fp64"])))
+    p.close()
+    return out
+
+
 def run_gpu(args):
     dist, rank, ws = dist_init()
     import torch
@@ -501,6 +586,12 @@ def run_gpu(args):
     e2e_t = max_over_ranks(dist, float(np.sum(e2e_lat)))
     e2e_value = ws * len(e2e_lat) / e2e_t
 
+    # config 3 (the streaming case, 0.5 nonzeros per row): sigma against the
+    # HBM roofline in both precisions, and one solve per precision
+    config3 = None
+    if rank == 0 and not args.no_config3:
+        config3 = config3_block(eng, peak, peak_kind)
+
     traffic = None
     prof_path = os.path.join(ROOT, "profiles", "sigma_traffic.json")
     if os.path.exists(prof_path):
@@ -587,6 +678,7 @@ def run_gpu(args):
                                   "fp64_tensor_peak": rates["dmma_tflops"],
                                   "flops": "2 x (nnz_off + N) per sigma"}},
             "mixed_precision": mixed,
+            "config3_sigma": config3,
             "serving": serving,
             "batched": batched,
             "cpu_baseline": cpu,
@@ -611,6 +703,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=None, help="end-to-end solves (default: --steps)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-config3", action="store_true", help="skip the config-3 sigma roofline block")
     ap.add_argument("--mixed-steps", type=int, default=2)
     ap.add_argument("--serve-requests", type=int, default=48, help="config-4 requests for the serving block (0: skip)")
     ap.add_argument("--serve-workers", type=int, default=16)
@@ -627,7 +720,14 @@ def main():
     ap.add_argument("--nroots", type=int, default=2, help="--sigma-probe: roots of the solve")
     ap.add_argument("--strings", type=int, default=0,
                     help="--sigma-probe 0/1/3: strings per spin instead of the configuration's (a smaller case)")
+    ap.add_argument("--fp64-rates", action="store_true",
+                    help="print the measured FP64 FMA and MMA rates and their overlap, then exit")
     args = ap.parse_args()
+    if args.fp64_rates:
+        from sbd_gb300 import build as b
+        b.build()
+        print(json.dumps({**measure_fp64_rates(0), **measure_fp64_overlap(0)}))
+        return 0
     if args.sigma_probe is not None:
         return run_sigma_probe(args)
     if args.impl == "reference":

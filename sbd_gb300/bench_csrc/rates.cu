@@ -41,7 +41,67 @@ __global__ void __launch_bounds__(kRateThreads) k_rate_dmma(double *out) {
   if (s == 12345.0) out[blockIdx.x] = s;
 }
 
+// Both loops' work in one loop: the FP64 FMAs and the FP64 MMAs interleaved.
+// Timed against the two loops alone, it tells whether the FMA pipe and the
+// FP64 tensor path run concurrently (time near the longer one) or share the
+// FP64 units (time near their sum).
+__global__ void __launch_bounds__(kRateThreads) k_rate_both(double *out) {
+  double a = 1.0 + threadIdx.x * 1e-9, b = 1.0 - threadIdx.x * 1e-9;
+  double c[8] = {};
+  double m[4][2] = {};
+  for (int i = 0; i < kRateIters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                   : "+d"(m[u][0]), "+d"(m[u][1])
+                   : "d"(a), "d"(b));
+      c[2 * u] = fma(a, b, c[2 * u]);
+      c[2 * u + 1] = fma(a, b, c[2 * u + 1]);
+    }
+  }
+  double s = 0.0;
+  for (int u = 0; u < 8; ++u) s += c[u];
+  for (int u = 0; u < 4; ++u) s += m[u][0] + m[u][1];
+  if (s == 12345.0) out[blockIdx.x] = s;
+}
+
 }  // namespace
+
+// Milliseconds of the FMA loop, the MMA loop and the interleaved loop (same
+// work as both), each after one untimed run.  Returns 0, or 3 on a CUDA error.
+extern "C" int sbdgb_measure_fp64_overlap(int device, float *ms_fma, float *ms_mma, float *ms_both) {
+  if (!ms_fma || !ms_mma || !ms_both) return 1;
+  int sms = 0;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+    cudaGetLastError();
+    return 3;
+  }
+  const int blocks = sms * 8;
+  double *out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = 0;
+  if (cudaMalloc(&out, sizeof(double) * blocks) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess)
+    rc = 3;
+  float *dst[3] = {ms_fma, ms_mma, ms_both};
+  for (int kind = 0; kind < 3 && rc == 0; ++kind)
+    for (int rep = 0; rep < 2 && rc == 0; ++rep) {
+      cudaEventRecord(e0, 0);
+      if (kind == 0) k_rate_dfma<<<blocks, kRateThreads>>>(out);
+      if (kind == 1) k_rate_dmma<<<blocks, kRateThreads>>>(out);
+      if (kind == 2) k_rate_both<<<blocks, kRateThreads>>>(out);
+      cudaEventRecord(e1, 0);
+      if (cudaEventSynchronize(e1) != cudaSuccess) rc = 3;
+      cudaEventElapsedTime(dst[kind], e0, e1);
+    }
+  if (rc == 0 && cudaGetLastError() != cudaSuccess) rc = 3;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (out) cudaFree(out);
+  cudaGetLastError();
+  return rc;
+}
 
 extern "C" int sbdgb_measure_fp64_rates(int device, double *dfma_tflops, double *dmma_tflops) {
   if (!dfma_tflops || !dmma_tflops) return 1;

@@ -528,106 +528,134 @@ __global__ void k_sum_partials_mat(const double *__restrict__ partial, int nbloc
   if (sym) M[j + (size_t)ld * i] = x;
 }
 
-constexpr int kRR = 64;  // largest projected matrix (max_nb <= 64)
+constexpr int kRR = 64;          // largest projected matrix (max_nb <= 64)
+constexpr int kRRThreads = 1024;  // one element of the n x n matrices per thread (n <= 32)
 
-__device__ __forceinline__ double block_sum64(double v, double *tmp) {
+// Sum over the block (kRRThreads threads) of one value per thread.
+__device__ __forceinline__ double rr_block_sum(double v, double *tmp) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   if ((threadIdx.x & 31) == 0) tmp[threadIdx.x >> 5] = v;
   __syncthreads();
-  const double r = tmp[0] + tmp[1];
+  double r = 0.0;
+  for (int w = 0; w < kRRThreads / 32; ++w) r += tmp[w];
   __syncthreads();
   return r;
 }
 
 // Eigenvalues (ascending) and eigenvectors of the symmetric part of the n x n
-// leading block of Hs (ld), n <= 64, by one block of 64 threads: out[0..n) the
-// eigenvalues, out[n + i + n j] the eigenvector matrix (column j).  The
-// reference solves this with LAPACK dsyev on the host (framework/hp_numeric.h:
-// 503-520); here it is a parallel-order Jacobi: each sweep is n' - 1 rounds
-// (n' = n rounded up to even) of the round-robin pairing, the n'/2 rotations of
-// a round act on disjoint index pairs, so their parameters are computed by
-// n'/2 threads at once and applied together (thread l updates row / column l).
-// FP64 divisions and square roots, 1/64 rate on this GPU, are taken once per
-// round instead of once per pair.
-__global__ void __launch_bounds__(kRR) k_rr(const double *__restrict__ Hs, int ld, int n, double *__restrict__ out) {
+// leading block of Hs (ld), n <= 64, by one block: out[0..n) the eigenvalues,
+// out[n + i + n j] the eigenvector matrix (column j).  The reference solves
+// this with LAPACK dsyev on the host (framework/hp_numeric.h:503-520).
+//
+// Parallel-order Jacobi: each sweep is n' - 1 rounds (n' = n rounded up to
+// even) of the round-robin pairing; the n'/2 rotations of a round act on
+// disjoint index pairs, so n'/2 threads compute them at once and every
+// element of A <- J^T A J and of V <- V J is then formed by its own thread
+// from four (two) elements of the previous round.
+//
+// Warm start: when the first nw basis columns are unchanged since the
+// previous call (the subspace only grew), that call's eigenvectors, still in
+// out (n = nw), diagonalise their block.  The iteration then starts from
+// Y^T A Y with Y = diag(those eigenvectors, identity): diagonal but for the
+// new rows and columns, so a few sweeps converge it.
+__global__ void __launch_bounds__(kRRThreads) k_rr(const double *__restrict__ Hs, int ld, int n, int nw,
+                                                   double *__restrict__ out) {
   extern __shared__ double sm[];
-  double *Aw = sm, *Wv = sm + (size_t)n * n;
-  __shared__ double rc[kRR / 2], rs[kRR / 2], tmp[2];
-  __shared__ int rp[kRR / 2], rq[kRR / 2];
-  const int l = threadIdx.x;
-  for (int t = l; t < n * n; t += kRR) {
+  const int nn = n * n;
+  double *Acur = sm, *Anext = sm + nn, *Vcur = sm + 2 * nn, *Vnext = sm + 3 * nn;
+  __shared__ double ca[kRR], cb[kRR], tmp[kRRThreads / 32];
+  __shared__ int partner[kRR];
+  const int tid = threadIdx.x;
+  for (int t = tid; t < nn; t += kRRThreads) {
     const int i = t % n, j = t / n;
-    Aw[t] = 0.5 * (Hs[i + (size_t)ld * j] + Hs[j + (size_t)ld * i]);
-    Wv[t] = (i == j) ? 1.0 : 0.0;
+    Anext[t] = 0.5 * (Hs[i + (size_t)ld * j] + Hs[j + (size_t)ld * i]);
+    Vcur[t] = (i < nw && j < nw) ? out[nw + i + nw * j] : (i == j ? 1.0 : 0.0);
+  }
+  __syncthreads();
+  if (nw > 0) {
+    // Vnext = A Y, then Acur = Y^T (A Y); Y is block diagonal (Y_old, I)
+    for (int t = tid; t < nn; t += kRRThreads) {
+      const int i = t % n, j = t / n;
+      double x = 0.0;
+      if (j < nw)
+        for (int k = 0; k < nw; ++k) x = fma(Anext[i + n * k], Vcur[k + n * j], x);
+      else
+        x = Anext[i + n * j];
+      Vnext[t] = x;
+    }
+    __syncthreads();
+    for (int t = tid; t < nn; t += kRRThreads) {
+      const int i = t % n, j = t / n;
+      double x = 0.0;
+      if (i < nw)
+        for (int k = 0; k < nw; ++k) x = fma(Vcur[k + n * i], Vnext[k + n * j], x);
+      else
+        x = Vnext[i + n * j];
+      Acur[t] = x;
+    }
+  } else {
+    for (int t = tid; t < nn; t += kRRThreads) Acur[t] = Anext[t];
   }
   __syncthreads();
   const int n2 = (n + 1) & ~1, np = n2 / 2;
   auto idx = [&](int pos, int r) { return pos == 0 ? 0 : 1 + (pos - 1 + r) % (n2 - 1); };
   for (int sweep = 0; sweep < 60 && n > 1; ++sweep) {
     double off = 0.0, dg = 0.0;
-    if (l < n)
-      for (int j = 0; j < n; ++j) {
-        const double x = Aw[l + n * j];
-        if (l == j) dg += x * x; else off += x * x;
-      }
-    off = block_sum64(off, tmp);
-    dg = block_sum64(dg, tmp);
+    for (int t = tid; t < nn; t += kRRThreads) {
+      const double x = Acur[t];
+      if (t % n == t / n) dg += x * x; else off += x * x;
+    }
+    off = rr_block_sum(off, tmp);
+    dg = rr_block_sum(dg, tmp);
     if (off <= 1e-30 * (dg + 1e-300)) break;
     for (int r = 0; r < n2 - 1; ++r) {
-      if (l < np) {
-        const int a = idx(l, r), b = idx(n2 - 1 - l, r);
+      if (tid < np) {
+        const int a = idx(tid, r), b = idx(n2 - 1 - tid, r);
         const int pp = min(a, b), q = max(a, b);
         double c = 1.0, sn = 0.0;
         if (q < n) {  // q == n is the padding index of odd n
-          const double apq = Aw[pp + n * q];
+          const double apq = Acur[pp + n * q];
           if (fabs(apq) >= 1e-300) {
-            const double th = (Aw[q + n * q] - Aw[pp + n * pp]) / (2.0 * apq);
-            const double t = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
-            c = 1.0 / sqrt(t * t + 1.0);
-            sn = t * c;
+            const double th = (Acur[q + n * q] - Acur[pp + n * pp]) / (2.0 * apq);
+            const double tt = (th >= 0 ? 1.0 : -1.0) / (fabs(th) + sqrt(th * th + 1.0));
+            c = 1.0 / sqrt(tt * tt + 1.0);
+            sn = tt * c;
           }
+          // new column p = c col_p - s col_q, new column q = s col_p + c col_q
+          partner[q] = pp;
+          ca[q] = c;
+          cb[q] = sn;
         }
-        rp[l] = pp;
-        rq[l] = q;
-        rc[l] = c;
-        rs[l] = sn;
+        partner[pp] = q < n ? q : pp;
+        ca[pp] = c;
+        cb[pp] = q < n ? -sn : 0.0;
       }
       __syncthreads();
-      if (l < n)  // columns p, q of every pair: row l
-        for (int i = 0; i < np; ++i) {
-          const int pp = rp[i], q = rq[i];
-          if (q >= n || rs[i] == 0.0) continue;
-          const double c = rc[i], sn = rs[i];
-          const double akp = Aw[l + n * pp], akq = Aw[l + n * q];
-          Aw[l + n * pp] = c * akp - sn * akq;
-          Aw[l + n * q] = sn * akp + c * akq;
-        }
+      for (int t = tid; t < nn; t += kRRThreads) {
+        const int i = t % n, j = t / n, pi = partner[i], pj = partner[j];
+        const double ci = ca[i], si = cb[i], cj = ca[j], sj = cb[j];
+        Anext[t] = ci * (cj * Acur[i + n * j] + sj * Acur[i + n * pj]) + si * (cj * Acur[pi + n * j] + sj * Acur[pi + n * pj]);
+        Vnext[t] = cj * Vcur[i + n * j] + sj * Vcur[i + n * pj];
+      }
       __syncthreads();
-      if (l < n)  // rows p, q of every pair: column l; and the eigenvectors: row l
-        for (int i = 0; i < np; ++i) {
-          const int pp = rp[i], q = rq[i];
-          if (q >= n || rs[i] == 0.0) continue;
-          const double c = rc[i], sn = rs[i];
-          const double apk = Aw[pp + n * l], aqk = Aw[q + n * l];
-          Aw[pp + n * l] = c * apk - sn * aqk;
-          Aw[q + n * l] = sn * apk + c * aqk;
-          const double vkp = Wv[l + n * pp], vkq = Wv[l + n * q];
-          Wv[l + n * pp] = c * vkp - sn * vkq;
-          Wv[l + n * q] = sn * vkp + c * vkq;
-        }
-      __syncthreads();
+      double *x = Acur;
+      Acur = Anext;
+      Anext = x;
+      x = Vcur;
+      Vcur = Vnext;
+      Vnext = x;
     }
   }
   // ascending order: rank of each eigenvalue (ties by index), then scatter
-  if (l < n) {
-    const double e = Aw[l + n * l];
+  if (tid < n) {
+    const double e = Acur[tid + n * tid];
     int rank = 0;
     for (int j = 0; j < n; ++j) {
-      const double f = Aw[j + n * j];
-      rank += (f < e) || (f == e && j < l);
+      const double f = Acur[j + n * j];
+      rank += (f < e) || (f == e && j < tid);
     }
     out[rank] = e;
-    for (int i = 0; i < n; ++i) out[n + i + (size_t)n * rank] = Wv[i + n * l];
+    for (int i = 0; i < n; ++i) out[n + i + (size_t)n * rank] = Vcur[i + n * tid];
   }
 }
 
@@ -682,11 +710,14 @@ struct Solver {
 
   // Rayleigh-Ritz of the leading n x n block of the device projected matrix,
   // on the device (k_rr); the result stays in rr until read back.
-  void rayleigh_ritz(int n) {
+  // nw > 0: the first nw basis columns are those of the previous call (no
+  // change of basis since), whose eigenvectors are still in rr.
+  void rayleigh_ritz(int n, int nw = 0) {
     SBDGB_REQUIRE(n >= 1 && n <= kRR, SBDGB_E_UNSUPPORTED, "projected matrix larger than 64");
-    const size_t smem = sizeof(double) * 2 * (size_t)n * n;
+    if (nw > n) nw = 0;
+    const size_t smem = sizeof(double) * 4 * (size_t)n * n;
     SBDGB_CUDA(cudaFuncSetAttribute(k_rr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    k_rr<<<1, kRR, smem, s>>>(hs, kRR, n, rr);
+    k_rr<<<1, kRRThreads, smem, s>>>(hs, kRR, n, nw, rr);
     count_launch(p.ctx);
     SBDGB_CUDA(cudaGetLastError());
   }
@@ -1108,6 +1139,7 @@ void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph
   std::vector<double> cprev;  // previous step's Ritz coefficients in the current basis (nvprev x kk)
   int nvprev = 0, kprev = 0;
   bool converged = false, rotated = false;  // rotated: the basis changed since the last Rayleigh-Ritz
+  int nv_rr = 0;  // basis size at the last Rayleigh-Ritz (its eigenvectors warm-start the next)
   int iter = 0, kk = 0;
   int max_steps = std::max(1, o.max_it) * max_nb;
   if (ph.step_cap > 0) max_steps = std::min(max_steps, ph.step_cap);
@@ -1116,7 +1148,8 @@ void davidson_core(Problem &p, const sbdgb_davidson_opts &o, const CorePhase &ph
     // Rayleigh-Ritz on the device projected matrix (FP64, on the GPU), then
     // the residual norms and preconditioned corrections from its result
     // (Ritz vectors not materialised); the eigenpairs come back with the norms
-    sv.rayleigh_ritz(nv);
+    sv.rayleigh_ritz(nv, rotated ? 0 : nv_rr);
+    nv_rr = nv;
     rotated = false;
     kk = std::min(k, nv);
     std::vector<double> rrh;

@@ -55,10 +55,23 @@ constexpr int kThreads = 128;
 template <int TA, int CPT, typename T, typename Wd, bool kFused, bool kB>
 __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
   constexpr int TB = kThreads * CPT;
-  const uint32_t tile = ldg(a.tile_order + blockIdx.x);
+  // Grid order.  Two sweeps: row tiles fastest (2-D grid), so that a column
+  // chunk's slab of C stays in L2 while the tiles gather from it.  Fused: one
+  // dimension with column chunks fastest, so that the CTAs of a row tile run
+  // together and the beta pairs' gathers along its C rows hit L2.
+  uint32_t bt, bc;
+  if constexpr (kFused) {
+    const uint32_t nch = (a.nb + TB - 1) / TB;
+    bt = blockIdx.x / nch;
+    bc = blockIdx.x - bt * nch;
+  } else {
+    bt = blockIdx.x;
+    bc = blockIdx.y;
+  }
+  const uint32_t tile = ldg(a.tile_order + bt);
   const uint32_t ia0 = ldg(a.tile_start + tile);
   const uint32_t rend = ldg(a.tile_start + tile + 1) - ia0;  // <= TA
-  const uint32_t ib0 = blockIdx.y * TB;
+  const uint32_t ib0 = bc * TB;
   uint32_t col[CPT], q0[CPT], q1[CPT];
   bool ok[CPT];
   Wd beta[CPT];
@@ -500,7 +513,7 @@ void launch_a_shape(const Problem &p, Args<T> a, cudaStream_t s) {
   constexpr int v = TA == 8 ? 0 : 1;
   a.tile_start = p.tile_start[0][v];
   a.tile_order = p.tile_order[0][v];
-  dim3 g(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
+  const dim3 g = F ? dim3(p.n_tiles[0][v] * ((p.nb + TB - 1) / TB)) : dim3(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
   if (kB || p.norb <= 32)
     k_sigma_alpha<TA, CPT, T, uint32_t, F, kB><<<g, kThreads, 0, s>>>(a);
   else
@@ -869,10 +882,19 @@ template <int TA, int CPT, int NV, typename Wd, bool kFused, bool kB>
 __global__ void __launch_bounds__(kThreads) k_sigma_alpha_mv(ArgsMV m) {
   const Args<float> &a = m.a;
   constexpr int TB = kThreads * CPT;
-  const uint32_t tile = ldg(a.tile_order + blockIdx.x);
+  uint32_t bt, bc;  // grid order as in k_sigma_alpha
+  if constexpr (kFused) {
+    const uint32_t nch = (a.nb + TB - 1) / TB;
+    bt = blockIdx.x / nch;
+    bc = blockIdx.x - bt * nch;
+  } else {
+    bt = blockIdx.x;
+    bc = blockIdx.y;
+  }
+  const uint32_t tile = ldg(a.tile_order + bt);
   const uint32_t ia0 = ldg(a.tile_start + tile);
   const uint32_t rend = ldg(a.tile_start + tile + 1) - ia0;
-  const uint32_t ib0 = blockIdx.y * TB;
+  const uint32_t ib0 = bc * TB;
   uint32_t col[CPT], q0[CPT], q1[CPT], d0[CPT], d1[CPT];
   bool ok[CPT];
   Wd beta[CPT];
@@ -1039,7 +1061,7 @@ void launch_a_mv_shape(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
   constexpr int v = TA == 8 ? 0 : 1;
   m.a.tile_start = p.tile_start[0][v];
   m.a.tile_order = p.tile_order[0][v];
-  dim3 g(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
+  const dim3 g = F ? dim3(p.n_tiles[0][v] * ((p.nb + TB - 1) / TB)) : dim3(p.n_tiles[0][v], (p.nb + TB - 1) / TB);
   if (kB || p.norb <= 32)
     k_sigma_alpha_mv<TA, CPT, NV, uint32_t, F, kB><<<g, kThreads, 0, s>>>(m);
   else

@@ -15,7 +15,9 @@
 // P_p, each (P|Q) value signed by its alpha single's phase, interleaved so that
 // the kG values of one column (of one pair Q) form one 16-byte vector.  Every
 // warp then walks the beta singles of 32 columns: per beta single one 16-byte
-// shared load of C values, one of (P|Q) values and kG multiply-adds.
+// shared load of C values, one of (P|Q) values and kG multiply-adds (one
+// instruction per term: the phase is applied to the (P|Q) value's sign bit,
+// which matters where the FP64 pipe is the bound).
 //
 // Beta singles layout (built once per problem, build_ab_order): the columns
 // sorted by decreasing single count, cut into slices of 32; in a slice, entry
@@ -108,20 +110,35 @@ __global__ void __launch_bounds__(kAbThreads) k_sigma_ab(Args<T> a, AbOrder o) {
       Ks[Q] = k;
     }
     __syncthreads();
-    for (uint32_t sl = warp; sl < o.nslices; sl += kAbWarps) {
+    // slices (longest first) dealt to the warps in snake order, so that every
+    // warp gets a similar share of entries before the next barrier
+    for (uint32_t base = 0; base < o.nslices; base += kAbWarps) {
+      const uint32_t round = base / kAbWarps;
+      const uint32_t sl = base + ((round & 1u) ? kAbWarps - 1u - warp : warp);
+      if (sl >= o.nslices) continue;
       const uint32_t e0 = ldg(o.slice + sl), e1 = ldg(o.slice + sl + 1);
       const uint32_t k = sl * 32u + lane;
       const uint32_t ib = k < a.nb ? ldg(o.cols + k) : 0u;
       T acc = T(0);
       if constexpr (kB) {
-        for (uint32_t e = e0 + lane; e < e1; e += 32u) {
+        // one multiply-add per term with the sign on the (P|Q) value; two
+        // entries per step so that two loads are in flight
+        uint32_t e = e0 + lane;
+        for (; e + 32u < e1; e += 64u) {
+          const uint32_t w0 = ldg(o.ent + e), w1 = ldg(o.ent + e + 32u);
+          const V k0 = Ks[(w0 >> 1) & 0xfffu], k1 = Ks[(w1 >> 1) & 0xfffu];
+          const V c0 = Cs[w0 >> 13], c1 = Cs[w1 >> 13];
+#pragma unroll
+          for (int g = 0; g < G; ++g) acc = fma(flip(k0.v[g], w0 & 1u), c0.v[g], acc);
+#pragma unroll
+          for (int g = 0; g < G; ++g) acc = fma(flip(k1.v[g], w1 & 1u), c1.v[g], acc);
+        }
+        if (e < e1) {
           const uint32_t w = ldg(o.ent + e);
           const V kv = Ks[(w >> 1) & 0xfffu];
           const V cv = Cs[w >> 13];
-          T t = kv.v[0] * cv.v[0];
 #pragma unroll
-          for (int g = 1; g < G; ++g) t = fma(kv.v[g], cv.v[g], t);
-          acc += flip(t, w & 1u);
+          for (int g = 0; g < G; ++g) acc = fma(flip(kv.v[g], w & 1u), cv.v[g], acc);
         }
       } else {
         const Wd bw = word<Wd>(a.bstr, ib);

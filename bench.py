@@ -399,6 +399,8 @@ def run_sigma_probe(a) -> int:
             out[f"sigma_mixed_block{nv}_ms_per_vector"] = ms_b / nv
     if a.davidson:
         for prec, name in ((0, "fp64"), (MIXED, "mixed")):
+            # an untimed solve first: it tunes the solver's sigma shapes
+            p.davidson(nroots=a.nroots, max_nb=max_nb, eps=eps, init=1, precision=prec, want_vectors=False)
             torch.cuda.synchronize()
             eng.enable_timing(True)
             eng.sigma_timing()

@@ -183,7 +183,9 @@ int sbdgb_problem_set_split(sbdgb_problem *p, int precision, int split);
  * is a file-scope device array of 2,097,152 doubles (16 MiB, held on every
  * device that loads the library until exit); larger problems return
  * SBDGB_E_UNSUPPORTED.  The first call on a device looks up the array's
- * address (make it before any stream capture).  All calls share the array:
+ * address (make it before any stream capture; no other entry point, table
+ * building and diagonal included, makes that lookup), and that address is
+ * kept for the process: do not call it again after resetting the device.  All calls share the array:
  * calls that overlap on the GPU race and must be serialised by the caller.
  * It uses the autotuned tile shapes when the problem has them, the default
  * shape otherwise, and records no timing events. */

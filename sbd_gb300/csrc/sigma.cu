@@ -52,6 +52,26 @@ constexpr int kThreads = 128;
 // added here too, reading row ia of C directly (per-thread pair lists, no
 // transposed copy); for sparse beta lists this replaces the transpose and the
 // beta sweep.
+// The diagonal operands of one element: hii (FP64; FP32 in .hi with .lo = 0
+// for the unshifted FP32 product, hi + lo otherwise) and C.
+template <typename T>
+using DiagOp = typename std::conditional<std::is_same<T, double>::value, double, dfloat>::type;
+template <typename T>
+__device__ __forceinline__ void load_diag(const Args<T> &a, size_t k, bool ok, DiagOp<T> &h, T &x) {
+  if (!ok) {
+    h = DiagOp<T>(0.0);
+    x = T(0);
+    return;
+  }
+  x = ldg(a.C + k);
+  if constexpr (std::is_same<T, double>::value)
+    h = ldg(a.hii + k);
+  else if constexpr (std::is_same<T, float>::value)
+    h = a.hii_f ? dfloat(ldg(a.hii_f + k), 0.f) : ldg(a.hii_df + k);
+  else
+    h = ldg(a.hii_df + k);
+}
+
 template <int TA, int CPT, typename T, typename Wd, bool kFused, bool kB>
 __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
   constexpr int TB = kThreads * CPT;
@@ -83,36 +103,68 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
     q0[c] = ok[c] ? ldg(a.B.off_s + col[c]) : 0u;
     q1[c] = ok[c] ? ldg(a.B.off_s + col[c] + 1) : 0u;
   }
-  uint32_t d0[kFused ? CPT : 1], d1[kFused ? CPT : 1];
+  // Fused: the beta doubles of this thread's columns are the same for every
+  // row; the first kPre of each column are held in registers (ket, value,
+  // mask), so that on each row their C gathers issue with the diagonal's
+  // loads instead of after a chain of table loads.
+  constexpr int kPre = 2;
+  constexpr int CF = kFused ? CPT : 1;
+  uint32_t d0[CF], d1[CF], pjb[CF][kPre];
+  T pval[CF][kPre];
+  Wd pmask[CF][kPre];
   if constexpr (kFused) {
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       d0[c] = ok[c] ? ldg(a.B.off_d + col[c]) : 0u;
       d1[c] = ok[c] ? ldg(a.B.off_d + col[c] + 1) : 0u;
+#pragma unroll
+      for (int u = 0; u < kPre; ++u) {
+        const bool has = d0[c] + u < d1[c];
+        pjb[c][u] = has ? ldg(a.B.ket_d + d0[c] + u) : 0u;
+        pval[c][u] = has ? ldg(a.val_db + d0[c] + u) : T(0);
+        pmask[c][u] = has ? mask_of<kB, Wd>(a.B.mask_d, d0[c] + u) : Wd(0);
+      }
     }
   }
+  DiagOp<T> hnext[CPT];
+  T cnext[CPT];
+#pragma unroll
+  for (int c = 0; c < CPT; ++c) load_diag(a, (size_t)ia0 * a.nb + col[c], ok[c], hnext[c], cnext[c]);
 #pragma unroll 1
   for (uint32_t r = 0; r < rend; ++r) {
     const uint32_t ia = ia0 + r;
     AccT<T> acc[CPT];
+    // the prefetched beta doubles' gathers along row ia, issued first
+    T xpre[CF][kPre];
+    if constexpr (kFused) {
+#pragma unroll
+      for (int c = 0; c < CPT; ++c)
+#pragma unroll
+        for (int u = 0; u < kPre; ++u)
+          xpre[c][u] = d0[c] + u < d1[c] ? ldg(a.C + (size_t)ia * a.nb + pjb[c][u]) : T(0);
+    }
     // diagonal term (mult.h:169-174): FP64, or hi/lo FP32 parts of the FP64
-    // diagonal in the mixed form
+    // diagonal in the mixed form.  Its operands were loaded one row ahead
+    // (hcur, ccur), and the next row's are requested now, so that each thread
+    // has two rows' streaming loads in flight.
+    DiagOp<T> hcur[CPT];
+    T ccur[CPT];
 #pragma unroll
     for (int c = 0; c < CPT; ++c) {
-      const size_t k = (size_t)ia * a.nb + col[c];
+      hcur[c] = hnext[c];
+      ccur[c] = cnext[c];
+      if (r + 1 < rend) load_diag(a, (size_t)(ia + 1) * a.nb + col[c], ok[c], hnext[c], cnext[c]);
       acc_zero(acc[c]);
       if (ok[c]) {
         if constexpr (std::is_same<T, double>::value) {
-          acc[c] = ldg(a.hii + k) * ldg(a.C + k);  // the FP64 form has no shift: one FP64 op
+          acc[c] = hcur[c] * ccur[c];  // the FP64 form has no shift: one FP64 op
         } else if constexpr (std::is_same<T, float>::value) {
-          if (a.hii_f) {
-            acc[c] = ff_prod(ldg(a.hii_f + k), ldg(a.C + k));
-          } else {
-            const dfloat h = ldg(a.hii_df + k);
-            acc[c] = ff_diag(h.hi, h.lo, a.shift_df.hi, a.shift_df.lo, ldg(a.C + k));
-          }
+          if (a.hii_f)
+            acc[c] = ff_prod(hcur[c].hi, ccur[c]);
+          else
+            acc[c] = ff_diag(hcur[c].hi, hcur[c].lo, a.shift_df.hi, a.shift_df.lo, ccur[c]);
         } else {
-          acc[c] = (ldg(a.hii_df + k) - a.shift_df) * ldg(a.C + k);
+          acc[c] = (hcur[c] - a.shift_df) * ccur[c];
         }
       }
     }
@@ -156,7 +208,10 @@ __global__ void __launch_bounds__(kThreads) k_sigma_alpha(Args<T> a) {
           const T j = ldg(a.Ja + (size_t)((cb >> 16) & 0x7fffu) * a.na + ia);
           madd(acc[c], part[c], flip(ldg(a.val_sb + q) + j, ph), ldg(crow_a + jb));
         }
-        for (uint32_t q = d0[c]; q < d1[c]; ++q) {
+#pragma unroll
+        for (int u = 0; u < kPre; ++u)
+          if (d0[c] + u < d1[c]) madd(acc[c], part[c], flip(pval[c][u], par<kB>(arow & pmask[c][u])), xpre[c][u]);
+        for (uint32_t q = d0[c] + kPre; q < d1[c]; ++q) {
           const uint32_t jb = ldg(a.B.ket_d + q);
           madd(acc[c], part[c], flip(ldg(a.val_db + q), par<kB>(arow & mask_of<kB, Wd>(a.B.mask_d, q))),
                ldg(crow_a + jb));

@@ -32,7 +32,10 @@ std::mutex g_mu;
 double *g_scratch_on[kMaxDevices] = {};
 
 // Device address of the scratch on the current device, looked up once per
-// device (with that device current) and cached.
+// device (with that device current) and cached.  The cache belongs to the
+// device's primary context as it was at that first call: a caller that
+// resets the device (cudaDeviceReset) must not call this entry point again in
+// the same process.
 double *scratch_address() {
   int dev = 0;
   SBDGB_CUDA(cudaGetDevice(&dev));

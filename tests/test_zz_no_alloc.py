@@ -62,6 +62,39 @@ def test_noalloc_sigma_matches_regular_sigma():
     eng.close()
 
 
+@pytest.mark.parametrize("shapes,split", [((1, 1), 0), ((1, 4), 0), ((0, 5), 0), ((1, 1), 1), ((1, 4), 1)])
+def test_noalloc_sigma_in_every_kind_of_shape(shapes, split):
+    """The allocation-free sigma follows the problem's tuned shapes: two sweeps
+    on the transposed copy (the scratch in use), the fused kernel and the
+    sparse-row kernel (no transposed copy), with and without the alpha x beta
+    kernel; each against the regular sigma in the same shapes."""
+    torch = pytest.importorskip("torch")
+    from sbd_gb300.engine import Engine, TPBProblem
+    from sbd_gb300.generators import make_problem
+
+    eng = Engine(0)
+    prob = make_problem(12, 4, 4, 200, 190, seed=78)
+    p = TPBProblem.from_problem(eng, prob)
+    p.build_tables()
+    p.diag_terms()
+    p.set_tuning(0, *shapes)
+    p.set_split(0, split)
+    f = _entry(eng.lib)
+    rng = np.random.default_rng(12)
+    C1 = torch.tensor(rng.uniform(-1, 1, prob.ndet), dtype=torch.float64, device="cuda")
+    before = eng.bytes_in_use
+    s = torch.full_like(C1, float("nan"))
+    assert f(p.h, C1.data_ptr(), s.data_ptr(), 0, None) == 0, eng.lib.sbdgb_last_error(eng.h)
+    torch.cuda.synchronize()
+    assert eng.bytes_in_use == before
+    ref = torch.zeros_like(C1)
+    p.sigma_device(C1.data_ptr(), ref.data_ptr(), accumulate=False, stream=0)
+    torch.cuda.synchronize()
+    assert max_rel(s.cpu().numpy(), ref.cpu().numpy()) <= 1e-12
+    p.close()
+    eng.close()
+
+
 def test_noalloc_sigma_rejects_large_problems():
     torch = pytest.importorskip("torch")
     from sbd_gb300.engine import Engine, TPBProblem

@@ -45,6 +45,18 @@ void *dev_alloc(Problem &p, size_t bytes) {
   return d;
 }
 
+void ensure_dynamic_smem(const void *kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> set;
+  int dev = 0;
+  SBDGB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &have = set[{dev, kernel}];
+  if (bytes <= have) return;
+  SBDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  have = bytes;
+}
+
 void *workspace(Problem &p, int slot, size_t bytes) {
   if (bytes == 0) bytes = 8;
   if (p.ws[slot] && p.ws_bytes[slot] >= bytes) return p.ws[slot];

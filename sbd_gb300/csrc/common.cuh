@@ -207,6 +207,12 @@ double *pinned_buffer(Ctx *c);
 cudaEvent_t timing_event(Ctx *c);
 
 void *dev_alloc(Problem &p, size_t bytes);
+// Raises a kernel's dynamic shared-memory limit on the current device to at
+// least `bytes`, never lowering it.  The limit belongs to the function, not to
+// a context or a stream: serving workers run problems of different sizes on
+// concurrent threads, and one that set a smaller limit between another's
+// setting and launch made that launch fail.
+void ensure_dynamic_smem(const void *kernel, size_t bytes);
 // Temporary device buffer outside the problem's accounting (pool-aware).
 void *tmp_alloc(Ctx *c, size_t bytes);
 void tmp_free(Ctx *c, void *d);

@@ -716,7 +716,7 @@ struct Solver {
     SBDGB_REQUIRE(n >= 1 && n <= kRR, SBDGB_E_UNSUPPORTED, "projected matrix larger than 64");
     if (nw > n) nw = 0;
     const size_t smem = sizeof(double) * 4 * (size_t)n * n;
-    SBDGB_CUDA(cudaFuncSetAttribute(k_rr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ensure_dynamic_smem((const void *)k_rr, smem);
     k_rr<<<1, kRRThreads, smem, s>>>(hs, kRR, n, nw, rr);
     count_launch(p.ctx);
     SBDGB_CUDA(cudaGetLastError());

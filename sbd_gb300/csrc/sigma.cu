@@ -1133,11 +1133,11 @@ void launch_b_mv_shape(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
   const size_t smem = sizeof(FF) * NV * TA * TB;
   if (kB || p.norb <= 32) {
     auto k = k_sigma_beta_mv<TA, CPT, NV, uint32_t, kB>;
-    SBDGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ensure_dynamic_smem((const void *)k, smem);
     k<<<g, kThreads, smem, s>>>(m);
   } else {
     auto k = k_sigma_beta_mv<TA, CPT, NV, unsigned long long, kB>;
-    SBDGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    ensure_dynamic_smem((const void *)k, smem);
     k<<<g, kThreads, smem, s>>>(m);
   }
 }

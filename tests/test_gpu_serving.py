@@ -123,3 +123,32 @@ def test_small_requests_are_batched(alone):
     for (p, k), r, a in zip(mix, res, alone):
         assert r["status"] == 0, r["message"]
         assert abs(r["energies"][0] - a.energies[0]) <= 1e-10
+
+
+def test_concurrent_solves_of_different_sizes_all_converge():
+    """Requests above the batching threshold run concurrently on separate
+    workers, each with its own row length, so their kernels ask for different
+    amounts of dynamic shared memory at the same time (the alpha x beta kernel,
+    the Rayleigh-Ritz kernel).  Every request converges to its lone result."""
+    from sbd_gb300.engine import Engine, TPBProblem
+    from sbd_gb300.generators import make_problem
+    from sbd_gb300.serving import Server
+    specs = [(16, 5, 620, 560), (16, 5, 700, 650), (16, 5, 560, 900), (18, 6, 820, 480), (16, 5, 900, 500),
+             (18, 6, 600, 700), (16, 5, 760, 610), (18, 6, 950, 420)]
+    mix = [make_problem(L, n, n, na, nb, seed=700 + i) for i, (L, n, na, nb) in enumerate(specs)]
+    assert min(p.ndet for p in mix) > 300000  # above the batching threshold: one solve per worker
+    eng = Engine(0)
+    lone = []
+    for p in mix:
+        t = TPBProblem.from_problem(eng, p)
+        lone.append(t.davidson(nroots=1, eps=1e-8, max_nb=20, init=1, want_vectors=False).energies)
+        t.close()
+    eng.close()
+    with Server(0, workers=8) as srv:
+        tickets = [srv.submit_problem(p, nroots=1, eps=1e-8, max_nb=20, init=1) for p in mix]
+        res = [srv.wait(t, timeout=600) for t in tickets]
+        st = srv.stats()
+    assert st["failed"] == 0 and st["peak_running"] >= 2
+    for r, e in zip(res, lone):
+        assert r["status"] == 0 and r["converged"], r["message"]
+        assert abs(r["energies"][0] - e[0]) <= 1e-8

@@ -147,18 +147,22 @@ int sbdgb_sigma_mixed_block(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev
  * transposed copy; chosen when that is faster, typically for short beta lists);
  * shape_b = 5 means the single streaming kernel for sparse rows (16-byte
  * accesses along beta, every task type in one pass), with shape_a 0 or 1 for
- * row tiles of 8 or 16 rows (chosen for problems with a few nonzeros per row).
+ * row tiles of 8 or 16 rows (chosen for problems with a few nonzeros per row);
+ * shape_b = 6 is the streaming kernel whose beta pairs are taken per warp
+ * (sigma_stream.cu), shape_a 0 or 1 likewise.
  * The first product of each precision tunes (and synchronises), so make it
  * before any stream capture. */
 int sbdgb_problem_tuning(const sbdgb_problem *p, int precision, int *shape_a, int *shape_b, float *ms_a,
                          float *ms_b, int n_shapes);
 /* The autotuner's times (ms, 0 where not measured) of the fused kernel in
- * shapes 0..3 (ms_fused[4]) and of the sparse-row kernel with 8 and 16 rows
- * per tile (ms_sparse[2]); either pointer may be NULL. */
-int sbdgb_problem_tuning_times(const sbdgb_problem *p, int precision, float *ms_fused, float *ms_sparse);
+ * shapes 0..3 (ms_fused[4]), of the sparse-row kernel (ms_sparse[2]) and of
+ * the per-warp streaming kernel (ms_stream[2]) with 8 and 16 rows per tile;
+ * any pointer may be NULL. */
+int sbdgb_problem_tuning_times(const sbdgb_problem *p, int precision, float *ms_fused, float *ms_sparse,
+                               float *ms_stream);
 /* Sets the sigma tile shapes of one precision instead of the autotuner's
- * choice (shape_a 0..3 with shape_b 0..4, or shape_a 0..1 with shape_b 5, as
- * above); results do not depend on it beyond the order of floating-point sums. */
+ * choice (shape_a 0..3 with shape_b 0..4, or shape_a 0..1 with shape_b 5 or 6,
+ * as above); results do not depend on it beyond the order of floating-point sums. */
 int sbdgb_problem_set_tuning(sbdgb_problem *p, int precision, int shape_a, int shape_b);
 /* Whether the alpha x beta single pairs of sigma (task type 0) run in a kernel
  * of their own (split = 1: the tuned shapes skip them and a kernel that stages

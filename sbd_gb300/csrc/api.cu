@@ -114,7 +114,7 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
   // strings, h1, (P|Q)
   b += 8 * (na + nb) + 8 * L * L + 8 * npair * npair;
   // tables: per spin four offset arrays, 24 bytes per entry; (pp|qq), (pq|qp), Coulomb rows
-  b += 16 * (na + nb + 2) + 16 + 24 * (entries_a + entries_b) + 16 * L * L + 8 * npair * (na + nb);
+  b += 16 * (na + nb + 2) + 16 + 28 * (entries_a + entries_b) + 16 * L * L + 8 * npair * (na + nb);
   b += 16 * (na + nb + 4);  // sigma row tiles (two row caps, start + order per spin)
   // diagonal and its workspaces
   b += 8 * N + 8 * (na + nb + 2) + 8 * (na * L + 1);
@@ -122,6 +122,7 @@ size_t solve_footprint(int norb, size_t na, size_t nb, const sbdgb_davidson_opts
   // 12 bytes per beta single in slices of 32 (padding at most 31 x the
   // longest list, itself at most L^2 / 4 singles)
   b += 4 * (na + nb) + 4 * (nb / 32 + 2) + 12 * (entries_b + 32 * (L * L / 4 + 1));
+  b += 16 * (entries_b + 32 * (nb + 1)) + 4 * na;  // the row kernel's beta pair list (padded) and row order
   // FP64 sigma transpose scratch (also used by the mixed refinement)
   b += 8 * N;
   // solver reductions (partial sums of at most 4 blocks per SM of 64 values, staging)
@@ -457,19 +458,22 @@ int sbdgb_problem_tuning(const sbdgb_problem *pr, int precision, int *shape_a, i
   return SBDGB_OK;
 }
 
-int sbdgb_problem_tuning_times(const sbdgb_problem *pr, int precision, float *ms_fused, float *ms_sparse) {
+int sbdgb_problem_tuning_times(const sbdgb_problem *pr, int precision, float *ms_fused, float *ms_sparse,
+                               float *ms_stream) {
   if (!pr || precision < 0 || precision > 5) return SBDGB_E_INPUT;
   const sbdgb::Problem &p = pr->p;
   for (int i = 0; i < 4; ++i)
     if (ms_fused) ms_fused[i] = p.tune_ms[precision][2][i];
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < 2; ++i) {
     if (ms_sparse) ms_sparse[i] = p.tune_ms[precision][2][4 + i];
+    if (ms_stream) ms_stream[i] = p.tune_ms[precision][2][6 + i];
+  }
   return SBDGB_OK;
 }
 
 int sbdgb_problem_set_tuning(sbdgb_problem *pr, int precision, int shape_a, int shape_b) {
   if (!pr || precision < 0 || precision > 5) return SBDGB_E_INPUT;
-  if (shape_a < 0 || shape_a > 3 || shape_b < 0 || shape_b > 5 || (shape_b == 5 && shape_a > 1)) return SBDGB_E_INPUT;
+  if (shape_a < 0 || shape_a > 3 || shape_b < 0 || shape_b > 6 || (shape_b >= 5 && shape_a > 1)) return SBDGB_E_INPUT;
   pr->p.tune_a[precision] = shape_a;
   pr->p.tune_b[precision] = shape_b;
   return SBDGB_OK;

@@ -85,6 +85,7 @@ struct SpinTables {
   uint32_t *code_s = nullptr, *code_d = nullptr;
   double *val_s = nullptr, *val_d = nullptr;
   uint64_t *mask_s = nullptr, *mask_d = nullptr;
+  uint32_t *bra_s = nullptr, *bra_d = nullptr;  // bra string of each entry (the CSR row, flattened)
 };
 
 struct SigmaArgs {
@@ -165,6 +166,12 @@ struct Problem {
   uint32_t *ab_rows = nullptr, *ab_cols = nullptr, *ab_slice = nullptr, *ab_ent = nullptr;
   uint64_t *ab_mask = nullptr;
   uint32_t n_ab_rows = 0, n_ab_slices = 0;
+  // the row kernel for sparse rows (sigma_stream.cu): every beta pair in
+  // column order, runs padded not to cross 32 entries, and its row order
+  uint4 *rp_ent = nullptr;
+  uint32_t *rp_rows = nullptr;
+  uint32_t rp_n = 0, rp_maxrun = 0;
+  bool rp_ready = false;
   size_t bytes = 0;
   std::vector<void *> allocs;
   // host copies of strings
@@ -242,6 +249,13 @@ template <typename T>
 bool ab_fits(const Problem &p);
 void build_ab_order(Problem &p, const std::vector<uint32_t> &off_a, const std::vector<uint32_t> &off_b,
                     cudaStream_t s);
+// sigma_stream.cu: the row kernel's beta pair list (off_s, off_d: host copies
+// of the beta tables' offsets; rows: the order the CTAs take the alpha rows),
+// and whether the kernel fits this problem in element type T.
+void build_row_pairs(Problem &p, const std::vector<uint32_t> &off_s, const std::vector<uint32_t> &off_d,
+                     const std::vector<uint32_t> &rows, cudaStream_t s);
+template <typename T>
+bool rows_fit(const Problem &p);
 // block: the block-ordering product (H_block = eta H eta, no opposite-spin
 // parities) that the solvers use on eta-signed vectors; false: the
 // reference's interleaved convention.

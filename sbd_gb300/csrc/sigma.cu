@@ -298,40 +298,6 @@ __global__ void __launch_bounds__(kThreads) k_sigma_beta(Args<T> a) {
 // Rows are unrolled (TA accumulators per column live in registers).  FP32
 // (mixed form): FP32 products and partial sums, float-float accumulation per
 // element, no FP64 instruction.
-template <int VW, typename T>
-__device__ __forceinline__ void load_v(const T *__restrict__ p, T (&x)[VW]) {
-  static_assert(VW == 1 || sizeof(T) * VW == 8 || sizeof(T) * VW == 16 || sizeof(T) * VW == 32,
-                "vector loads of 8, 16 or 32 bytes");
-  if constexpr (VW == 1) {
-    x[0] = ldg(p);
-  } else if constexpr (sizeof(T) * VW == 32) {  // the double-float diagonal of four FP32 columns
-    const uint4 u0 = ldg(reinterpret_cast<const uint4 *>(p)), u1 = ldg(reinterpret_cast<const uint4 *>(p) + 1);
-    memcpy(x, &u0, 16);
-    memcpy(reinterpret_cast<char *>(x) + 16, &u1, 16);
-  } else if constexpr (sizeof(T) * VW == 16) {
-    const uint4 u = ldg(reinterpret_cast<const uint4 *>(p));
-    memcpy(x, &u, 16);
-  } else {
-    const uint2 u = ldg(reinterpret_cast<const uint2 *>(p));
-    memcpy(x, &u, 8);
-  }
-}
-template <int VW, typename T>
-__device__ __forceinline__ void store_v(T *__restrict__ p, const T (&x)[VW]) {
-  static_assert(VW == 1 || sizeof(T) * VW == 8 || sizeof(T) * VW == 16, "vector stores of 8 or 16 bytes");
-  if constexpr (VW == 1) {
-    *p = x[0];
-  } else if constexpr (sizeof(T) * VW == 16) {
-    uint4 u;
-    memcpy(&u, x, 16);
-    *reinterpret_cast<uint4 *>(p) = u;
-  } else {
-    uint2 u;
-    memcpy(&u, x, 8);
-    *reinterpret_cast<uint2 *>(p) = u;
-  }
-}
-
 template <int RG, int VW, typename T, typename Wd, bool kB>
 __device__ __forceinline__ void sparse_rows(const Args<T> &a, uint32_t ia0, uint32_t nr, uint32_t c0,
                                             const Wd (&beta)[VW], const uint32_t (&q0)[VW],
@@ -556,7 +522,10 @@ constexpr int kNumShapes = 4;
 constexpr int kFusedShape = 4;   // tune_b value meaning "beta sweep fused into kernel A"
 constexpr int kSparseShape = 5;  // tune_b value meaning "k_sigma_sparse"; tune_a 0/1 = 8/16 rows per tile
 constexpr int kNumSparse = 2;
-inline bool needs_transpose(int shape_b) { return shape_b != kFusedShape && shape_b != kSparseShape; }
+constexpr int kStreamShape = 6;  // tune_b value meaning "k_sigma_stream"; tune_a 0/1 = 8/16 rows per tile
+inline bool needs_transpose(int shape_b) {
+  return shape_b != kFusedShape && shape_b != kSparseShape && shape_b != kStreamShape;
+}
 constexpr int kShapeTA[kNumShapes] = {8, 8, 8, 16};
 constexpr int kShapeCPT[kNumShapes] = {1, 2, 4, 2};
 
@@ -643,6 +612,16 @@ void launch_b(const Problem &p, const Args<T> &a, int shape, cudaStream_t s) {
   }
 }
 
+// The row kernel when its pair list fits the problem, the sparse-row kernel
+// otherwise (same results up to the order of floating-point sums).
+template <typename T, bool kB>
+void launch_stream_or_sparse(const Problem &p, const Args<T> &a, int variant, cudaStream_t s) {
+  if (rows_fit<T>(p))
+    launch_stream<T, kB>(p, a, variant, s);
+  else
+    launch_sparse<T, kB>(p, a, variant, s);
+}
+
 // One product in shapes (sa, sb) on a transposed copy already made when the
 // shapes need one; with split > 0 those kernels skip the alpha x beta single
 // pairs and k_sigma_ab adds them afterwards.
@@ -652,6 +631,9 @@ void launch_shapes(Problem &p, const Args<T> &a, int sa, int sb, int split, cuda
   b.skip_ab = split > 0 ? 1 : 0;
   if (sb == kSparseShape) {
     launch_sparse<T, kB>(p, b, sa, s);
+    count_launch(p.ctx, 1);
+  } else if (sb == kStreamShape) {
+    launch_stream_or_sparse<T, kB>(p, b, sa, s);
     count_launch(p.ctx, 1);
   } else if (sb == kFusedShape) {
     launch_fused<T, kB>(p, b, sa, s);
@@ -768,7 +750,30 @@ void autotune(Problem &p, Args<T> a, cudaStream_t s) {
       best_ss = sh;
     }
   }
-  if (best_s < two_kernels && best_s <= best_f) {
+  // the streaming kernel for sparse rows (per-warp beta pairs)
+  float best_t = 1e30f;
+  int best_ts = 0;
+  for (int sh = 0; sh < kNumSparse && rows_fit<T>(p); ++sh) {
+    for (int rep = 0; rep < 2; ++rep) {
+      SBDGB_CUDA(cudaEventRecord(e0, s));
+      launch_stream<T, kB>(p, a, sh, s);
+      SBDGB_CUDA(cudaEventRecord(e1, s));
+      count_launch(p.ctx);
+    }
+    SBDGB_CUDA(cudaGetLastError());
+    SBDGB_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    SBDGB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    p.tune_ms[prec][2][kNumShapes + kNumSparse + sh] = ms;
+    if (ms < best_t) {
+      best_t = ms;
+      best_ts = sh;
+    }
+  }
+  if (best_t < two_kernels && best_t <= best_f && best_t <= best_s) {
+    p.tune_a[prec] = best_ts;
+    p.tune_b[prec] = kStreamShape;
+  } else if (best_s < two_kernels && best_s <= best_f) {
     p.tune_a[prec] = best_ss;
     p.tune_b[prec] = kSparseShape;
   } else if (best_f < two_kernels) {
@@ -829,7 +834,7 @@ bool needs_tuning(Problem &p) {
       (ab_fits<T>(p) && (double)p.A.ns * (double)p.B.ns >= kAbSplitPerElement * (double)p.N) ? 1 : 0;
   if (nnz_per_row(p) <= 8.0) {
     p.tune_a[prec] = 0;
-    p.tune_b[prec] = kSparseShape;
+    p.tune_b[prec] = rows_fit<T>(p) ? kStreamShape : kSparseShape;
     return false;
   }
   p.tune_a[prec] = size_shape(p.nb);
@@ -1174,12 +1179,15 @@ void launch_mv(const Problem &p, const ArgsMV &mv, cudaStream_t s) {
   const bool split = p.split_ab[ts] > 0;
   ArgsMV m = mv;
   m.a.skip_ab = split ? 1 : 0;
-  if (p.tune_b[ts] == kSparseShape) {  // a stream per vector: nothing to share between vectors
+  if (p.tune_b[ts] == kSparseShape || p.tune_b[ts] == kStreamShape) {  // one stream per vector
     for (int n = 0; n < NV; ++n) {
       Args<float> a = m.a;
       a.C = m.Cv[n];
       a.S = m.Sv[n];
-      launch_sparse<float, kB>(p, a, p.tune_a[ts], s);
+      if (p.tune_b[ts] == kSparseShape)
+        launch_sparse<float, kB>(p, a, p.tune_a[ts], s);
+      else
+        launch_stream_or_sparse<float, kB>(p, a, p.tune_a[ts], s);
     }
   } else if (p.tune_b[ts] == kFusedShape) {
     launch_a_mv<NV, true, kB>(p, m, p.tune_a[ts], s);
@@ -1341,6 +1349,13 @@ void build_row_tiles(Problem &p, cudaStream_t s) {
     }
   }
   build_ab_order(p, os[0], os[1], s);
+  {  // the row kernel: rows with the most alpha pairs first
+    std::vector<uint32_t> rows(p.na);
+    for (uint32_t r = 0; r < p.na; ++r) rows[r] = r;
+    auto w = [&](uint32_t r) { return os[0][r + 1] - os[0][r] + od[0][r + 1] - od[0][r]; };
+    std::stable_sort(rows.begin(), rows.end(), [&](uint32_t x, uint32_t y) { return w(x) > w(y); });
+    build_row_pairs(p, os[1], od[1], rows, s);
+  }
   SBDGB_CUDA(cudaStreamSynchronize(s));  // the host vectors go out of scope
 }
 
@@ -1530,7 +1545,8 @@ void sigma_mixed_multi_impl(Problem &p, const float *C, float *S, int nvec, cuda
     default: launch_mv<4, kB>(p, m, s); break;
   }
   end_timing(p, s, ev0, ev1);
-  count_launch(p.ctx, p.tune_b[ts] == kSparseShape ? nvec : fused ? 1 : 2);  // (k_sigma_ab counts its own)
+  count_launch(p.ctx, (p.tune_b[ts] == kSparseShape || p.tune_b[ts] == kStreamShape) ? nvec : fused ? 1 : 2);
+  // (k_sigma_ab counts its own launches)
   SBDGB_CUDA(cudaGetLastError());
 }
 }  // namespace

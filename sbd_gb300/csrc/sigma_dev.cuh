@@ -162,6 +162,41 @@ __device__ __forceinline__ void madd(double &acc, double &, double v, double x) 
 __device__ __forceinline__ void madd(dfloat &acc, dfloat &, dfloat v, dfloat x) { acc = fma(v, x, acc); }
 __device__ __forceinline__ void madd(FF &, float &part, float v, float x) { part = fmaf(v, x, part); }
 
+// Vector loads and stores of VW consecutive elements (8, 16 or 32 bytes).
+template <int VW, typename T>
+__device__ __forceinline__ void load_v(const T *__restrict__ p, T (&x)[VW]) {
+  static_assert(VW == 1 || sizeof(T) * VW == 8 || sizeof(T) * VW == 16 || sizeof(T) * VW == 32,
+                "vector loads of 8, 16 or 32 bytes");
+  if constexpr (VW == 1) {
+    x[0] = ldg(p);
+  } else if constexpr (sizeof(T) * VW == 32) {  // the double-float diagonal of four FP32 columns
+    const uint4 u0 = ldg(reinterpret_cast<const uint4 *>(p)), u1 = ldg(reinterpret_cast<const uint4 *>(p) + 1);
+    memcpy(x, &u0, 16);
+    memcpy(reinterpret_cast<char *>(x) + 16, &u1, 16);
+  } else if constexpr (sizeof(T) * VW == 16) {
+    const uint4 u = ldg(reinterpret_cast<const uint4 *>(p));
+    memcpy(x, &u, 16);
+  } else {
+    const uint2 u = ldg(reinterpret_cast<const uint2 *>(p));
+    memcpy(x, &u, 8);
+  }
+}
+template <int VW, typename T>
+__device__ __forceinline__ void store_v(T *__restrict__ p, const T (&x)[VW]) {
+  static_assert(VW == 1 || sizeof(T) * VW == 8 || sizeof(T) * VW == 16, "vector stores of 8 or 16 bytes");
+  if constexpr (VW == 1) {
+    *p = x[0];
+  } else if constexpr (sizeof(T) * VW == 16) {
+    uint4 u;
+    memcpy(&u, x, 16);
+    *reinterpret_cast<uint4 *>(p) = u;
+  } else {
+    uint2 u;
+    memcpy(&u, x, 8);
+    *reinterpret_cast<uint2 *>(p) = u;
+  }
+}
+
 // Same-spin excitations of one row applied to this thread's CPT columns.
 // In: ket-major input rows (ld = ldin); Jo: opposite-spin Coulomb table
 // [npair][ldj] for the single excitations.  Element offsets are 32-bit
@@ -260,5 +295,9 @@ __device__ __forceinline__ void same_spin_row(const SpinTables &Tb, const T *__r
 // into a.S (block: the block ordering's phases).
 template <typename T>
 void launch_ab(const Problem &p, const sdev::Args<T> &a, bool block, cudaStream_t s);
+// sigma_stream.cu: the streaming kernel for problems with few nonzeros per row
+// (every task type in one pass; variant 0/1 = row tiles of 8/16 rows).
+template <typename T, bool kB>
+void launch_stream(const Problem &p, const sdev::Args<T> &a, int variant, cudaStream_t s);
 
 }  // namespace sbdgb

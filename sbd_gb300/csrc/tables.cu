@@ -11,6 +11,8 @@
 // the pair that does not depend on the opposite-spin string: the same-spin
 // phase, the opposite-spin phase mask and the integral part of the matrix
 // element (see SpinTables in common.cuh).
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace sbdgb {
@@ -199,6 +201,13 @@ __global__ void k_fill(FillArgs a) {
 // Jo[P][i] = sum_{q occupied in strs[i]} (P|qq): the opposite-spin Coulomb
 // part of the single-excitation elements (OneExcite terms with j of the other
 // spin, whose exchange integral vanishes by spin).
+// bra[e] = i for the entries e of CSR row i (the row of every entry, for
+// kernels that walk entries rather than rows).
+__global__ void k_bra_index(const uint32_t *__restrict__ off, uint32_t n, uint32_t *__restrict__ bra) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    for (uint32_t e = off[i]; e < off[i + 1]; ++e) bra[e] = i;
+}
+
 __global__ void k_opp_coulomb(const uint64_t *__restrict__ strs, uint32_t n, const double *__restrict__ Kp,
                               int npair, double *__restrict__ Jo) {
   const int P = blockIdx.y;
@@ -251,7 +260,12 @@ void build_spin(Problem &p, int spin, cudaStream_t s) {
   FillArgs fa{strs, n, spin, p.norb, p.npair, p.Kp, p.h1, T.off_s, T.off_d, T.ket_s, T.ket_d,
               T.code_s, T.code_d, T.val_s, T.val_d, T.mask_s, T.mask_d};
   k_fill<<<blocks, threads, 0, s>>>(fa);
-  count_launch(p.ctx);
+  T.bra_s = (uint32_t *)dev_alloc(p, sizeof(uint32_t) * ns1);
+  T.bra_d = (uint32_t *)dev_alloc(p, sizeof(uint32_t) * nd1);
+  const unsigned bb = (unsigned)std::min<uint32_t>((n + 255) / 256 + 1, 4096);
+  k_bra_index<<<bb, 256, 0, s>>>(T.off_s, n, T.bra_s);
+  k_bra_index<<<bb, 256, 0, s>>>(T.off_d, n, T.bra_d);
+  count_launch(p.ctx, 3);
   SBDGB_CUDA(cudaGetLastError());
 }
 

@@ -123,7 +123,8 @@ def load(path: str = LIB_PATH):
     L.sbdgb_mult_host.argtypes = [vp, vp, _f64p, _f64p]
     L.sbdgb_problem_tuning.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                        C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int]
-    L.sbdgb_problem_tuning_times.argtypes = [vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float)]
+    L.sbdgb_problem_tuning_times.argtypes = [vp, C.c_int, C.POINTER(C.c_float), C.POINTER(C.c_float),
+                                             C.POINTER(C.c_float)]
     L.sbdgb_problem_split.argtypes = [vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_float)]
     L.sbdgb_problem_set_split.argtypes = [vp, C.c_int, C.c_int]
     L.sbdgb_problem_set_tuning.argtypes = [vp, C.c_int, C.c_int, C.c_int]
@@ -313,15 +314,16 @@ class TPBProblem:
         a, b = C.c_int(-1), C.c_int(-1)
         ma, mb = (C.c_float * 4)(), (C.c_float * 4)()
         self.engine.check(self.lib.sbdgb_problem_tuning(self.h, precision, C.byref(a), C.byref(b), ma, mb, 4))
-        mf, ms = (C.c_float * 4)(), (C.c_float * 2)()
-        self.engine.check(self.lib.sbdgb_problem_tuning_times(self.h, precision, mf, ms))
-        shapes = ["8x128", "8x256", "8x512", "16x256", "fused", "sparse"]
+        mf, ms, mt = (C.c_float * 4)(), (C.c_float * 2)(), (C.c_float * 2)()
+        self.engine.check(self.lib.sbdgb_problem_tuning_times(self.h, precision, mf, ms, mt))
+        shapes = ["8x128", "8x256", "8x512", "16x256", "fused", "sparse", "stream"]
         alpha = shapes[a.value] if a.value >= 0 else None
-        if b.value == 5:
+        if b.value >= 5:
             alpha = ["8 rows", "16 rows"][a.value]
         return {"alpha_shape": alpha, "beta_shape": shapes[b.value] if b.value >= 0 else None,
                 "alpha_ms": [round(x, 4) for x in ma], "beta_ms": [round(x, 4) for x in mb],
                 "fused_ms": [round(x, 4) for x in mf], "sparse_ms": [round(x, 4) for x in ms],
+                "stream_ms": [round(x, 4) for x in mt],
                 "alpha_beta": self.split(precision)}
 
     def set_tuning(self, precision: int, shape_a: int, shape_b: int):

@@ -144,13 +144,19 @@ def run_batch(reqs, cfg: int, chunk: int, precision: int = 0):
 def summarize(results, wall, st, ref_E, precision, rate):
     lat = [r["total_seconds"] for r in results]
     failed = [r for r in results if r["status"] != 0]
-    dE = 0.0
+    dE, compared, nonfinite = 0.0, 0, 0
     for r, e in zip(results, ref_E):
         if r["status"] == 0 and e is not None:
-            dE = max(dE, float(np.max(np.abs(r["energies"] - e))))
+            d = np.abs(np.asarray(r["energies"], dtype=np.float64) - np.asarray(e, dtype=np.float64))
+            if not np.all(np.isfinite(d)):
+                nonfinite += 1  # counted, never silently dropped by max()
+                continue
+            dE = max(dE, float(np.max(d)))
+            compared += 1
     return {"precision": "mixed" if precision else "fp64", "rate": "inf" if math.isinf(rate) else rate,
             "requests": len(results), "wall_s": wall, "solves_per_s": len(results) / wall,
-            "p50_s": pct(lat, 50), "p99_s": pct(lat, 99), "max_abs_dE": dE,
+            "p50_s": pct(lat, 50), "p99_s": pct(lat, 99), "max_abs_dE": dE, "dE_compared": compared,
+            "dE_nonfinite": nonfinite,
             "failed": len(failed), "first_error": failed[0]["message"] if failed else None,
             "not_converged": sum(1 for r in results if not r["converged"]),
             "peak_running": st["peak_running"], "peak_reserved_GB": st["peak_reserved_bytes"] / 1e9,

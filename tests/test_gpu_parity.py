@@ -113,10 +113,11 @@ def test_rdms_match_reference(gcase):
     assert none is None and np.abs(one_only - c.rdm1).max() <= 1e-12 * np.abs(c.rdm1).max()
 
 
-@pytest.mark.parametrize("shapes", [(0, 0), (1, 2), (3, 3), (0, 4), (2, 4), (3, 4), (0, 5), (1, 5)])
+@pytest.mark.parametrize("shapes", [(0, 0), (1, 2), (3, 3), (0, 4), (2, 4), (3, 4), (0, 5), (1, 5), (0, 6), (1, 6)])
 def test_sigma_every_tile_shape(gcase, shapes):
-    """Every tile shape, the fused single kernel (shape_b 4) and the sparse-row
-    streaming kernel (shape_b 5) give the reference sigma, in both precisions."""
+    """Every tile shape, the fused single kernel (shape_b 4) and the two
+    streaming kernels for sparse rows (shape_b 5, 6) give the reference sigma,
+    in both precisions."""
     c, p = gcase
     p.diag_terms()
     p.set_tuning(0, *shapes)
@@ -130,7 +131,7 @@ def test_sigma_every_tile_shape(gcase, shapes):
     assert max_rel(S32.double().cpu().numpy(), c.sigma) <= 1e-5
 
 
-@pytest.mark.parametrize("shapes", [(0, 0), (1, 2), (3, 3), (0, 4), (3, 4), (0, 5)])
+@pytest.mark.parametrize("shapes", [(0, 0), (1, 2), (3, 3), (0, 4), (3, 4), (0, 5), (1, 6)])
 @pytest.mark.parametrize("nvec", [2, 3, 4, 5])
 def test_mixed_block_sigma_equals_single(gcase, shapes, nvec):
     """The multi-vector FP32 product gives each vector's single-vector product: bit
@@ -150,7 +151,7 @@ def test_mixed_block_sigma_equals_single(gcase, shapes, nvec):
         y = torch.empty(N, dtype=torch.float32, device="cuda")
         p.sigma_mixed_device(X[j].data_ptr(), y.data_ptr(), stream=0)
         torch.cuda.synchronize()
-        if c.norb > 32 or shapes[1] == 5:
+        if c.norb > 32 or shapes[1] >= 5:
             assert torch.equal(Y[j], y), (j, shapes)
         else:
             assert max_rel(Y[j].double().cpu().numpy(), y.double().cpu().numpy()) <= 2e-6, (j, shapes)
@@ -163,7 +164,7 @@ def _df(x):
     return np.stack([hi, lo], axis=-1).ravel()
 
 
-@pytest.mark.parametrize("shapes", [None, (1, 1), (3, 4), (0, 5)])
+@pytest.mark.parametrize("shapes", [None, (1, 1), (3, 4), (0, 5), (1, 6)])
 def test_double_float_sigma_matches_reference(gcase, shapes):
     """The double-float sigma (48-bit values, FP32-pipe arithmetic) against the
     reference sigma at 1e-12, in the autotuned shape and forced ones, in the
@@ -186,7 +187,7 @@ def test_double_float_sigma_matches_reference(gcase, shapes):
     assert max_rel(y, base + c.sigma) <= 1e-12
 
 
-@pytest.mark.parametrize("shapes", [(1, 1), (3, 4), (1, 5)])
+@pytest.mark.parametrize("shapes", [(1, 1), (3, 4), (1, 5), (0, 6)])
 def test_sigma_alpha_beta_kernel(gcase, shapes):
     """The alpha x beta single pairs in their own kernel (k_sigma_ab: the C rows
     and (P|Q) rows of each alpha row's singles staged in shared memory) next to

@@ -2,6 +2,7 @@
 // validation, HBM accounting, and the status/exception boundary.
 #include <algorithm>
 #include <cstring>
+#include <set>
 
 #include "common.cuh"
 
@@ -55,6 +56,17 @@ void ensure_dynamic_smem(const void *kernel, size_t bytes) {
   if (bytes <= have) return;
   SBDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   have = bytes;
+}
+
+void prefer_shared_carveout(const void *kernel) {
+  static std::mutex mu;
+  static std::set<std::pair<int, const void *>> done;
+  int dev = 0;
+  SBDGB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (!done.insert({dev, kernel}).second) return;
+  SBDGB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  (int)cudaSharedmemCarveoutMaxShared));
 }
 
 void *workspace(Problem &p, int slot, size_t bytes) {

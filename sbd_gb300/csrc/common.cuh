@@ -220,6 +220,9 @@ void *dev_alloc(Problem &p, size_t bytes);
 // concurrent threads, and one that set a smaller limit between another's
 // setting and launch made that launch fail.
 void ensure_dynamic_smem(const void *kernel, size_t bytes);
+// Asks for the largest shared-memory carveout for a kernel (once per kernel and
+// device): kernels that stage tens of KB per CTA otherwise fit one CTA per SM.
+void prefer_shared_carveout(const void *kernel);
 // Temporary device buffer outside the problem's accounting (pool-aware).
 void *tmp_alloc(Ctx *c, size_t bytes);
 void tmp_free(Ctx *c, void *d);

@@ -147,6 +147,21 @@ struct CombineArgs {
   const double *theta_dev;
 };
 
+// 1/x.  FP64: the correctly rounded FP32 reciprocal refined by one
+// Newton-Raphson step, r <- r + r (1 - x r), which squares its relative error
+// (2^-24 -> 2^-48, then FP64 rounding): two FP64 FMAs and two conversions in
+// place of an FP64 division, whose instruction sequence on this GPU's 1/64-rate
+// FP64 pipe cost more than the combine's multiply-adds.  |x| >= 1e-12 here
+// (the preconditioner's guard), well inside the FP32 range.  FP32 and
+// double-float: their own division.
+__device__ __forceinline__ double recip(double x) {
+  if (!(fabs(x) < 1e30)) return 1.0 / x;  // outside the FP32 range of the seed
+  const double r = (double)(1.0f / (float)x);
+  return fma(r, fma(-x, r, 1.0), r);
+}
+__device__ __forceinline__ float recip(float x) { return 1.0f / x; }
+__device__ __forceinline__ dfloat recip(dfloat x) { return dfloat(1.0f, 0.0f) / x; }
+
 // X_r = V c_r, HX_r = HV c_r, R_r = HX_r - theta_r X_r, T_r = R_r / (theta_r - d)
 // (davidson.h:818-843 and the preconditioner :899-908, 1e-12 guard).  With U
 // it also writes U_r = X_r / (theta_r - d) and sums x.T and x.U, from which
@@ -199,10 +214,11 @@ __global__ void __launch_bounds__(kRed) k_combine(CombineArgs<F> a) {
       if (a.T) {
         F den = th[r] - d;
         if (fabs(den) <= F(1.0e-12)) den -= F(1.0e-12);
-        const F t = res / den;
+        const F inv = recip(den);  // one reciprocal for both quotients
+        const F t = res * inv;
         a.T[(size_t)r * a.N + e] = t;
         if (a.U) {
-          const F u = x[r] / den;
+          const F u = x[r] * inv;
           a.U[(size_t)r * a.N + e] = u;
           xt[r] = fma(x[r], t, xt[r]);
           xu[r] = fma(x[r], u, xu[r]);

@@ -175,6 +175,7 @@ void launch_ab_kernel(const Problem &p, const Args<T> &a, cudaStream_t s) {
   const size_t smem = ab_smem<T>(p);
   auto k = k_sigma_ab<T, Wd, kB>;
   ensure_dynamic_smem((const void *)k, smem);
+  prefer_shared_carveout((const void *)k);
   const AbOrder o{p.ab_rows, p.ab_cols, p.ab_slice, p.ab_ent, p.ab_mask, p.n_ab_slices};
   k<<<p.n_ab_rows, kAbThreads, smem, s>>>(a, o);
 }

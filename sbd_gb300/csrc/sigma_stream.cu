@@ -222,10 +222,12 @@ void launch_rows_nt(const Problem &p, Args<T> a, cudaStream_t s) {
   if (vec) {
     auto k = k_sigma_rows<NT, VW, T, Wd, kB>;
     ensure_dynamic_smem((const void *)k, smem);
+    prefer_shared_carveout((const void *)k);
     k<<<p.na, NT, smem, s>>>(a, rp);
   } else {
     auto k = k_sigma_rows<NT, 1, T, Wd, kB>;
     ensure_dynamic_smem((const void *)k, smem);
+    prefer_shared_carveout((const void *)k);
     k<<<p.na, NT, smem, s>>>(a, rp);
   }
 }

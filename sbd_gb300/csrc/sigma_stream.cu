@@ -25,8 +25,9 @@
 // Steps per row: (1) the row of C to shared memory; (2) the beta pairs'
 // products and run sums (kept in registers); (3) each thread's columns: the
 // diagonal, alpha pairs (type 2, :450-488; warp-uniform table loads, C rows
-// read as 16-byte vectors) and alpha x beta pairs (type 0, :527-557), written
-// over the staged row; (4) the runs' totals added; (5) the row written out.
+// read as 16-byte vectors) and alpha x beta pairs (type 0, :527-557), into a
+// second shared row (so (2) and (3) need no barrier between them and their
+// loads overlap); (4) the runs' totals added; (5) the row written out.
 // Deterministic: fixed summation order, no atomics.
 #include <algorithm>
 
@@ -55,7 +56,8 @@ struct RowPairs {
 template <int NT, int VW, typename T, typename Wd, bool kB>
 __global__ void __launch_bounds__(NT) k_sigma_rows(Args<T> a, RowPairs rp) {
   extern __shared__ __align__(16) unsigned char rows_smem[];
-  T *Cs = reinterpret_cast<T *>(rows_smem);
+  T *Cs = reinterpret_cast<T *>(rows_smem);  // the row of C
+  T *Ss = Cs + a.nb;                          // the row of sigma being formed
   const uint32_t ia = ldg(a.tile_order + blockIdx.x);  // rows, most alpha pairs first
   const size_t rk = (size_t)ia * a.nb;
   const uint32_t tid = threadIdx.x, lane = tid & 31u;
@@ -104,8 +106,8 @@ __global__ void __launch_bounds__(NT) k_sigma_rows(Args<T> a, RowPairs rp) {
     tot[k] = t;
     key[k] = (kk != ~0u && (lane == 31u || kn != kk)) ? kk : ~0u;  // run tails only
   }
-  __syncthreads();  // every pair has read the staged row
-  // (3) each thread's columns, written over the staged row
+  // (3) each thread's columns into the sigma row (no barrier before: the
+  // pairs above only read the C row, so their loads and these overlap)
   const uint32_t p0 = ldg(a.A.off_s + ia), p1 = ldg(a.A.off_s + ia + 1);
   const uint32_t e0 = ldg(a.A.off_d + ia), e1 = ldg(a.A.off_d + ia + 1);
   for (uint32_t c = tid * VW; c < a.nb; c += NT * VW) {
@@ -181,20 +183,20 @@ __global__ void __launch_bounds__(NT) k_sigma_rows(Args<T> a, RowPairs rp) {
 #pragma unroll
     for (int v = 0; v < VW; ++v) {
       acc_add_part(acc[v], part[v]);
-      Cs[c + v] = (T)acc_value(acc[v]);
+      Ss[c + v] = (T)acc_value(acc[v]);
     }
   }
   __syncthreads();
   // (4) the beta pairs' run totals
 #pragma unroll
   for (int k = 0; k < kRowChunks; ++k)
-    if (key[k] != ~0u) Cs[key[k]] = Cs[key[k]] + tot[k];
+    if (key[k] != ~0u) Ss[key[k]] = Ss[key[k]] + tot[k];
   __syncthreads();
   // (5) the row out
   for (uint32_t c = tid * VW; c < a.nb; c += NT * VW) {
     T out[VW];
 #pragma unroll
-    for (int v = 0; v < VW; ++v) out[v] = Cs[c + v];
+    for (int v = 0; v < VW; ++v) out[v] = Ss[c + v];
     if (a.accumulate) {
       T old[VW];
       load_v<VW>(a.S + rk + c, old);
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(NT) k_sigma_rows(Args<T> a, RowPairs rp) {
 
 template <typename T>
 size_t rows_smem(const Problem &p) {
-  return sizeof(T) * (size_t)p.nb;
+  return 2 * sizeof(T) * (size_t)p.nb;  // the row of C and the row of sigma
 }
 
 template <typename T, int NT, typename Wd, bool kB>

@@ -39,7 +39,7 @@ namespace sbdgb {
 namespace {
 
 using namespace sdev;
-constexpr int kRowChunks = 8;  // pair chunks per thread held in registers
+constexpr int kRowEntries = 4096;  // beta pair entries (padding included) the row kernels hold
 
 __device__ __forceinline__ double shfl_up(double v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
 __device__ __forceinline__ float shfl_up(float v, int d) { return __shfl_up_sync(0xffffffffu, v, d); }
@@ -53,33 +53,27 @@ struct RowPairs {
   uint32_t maxrun;   // longest run of one column's entries (<= 32)
 };
 
+// Steps (2)-(5) of one row, with the row of C staged in Cs.  Ss receives the
+// row of sigma; Hs, when not null, is the row of hii staged in FP32 (the
+// unshifted FP32 product) and may be Ss itself (each thread reads its own
+// columns' hii before writing their sigma).  Ends with the row stored.
 template <int NT, int VW, typename T, typename Wd, bool kB>
-__global__ void __launch_bounds__(NT) k_sigma_rows(Args<T> a, RowPairs rp) {
-  extern __shared__ __align__(16) unsigned char rows_smem[];
-  T *Cs = reinterpret_cast<T *>(rows_smem);  // the row of C
-  T *Ss = Cs + a.nb;                          // the row of sigma being formed
-  const uint32_t ia = ldg(a.tile_order + blockIdx.x);  // rows, most alpha pairs first
+__device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, uint32_t ia, const T *Cs, T *Ss,
+                                          const float *Hs) {
   const size_t rk = (size_t)ia * a.nb;
   const uint32_t tid = threadIdx.x, lane = tid & 31u;
-  // (1) the row of C
-  for (uint32_t c = tid * VW; c < a.nb; c += NT * VW) {
-    T x[VW];
-    load_v<VW>(a.C + rk + c, x);
-#pragma unroll
-    for (int v = 0; v < VW; ++v) Cs[c + v] = x[v];
-  }
   const Wd arow = kB ? Wd(0) : word<Wd>(a.astr, ia);
-  __syncthreads();
   // (2) the beta pairs: products and run sums
-  T tot[kRowChunks];
-  uint32_t key[kRowChunks];
+  constexpr int RC = kRowEntries / NT;  // pair chunks per thread, held in registers
+  T tot[RC];
+  uint32_t key[RC];
 #pragma unroll
-  for (int k = 0; k < kRowChunks; ++k) {
+  for (int k = 0; k < RC; ++k) {
     tot[k] = T(0);
     key[k] = ~0u;
   }
 #pragma unroll
-  for (int k = 0; k < kRowChunks; ++k) {
+  for (int k = 0; k < RC; ++k) {
     if ((uint32_t)k * NT + (tid & ~31u) >= rp.n) break;  // warp-uniform
     const uint32_t e = tid + (uint32_t)k * NT;
     T t = T(0);
@@ -128,7 +122,13 @@ __global__ void __launch_bounds__(NT) k_sigma_rows(Args<T> a, RowPairs rp) {
 #pragma unroll
       for (int v = 0; v < VW; ++v) acc[v] = h[v] * x[v];
     } else if constexpr (std::is_same<T, float>::value) {
-      if (a.hii_f) {
+      if (Hs) {
+        float h[VW];
+#pragma unroll
+        for (int v = 0; v < VW; ++v) h[v] = Hs[c + v];
+#pragma unroll
+        for (int v = 0; v < VW; ++v) acc[v] = ff_prod(h[v], x[v]);
+      } else if (a.hii_f) {
         float h[VW];
         load_v<VW>(a.hii_f + k, h);
 #pragma unroll
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(NT) k_sigma_rows(Args<T> a, RowPairs rp) {
   __syncthreads();
   // (4) the beta pairs' run totals
 #pragma unroll
-  for (int k = 0; k < kRowChunks; ++k)
+  for (int k = 0; k < RC; ++k)
     if (key[k] != ~0u) Ss[key[k]] = Ss[key[k]] + tot[k];
   __syncthreads();
   // (5) the row out
@@ -204,6 +204,66 @@ __global__ void __launch_bounds__(NT) k_sigma_rows(Args<T> a, RowPairs rp) {
       for (int v = 0; v < VW; ++v) out[v] = old[v] + out[v];
     }
     store_v<VW>(a.S + rk + c, out);
+  }
+}
+
+
+// One row per CTA: the row of C loaded into shared memory, then its steps.
+template <int NT, int VW, typename T, typename Wd, bool kB>
+__global__ void __launch_bounds__(NT) k_sigma_rows(Args<T> a, RowPairs rp) {
+  extern __shared__ __align__(16) unsigned char rows_smem[];
+  T *Cs = reinterpret_cast<T *>(rows_smem);  // the row of C
+  T *Ss = Cs + a.nb;                          // the row of sigma being formed
+  const uint32_t ia = ldg(a.tile_order + blockIdx.x);  // rows, most alpha pairs first
+  const size_t rk = (size_t)ia * a.nb;
+  // (1) the row of C
+  for (uint32_t c = threadIdx.x * VW; c < a.nb; c += NT * VW) {
+    T x[VW];
+    load_v<VW>(a.C + rk + c, x);
+#pragma unroll
+    for (int v = 0; v < VW; ++v) Cs[c + v] = x[v];
+  }
+  __syncthreads();
+  row_steps<NT, VW, T, Wd, kB>(a, rp, ia, Cs, Ss, nullptr);
+}
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const uint32_t sa = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// The unshifted FP32 product, persistent: each CTA takes rows blockIdx.x,
+// + gridDim.x, ...  The next row's C and hii are copied into the other half of
+// a double buffer (cp.async, 16 bytes per thread and copy) while the current
+// row is computed, so the row's streaming loads are off the critical path;
+// the staged hii row is overwritten by the sigma row.  Needs 16 nb bytes of
+// shared memory, nb a multiple of 4 and 16-byte aligned rows.
+template <int NT, typename Wd, bool kB>
+__global__ void __launch_bounds__(NT) k_sigma_rows_pipe(Args<float> a, RowPairs rp) {
+  constexpr int VW = 4;
+  extern __shared__ __align__(16) unsigned char rows_smem[];
+  float *Cb[2], *Hb[2];
+  Cb[0] = reinterpret_cast<float *>(rows_smem);
+  Cb[1] = Cb[0] + a.nb;
+  Hb[0] = Cb[1] + a.nb;
+  Hb[1] = Hb[0] + a.nb;
+  auto stage = [&](int slot, uint32_t ia) {
+    const size_t rk = (size_t)ia * a.nb;
+    for (uint32_t c = threadIdx.x * VW; c < a.nb; c += NT * VW) {
+      cp_async16(Cb[slot] + c, a.C + rk + c);
+      cp_async16(Hb[slot] + c, a.hii_f + rk + c);
+    }
+    cp_async_commit();
+  };
+  uint32_t i = blockIdx.x;
+  if (i < a.na) stage(0, ldg(a.tile_order + i));
+  for (int slot = 0; i < a.na; i += gridDim.x, slot ^= 1) {
+    cp_async_wait_all();  // this row's copies (the only ones in flight)
+    __syncthreads();      // ... visible to all, and every thread is done with the other half
+    if (i + gridDim.x < a.na) stage(slot ^ 1, ldg(a.tile_order + i + gridDim.x));
+    row_steps<NT, VW, float, Wd, kB>(a, rp, ldg(a.tile_order + i), Cb[slot], Hb[slot], Hb[slot]);
   }
 }
 
@@ -280,20 +340,48 @@ void build_row_pairs(Problem &p, const std::vector<uint32_t> &off_s, const std::
 template <typename T>
 bool rows_fit(const Problem &p) {
   if (!p.rp_ready) return false;
-  if ((size_t)p.rp_n > (size_t)kRowChunks * 512) return false;  // more pair chunks than a 512-thread CTA holds
+  if ((size_t)p.rp_n > (size_t)kRowEntries) return false;  // more pair entries than the kernels hold
   int dev = 0, optin = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return false;
   if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return false;
   return rows_smem<T>(p) <= (size_t)optin;
 }
 
+// The pipelined FP32 form when it applies (unshifted product, 16-byte rows,
+// 16 nb bytes of shared memory); false otherwise.
+template <typename T, typename Wd, bool kB>
+bool launch_rows_pipe(const Problem &p, Args<T> a, cudaStream_t s) {
+  if constexpr (!std::is_same<T, float>::value) {
+    return false;
+  } else {
+    auto al = [](const void *x) { return ((uintptr_t)x & 15u) == 0; };
+    int dev = 0, optin = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return false;
+    const size_t smem = 16 * (size_t)p.nb;
+    if (!a.hii_f || p.nb % 4 != 0 || smem > (size_t)optin || !al(a.C) || !al(a.S) || !al(a.Jb) || !al(a.hii_f))
+      return false;
+    a.tile_order = p.rp_rows;
+    const RowPairs rp{p.rp_ent, p.rp_n, p.rp_maxrun};
+    auto k = k_sigma_rows_pipe<1024, Wd, kB>;
+    ensure_dynamic_smem((const void *)k, smem);
+    prefer_shared_carveout((const void *)k);
+    k<<<(unsigned)std::min<uint32_t>(p.na, (uint32_t)sms), 1024, smem, s>>>(a, rp);
+    return true;
+  }
+}
+
 template <typename T, bool kB>
 void launch_stream(const Problem &p, const sdev::Args<T> &a, int variant, cudaStream_t s) {
   SBDGB_REQUIRE(rows_fit<T>(p), SBDGB_E_UNSUPPORTED, "the row kernel does not fit this problem");
   if (kB || p.norb <= 32) {
+    if (variant == 0 && launch_rows_pipe<T, uint32_t, kB>(p, a, s)) return;
     if (variant == 0) launch_rows_nt<T, 512, uint32_t, kB>(p, a, s);
     else launch_rows_nt<T, 1024, uint32_t, kB>(p, a, s);
   } else {
+    if (variant == 0 && launch_rows_pipe<T, unsigned long long, kB>(p, a, s)) return;
     if (variant == 0) launch_rows_nt<T, 512, unsigned long long, kB>(p, a, s);
     else launch_rows_nt<T, 1024, unsigned long long, kB>(p, a, s);
   }

@@ -47,6 +47,18 @@ __device__ __forceinline__ dfloat shfl_up(dfloat v, int d) {
   return dfloat(__shfl_up_sync(0xffffffffu, v.hi, d), __shfl_up_sync(0xffffffffu, v.lo, d));
 }
 
+// VW elements from shared memory in one access (16 bytes when VW > 1).
+template <int VW, typename T>
+__device__ __forceinline__ void lds_v(const T *p, T (&x)[VW]) {
+  static_assert(VW == 1 || sizeof(T) * VW == 16, "shared vectors of 16 bytes");
+  if constexpr (VW == 1) {
+    x[0] = *p;
+  } else {
+    const uint4 u = *reinterpret_cast<const uint4 *>(p);
+    memcpy(x, &u, 16);
+  }
+}
+
 struct RowPairs {
   const uint4 *ent;  // {column, ket column, info = single | P << 1 | phase << 31, table index}
   uint32_t n;        // entries, padding included
@@ -56,8 +68,10 @@ struct RowPairs {
 // Steps (2)-(5) of one row, with the row of C staged in Cs.  Ss receives the
 // row of sigma; Hs, when not null, is the row of hii staged in FP32 (the
 // unshifted FP32 product) and may be Ss itself (each thread reads its own
-// columns' hii before writing their sigma).  Ends with the row stored.
-template <int NT, int VW, typename T, typename Wd, bool kB>
+// columns' hii before writing their sigma).  kInPlace: Ss is Cs, so a barrier
+// separates the pair products (any column of C) from step (3) (each thread
+// reads its own columns of C, then overwrites them).  Ends with the row stored.
+template <int NT, int VW, typename T, typename Wd, bool kB, bool kInPlace = false>
 __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, uint32_t ia, const T *Cs, T *Ss,
                                           const float *Hs) {
   const size_t rk = (size_t)ia * a.nb;
@@ -100,6 +114,7 @@ __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, 
     tot[k] = t;
     key[k] = (kk != ~0u && (lane == 31u || kn != kk)) ? kk : ~0u;  // run tails only
   }
+  if constexpr (kInPlace) __syncthreads();
   // (3) each thread's columns into the sigma row (no barrier before: the
   // pairs above only read the C row, so their loads and these overlap)
   const uint32_t p0 = ldg(a.A.off_s + ia), p1 = ldg(a.A.off_s + ia + 1);
@@ -110,11 +125,11 @@ __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, 
     T part[VW];
     T x[VW];
     Wd beta[VW];
+    lds_v<VW>(Cs + c, x);
 #pragma unroll
     for (int v = 0; v < VW; ++v) {
-      x[v] = Cs[c + v];
       part[v] = T(0);
-      beta[v] = kB ? Wd(0) : word<Wd>(a.bstr, c + v);
+      beta[v] = kB ? Wd(0) : word<Wd>(a.bstr, c + v);  // only the alpha pairs' phases use it
     }
     if constexpr (std::is_same<T, double>::value) {
       double h[VW];
@@ -124,8 +139,7 @@ __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, 
     } else if constexpr (std::is_same<T, float>::value) {
       if (Hs) {
         float h[VW];
-#pragma unroll
-        for (int v = 0; v < VW; ++v) h[v] = Hs[c + v];
+        lds_v<VW>(Hs + c, h);
 #pragma unroll
         for (int v = 0; v < VW; ++v) acc[v] = ff_prod(h[v], x[v]);
       } else if (a.hii_f) {
@@ -180,11 +194,13 @@ __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, 
 #pragma unroll
       for (int v = 0; v < VW; ++v) madd(acc[v], part[v], flip(val, par<kB>(beta[v] & m)), y[v]);
     }
+    T out[VW];
 #pragma unroll
     for (int v = 0; v < VW; ++v) {
       acc_add_part(acc[v], part[v]);
-      Ss[c + v] = (T)acc_value(acc[v]);
+      out[v] = (T)acc_value(acc[v]);
     }
+    store_v<VW>(Ss + c, out);
   }
   __syncthreads();
   // (4) the beta pairs' run totals
@@ -195,8 +211,7 @@ __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, 
   // (5) the row out
   for (uint32_t c = tid * VW; c < a.nb; c += NT * VW) {
     T out[VW];
-#pragma unroll
-    for (int v = 0; v < VW; ++v) out[v] = Ss[c + v];
+    lds_v<VW>(Ss + c, out);
     if (a.accumulate) {
       T old[VW];
       load_v<VW>(a.S + rk + c, old);
@@ -264,6 +279,32 @@ __global__ void __launch_bounds__(NT) k_sigma_rows_pipe(Args<float> a, RowPairs 
     __syncthreads();      // ... visible to all, and every thread is done with the other half
     if (i + gridDim.x < a.na) stage(slot ^ 1, ldg(a.tile_order + i + gridDim.x));
     row_steps<NT, VW, float, Wd, kB>(a, rp, ldg(a.tile_order + i), Cb[slot], Hb[slot], Hb[slot]);
+  }
+}
+
+// The same for the 8-byte products (FP64, double-float): two C rows fill
+// 16 nb bytes, so the sigma row is formed in place of the current C row and
+// hii is read from global memory.  nb a multiple of 2 and 16-byte aligned rows.
+template <int NT, typename T, typename Wd, bool kB>
+__global__ void __launch_bounds__(NT) k_sigma_rows_pipe8(Args<T> a, RowPairs rp) {
+  static_assert(sizeof(T) == 8, "8-byte products");
+  constexpr int VW = 2;
+  extern __shared__ __align__(16) unsigned char rows_smem[];
+  T *Cb[2];
+  Cb[0] = reinterpret_cast<T *>(rows_smem);
+  Cb[1] = Cb[0] + a.nb;
+  auto stage = [&](int slot, uint32_t ia) {
+    const size_t rk = (size_t)ia * a.nb;
+    for (uint32_t c = threadIdx.x * VW; c < a.nb; c += NT * VW) cp_async16(Cb[slot] + c, a.C + rk + c);
+    cp_async_commit();
+  };
+  uint32_t i = blockIdx.x;
+  if (i < a.na) stage(0, ldg(a.tile_order + i));
+  for (int slot = 0; i < a.na; i += gridDim.x, slot ^= 1) {
+    cp_async_wait_all();
+    __syncthreads();
+    if (i + gridDim.x < a.na) stage(slot ^ 1, ldg(a.tile_order + i + gridDim.x));
+    row_steps<NT, VW, T, Wd, kB, true>(a, rp, ldg(a.tile_order + i), Cb[slot], Cb[slot], nullptr);
   }
 }
 
@@ -347,30 +388,36 @@ bool rows_fit(const Problem &p) {
   return rows_smem<T>(p) <= (size_t)optin;
 }
 
-// The pipelined FP32 form when it applies (unshifted product, 16-byte rows,
-// 16 nb bytes of shared memory); false otherwise.
+// The pipelined form when it applies (16-byte rows, 16 nb bytes of shared
+// memory; for FP32 the unshifted product); false otherwise.
 template <typename T, typename Wd, bool kB>
 bool launch_rows_pipe(const Problem &p, Args<T> a, cudaStream_t s) {
-  if constexpr (!std::is_same<T, float>::value) {
+  auto al = [](const void *x) { return ((uintptr_t)x & 15u) == 0; };
+  int dev = 0, optin = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return false;
-  } else {
-    auto al = [](const void *x) { return ((uintptr_t)x & 15u) == 0; };
-    int dev = 0, optin = 0, sms = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-      return false;
-    const size_t smem = 16 * (size_t)p.nb;
-    if (!a.hii_f || p.nb % 4 != 0 || smem > (size_t)optin || !al(a.C) || !al(a.S) || !al(a.Jb) || !al(a.hii_f))
-      return false;
-    a.tile_order = p.rp_rows;
-    const RowPairs rp{p.rp_ent, p.rp_n, p.rp_maxrun};
+  const size_t smem = 16 * (size_t)p.nb;
+  const unsigned grid = (unsigned)std::min<uint32_t>(p.na, (uint32_t)sms);
+  if (smem > (size_t)optin || !al(a.C) || !al(a.S) || !al(a.Jb)) return false;
+  a.tile_order = p.rp_rows;
+  const RowPairs rp{p.rp_ent, p.rp_n, p.rp_maxrun};
+  if constexpr (std::is_same<T, float>::value) {
+    if (!a.hii_f || p.nb % 4 != 0 || !al(a.hii_f)) return false;
     auto k = k_sigma_rows_pipe<1024, Wd, kB>;
     ensure_dynamic_smem((const void *)k, smem);
     prefer_shared_carveout((const void *)k);
-    k<<<(unsigned)std::min<uint32_t>(p.na, (uint32_t)sms), 1024, smem, s>>>(a, rp);
-    return true;
+    k<<<grid, 1024, smem, s>>>(a, rp);
+  } else {
+    if (p.nb % 2 != 0 || !al(std::is_same<T, double>::value ? (const void *)a.hii : (const void *)a.hii_df))
+      return false;
+    auto k = k_sigma_rows_pipe8<1024, T, Wd, kB>;
+    ensure_dynamic_smem((const void *)k, smem);
+    prefer_shared_carveout((const void *)k);
+    k<<<grid, 1024, smem, s>>>(a, rp);
   }
+  return true;
 }
 
 template <typename T, bool kB>

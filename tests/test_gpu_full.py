@@ -182,6 +182,50 @@ def test_measured_fp64_rates():
     assert 0.05 < r["dfma_tflops"] < 200.0 and 0.05 < r["dmma_tflops"] < 200.0
 
 
+@pytest.mark.parametrize("nb", [280, 282, 283])
+@pytest.mark.parametrize("variant", [0, 1])
+def test_row_kernel_against_oracle(engine, nb, variant):
+    """The row kernel (shape_b 6; norb 40, 10+10 electrons, 300 x nb strings:
+    at most 17 beta pairs per column).  Variant 0 is the persistent,
+    double-buffered form where it applies (FP32: nb a multiple of 4, 280;
+    FP64 and double-float: nb even, 280 and 282) and the one-row-per-CTA form
+    otherwise (283, one element per thread); variant 1 is the 1024-thread
+    one-row-per-CTA form.  FP64 and double-float at 1e-12 against the oracle,
+    overwrite and accumulate; FP32 at its bound."""
+    torch = pytest.importorskip("torch")
+    prob = make_problem(40, 10, 10, 300, nb, seed=43)
+    p = TPBProblem.from_problem(engine, prob)
+    p.build_tables()
+    p.diag_terms()
+    for prec in (0, 1, 2):
+        p.set_tuning(prec, variant, 6)
+    o = Oracle.from_problem(prob)
+    rng = np.random.default_rng(7 * variant + nb)
+    C = rng.uniform(-1, 1, prob.ndet)
+    ref = o.mult(C)
+    assert max_rel(p.mult(C), ref) <= 1e-12
+    base = rng.uniform(-1, 1, prob.ndet)
+    st = torch.cuda.current_stream().cuda_stream
+    c = torch.tensor(C, device="cuda")
+    s = torch.tensor(base, device="cuda")
+    p.sigma_device(c.data_ptr(), s.data_ptr(), accumulate=True, stream=st)
+    torch.cuda.synchronize()
+    assert max_rel(s.cpu().numpy(), base + ref) <= 1e-12
+    c32 = c.float()
+    s32 = torch.empty_like(c32)
+    p.sigma_mixed_device(c32.data_ptr(), s32.data_ptr(), stream=st)
+    torch.cuda.synchronize()
+    assert max_rel(s32.double().cpu().numpy(), ref) <= 5e-6
+    hi = C.astype(np.float32)
+    lo = (C - hi.astype(np.float64)).astype(np.float32)
+    X = torch.tensor(np.stack([hi, lo], axis=-1).ravel(), device="cuda")
+    Y = torch.zeros_like(X)
+    p.sigma_df_device(X.data_ptr(), Y.data_ptr(), stream=st)
+    torch.cuda.synchronize()
+    assert max_rel(Y.double().cpu().numpy().reshape(-1, 2).sum(axis=1), ref) <= 1e-12
+    p.close()
+
+
 @pytest.mark.parametrize("nb", [280, 283])
 @pytest.mark.parametrize("variant", [0, 1])
 def test_sparse_kernel_against_oracle(engine, nb, variant):

@@ -65,6 +65,49 @@ struct RowPairs {
   uint32_t maxrun;   // longest run of one column's entries (<= 32)
 };
 
+// The alpha singles (with their alpha x beta pairs, task types 2 and 0) and
+// alpha doubles of row ia for columns c .. c + VW - 1 of one thread, added
+// into acc / part in table order.  beta: the columns' beta words
+// (interleaved ordering only).
+template <int VW, typename T, typename Wd, bool kB>
+__device__ __forceinline__ void alpha_pairs(const Args<T> &a, uint32_t c, const Wd (&beta)[VW], AccT<T> (&acc)[VW],
+                                            T (&part)[VW], uint32_t p0, uint32_t p1, uint32_t e0, uint32_t e1) {
+  for (uint32_t p = p0; p < p1; ++p) {
+    const uint32_t ja = ldg(a.A.ket_s + p), code = ldg(a.A.code_s + p);
+    const T val = ldg(a.val_sa + p);
+    const Wd m = mask_of<kB, Wd>(a.A.mask_s, p);
+    const uint32_t P = (code >> 16) & 0x7fffu;
+    T y[VW], j[VW];
+    load_v<VW>(a.C + (size_t)ja * a.nb + c, y);
+    load_v<VW>(a.Jb + (size_t)P * a.nb + c, j);
+#pragma unroll
+    for (int v = 0; v < VW; ++v) madd(acc[v], part[v], flip(val + j[v], par<kB>(beta[v] & m) ^ (code >> 31)), y[v]);
+    if (!a.skip_ab) {
+      const Wd aket = word<Wd>(a.astr, ja);
+      const T *krow = a.Kp + (size_t)P * a.npair;
+#pragma unroll
+      for (int v = 0; v < VW; ++v) {
+        const uint32_t q0 = ldg(a.B.off_s + c + v), q1 = ldg(a.B.off_s + c + v + 1);
+        for (uint32_t q = q0; q < q1; ++q) {
+          const uint32_t jb = ldg(a.B.ket_s + q), cb = ldg(a.B.code_s + q);
+          const uint32_t ph =
+              (par<kB>(beta[v] & m) ^ par<kB>(aket & mask_of<kB, Wd>(a.B.mask_s, q)) ^ (code >> 31) ^ (cb >> 31)) & 1u;
+          madd(acc[v], part[v], flip(ldg(krow + ((cb >> 16) & 0x7fffu)), ph), ldg(a.C + (size_t)ja * a.nb + jb));
+        }
+      }
+    }
+  }
+  for (uint32_t p = e0; p < e1; ++p) {
+    const uint32_t ja = ldg(a.A.ket_d + p);
+    const T val = ldg(a.val_da + p);
+    const Wd m = mask_of<kB, Wd>(a.A.mask_d, p);
+    T y[VW];
+    load_v<VW>(a.C + (size_t)ja * a.nb + c, y);
+#pragma unroll
+    for (int v = 0; v < VW; ++v) madd(acc[v], part[v], flip(val, par<kB>(beta[v] & m)), y[v]);
+  }
+}
+
 // Steps (2)-(5) of one row, with the row of C staged in Cs.  Ss receives the
 // row of sigma; Hs, when not null, is the row of hii staged in FP32 (the
 // unshifted FP32 product) and may be Ss itself (each thread reads its own
@@ -119,24 +162,67 @@ __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, 
   // pairs above only read the C row, so their loads and these overlap)
   const uint32_t p0 = ldg(a.A.off_s + ia), p1 = ldg(a.A.off_s + ia + 1);
   const uint32_t e0 = ldg(a.A.off_d + ia), e1 = ldg(a.A.off_d + ia + 1);
-  for (uint32_t c = tid * VW; c < a.nb; c += NT * VW) {
-    const size_t k = rk + c;
-    AccT<T> acc[VW];
-    T part[VW];
-    T x[VW];
-    Wd beta[VW];
-    lds_v<VW>(Cs + c, x);
+  if constexpr (sizeof(T) == 8) {
+    // FP64 and double-float: hii comes from global memory, so the diagonal
+    // goes first with several chunks' loads in flight, and the alpha pairs
+    // (few rows of a sparse problem have any) are added to it afterwards:
+    // the same order of operations as one pass.
+    constexpr int U = 2;
+    for (uint32_t c0 = tid * VW; c0 < a.nb; c0 += U * NT * VW) {
+      T h[U][VW];
 #pragma unroll
-    for (int v = 0; v < VW; ++v) {
-      part[v] = T(0);
-      beta[v] = kB ? Wd(0) : word<Wd>(a.bstr, c + v);  // only the alpha pairs' phases use it
+      for (int u = 0; u < U; ++u) {
+        const uint32_t c = c0 + (uint32_t)u * NT * VW;
+        if (c < a.nb) {
+          if constexpr (std::is_same<T, double>::value) load_v<VW>(a.hii + rk + c, h[u]);
+          else load_v<VW>(a.hii_df + rk + c, h[u]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const uint32_t c = c0 + (uint32_t)u * NT * VW;
+        if (c < a.nb) {
+          T x[VW], out[VW];
+          lds_v<VW>(Cs + c, x);
+#pragma unroll
+          for (int v = 0; v < VW; ++v) {
+            if constexpr (std::is_same<T, double>::value) out[v] = h[u][v] * x[v];
+            else out[v] = (h[u][v] - a.shift_df) * x[v];
+          }
+          store_v<VW>(Ss + c, out);
+        }
+      }
     }
-    if constexpr (std::is_same<T, double>::value) {
-      double h[VW];
-      load_v<VW>(a.hii + k, h);
+    if (p1 > p0 || e1 > e0) {
+      for (uint32_t c = tid * VW; c < a.nb; c += NT * VW) {
+        T acc[VW], part[VW];
+        Wd beta[VW];
+        lds_v<VW>(Ss + c, acc);
 #pragma unroll
-      for (int v = 0; v < VW; ++v) acc[v] = h[v] * x[v];
-    } else if constexpr (std::is_same<T, float>::value) {
+        for (int v = 0; v < VW; ++v) {
+          part[v] = T(0);
+          beta[v] = kB ? Wd(0) : word<Wd>(a.bstr, c + v);
+        }
+        alpha_pairs<VW, T, Wd, kB>(a, c, beta, acc, part, p0, p1, e0, e1);
+        store_v<VW>(Ss + c, acc);
+      }
+    }
+  } else {
+    // FP32: each column's diagonal (hii staged in shared memory or read as
+    // FP32 or as the shifted hi/lo pair) and its alpha pairs in one pass,
+    // into float-float accumulators
+    for (uint32_t c = tid * VW; c < a.nb; c += NT * VW) {
+      const size_t k = rk + c;
+      AccT<T> acc[VW];
+      T part[VW];
+      T x[VW];
+      Wd beta[VW];
+      lds_v<VW>(Cs + c, x);
+#pragma unroll
+      for (int v = 0; v < VW; ++v) {
+        part[v] = T(0);
+        beta[v] = kB ? Wd(0) : word<Wd>(a.bstr, c + v);  // only the alpha pairs' phases use it
+      }
       if (Hs) {
         float h[VW];
         lds_v<VW>(Hs + c, h);
@@ -153,54 +239,15 @@ __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, 
 #pragma unroll
         for (int v = 0; v < VW; ++v) acc[v] = ff_diag(h[v].hi, h[v].lo, a.shift_df.hi, a.shift_df.lo, x[v]);
       }
-    } else {
-      dfloat h[VW];
-      load_v<VW>(a.hii_df + k, h);
+      alpha_pairs<VW, T, Wd, kB>(a, c, beta, acc, part, p0, p1, e0, e1);
+      T out[VW];
 #pragma unroll
-      for (int v = 0; v < VW; ++v) acc[v] = (h[v] - a.shift_df) * x[v];
-    }
-    // alpha singles (with their alpha x beta pairs) and doubles of the row
-    for (uint32_t p = p0; p < p1; ++p) {
-      const uint32_t ja = ldg(a.A.ket_s + p), code = ldg(a.A.code_s + p);
-      const T val = ldg(a.val_sa + p);
-      const Wd m = mask_of<kB, Wd>(a.A.mask_s, p);
-      const uint32_t P = (code >> 16) & 0x7fffu;
-      T y[VW], j[VW];
-      load_v<VW>(a.C + (size_t)ja * a.nb + c, y);
-      load_v<VW>(a.Jb + (size_t)P * a.nb + c, j);
-#pragma unroll
-      for (int v = 0; v < VW; ++v) madd(acc[v], part[v], flip(val + j[v], par<kB>(beta[v] & m) ^ (code >> 31)), y[v]);
-      if (!a.skip_ab) {
-        const Wd aket = word<Wd>(a.astr, ja);
-        const T *krow = a.Kp + (size_t)P * a.npair;
-#pragma unroll
-        for (int v = 0; v < VW; ++v) {
-          const uint32_t q0 = ldg(a.B.off_s + c + v), q1 = ldg(a.B.off_s + c + v + 1);
-          for (uint32_t q = q0; q < q1; ++q) {
-            const uint32_t jb = ldg(a.B.ket_s + q), cb = ldg(a.B.code_s + q);
-            const uint32_t ph =
-                (par<kB>(beta[v] & m) ^ par<kB>(aket & mask_of<kB, Wd>(a.B.mask_s, q)) ^ (code >> 31) ^ (cb >> 31)) & 1u;
-            madd(acc[v], part[v], flip(ldg(krow + ((cb >> 16) & 0x7fffu)), ph), ldg(a.C + (size_t)ja * a.nb + jb));
-          }
-        }
+      for (int v = 0; v < VW; ++v) {
+        acc_add_part(acc[v], part[v]);
+        out[v] = (T)acc_value(acc[v]);
       }
+      store_v<VW>(Ss + c, out);
     }
-    for (uint32_t p = e0; p < e1; ++p) {
-      const uint32_t ja = ldg(a.A.ket_d + p);
-      const T val = ldg(a.val_da + p);
-      const Wd m = mask_of<kB, Wd>(a.A.mask_d, p);
-      T y[VW];
-      load_v<VW>(a.C + (size_t)ja * a.nb + c, y);
-#pragma unroll
-      for (int v = 0; v < VW; ++v) madd(acc[v], part[v], flip(val, par<kB>(beta[v] & m)), y[v]);
-    }
-    T out[VW];
-#pragma unroll
-    for (int v = 0; v < VW; ++v) {
-      acc_add_part(acc[v], part[v]);
-      out[v] = (T)acc_value(acc[v]);
-    }
-    store_v<VW>(Ss + c, out);
   }
   __syncthreads();
   // (4) the beta pairs' run totals

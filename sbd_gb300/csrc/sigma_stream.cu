@@ -113,8 +113,10 @@ __device__ __forceinline__ void alpha_pairs(const Args<T> &a, uint32_t c, const 
 // unshifted FP32 product) and may be Ss itself (each thread reads its own
 // columns' hii before writing their sigma).  kInPlace: Ss is Cs, so a barrier
 // separates the pair products (any column of C) from step (3) (each thread
-// reads its own columns of C, then overwrites them).  Ends with the row stored.
-template <int NT, int VW, typename T, typename Wd, bool kB, bool kInPlace = false>
+// reads its own columns of C, then overwrites them).  kStagedH: Hs is never
+// null (the pipelined FP32 kernel), which enables the one-multiply branch for
+// rows without alpha pairs.  Ends with the row stored.
+template <int NT, int VW, typename T, typename Wd, bool kB, bool kInPlace = false, bool kStagedH = false>
 __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, uint32_t ia, const T *Cs, T *Ss,
                                           const float *Hs) {
   const size_t rk = (size_t)ia * a.nb;
@@ -206,6 +208,18 @@ __device__ __forceinline__ void row_steps(const Args<T> &a, const RowPairs &rp, 
         alpha_pairs<VW, T, Wd, kB>(a, c, beta, acc, part, p0, p1, e0, e1);
         store_v<VW>(Ss + c, acc);
       }
+    }
+  } else if (kStagedH && p1 == p0 && e1 == e0) {
+    // FP32, unshifted, a row without alpha pairs: the float-float
+    // accumulator of the general branch would hold h x exactly as hi + lo and
+    // round it back to fl(h x), so one multiply gives the same bits
+    for (uint32_t c = tid * VW; c < a.nb; c += NT * VW) {
+      float h[VW], x[VW], out[VW];
+      lds_v<VW>(Cs + c, x);
+      lds_v<VW>(Hs + c, h);
+#pragma unroll
+      for (int v = 0; v < VW; ++v) out[v] = h[v] * x[v];
+      store_v<VW>(Ss + c, out);
     }
   } else {
     // FP32: each column's diagonal (hii staged in shared memory or read as
@@ -325,7 +339,7 @@ __global__ void __launch_bounds__(NT) k_sigma_rows_pipe(Args<float> a, RowPairs 
     cp_async_wait_all();  // this row's copies (the only ones in flight)
     __syncthreads();      // ... visible to all, and every thread is done with the other half
     if (i + gridDim.x < a.na) stage(slot ^ 1, ldg(a.tile_order + i + gridDim.x));
-    row_steps<NT, VW, float, Wd, kB>(a, rp, ldg(a.tile_order + i), Cb[slot], Hb[slot], Hb[slot]);
+    row_steps<NT, VW, float, Wd, kB, false, true>(a, rp, ldg(a.tile_order + i), Cb[slot], Hb[slot], Hb[slot]);
   }
 }
 

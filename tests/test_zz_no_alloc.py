@@ -95,6 +95,44 @@ def test_noalloc_sigma_in_every_kind_of_shape(shapes, split):
     eng.close()
 
 
+def test_noalloc_sigma_captures_into_a_cuda_graph():
+    """A call made under stream capture (global mode: an allocation, a
+    synchronisation or any other call that capture forbids would fail it)
+    records into a graph; replaying the graph gives the regular sigma, twice."""
+    torch = pytest.importorskip("torch")
+    from sbd_gb300.engine import Engine, TPBProblem
+    from sbd_gb300.generators import make_problem
+
+    eng = Engine(0)
+    prob = make_problem(16, 5, 5, 300, 280, seed=79)
+    p = TPBProblem.from_problem(eng, prob)
+    p.build_tables()
+    p.diag_terms()
+    f = _entry(eng.lib)
+    rng = np.random.default_rng(13)
+    C1 = torch.tensor(rng.uniform(-1, 1, prob.ndet), dtype=torch.float64, device="cuda")
+    s = torch.zeros_like(C1)
+    assert f(p.h, C1.data_ptr(), s.data_ptr(), 0, None) == 0  # first call on the device: outside capture
+    ref = torch.zeros_like(C1)
+    p.sigma_device(C1.data_ptr(), ref.data_ptr(), accumulate=False, stream=0)  # allocates its own scratch
+    torch.cuda.synchronize()
+    before = eng.bytes_in_use
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        rc = f(p.h, C1.data_ptr(), s.data_ptr(), 0, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, eng.lib.sbdgb_last_error(eng.h)
+    assert eng.bytes_in_use == before
+    for _ in range(2):
+        s.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        assert max_rel(s.cpu().numpy(), ref.cpu().numpy()) <= 1e-12
+    assert eng.bytes_in_use == before
+    del g
+    p.close()
+    eng.close()
+
+
 def test_noalloc_sigma_rejects_large_problems():
     torch = pytest.importorskip("torch")
     from sbd_gb300.engine import Engine, TPBProblem

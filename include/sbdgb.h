@@ -148,16 +148,19 @@ int sbdgb_sigma_mixed_block(sbdgb_problem *p, const float *Wk_dev, float *Wb_dev
  * shape_b = 5 means the single streaming kernel for sparse rows (16-byte
  * accesses along beta, every task type in one pass), with shape_a 0 or 1 for
  * row tiles of 8 or 16 rows (chosen for problems with a few nonzeros per row);
- * shape_b = 6 is the streaming kernel whose beta pairs are taken per warp
- * (sigma_stream.cu), shape_a 0 or 1 likewise.
+ * shape_b = 6 is the row kernel (sigma_stream.cu: one alpha row per CTA at a
+ * time, every beta pair of the problem a lane's product with the row of C in
+ * shared memory), with shape_a 0 = its persistent double-buffered form where
+ * the row length and alignment allow it (one row per CTA of 512 threads
+ * otherwise) or 1 = one row per CTA of 1024 threads.
  * The first product of each precision tunes (and synchronises), so make it
  * before any stream capture. */
 int sbdgb_problem_tuning(const sbdgb_problem *p, int precision, int *shape_a, int *shape_b, float *ms_a,
                          float *ms_b, int n_shapes);
 /* The autotuner's times (ms, 0 where not measured) of the fused kernel in
- * shapes 0..3 (ms_fused[4]), of the sparse-row kernel (ms_sparse[2]) and of
- * the per-warp streaming kernel (ms_stream[2]) with 8 and 16 rows per tile;
- * any pointer may be NULL. */
+ * shapes 0..3 (ms_fused[4]), of the sparse-row kernel with 8 and 16 rows per
+ * tile (ms_sparse[2]) and of the row kernel's two forms (ms_stream[2], in
+ * shape_a order); any pointer may be NULL. */
 int sbdgb_problem_tuning_times(const sbdgb_problem *p, int precision, float *ms_fused, float *ms_sparse,
                                float *ms_stream);
 /* Sets the sigma tile shapes of one precision instead of the autotuner's

@@ -522,7 +522,7 @@ constexpr int kNumShapes = 4;
 constexpr int kFusedShape = 4;   // tune_b value meaning "beta sweep fused into kernel A"
 constexpr int kSparseShape = 5;  // tune_b value meaning "k_sigma_sparse"; tune_a 0/1 = 8/16 rows per tile
 constexpr int kNumSparse = 2;
-constexpr int kStreamShape = 6;  // tune_b value meaning "k_sigma_stream"; tune_a 0/1 = 8/16 rows per tile
+constexpr int kStreamShape = 6;  // tune_b value meaning "the row kernel" (sigma_stream.cu); tune_a 0/1 = its two forms
 inline bool needs_transpose(int shape_b) {
   return shape_b != kFusedShape && shape_b != kSparseShape && shape_b != kStreamShape;
 }
